@@ -1,0 +1,185 @@
+/*
+ * ltpmg_gb300.h -- C ABI of the GB300-native batched transaction-processing
+ * hot path (one GPU, hand-written sm_103a CUDA).
+ *
+ * The reference exposes eight C++ entry points between its host program and
+ * its CUDA library (cuda/src/gpuscheduler.cu:3-47, declared in
+ * include/database.h:66-70, include/query.h:63-70, include/scheduler.h:33-37).
+ * This header is the plain-pointer layer those entry points forward to; the
+ * reference-compatible C++ shims live in include/ltpmg_compat.h.  Every
+ * function returns LTP_OK (0) or a negative LTP_E_* status and never exits
+ * the process (the reference's CHECK macro printed and called exit(-1),
+ * cuda/include/define.cuh:57-65).
+ *
+ * Data model
+ *  - A context owns one CUDA device, its tables and all scratch memory.
+ *  - A table is column-store: one contiguous int32 array per column.  Cells
+ *    are addressed by (table, row = key, column).
+ *  - A batch is a transaction-major list of operations: transaction t owns
+ *    ops [txn_first[t], txn_first[t+1]); its TID is t.  Each op is a 64-bit
+ *    key (the row id) and a 32-bit opword (LTP_OPW below).
+ *  - Outputs per batch: commit[t] (1 committed, 0 aborted) and, per op, the
+ *    value of the cell immediately after the op in the serial order (the
+ *    value read, or the value the read-modify-write produced; 0 for ops of
+ *    aborted transactions).  The table state is read back with
+ *    ltp_table_download.
+ *
+ * Rules (ltp_config.rule)
+ *  - LTP_RULE_ORDERED: every op on a cell runs in ascending (TID, op) order
+ *    and every transaction commits -- the reference's rule (per-row TID
+ *    order: cuda/src/gpulauncher.cu:382-418, 2439-2671).
+ *  - LTP_RULE_PRIORITY: deterministic TID-priority abort: a transaction
+ *    aborts when a smaller TID writes a cell it reads or writes.
+ */
+#ifndef LTPMG_GB300_H
+#define LTPMG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LTP_OK 0
+#define LTP_E_CUDA (-1)          /* a CUDA runtime call failed */
+#define LTP_E_CAPACITY (-2)      /* a size exceeds what the context or batch holds */
+#define LTP_E_TIMEOUT (-3)       /* a bounded device-side wait ran out */
+#define LTP_E_BADARG (-4)        /* invalid argument or malformed operation */
+#define LTP_E_DEVICE_ASSERT (-5) /* a kernel's own consistency check failed */
+#define LTP_E_NOMEM (-6)         /* device or pinned-host allocation failed */
+#define LTP_E_STATE (-7)         /* call out of order (e.g. results before execute) */
+
+#define LTP_RULE_ORDERED 0
+#define LTP_RULE_PRIORITY 1
+
+#define LTP_MAX_TABLES 16
+#define LTP_MAX_COLS 64
+
+/* opword: bits 0-1 kind, 2-7 column, 8-11 table, 12-31 signed immediate */
+#define LTP_OP_READ 0u
+#define LTP_OP_ADD 1u /* read-modify-write: cell += immediate (two's-complement wrap) */
+#define LTP_OPW(kind, col, table, imm) \
+    ((uint32_t)(kind) | ((uint32_t)(col) << 2) | ((uint32_t)(table) << 8) | (((uint32_t)(imm) & 0xFFFFFu) << 12))
+
+#define LTP_FLAG_STAGE_TIMING 1u /* record CUDA events around every stage */
+
+typedef struct ltp_ctx ltp_ctx;
+typedef struct ltp_batch ltp_batch;
+
+typedef struct {
+    int32_t device;       /* CUDA device ordinal */
+    int32_t rule;         /* LTP_RULE_* */
+    uint64_t reserve_ops; /* pre-size scratch for batches of this many ops (0: on demand) */
+    uint32_t flags;       /* LTP_FLAG_* */
+    uint32_t reserved;
+} ltp_config;
+
+typedef struct {
+    uint32_t n_cols; /* 1..LTP_MAX_COLS int32 columns */
+    uint32_t reserved;
+} ltp_schema;
+
+#define LTP_N_STAGES 8
+typedef struct {
+    uint64_t txns, ops, committed, aborted;
+    uint64_t contended_ops;   /* ops on cells touched >1 time with >=1 write */
+    uint64_t contended_cells;
+    uint64_t touched_words;   /* 32-cell bitmap words touched by the batch */
+    uint64_t bytes_algorithmic;
+    float ms_stage[LTP_N_STAGES]; /* mark, ids, classify, sort, apply, finish, priority, total */
+} ltp_stats;
+
+typedef struct {
+    uint64_t seed;
+    uint64_t n_rows;
+    uint32_t n_cols;
+    uint32_t ops_min, ops_max; /* ops per transaction, uniform in [ops_min, ops_max] */
+    int32_t rmw_delta;         /* immediate of every RMW op */
+    double read_frac;          /* probability that an op is a read */
+    double theta;              /* 0: uniform keys; else Zipf(theta) over a seeded permutation */
+} ltp_ycsb_params;
+
+/* ---- version / errors ------------------------------------------------ */
+const char *ltp_version(void);
+const char *ltp_status_string(int status);
+const char *ltp_last_error(const ltp_ctx *ctx);
+
+/* ---- context --------------------------------------------------------- */
+/* Replaces GPUScheduler's global state (cuda/include/gpuscheduler.cuh:54). */
+int ltp_init(const ltp_config *cfg, ltp_ctx **out);
+int ltp_shutdown(ltp_ctx *ctx);
+/* Raw cudaStream_t of the context's own stream (used when a NULL stream is passed). */
+void *ltp_default_stream(ltp_ctx *ctx);
+int ltp_sync(ltp_ctx *ctx, void *stream);
+
+/* ---- tables (GPUdatabase::malloc_global_row / copy_to_global_row,
+ *      cuda/src/gpudatabase.cu:9-238, made column-store) ---------------- */
+int ltp_table_create(ltp_ctx *ctx, const ltp_schema *schema, uint64_t rows, uint32_t *table_id);
+/* Copies rows [row0, row0+n) of one column from host memory (int32). */
+int ltp_table_upload(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, const int32_t *src);
+/* New: the reference never copies tables back (gpudatabase.cu:240-339). */
+int ltp_table_download(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, int32_t *dst);
+/* Device-side fill with ltp_table_value(seed, row, col, n_cols). */
+int ltp_table_fill_seeded(ltp_ctx *ctx, uint32_t table, uint64_t seed, void *stream);
+/* FNV-1a 64 of the whole table (column-major bytes), computed on the host
+ * from a download; for checkpoints and tests. */
+int ltp_table_fingerprint(ltp_ctx *ctx, uint32_t table, uint64_t *out);
+
+/* ---- batches (GPUquery::malloc_global_txn / copy_global_txn,
+ *      cuda/src/gpuquery.cu:17-627) -------------------------------------- */
+int ltp_batch_create(ltp_ctx *ctx, uint64_t max_txns, uint64_t max_ops, ltp_batch **out);
+int ltp_batch_free(ltp_ctx *ctx, ltp_batch *b);
+/* Asynchronous host->device copy of a batch.  txn_first has n_txns+1
+ * entries; when it is NULL every transaction has ops_per_txn ops. */
+int ltp_batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
+                   uint64_t n_ops, const uint64_t *keys, const uint32_t *opw, void *stream);
+/* Executes one batch against the context's tables (replaces
+ * GPUlauncher::txn_kernel_launcher, cuda/src/gpulauncher.cu:755-1116). */
+int ltp_batch_execute(ltp_ctx *ctx, ltp_batch *b, void *stream);
+/* Asynchronous device->host copy of the outputs (commit may be NULL, vals
+ * may be NULL). */
+int ltp_batch_fetch(ltp_ctx *ctx, ltp_batch *b, uint8_t *commit, int32_t *vals, void *stream);
+/* Synchronises the stream, then fills stats (may be NULL) and reports any
+ * device-side error of the batch. */
+int ltp_batch_finish(ltp_ctx *ctx, ltp_batch *b, ltp_stats *stats, void *stream);
+/* Convenience: fetch + finish. */
+int ltp_batch_results(ltp_ctx *ctx, ltp_batch *b, uint8_t *commit, int32_t *vals, ltp_stats *stats);
+/* Device pointers of a loaded batch's arrays (for zero-copy callers). */
+int ltp_batch_device_ptrs(ltp_batch *b, uint64_t **keys, uint32_t **opw, uint32_t **txn_first, int32_t **vals,
+                          uint8_t **commit);
+
+/* ---- pinned host memory ------------------------------------------------ */
+void *ltp_host_alloc(size_t bytes);
+void ltp_host_free(void *p);
+
+/* ---- seeded workload generator (host; Txn_Generator<YCSB_*> +
+ *      Query::generate_txn, src/txn_generator.cpp:601-673,
+ *      src/query.cpp:270-311, made seedable) ---------------------------- */
+/* Returns the op count, or UINT64_MAX when cap_ops is too small or the
+ * parameters are invalid.  n_threads <= 0: all hardware threads. */
+uint64_t ltp_gen_ycsb(const ltp_ycsb_params *p, uint64_t batch, uint64_t n_txns, uint32_t *txn_first, uint64_t *keys,
+                      uint32_t *opw, uint64_t cap_ops, int n_threads);
+int32_t ltp_table_value(uint64_t seed, uint64_t row, uint32_t col, uint32_t n_cols);
+
+/* ---- tuning --------------------------------------------------------------- */
+typedef struct {
+    uint32_t block;      /* threads per block of the streaming kernels: 128, 256, 512 */
+    uint32_t ipt;        /* ops per thread per tile: 1, 2, 4, 8 */
+    uint32_t word_bits;  /* bitmap word granularity: 32 or 64 */
+    uint32_t reserved;
+} ltp_tuning;
+/* Tuning used for batches whose op count falls in size bucket floor(log2(ops)). */
+int ltp_set_tuning(ltp_ctx *ctx, uint32_t bucket, const ltp_tuning *t);
+int ltp_get_tuning(ltp_ctx *ctx, uint32_t bucket, ltp_tuning *t);
+
+/* ---- failure injection for tests (host-side; no GPU fault) ------------- */
+/* While set, the next execute's first stage polls a flag that nothing sets,
+ * gives up after about `ms` milliseconds and the batch reports LTP_E_TIMEOUT;
+ * the context stays usable. */
+int ltp_debug_stall_next(ltp_ctx *ctx, uint32_t ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,66 @@
+"""In-tree build of libltpmg_gb300.so (sm_103a) with nvcc and g++.
+
+Translation units compile in parallel into ltpmg_gb300/_build/ and link into
+ltpmg_gb300/libltpmg_gb300.so.  No cmake, one -gencode, a minute or less.
+"""
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libltpmg_gb300.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "-I", os.path.join(ROOT, "include")]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I", os.path.join(ROOT, "include")]
+
+CU_SOURCES = ["ltp_kernels.cu", "ltp_api.cu"]
+CXX_SOURCES = ["ltp_gen.cpp"]
+
+
+def _nvcc():
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stdout + r.stderr
+
+
+def build(verbose=False, extra_nvcc=()):
+    os.makedirs(BUILD, exist_ok=True)
+    nvcc = _nvcc()
+    jobs = []
+    objs = []
+    for src in CU_SOURCES:
+        obj = os.path.join(BUILD, src + ".o")
+        objs.append(obj)
+        jobs.append([nvcc] + ARCH + NVCC_FLAGS + list(extra_nvcc) + ["-c", os.path.join(CSRC, src), "-o", obj])
+    for src in CXX_SOURCES:
+        obj = os.path.join(BUILD, src + ".o")
+        objs.append(obj)
+        jobs.append(["g++"] + CXX_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj])
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        outs = list(ex.map(_run, jobs))
+    if verbose:
+        for o in outs:
+            if o.strip():
+                print(o)
+    tmp = LIB + ".tmp"
+    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

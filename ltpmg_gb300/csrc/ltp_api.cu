@@ -1,0 +1,558 @@
+// ltp_api.cu -- C ABI of the hot path: context, column-store tables, batches,
+// execution and results.  Replaces the reference's GPUScheduler singleton
+// (cuda/include/gpuscheduler.cuh:54) with an explicit context handle; every
+// call returns a status instead of exiting the process.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "ltp_internal.cuh"
+
+using namespace ltp;
+
+struct TableHost {
+    TableDev dev;
+    uint32_t n_cols;
+};
+
+struct ltp_ctx {
+    int device = 0;
+    int rule = LTP_RULE_ORDERED;
+    uint32_t flags = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<TableHost> tables;
+    uint64_t total_cells = 0;
+    Scratch s;
+    uint64_t alloc_words = 0;  // bitmap words currently allocated
+    Counters *ctr = nullptr;
+    std::string last_error;
+    Tuning tuning[64];
+    cudaEvent_t ev[LTP_N_STAGES + 1];
+    bool have_events = false;
+    uint32_t stall_ms_next = 0;
+    bool dirty = false;  // scratch must be reset before the next batch
+};
+
+struct ltp_batch {
+    uint64_t cap_txns = 0, cap_ops = 0;
+    uint64_t *keys = nullptr;
+    uint32_t *opw = nullptr, *txn_first = nullptr, *op_txn = nullptr;
+    int32_t *out = nullptr;
+    uint8_t *commit = nullptr;
+    uint64_t n_txns = 0, n_ops = 0;
+    uint32_t ops_per_txn = 0;
+    bool loaded = false, executed = false;
+    int rule = 0;
+    Counters *snap = nullptr;  // device copy of the counters after this batch
+};
+
+namespace {
+
+int fail(ltp_ctx *ctx, int status, const char *fmt, const char *detail = "") {
+    if (ctx) {
+        char buf[512];
+        snprintf(buf, sizeof(buf), fmt, detail);
+        ctx->last_error = buf;
+    }
+    return status;
+}
+
+int cuda_fail(ltp_ctx *ctx, cudaError_t e, const char *where) {
+    std::string msg = std::string(where) + ": " + cudaGetErrorString(e);
+    if (ctx) ctx->last_error = msg;
+    return (e == cudaErrorMemoryAllocation) ? LTP_E_NOMEM : LTP_E_CUDA;
+}
+
+#define CK(call)                                                \
+    do {                                                        \
+        cudaError_t _e = (call);                                \
+        if (_e != cudaSuccess) return cuda_fail(ctx, _e, #call); \
+    } while (0)
+
+cudaStream_t pick_stream(ltp_ctx *ctx, void *stream) { return stream ? (cudaStream_t)stream : ctx->stream; }
+
+template <typename T>
+cudaError_t dalloc(T **p, uint64_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void **)p, count * sizeof(T));
+}
+
+void free_scratch_ops(Scratch &s) {
+    cudaFree(s.tw_list);
+    cudaFree(s.list[0]);
+    cudaFree(s.list[1]);
+    cudaFree(s.dcell);
+    cudaFree(s.dbase);
+    cudaFree(s.dminw);
+    cudaFree(s.st_sort[0]);
+    cudaFree(s.st_sort[1]);
+    cudaFree(s.st_ids);
+    cudaFree(s.st_cls);
+    cudaFree(s.st_apply);
+    s.tw_list = nullptr;
+    s.list[0] = s.list[1] = nullptr;
+    s.dcell = nullptr;
+    s.dbase = nullptr;
+    s.dminw = nullptr;
+    s.st_sort[0] = s.st_sort[1] = nullptr;
+    s.st_ids = s.st_cls = s.st_apply = nullptr;
+    s.cap_ops = 0;
+}
+
+void free_scratch_words(Scratch &s) {
+    cudaFree(s.touch);
+    cudaFree(s.multi);
+    cudaFree(s.wbits);
+    cudaFree(s.cwx);
+    s.touch = s.multi = s.wbits = nullptr;
+    s.cwx = nullptr;
+}
+
+// Sizes the bitmaps to the cell space and the per-op scratch to n_ops.
+int ensure_scratch(ltp_ctx *ctx, uint64_t n_ops) {
+    Scratch &s = ctx->s;
+    const uint64_t words = (ctx->total_cells + 31) / 32 + 1;
+    if (words > ctx->alloc_words) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        free_scratch_words(s);
+        CK(dalloc(&s.touch, words));
+        CK(dalloc(&s.multi, words));
+        CK(dalloc(&s.wbits, words));
+        CK(dalloc(&s.cwx, words));
+        CK(cudaMemset(s.touch, 0, words * 4));
+        CK(cudaMemset(s.multi, 0, words * 4));
+        CK(cudaMemset(s.wbits, 0, words * 4));
+        ctx->alloc_words = words;
+    }
+    s.n_words = words;
+    if (n_ops > s.cap_ops) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        free_scratch_ops(s);
+        uint64_t cap = 1024;
+        while (cap < n_ops) cap <<= 1;
+        const uint64_t tiles = cap / kMinTile + 2;
+        const uint64_t stiles = cap / kSortTile + 2;
+        CK(dalloc(&s.tw_list, cap));
+        CK(dalloc(&s.list[0], cap));
+        CK(dalloc(&s.list[1], cap));
+        CK(dalloc(&s.dcell, cap));
+        CK(dalloc(&s.dbase, cap));
+        CK(dalloc(&s.dminw, cap));
+        CK(dalloc(&s.st_sort[0], stiles * 256));
+        CK(dalloc(&s.st_sort[1], stiles * 256));
+        CK(dalloc(&s.st_ids, tiles));
+        CK(dalloc(&s.st_cls, tiles));
+        CK(dalloc(&s.st_apply, tiles));
+        s.cap_ops = cap;
+        s.cap_tiles = tiles;
+        s.cap_sort_tiles = stiles;
+        CK(launch_reset_scratch(ctx->stream, s));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return LTP_OK;
+}
+
+TablesDev tables_dev(const ltp_ctx *ctx) {
+    TablesDev T;
+    memset(&T, 0, sizeof(T));
+    T.n = (uint32_t)ctx->tables.size();
+    for (size_t i = 0; i < ctx->tables.size(); i++) T.t[i] = ctx->tables[i].dev;
+    return T;
+}
+
+uint32_t bucket_of(uint64_t n) {
+    uint32_t b = 0;
+    while (b < 63 && (2ull << b) <= n) b++;
+    return b;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *ltp_version(void) { return "ltpmg_gb300 0.1 (sm_103a)"; }
+
+const char *ltp_status_string(int status) {
+    switch (status) {
+    case LTP_OK: return "ok";
+    case LTP_E_CUDA: return "CUDA runtime error";
+    case LTP_E_CAPACITY: return "capacity exceeded";
+    case LTP_E_TIMEOUT: return "device-side wait timed out";
+    case LTP_E_BADARG: return "invalid argument or malformed operation";
+    case LTP_E_DEVICE_ASSERT: return "device consistency check failed";
+    case LTP_E_NOMEM: return "out of memory";
+    case LTP_E_STATE: return "call out of order";
+    default: return "unknown status";
+    }
+}
+
+const char *ltp_last_error(const ltp_ctx *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+int ltp_init(const ltp_config *cfg, ltp_ctx **out) {
+    if (!cfg || !out) return LTP_E_BADARG;
+    *out = nullptr;
+    if (cfg->rule != LTP_RULE_ORDERED && cfg->rule != LTP_RULE_PRIORITY) return LTP_E_BADARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return LTP_E_CUDA;
+    if (cfg->device < 0 || cfg->device >= ndev) return LTP_E_BADARG;
+    ltp_ctx *ctx = new ltp_ctx();
+    ctx->device = cfg->device;
+    ctx->rule = cfg->rule;
+    ctx->flags = cfg->flags;
+    memset(&ctx->s, 0, sizeof(ctx->s));
+    for (int i = 0; i < 64; i++) ctx->tuning[i] = Tuning{256, 4, 32};
+    cudaError_t e = cudaSetDevice(cfg->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, cfg->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->ctr, sizeof(Counters));
+    if (e == cudaSuccess) e = cudaMemset(ctx->ctr, 0, sizeof(Counters));
+    for (int i = 0; e == cudaSuccess && i <= LTP_N_STAGES; i++) e = cudaEventCreate(&ctx->ev[i]);
+    if (e != cudaSuccess) {
+        ltp_shutdown(ctx);
+        return e == cudaErrorMemoryAllocation ? LTP_E_NOMEM : LTP_E_CUDA;
+    }
+    ctx->have_events = true;
+    if (cfg->reserve_ops) {
+        int rc = ensure_scratch(ctx, cfg->reserve_ops);
+        if (rc) {
+            ltp_shutdown(ctx);
+            return rc;
+        }
+    }
+    *out = ctx;
+    return LTP_OK;
+}
+
+int ltp_shutdown(ltp_ctx *ctx) {
+    if (!ctx) return LTP_E_BADARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto &t : ctx->tables) cudaFree(t.dev.data);
+    free_scratch_ops(ctx->s);
+    free_scratch_words(ctx->s);
+    cudaFree(ctx->ctr);
+    if (ctx->have_events)
+        for (int i = 0; i <= LTP_N_STAGES; i++) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return LTP_OK;
+}
+
+void *ltp_default_stream(ltp_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int ltp_sync(ltp_ctx *ctx, void *stream) {
+    if (!ctx) return LTP_E_BADARG;
+    CK(cudaStreamSynchronize(pick_stream(ctx, stream)));
+    return LTP_OK;
+}
+
+int ltp_table_create(ltp_ctx *ctx, const ltp_schema *schema, uint64_t rows, uint32_t *table_id) {
+    if (!ctx || !schema || !table_id) return LTP_E_BADARG;
+    if (schema->n_cols == 0 || schema->n_cols > LTP_MAX_COLS) return fail(ctx, LTP_E_BADARG, "n_cols must be 1..64");
+    if (rows == 0 || rows > (1ull << 40)) return fail(ctx, LTP_E_BADARG, "rows must be 1..2^40");
+    if (ctx->tables.size() >= LTP_MAX_TABLES) return fail(ctx, LTP_E_CAPACITY, "at most 16 tables");
+    const uint64_t cells = rows * schema->n_cols;
+    if ((ctx->total_cells + cells + 31) / 32 >= (1ull << 32))
+        return fail(ctx, LTP_E_CAPACITY, "cell space exceeds 2^37 cells");
+    CK(cudaSetDevice(ctx->device));
+    TableHost t;
+    memset(&t, 0, sizeof(t));
+    t.n_cols = schema->n_cols;
+    t.dev.rows_cap = (rows + 63) & ~63ull;  // 256-byte aligned columns
+    t.dev.n_rows = rows;
+    t.dev.n_cols = schema->n_cols;
+    t.dev.cell_base = ctx->total_cells;
+    CK(cudaMalloc((void **)&t.dev.data, t.dev.rows_cap * schema->n_cols * sizeof(int32_t)));
+    CK(cudaMemset(t.dev.data, 0, t.dev.rows_cap * schema->n_cols * sizeof(int32_t)));
+    // keep the next table's cells in a fresh bitmap word
+    ctx->total_cells += (cells + 31) & ~31ull;
+    *table_id = (uint32_t)ctx->tables.size();
+    ctx->tables.push_back(t);
+    return LTP_OK;
+}
+
+static int check_table(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n) {
+    if (!ctx) return LTP_E_BADARG;
+    if (table >= ctx->tables.size()) return fail(ctx, LTP_E_BADARG, "no such table");
+    const TableHost &t = ctx->tables[table];
+    if (col >= t.n_cols) return fail(ctx, LTP_E_BADARG, "no such column");
+    if (row0 > t.dev.n_rows || n > t.dev.n_rows - row0) return fail(ctx, LTP_E_BADARG, "row range out of bounds");
+    return LTP_OK;
+}
+
+int ltp_table_upload(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, const int32_t *src) {
+    int rc = check_table(ctx, table, col, row0, n);
+    if (rc) return rc;
+    if (!src && n) return LTP_E_BADARG;
+    const TableHost &t = ctx->tables[table];
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(t.dev.data + col * t.dev.rows_cap + row0, src, n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return LTP_OK;
+}
+
+int ltp_table_download(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, int32_t *dst) {
+    int rc = check_table(ctx, table, col, row0, n);
+    if (rc) return rc;
+    if (!dst && n) return LTP_E_BADARG;
+    const TableHost &t = ctx->tables[table];
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaDeviceSynchronize());
+    CK(cudaMemcpyAsync(dst, t.dev.data + col * t.dev.rows_cap + row0, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return LTP_OK;
+}
+
+int ltp_table_fill_seeded(ltp_ctx *ctx, uint32_t table, uint64_t seed, void *stream) {
+    if (!ctx || table >= ctx->tables.size()) return LTP_E_BADARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(launch_fill_seeded(pick_stream(ctx, stream), ctx->tables[table].dev, seed));
+    return LTP_OK;
+}
+
+int ltp_table_fingerprint(ltp_ctx *ctx, uint32_t table, uint64_t *out) {
+    if (!ctx || !out || table >= ctx->tables.size()) return LTP_E_BADARG;
+    const TableHost &t = ctx->tables[table];
+    std::vector<int32_t> buf(t.dev.n_rows);
+    uint64_t h = 0xCBF29CE484222325ull;
+    for (uint32_t c = 0; c < t.n_cols; c++) {
+        int rc = ltp_table_download(ctx, table, c, 0, t.dev.n_rows, buf.data());
+        if (rc) return rc;
+        const uint8_t *p = (const uint8_t *)buf.data();
+        for (uint64_t i = 0; i < t.dev.n_rows * 4; i++) {
+            h ^= p[i];
+            h *= 0x100000001B3ull;
+        }
+    }
+    *out = h;
+    return LTP_OK;
+}
+
+int ltp_batch_create(ltp_ctx *ctx, uint64_t max_txns, uint64_t max_ops, ltp_batch **out) {
+    if (!ctx || !out) return LTP_E_BADARG;
+    *out = nullptr;
+    if (max_ops >= (1ull << 30)) return fail(ctx, LTP_E_CAPACITY, "a batch holds fewer than 2^30 ops");
+    if (max_txns >= (1ull << 32)) return fail(ctx, LTP_E_CAPACITY, "a batch holds fewer than 2^32 transactions");
+    CK(cudaSetDevice(ctx->device));
+    ltp_batch *b = new ltp_batch();
+    b->cap_txns = max_txns;
+    b->cap_ops = max_ops;
+    cudaError_t e = dalloc(&b->keys, max_ops);
+    if (e == cudaSuccess) e = dalloc(&b->opw, max_ops);
+    if (e == cudaSuccess) e = dalloc(&b->op_txn, max_ops);
+    if (e == cudaSuccess) e = dalloc(&b->out, max_ops);
+    if (e == cudaSuccess) e = dalloc(&b->txn_first, max_txns + 1);
+    if (e == cudaSuccess) e = dalloc(&b->commit, max_txns);
+    if (e == cudaSuccess) e = dalloc(&b->snap, 1);
+    if (e != cudaSuccess) {
+        ltp_batch_free(ctx, b);
+        return cuda_fail(ctx, e, "ltp_batch_create");
+    }
+    int rc = ensure_scratch(ctx, max_ops);
+    if (rc) {
+        ltp_batch_free(ctx, b);
+        return rc;
+    }
+    *out = b;
+    return LTP_OK;
+}
+
+int ltp_batch_free(ltp_ctx *ctx, ltp_batch *b) {
+    if (!b) return LTP_E_BADARG;
+    if (ctx) cudaSetDevice(ctx->device);
+    cudaFree(b->keys);
+    cudaFree(b->opw);
+    cudaFree(b->op_txn);
+    cudaFree(b->out);
+    cudaFree(b->txn_first);
+    cudaFree(b->commit);
+    cudaFree(b->snap);
+    delete b;
+    return LTP_OK;
+}
+
+int ltp_batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
+                   uint64_t n_ops, const uint64_t *keys, const uint32_t *opw, void *stream) {
+    if (!ctx || !b) return LTP_E_BADARG;
+    if (n_txns > b->cap_txns || n_ops > b->cap_ops) return fail(ctx, LTP_E_CAPACITY, "batch larger than its capacity");
+    if (n_ops && (!keys || !opw)) return fail(ctx, LTP_E_BADARG, "null op arrays");
+    if (txn_first) {
+        if (txn_first[0] != 0 || txn_first[n_txns] != n_ops)
+            return fail(ctx, LTP_E_BADARG, "txn_first must start at 0 and end at n_ops");
+        for (uint64_t t = 0; t < n_txns; t++)
+            if (txn_first[t + 1] < txn_first[t]) return fail(ctx, LTP_E_BADARG, "txn_first must be non-decreasing");
+    } else if ((uint64_t)ops_per_txn * n_txns != n_ops || (n_txns && ops_per_txn == 0)) {
+        return fail(ctx, LTP_E_BADARG, "n_ops must equal n_txns * ops_per_txn");
+    }
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = pick_stream(ctx, stream);
+    if (n_ops) {
+        CK(cudaMemcpyAsync(b->keys, keys, n_ops * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(b->opw, opw, n_ops * 4, cudaMemcpyHostToDevice, st));
+    }
+    b->n_txns = n_txns;
+    b->n_ops = n_ops;
+    b->ops_per_txn = txn_first ? 0u : ops_per_txn;
+    if (txn_first) {
+        CK(cudaMemcpyAsync(b->txn_first, txn_first, (n_txns + 1) * 4, cudaMemcpyHostToDevice, st));
+        CK(launch_expand_op_txn(st, b->txn_first, n_txns, b->op_txn));
+    }
+    b->loaded = true;
+    b->executed = false;
+    return LTP_OK;
+}
+
+int ltp_batch_execute(ltp_ctx *ctx, ltp_batch *b, void *stream) {
+    if (!ctx || !b) return LTP_E_BADARG;
+    if (!b->loaded) return fail(ctx, LTP_E_STATE, "batch not loaded");
+    if (ctx->tables.empty()) return fail(ctx, LTP_E_STATE, "no tables");
+    CK(cudaSetDevice(ctx->device));
+    int rc = ensure_scratch(ctx, b->n_ops);
+    if (rc) return rc;
+    cudaStream_t st = pick_stream(ctx, stream);
+    if (ctx->dirty) {
+        CK(launch_reset_scratch(st, ctx->s));
+        ctx->dirty = false;
+    }
+    CK(cudaMemsetAsync(ctx->ctr, 0, sizeof(Counters), st));
+    if (b->n_txns) CK(cudaMemsetAsync(b->commit, 1, b->n_txns, st));
+    BatchDev bd;
+    bd.keys = (const u64 *)b->keys;
+    bd.opw = b->opw;
+    bd.txn_first = b->txn_first;
+    bd.op_txn = b->op_txn;
+    bd.out = b->out;
+    bd.commit = b->commit;
+    bd.n_ops = b->n_ops;
+    bd.n_txns = b->n_txns;
+    bd.ops_per_txn = b->ops_per_txn;
+    bd.pad = 0;
+    Launch L;
+    L.stream = st;
+    L.num_sms = ctx->num_sms;
+    L.rule = ctx->rule;
+    L.tune = ctx->tuning[bucket_of(b->n_ops)];
+    L.stall = ctx->stall_ms_next != 0;
+    L.stall_ms = ctx->stall_ms_next;
+    ctx->stall_ms_next = 0;
+    L.timing = (ctx->flags & LTP_FLAG_STAGE_TIMING) != 0;
+    for (int i = 0; i <= LTP_N_STAGES; i++) L.ev[i] = ctx->ev[i];
+    if (b->n_ops) CK(launch_execute(L, bd, tables_dev(ctx), ctx->s, ctx->ctr));
+    CK(cudaMemcpyAsync(b->snap, ctx->ctr, sizeof(Counters), cudaMemcpyDeviceToDevice, st));
+    b->rule = ctx->rule;
+    b->executed = true;
+    return LTP_OK;
+}
+
+int ltp_batch_fetch(ltp_ctx *ctx, ltp_batch *b, uint8_t *commit, int32_t *vals, void *stream) {
+    if (!ctx || !b) return LTP_E_BADARG;
+    if (!b->executed) return fail(ctx, LTP_E_STATE, "batch not executed");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = pick_stream(ctx, stream);
+    if (commit && b->n_txns) CK(cudaMemcpyAsync(commit, b->commit, b->n_txns, cudaMemcpyDeviceToHost, st));
+    if (vals && b->n_ops) CK(cudaMemcpyAsync(vals, b->out, b->n_ops * 4, cudaMemcpyDeviceToHost, st));
+    return LTP_OK;
+}
+
+int ltp_batch_finish(ltp_ctx *ctx, ltp_batch *b, ltp_stats *stats, void *stream) {
+    if (!ctx || !b) return LTP_E_BADARG;
+    if (!b->executed) return fail(ctx, LTP_E_STATE, "batch not executed");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = pick_stream(ctx, stream);
+    Counters c;
+    CK(cudaMemcpyAsync(&c, b->snap, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->txns = b->n_txns;
+        stats->ops = b->n_ops;
+        stats->committed = b->rule == LTP_RULE_PRIORITY ? c.committed : b->n_txns;
+        stats->aborted = b->n_txns - stats->committed;
+        stats->contended_ops = c.n_c;
+        stats->contended_cells = c.M;
+        stats->touched_words = c.n_tw;
+        stats->bytes_algorithmic = 28ull * b->n_ops + 4ull * b->n_txns;
+        if ((ctx->flags & LTP_FLAG_STAGE_TIMING) && b->n_ops) {
+            float total = 0;
+            for (int i = 0; i < 6; i++) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);
+                stats->ms_stage[i] = ms;
+                total += ms;
+            }
+            stats->ms_stage[7] = total;
+        }
+    }
+    if (c.err) {
+        ctx->dirty = true;
+        if (c.err == LTP_E_BADARG && c.bad_op) {
+            char buf[128];
+            snprintf(buf, sizeof(buf), "malformed op at index %llu (key/column/table/kind out of range)",
+                     (unsigned long long)~c.bad_op);
+            ctx->last_error = buf;
+        } else {
+            ctx->last_error = ltp_status_string(c.err);
+        }
+        return c.err;
+    }
+    return LTP_OK;
+}
+
+int ltp_batch_results(ltp_ctx *ctx, ltp_batch *b, uint8_t *commit, int32_t *vals, ltp_stats *stats) {
+    int rc = ltp_batch_fetch(ctx, b, commit, vals, nullptr);
+    if (rc) return rc;
+    return ltp_batch_finish(ctx, b, stats, nullptr);
+}
+
+int ltp_batch_device_ptrs(ltp_batch *b, uint64_t **keys, uint32_t **opw, uint32_t **txn_first, int32_t **vals,
+                          uint8_t **commit) {
+    if (!b) return LTP_E_BADARG;
+    if (keys) *keys = b->keys;
+    if (opw) *opw = b->opw;
+    if (txn_first) *txn_first = b->txn_first;
+    if (vals) *vals = b->out;
+    if (commit) *commit = b->commit;
+    return LTP_OK;
+}
+
+void *ltp_host_alloc(size_t bytes) {
+    void *p = nullptr;
+    if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) return nullptr;
+    return p;
+}
+
+void ltp_host_free(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
+int ltp_set_tuning(ltp_ctx *ctx, uint32_t bucket, const ltp_tuning *t) {
+    if (!ctx || !t || bucket >= 64) return LTP_E_BADARG;
+    if (t->block != 128 && t->block != 256 && t->block != 512) return fail(ctx, LTP_E_BADARG, "block must be 128/256/512");
+    if (t->ipt != 1 && t->ipt != 2 && t->ipt != 4 && t->ipt != 8) return fail(ctx, LTP_E_BADARG, "ipt must be 1/2/4/8");
+    if (t->word_bits != 32 && t->word_bits != 64) return fail(ctx, LTP_E_BADARG, "word_bits must be 32/64");
+    ctx->tuning[bucket] = Tuning{t->block, t->ipt, t->word_bits};
+    return LTP_OK;
+}
+
+int ltp_get_tuning(ltp_ctx *ctx, uint32_t bucket, ltp_tuning *t) {
+    if (!ctx || !t || bucket >= 64) return LTP_E_BADARG;
+    t->block = ctx->tuning[bucket].block;
+    t->ipt = ctx->tuning[bucket].ipt;
+    t->word_bits = ctx->tuning[bucket].word_bits;
+    t->reserved = 0;
+    return LTP_OK;
+}
+
+int ltp_debug_stall_next(ltp_ctx *ctx, uint32_t ms) {
+    if (!ctx || ms == 0 || ms > 10000) return LTP_E_BADARG;
+    ctx->stall_ms_next = ms;
+    return LTP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,125 @@
+// ltp_internal.cuh -- device-side data layout shared by the kernels and the
+// C-ABI layer of the batched transaction-processing hot path.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ltpmg_gb300.h"
+
+namespace ltp {
+
+typedef unsigned long long u64;
+typedef unsigned int u32;
+
+// opword fields (same layout as LTP_OPW in the public header)
+__host__ __device__ __forceinline__ u32 opw_kind(u32 w) { return w & 3u; }
+__host__ __device__ __forceinline__ u32 opw_col(u32 w) { return (w >> 2) & 63u; }
+__host__ __device__ __forceinline__ u32 opw_table(u32 w) { return (w >> 8) & 15u; }
+__host__ __device__ __forceinline__ int32_t opw_imm(u32 w) { return ((int32_t)w) >> 12; }
+
+// One column-store table: column c of row r lives at data[c * rows_cap + r].
+// Cells are numbered row-major within a table (cell_base + r * n_cols + c) so
+// that the cells of one row share a bitmap word.
+struct TableDev {
+    int32_t *data;
+    u64 rows_cap;
+    u64 n_rows;
+    u64 cell_base;
+    u32 n_cols;
+    u32 pad;
+};
+
+struct TablesDev {
+    TableDev t[LTP_MAX_TABLES];
+    u32 n;
+    u32 pad;
+};
+
+// Device view of one loaded batch.
+struct BatchDev {
+    const u64 *keys;       // [n_ops]
+    const u32 *opw;        // [n_ops]
+    const u32 *txn_first;  // [n_txns + 1]
+    const u32 *op_txn;     // [n_ops] transaction of each op (variable-length batches)
+    int32_t *out;          // [n_ops] value after each op
+    uint8_t *commit;       // [n_txns]
+    u64 n_ops;
+    u64 n_txns;
+    u32 ops_per_txn;       // > 0: fixed-length transactions (op_txn unused)
+    u32 pad;
+};
+
+// Look-back status slots of the kernels that use decoupled look-back.
+enum TileSlot { SLOT_IDS = 0, SLOT_CLASSIFY = 1, SLOT_SORT0 = 2, SLOT_APPLY = 6, SLOT_R1 = 7, N_SLOTS = 8 };
+
+// Per-batch device counters; zeroed by the host before every batch.
+struct Counters {
+    u64 n_tw;          // touched bitmap words
+    u64 n_c;           // contended ops
+    u64 bad_op;        // ~(lowest index of a malformed op); 0: none
+    u64 committed;
+    u32 M;             // contended cells
+    int err;           // first device-side error status (LTP_E_*), 0 = none
+    u32 tile_ctr[N_SLOTS];
+    u32 hist[4][256];  // radix digit histograms of the contended list
+    u32 stall;         // polled by the debug stall kernel; never set
+    u32 pad;
+};
+
+// Scratch owned by the context, sized by the cell space and the batch capacity.
+struct Scratch {
+    u32 *touch;     // [n_words] cell touched at least once
+    u32 *multi;     // [n_words] cell touched at least twice
+    u32 *wbits;     // [n_words] cell written at least once
+    u64 *cwx;       // [n_words] (contended-id prefix << 32) | contended bits
+    u32 *tw_list;   // [cap_ops] touched words
+    u64 *list[2];   // [cap_ops] contended-op records, ping-pong for the sort
+    u64 *dcell;     // [cap_ops] cell of each contended-cell id
+    int32_t *dbase; // [cap_ops] value of each contended cell before the batch
+    u32 *dminw;     // [cap_ops] smallest writer TID of each contended cell (priority rule)
+    u32 *st_sort[2];// [tiles * 256] radix look-back status
+    u64 *st_ids;    // [tiles] id-scan look-back status
+    u64 *st_cls;    // [tiles] classify look-back status
+    u64 *st_apply;  // [tiles] segmented-apply look-back status
+    u64 n_words;
+    u64 cap_ops;
+    u64 cap_tiles;  // tiles of the smallest look-back tile size at cap_ops
+    u64 cap_sort_tiles;
+};
+
+constexpr u32 kSortBlock = 256;
+constexpr u32 kSortIpt = 16;
+constexpr u32 kSortTile = kSortBlock * kSortIpt;
+constexpr u32 kIdsBlock = 256;
+constexpr u32 kIdsIpt = 8;
+constexpr u32 kIdsTile = kIdsBlock * kIdsIpt;
+constexpr u32 kApplyBlock = 256;
+constexpr u32 kApplyIpt = 16;
+constexpr u32 kApplyTile = kApplyBlock * kApplyIpt;
+constexpr u32 kMinTile = 128;  // smallest classify tile (block 128 x 1 op)
+
+struct Tuning {
+    u32 block, ipt, word_bits;
+};
+
+// Host-side launch plan for one batch.
+struct Launch {
+    cudaStream_t stream;
+    int num_sms;
+    int rule;
+    Tuning tune;
+    bool stall;
+    u32 stall_ms;
+    cudaEvent_t ev[LTP_N_STAGES + 1];
+    bool timing;
+};
+
+// Kernel launch wrappers (ltp_kernels.cu).  Each returns the CUDA status of
+// its launches.
+cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr);
+cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s);
+cudaError_t launch_fill_seeded(cudaStream_t st, const TableDev &t, u64 seed);
+cudaError_t launch_expand_op_txn(cudaStream_t st, const u32 *txn_first, u64 n_txns, u32 *op_txn);
+
+}  // namespace ltp

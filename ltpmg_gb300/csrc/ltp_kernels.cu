@@ -1,0 +1,874 @@
+// ltp_kernels.cu -- sm_103a kernels of the batched transaction-processing hot
+// path.  One batch runs as
+//
+//   mark      read/write-set bitmaps per cell (touched, touched twice,
+//             written) built with warp-aggregated atomicOr; records every
+//             bitmap word the batch touches
+//   ids       contended cell = touched twice and written; scan over the
+//             touched words gives every contended cell a dense id and
+//             snapshots its value before the batch
+//   classify  uncontended ops execute in place (one toucher, or no writer);
+//             contended ops are compacted in op order as (id, op) records
+//   sort      stable LSD radix sort of the contended records by id
+//   apply     segmented scan of the RMW immediates per id: every op gets
+//             base + (sum of earlier RMWs on its cell in TID order); the last
+//             op of each cell writes the final value back
+//   finish    clears exactly the bitmap words and look-back slots the batch
+//             used, so the next batch starts clean
+//
+// This replaces the reference's nine-stage pipeline (register, prefix,
+// bitmap compaction, per-row scatter, per-row merge sort, per-row serial
+// commit: cuda/src/gpulauncher.cu:755-1116) while keeping its rule that all
+// operations on a row (here: a cell) take effect in ascending TID order.
+// The priority rule (R1) replaces sort+apply by min-writer-TID / abort /
+// execute kernels.
+//
+// Every spin-wait (decoupled look-back, the debug stall) is bounded by the
+// global timer; on expiry the kernel records LTP_E_TIMEOUT and returns.
+#include <stdint.h>
+
+#include "ltp_internal.cuh"
+
+namespace ltp {
+
+#define FULL_MASK 0xFFFFFFFFu
+
+constexpr u64 kSpinLimitNs = 2000000000ull;  // 2 s per wait
+
+__device__ __forceinline__ u64 gtimer() {
+    u64 t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ u64 ld_acquire(const u64 *p) {
+    u64 v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(u64 *p, u64 v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ u32 ld_acquire32(const u32 *p) {
+    u32 v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release32(u32 *p, u32 v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ u32 lanemask_lt() {
+    u32 m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+__device__ __forceinline__ void set_err(Counters *c, int e) { atomicCAS(&c->err, 0, e); }
+__device__ __forceinline__ u64 mix64(u64 z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Claims the next tile for the whole block (tiles are handed out in order,
+// which is what makes decoupled look-back safe without co-residency).
+__device__ __forceinline__ u32 claim_tile(Counters *ctr, int slot) {
+    __shared__ u32 s_tile;
+    if (threadIdx.x == 0) s_tile = atomicAdd(&ctr->tile_ctr[slot], 1u);
+    __syncthreads();
+    u32 t = s_tile;
+    __syncthreads();
+    return t;
+}
+
+// ---- decoupled look-back, scalar sums (flag in bits 62-63) ---------------
+constexpr u64 kAgg = 1ull << 62, kInc = 2ull << 62, kValMask = (1ull << 62) - 1;
+
+__device__ u64 lookback_sum(u64 *status, u32 tile, u64 agg, Counters *ctr) {
+    if (tile == 0) {
+        st_release(&status[0], kInc | agg);
+        return 0;
+    }
+    st_release(&status[tile], kAgg | agg);
+    u64 excl = 0;
+    long long t = (long long)tile - 1;
+    u64 t0 = gtimer();
+    while (t >= 0) {
+        u64 s = ld_acquire(&status[t]);
+        u64 f = s >> 62;
+        if (f == 0) {
+            if (gtimer() - t0 > kSpinLimitNs) {
+                set_err(ctr, LTP_E_TIMEOUT);
+                return 0;
+            }
+            continue;
+        }
+        excl += s & kValMask;
+        if (f == 2) break;
+        t--;
+    }
+    st_release(&status[tile], kInc | (excl + agg));
+    return excl;
+}
+
+// ---- table addressing ------------------------------------------------------
+struct OpRef {
+    u64 cell;
+    int32_t *ptr;
+    bool valid;
+};
+
+__device__ __forceinline__ OpRef decode_op(const TablesDev &T, u64 key, u32 w) {
+    OpRef r;
+    u32 tb = opw_table(w), col = opw_col(w), kind = opw_kind(w);
+    r.valid = tb < T.n && kind <= 1u;
+    const TableDev &t = T.t[r.valid ? tb : 0];
+    r.valid = r.valid && key < t.n_rows && col < t.n_cols;
+    r.cell = r.valid ? t.cell_base + key * t.n_cols + col : ~0ull;
+    r.ptr = r.valid ? t.data + (u64)col * t.rows_cap + key : nullptr;
+    return r;
+}
+
+__device__ __forceinline__ int32_t *cell_ptr(const TablesDev &T, u64 cell) {
+    u32 k = 0;
+    for (u32 i = 1; i < T.n; i++)
+        if (cell >= T.t[i].cell_base) k = i;
+    const TableDev &t = T.t[k];
+    u64 local = cell - t.cell_base;
+    u64 row = local / t.n_cols;
+    u32 col = (u32)(local - row * t.n_cols);
+    return t.data + (u64)col * t.rows_cap + row;
+}
+
+__device__ __forceinline__ u32 op_tid(const BatchDev &b, u64 i) {
+    return b.ops_per_txn ? (u32)(i / b.ops_per_txn) : b.op_txn[i];
+}
+
+// ============================================================================
+// mark: read/write-set bitmaps
+// ============================================================================
+template <int BLOCK, int IPT>
+__global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    if (ctr->err) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const u64 n = b.n_ops;
+    constexpr u64 TILE = (u64)BLOCK * IPT;
+    for (u64 base = (u64)blockIdx.x * TILE; base < n; base += (u64)gridDim.x * TILE) {
+        const u64 wbase = base + (u64)warp * 32 * IPT;
+        u64 key[IPT];
+        u32 w[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            u64 i = wbase + (u64)k * 32 + lane;
+            key[k] = i < n ? b.keys[i] : 0;
+            w[k] = i < n ? b.opw[i] : 0xFFFFFFFFu;
+        }
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            u64 i = wbase + (u64)k * 32 + lane;
+            OpRef r = decode_op(T, key[k], w[k]);
+            bool in = i < n;
+            if (in && !r.valid) {  // record the lowest malformed op (stored inverted)
+                atomicMax(&ctr->bad_op, ~i);
+                set_err(ctr, LTP_E_BADARG);
+            }
+            const bool valid = in && r.valid;
+            const u64 word = valid ? (r.cell >> 5) : ~0ull;
+            const u32 bit = 1u << (r.cell & 31);
+            const u32 peers = __match_any_sync(FULL_MASK, word);
+            const u32 same = __match_any_sync(FULL_MASK, valid ? r.cell : ~0ull);
+            const u32 obits = __reduce_or_sync(peers, valid ? bit : 0u);
+            const u32 dup = __reduce_or_sync(peers, (valid && __popc(same) > 1) ? bit : 0u);
+            const u32 wb = __reduce_or_sync(peers, (valid && opw_kind(w[k]) != LTP_OP_READ) ? bit : 0u);
+            const int leader = __ffs(peers) - 1;
+            bool first = false;
+            if (valid && lane == leader) {
+                u32 old = atomicOr(&s.touch[word], obits);
+                first = (old == 0u);
+                u32 m = (old & obits) | dup;
+                if (m) atomicOr(&s.multi[word], m);
+                if (wb) atomicOr(&s.wbits[word], wb);
+            }
+            const u32 fb = __ballot_sync(FULL_MASK, first);
+            if (fb) {
+                u64 pos0 = 0;
+                if (lane == 0) pos0 = atomicAdd(&ctr->n_tw, (u64)__popc(fb));
+                pos0 = __shfl_sync(FULL_MASK, pos0, 0);
+                if (first) s.tw_list[pos0 + __popc(fb & lanemask_lt())] = (u32)word;
+            }
+        }
+    }
+}
+
+// ============================================================================
+// ids: dense ids of contended cells (touched twice and written)
+// ============================================================================
+template <bool PRIORITY>
+__global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Counters *ctr) {
+    if (ctr->err) return;
+    const u64 n = ctr->n_tw;
+    const u32 tiles = (u32)((n + kIdsTile - 1) / kIdsTile);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ u32 s_warp[kIdsBlock / 32];
+    __shared__ u64 s_prefix;
+    for (;;) {
+        const u32 tile = claim_tile(ctr, SLOT_IDS);
+        if (tile >= tiles) break;
+        u32 wd[kIdsIpt], cw[kIdsIpt];
+        u32 cnt = 0;
+        // blocked arrangement: thread owns kIdsIpt consecutive entries
+        const u64 t0 = (u64)tile * kIdsTile + (u64)threadIdx.x * kIdsIpt;
+#pragma unroll
+        for (int k = 0; k < kIdsIpt; k++) {
+            u64 j = t0 + k;
+            wd[k] = j < n ? s.tw_list[j] : 0u;
+            cw[k] = j < n ? (s.multi[wd[k]] & s.wbits[wd[k]]) : 0u;
+            cnt += __popc(cw[k]);
+        }
+        // block exclusive scan of cnt
+        u32 incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            u32 v = __shfl_up_sync(FULL_MASK, incl, d);
+            if (lane >= d) incl += v;
+        }
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            u32 run = 0;
+            for (int i = 0; i < kIdsBlock / 32; i++) {
+                u32 c = s_warp[i];
+                s_warp[i] = run;
+                run += c;
+            }
+            u64 excl = lookback_sum(s.st_ids, tile, run, ctr);
+            s_prefix = excl;
+            if (tile == tiles - 1) ctr->M = (u32)(excl + run);
+        }
+        __syncthreads();
+        u64 pre = s_prefix + s_warp[warp] + (incl - cnt);
+#pragma unroll
+        for (int k = 0; k < kIdsIpt; k++) {
+            u64 j = t0 + k;
+            if (j < n) {
+                s.cwx[wd[k]] = (pre << 32) | cw[k];
+                u32 bits = cw[k];
+                while (bits) {
+                    int bpos = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    u64 cell = ((u64)wd[k] << 5) | (u64)bpos;
+                    s.dcell[pre] = cell;
+                    s.dbase[pre] = *cell_ptr(T, cell);
+                    if (PRIORITY) s.dminw[pre] = 0xFFFFFFFFu;
+                    pre++;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ============================================================================
+// classify (ordered rule): execute uncontended ops, compact contended ones
+// ============================================================================
+template <int BLOCK, int IPT>
+__global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    if (ctr->err) return;
+    constexpr int NW = BLOCK / 32;
+    constexpr u64 TILE = (u64)BLOCK * IPT;
+    const u64 n = b.n_ops;
+    const u32 tiles = (u32)((n + TILE - 1) / TILE);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ u32 s_wcnt[NW];
+    __shared__ u64 s_prefix;
+    for (;;) {
+        const u32 tile = claim_tile(ctr, SLOT_CLASSIFY);
+        if (tile >= tiles) break;
+        const u64 wbase = (u64)tile * TILE + (u64)warp * 32 * IPT;
+        u64 key[IPT];
+        u32 w[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            u64 i = wbase + (u64)k * 32 + lane;
+            key[k] = i < n ? __ldcs(&b.keys[i]) : 0;
+            w[k] = i < n ? __ldcs(&b.opw[i]) : 0xFFFFFFFFu;
+        }
+        u64 cw[IPT];
+        OpRef r[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            u64 i = wbase + (u64)k * 32 + lane;
+            r[k] = decode_op(T, key[k], w[k]);
+            r[k].valid = r[k].valid && i < n;
+            cw[k] = r[k].valid ? s.cwx[r[k].cell >> 5] : 0ull;
+        }
+        u64 rec[IPT];
+        u32 wcnt = 0, lpos[IPT];
+        bool con[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            const u32 bit = 1u << (r[k].cell & 31);
+            con[k] = r[k].valid && ((u32)cw[k] & bit);
+            const u64 i = wbase + (u64)k * 32 + lane;
+            if (r[k].valid && !con[k]) {
+                int32_t v = *r[k].ptr;
+                if (opw_kind(w[k]) == LTP_OP_ADD) {
+                    v = (int32_t)((u32)v + (u32)opw_imm(w[k]));
+                    *r[k].ptr = v;
+                }
+                __stcs(&b.out[i], v);
+            }
+            const u32 m = (u32)(cw[k] >> 32) + __popc((u32)cw[k] & (bit - 1u));
+            rec[k] = ((u64)m << 32) | ((u64)(opw_kind(w[k]) == LTP_OP_ADD) << 31) | (u64)(u32)i;
+            const u32 bal = __ballot_sync(FULL_MASK, con[k]);
+            lpos[k] = wcnt + __popc(bal & lanemask_lt());
+            wcnt += __popc(bal);
+        }
+        if (lane == 0) s_wcnt[warp] = wcnt;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            u32 run = 0;
+            for (int i = 0; i < NW; i++) {
+                u32 c = s_wcnt[i];
+                s_wcnt[i] = run;
+                run += c;
+            }
+            u64 excl = lookback_sum(s.st_cls, tile, run, ctr);
+            s_prefix = excl;
+            if (tile == tiles - 1) ctr->n_c = excl + run;
+        }
+        __syncthreads();
+        const u64 pbase = s_prefix + s_wcnt[warp];
+#pragma unroll
+        for (int k = 0; k < IPT; k++)
+            if (con[k]) s.list[0][pbase + lpos[k]] = rec[k];
+        __syncthreads();
+    }
+}
+
+// ============================================================================
+// sort: stable LSD radix sort of the contended records by id (8-bit digits)
+// ============================================================================
+__host__ __device__ __forceinline__ int sort_passes(u32 M) {
+    if (M <= 1) return 0;
+    int bits = 32 - __builtin_clz(M - 1);
+    return (bits + 7) / 8;
+}
+__device__ __forceinline__ int sort_passes_dev(u32 M) {
+    if (M <= 1) return 0;
+    int bits = 32 - __clz(M - 1);
+    return (bits + 7) / 8;
+}
+
+__global__ void __launch_bounds__(256) k_sort_hist(Scratch s, Counters *ctr) {
+    if (ctr->err) return;
+    const int passes = sort_passes_dev(ctr->M);
+    if (passes == 0) return;
+    const u64 n = ctr->n_c;
+    __shared__ u32 sh[4][256];
+    for (int p = 0; p < 4; p++) sh[p][threadIdx.x] = 0;
+    __syncthreads();
+    for (u64 i = (u64)blockIdx.x * 256 + threadIdx.x; i - threadIdx.x < n; i += (u64)gridDim.x * 256) {
+        const bool v = i < n;
+        const u32 id = v ? (u32)(s.list[0][i] >> 32) : 0u;
+        for (int p = 0; p < passes; p++) {
+            u32 d = v ? (id >> (8 * p)) & 255u : 256u;
+            u32 peers = __match_any_sync(FULL_MASK, d);
+            if (v && (threadIdx.x & 31) == (u32)(__ffs(peers) - 1)) atomicAdd(&sh[p][d], (u32)__popc(peers));
+        }
+    }
+    __syncthreads();
+    for (int p = 0; p < passes; p++)
+        if (sh[p][threadIdx.x]) atomicAdd(&ctr->hist[p][threadIdx.x], sh[p][threadIdx.x]);
+}
+
+template <int P>
+__global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *ctr) {
+    if (ctr->err) return;
+    const int passes = sort_passes_dev(ctr->M);
+    if (P >= passes) return;
+    const u64 n = ctr->n_c;
+    const u32 tiles = (u32)((n + kSortTile - 1) / kSortTile);
+    const u64 *src = s.list[P & 1];
+    u64 *dst = s.list[(P + 1) & 1];
+    u32 *status = s.st_sort[P & 1];
+    if (P >= 1) {  // the previous pass is complete: recycle its look-back slots
+        u32 *other = s.st_sort[(P + 1) & 1];
+        for (u64 j = (u64)blockIdx.x * kSortBlock + threadIdx.x; j < (u64)tiles * 256; j += (u64)gridDim.x * kSortBlock)
+            other[j] = 0;
+    }
+    constexpr int NW = kSortBlock / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const u32 tid = threadIdx.x;
+    __shared__ u32 s_start[256];
+    __shared__ u32 s_whist[NW][256];
+    __shared__ u32 s_base[256];
+    __shared__ u32 s_wsum[NW];
+    {  // global start of every digit: exclusive scan of the histogram
+        u32 h = ctr->hist[P][tid];
+        u32 incl = h;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            u32 v = __shfl_up_sync(FULL_MASK, incl, d);
+            if (lane >= d) incl += v;
+        }
+        if (lane == 31) s_wsum[warp] = incl;
+        __syncthreads();
+        u32 off = 0;
+        for (int i = 0; i < warp; i++) off += s_wsum[i];
+        s_start[tid] = off + incl - h;
+        __syncthreads();
+    }
+    const int shift = 32 + 8 * P;
+    for (;;) {
+        const u32 tile = claim_tile(ctr, SLOT_SORT0 + P);
+        if (tile >= tiles) break;
+#pragma unroll
+        for (int w = 0; w < NW; w++) s_whist[w][tid] = 0;
+        __syncthreads();
+        const u64 wbase = (u64)tile * kSortTile + (u64)warp * 32 * kSortIpt;
+        u64 e[kSortIpt];
+        u32 rank[kSortIpt];
+#pragma unroll
+        for (int k = 0; k < kSortIpt; k++) {
+            u64 i = wbase + (u64)k * 32 + lane;
+            e[k] = i < n ? src[i] : ~0ull;
+        }
+#pragma unroll
+        for (int k = 0; k < kSortIpt; k++) {
+            u64 i = wbase + (u64)k * 32 + lane;
+            const bool v = i < n;
+            const u32 d = v ? (u32)(e[k] >> shift) & 255u : 256u;
+            const u32 peers = __match_any_sync(FULL_MASK, d);
+            const u32 before = v ? s_whist[warp][d] : 0u;
+            __syncwarp();
+            if (v && lane == __ffs(peers) - 1) s_whist[warp][d] = before + __popc(peers);
+            __syncwarp();
+            rank[k] = before + __popc(peers & lanemask_lt());
+        }
+        __syncthreads();
+        u32 run = 0;
+#pragma unroll
+        for (int w = 0; w < NW; w++) {
+            u32 c = s_whist[w][tid];
+            s_whist[w][tid] = run;
+            run += c;
+        }
+        // per-digit decoupled look-back (thread tid owns digit tid)
+        u32 excl = 0;
+        u32 *slot = &status[(u64)tile * 256 + tid];
+        if (tile == 0) {
+            st_release32(slot, (2u << 30) | run);
+        } else {
+            st_release32(slot, (1u << 30) | run);
+            long long t = (long long)tile - 1;
+            u64 t0 = gtimer();
+            while (t >= 0) {
+                u32 st = ld_acquire32(&status[(u64)t * 256 + tid]);
+                u32 f = st >> 30;
+                if (f == 0) {
+                    if (gtimer() - t0 > kSpinLimitNs) {
+                        set_err(ctr, LTP_E_TIMEOUT);
+                        break;
+                    }
+                    continue;
+                }
+                excl += st & 0x3FFFFFFFu;
+                if (f == 2) break;
+                t--;
+            }
+            st_release32(slot, (2u << 30) | (excl + run));
+        }
+        s_base[tid] = s_start[tid] + excl;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kSortIpt; k++) {
+            u64 i = wbase + (u64)k * 32 + lane;
+            if (i < n) {
+                u32 d = (u32)(e[k] >> shift) & 255u;
+                dst[s_base[d] + s_whist[warp][d] + rank[k]] = e[k];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ============================================================================
+// apply: segmented scan of RMW immediates per contended cell, write-back
+// ============================================================================
+// look-back status: bits 62-63 flag, bit 61 "tile holds a segment head",
+// bits 0-31 sum since the last head (wrapping int32 arithmetic)
+__global__ void __launch_bounds__(kApplyBlock) k_apply(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    if (ctr->err) return;
+    const u64 n = ctr->n_c;
+    const u32 tiles = (u32)((n + kApplyTile - 1) / kApplyTile);
+    const u64 *list = s.list[sort_passes_dev(ctr->M) & 1];
+    constexpr int NW = kApplyBlock / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ u32 s_wf[NW], s_ws[NW];
+    __shared__ u32 s_tf, s_ts;
+    for (;;) {
+        const u32 tile = claim_tile(ctr, SLOT_APPLY);
+        if (tile >= tiles) break;
+        const u64 wbase = (u64)tile * kApplyTile + (u64)warp * 32 * kApplyIpt;
+        u64 e[kApplyIpt];
+        u32 sv[kApplyIpt];
+        bool sf[kApplyIpt];
+        bool tail[kApplyIpt];
+#pragma unroll
+        for (int k = 0; k < kApplyIpt; k++) {
+            u64 i = wbase + (u64)k * 32 + lane;
+            e[k] = i < n ? list[i] : ~0ull;
+        }
+        u32 cf = 0, cs = 0;  // running carry within the warp
+#pragma unroll
+        for (int k = 0; k < kApplyIpt; k++) {
+            const u64 i = wbase + (u64)k * 32 + lane;
+            const bool v = i < n;
+            const u32 m = (u32)(e[k] >> 32);
+            const u64 prev = (v && i > 0) ? list[i - 1] : ~0ull;
+            const u64 next = (v && i + 1 < n) ? list[i + 1] : ~0ull;
+            const bool head = v && (i == 0 || (u32)(prev >> 32) != m);
+            tail[k] = v && (i + 1 == n || (u32)(next >> 32) != m);
+            u32 val = 0;
+            if (v && ((e[k] >> 31) & 1ull)) val = (u32)opw_imm(b.opw[(u32)e[k] & 0x7FFFFFFFu]);
+            u32 f = head ? 1u : 0u, sum = val;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                u32 us = __shfl_up_sync(FULL_MASK, sum, d);
+                u32 uf = __shfl_up_sync(FULL_MASK, f, d);
+                if (lane >= d) {
+                    if (!f) sum += us;
+                    f |= uf;
+                }
+            }
+            if (!f) sum += cs;
+            f |= cf;
+            sv[k] = sum;
+            sf[k] = f != 0;
+            cs = __shfl_sync(FULL_MASK, sum, 31);
+            cf = __shfl_sync(FULL_MASK, f, 31);
+        }
+        if (lane == 0) {
+            s_wf[warp] = cf;
+            s_ws[warp] = cs;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            // exclusive prefix over warps, then tile look-back
+            u32 af = 0, as = 0;
+            for (int w = 0; w < NW; w++) {
+                u32 f = s_wf[w], sm = s_ws[w];
+                s_wf[w] = af;
+                s_ws[w] = as;
+                if (f) {
+                    af = 1;
+                    as = sm;
+                } else {
+                    as += sm;
+                }
+            }
+            u64 agg = ((u64)af << 61) | as;
+            u64 *st = s.st_apply;
+            u32 ef = 0, es = 0;
+            if (tile == 0) {
+                st_release(&st[0], kInc | agg);
+            } else {
+                st_release(&st[tile], kAgg | agg);
+                long long t = (long long)tile - 1;
+                u64 t0 = gtimer();
+                while (t >= 0) {
+                    u64 x = ld_acquire(&st[t]);
+                    u64 fl = x >> 62;
+                    if (fl == 0) {
+                        if (gtimer() - t0 > kSpinLimitNs) {
+                            set_err(ctr, LTP_E_TIMEOUT);
+                            break;
+                        }
+                        continue;
+                    }
+                    if (!ef) {
+                        es += (u32)x;
+                        ef = (u32)((x >> 61) & 1ull);
+                    }
+                    if (fl == 2 || ef) break;
+                    t--;
+                }
+                u32 incf = af ? 1u : ef;
+                u32 incs = af ? as : es + as;
+                st_release(&st[tile], kInc | ((u64)incf << 61) | incs);
+            }
+            s_tf = ef;
+            s_ts = es;
+        }
+        __syncthreads();
+        // carry into this warp = combine(tile exclusive, warp exclusive)
+        const u32 wf = s_wf[warp], ws = s_ws[warp];
+        const u32 carry = wf ? ws : s_ts + ws;
+#pragma unroll
+        for (int k = 0; k < kApplyIpt; k++) {
+            const u64 i = wbase + (u64)k * 32 + lane;
+            if (i < n) {
+                const u32 m = (u32)(e[k] >> 32);
+                const u32 tot = sf[k] ? sv[k] : sv[k] + carry;
+                const int32_t val = (int32_t)((u32)s.dbase[m] + tot);
+                b.out[(u32)e[k] & 0x7FFFFFFFu] = val;
+                if (tail[k]) *cell_ptr(T, s.dcell[m]) = val;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ============================================================================
+// priority rule (R1): min writer TID per contended cell, aborts, execute
+// ============================================================================
+__device__ __forceinline__ bool contended_id(const Scratch &s, u64 cell, u32 *m) {
+    const u64 cw = s.cwx[cell >> 5];
+    const u32 bit = 1u << (cell & 31);
+    *m = (u32)(cw >> 32) + __popc((u32)cw & (bit - 1u));
+    return ((u32)cw & bit) != 0;
+}
+
+__global__ void __launch_bounds__(256) k_r1_minw(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    if (ctr->err) return;
+    const u64 n = b.n_ops;
+    for (u64 i = (u64)blockIdx.x * 256 + threadIdx.x; i - threadIdx.x < n; i += (u64)gridDim.x * 256) {
+        bool act = false;
+        u32 m = 0, tid = 0;
+        if (i < n) {
+            const u32 w = b.opw[i];
+            OpRef r = decode_op(T, b.keys[i], w);
+            if (r.valid && opw_kind(w) == LTP_OP_ADD && contended_id(s, r.cell, &m)) {
+                act = true;
+                tid = op_tid(b, i);
+            }
+        }
+        const u32 peers = __match_any_sync(FULL_MASK, act ? m : 0xFFFFFFFFu);
+        const u32 mn = __reduce_min_sync(peers, act ? tid : 0xFFFFFFFFu);
+        if (act && (threadIdx.x & 31) == (u32)(__ffs(peers) - 1)) atomicMin(&s.dminw[m], mn);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_r1_abort(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    if (ctr->err) return;
+    const u64 n = b.n_ops;
+    for (u64 i = (u64)blockIdx.x * 256 + threadIdx.x; i < n; i += (u64)gridDim.x * 256) {
+        const u32 w = b.opw[i];
+        OpRef r = decode_op(T, b.keys[i], w);
+        u32 m;
+        if (r.valid && contended_id(s, r.cell, &m)) {
+            const u32 tid = op_tid(b, i);
+            if (s.dminw[m] < tid) b.commit[tid] = 0;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_r1_exec(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    if (ctr->err) return;
+    const u64 n = b.n_ops;
+    for (u64 i = (u64)blockIdx.x * 256 + threadIdx.x; i < n; i += (u64)gridDim.x * 256) {
+        const u32 w = b.opw[i];
+        OpRef r = decode_op(T, b.keys[i], w);
+        if (!r.valid) continue;
+        const u32 tid = op_tid(b, i);
+        if (!b.commit[tid]) {
+            b.out[i] = 0;
+            continue;
+        }
+        u32 m;
+        const bool add = opw_kind(w) == LTP_OP_ADD;
+        if (contended_id(s, r.cell, &m)) {
+            // a committed op on a contended cell sees the pre-batch value; a
+            // committed RMW here is the cell's only committed writer
+            int32_t v = s.dbase[m];
+            if (add) {
+                v = (int32_t)((u32)v + (u32)opw_imm(w));
+                *r.ptr = v;
+            }
+            b.out[i] = v;
+        } else {
+            int32_t v = *r.ptr;
+            if (add) {
+                v = (int32_t)((u32)v + (u32)opw_imm(w));
+                *r.ptr = v;
+            }
+            b.out[i] = v;
+        }
+    }
+}
+
+// ============================================================================
+// finish: return the scratch to its clean state, count commits
+// ============================================================================
+__global__ void __launch_bounds__(256) k_finish(BatchDev b, Scratch s, Counters *ctr, int rule, u32 cls_tile) {
+    const u64 gsz = (u64)gridDim.x * 256, g0 = (u64)blockIdx.x * 256 + threadIdx.x;
+    const u64 ntw = ctr->n_tw;
+    for (u64 j = g0; j < ntw; j += gsz) {
+        const u32 w = s.tw_list[j];
+        s.touch[w] = 0;
+        s.multi[w] = 0;
+        s.wbits[w] = 0;
+    }
+    const u64 t_ids = (ntw + kIdsTile - 1) / kIdsTile;
+    for (u64 j = g0; j < t_ids; j += gsz) s.st_ids[j] = 0;
+    const u64 t_cls = (b.n_ops + cls_tile - 1) / cls_tile;
+    for (u64 j = g0; j < t_cls; j += gsz) s.st_cls[j] = 0;
+    const u64 nc = ctr->n_c;
+    const u64 t_apply = (nc + kApplyTile - 1) / kApplyTile;
+    for (u64 j = g0; j < t_apply; j += gsz) s.st_apply[j] = 0;
+    const int passes = sort_passes_dev(ctr->M);
+    if (passes > 0) {
+        u32 *st = s.st_sort[(passes - 1) & 1];
+        const u64 t_sort = (nc + kSortTile - 1) / kSortTile;
+        for (u64 j = g0; j < t_sort * 256; j += gsz) st[j] = 0;
+    }
+    if (rule == LTP_RULE_PRIORITY) {
+        u32 c = 0;
+        for (u64 t = g0; t < b.n_txns; t += gsz) c += b.commit[t];
+        c = __reduce_add_sync(FULL_MASK, c);
+        if ((threadIdx.x & 31) == 0 && c) atomicAdd(&ctr->committed, (u64)c);
+    }
+}
+
+__global__ void k_stall(Counters *ctr, u32 ms) {
+    const u64 t0 = gtimer();
+    const u64 lim = (u64)ms * 1000000ull;
+    volatile u32 *flag = &ctr->stall;
+    while (*flag == 0u) {
+        if (gtimer() - t0 > lim) {
+            set_err(ctr, LTP_E_TIMEOUT);
+            return;
+        }
+        __nanosleep(1000);
+    }
+}
+
+__global__ void k_fill_seeded(TableDev t, u64 seed) {
+    const u64 base = mix64(seed ^ 0x5441424C45ull);
+    const u64 total = t.n_rows * t.n_cols;
+    for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < total; j += (u64)gridDim.x * blockDim.x) {
+        const u64 col = j / t.n_rows, row = j - col * t.n_rows;
+        t.data[col * t.rows_cap + row] = (int32_t)(u32)mix64(base + row * t.n_cols + col);
+    }
+}
+
+__global__ void k_expand_op_txn(const u32 *txn_first, u64 n_txns, u32 *op_txn) {
+    for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < n_txns; t += (u64)gridDim.x * blockDim.x)
+        for (u32 i = txn_first[t]; i < txn_first[t + 1]; i++) op_txn[i] = (u32)t;
+}
+
+// ============================================================================
+// host-side launch plans
+// ============================================================================
+template <typename K>
+static int occ_grid(K kernel, int block, int num_sms) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    if (per_sm < 1) per_sm = 1;
+    return per_sm * num_sms;
+}
+
+template <int BLOCK, int IPT>
+static cudaError_t launch_front(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s,
+                                Counters *ctr, bool classify) {
+    const u64 tile = (u64)BLOCK * IPT;
+    const u64 tiles = (b.n_ops + tile - 1) / tile;
+    static int g_mark = 0, g_cls = 0;
+    static int dev_sms = 0;
+    if (dev_sms != L.num_sms) {
+        g_mark = occ_grid(k_mark<BLOCK, IPT>, BLOCK, L.num_sms);
+        g_cls = occ_grid(k_classify<BLOCK, IPT>, BLOCK, L.num_sms);
+        dev_sms = L.num_sms;
+    }
+    int gm = (int)(tiles < (u64)g_mark ? tiles : (u64)g_mark);
+    if (gm < 1) gm = 1;
+    k_mark<BLOCK, IPT><<<gm, BLOCK, 0, L.stream>>>(b, T, s, ctr);
+    if (L.timing) cudaEventRecord(L.ev[1], L.stream);
+    {
+        int gi = occ_grid(k_ids<false>, kIdsBlock, L.num_sms);
+        u64 ub = (b.n_ops + kIdsTile - 1) / kIdsTile;
+        if ((u64)gi > ub) gi = (int)(ub ? ub : 1);
+        if (L.rule == LTP_RULE_PRIORITY) k_ids<true><<<gi, kIdsBlock, 0, L.stream>>>(T, s, ctr);
+        else k_ids<false><<<gi, kIdsBlock, 0, L.stream>>>(T, s, ctr);
+    }
+    if (L.timing) cudaEventRecord(L.ev[2], L.stream);
+    if (classify) {
+        int gc = (int)(tiles < (u64)g_cls ? tiles : (u64)g_cls);
+        if (gc < 1) gc = 1;
+        k_classify<BLOCK, IPT><<<gc, BLOCK, 0, L.stream>>>(b, T, s, ctr);
+    }
+    return cudaGetLastError();
+}
+
+typedef cudaError_t (*front_fn)(const Launch &, const BatchDev &, const TablesDev &, const Scratch &, Counters *, bool);
+
+static front_fn pick_front(const Tuning &t) {
+#define LTP_FRONT(B, I) \
+    if (t.block == B && t.ipt == I) return launch_front<B, I>;
+    LTP_FRONT(128, 1) LTP_FRONT(128, 2) LTP_FRONT(128, 4) LTP_FRONT(128, 8)
+    LTP_FRONT(256, 1) LTP_FRONT(256, 2) LTP_FRONT(256, 4) LTP_FRONT(256, 8)
+    LTP_FRONT(512, 1) LTP_FRONT(512, 2) LTP_FRONT(512, 4) LTP_FRONT(512, 8)
+#undef LTP_FRONT
+    return launch_front<256, 4>;
+}
+
+cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+    if (L.timing) cudaEventRecord(L.ev[0], L.stream);
+    if (L.stall) k_stall<<<1, 1, 0, L.stream>>>(ctr, L.stall_ms);
+    const bool ordered = L.rule != LTP_RULE_PRIORITY;
+    cudaError_t e = pick_front(L.tune)(L, b, T, s, ctr, ordered);
+    if (e != cudaSuccess) return e;
+    if (L.timing) cudaEventRecord(L.ev[3], L.stream);
+    const int gs = occ_grid(k_sort_pass<0>, kSortBlock, L.num_sms);
+    const u64 ub_sort = (b.n_ops + kSortTile - 1) / kSortTile;
+    const int gsort = (int)((u64)gs < ub_sort ? (u64)gs : (ub_sort ? ub_sort : 1));
+    const int gstream = L.num_sms * 8;
+    if (ordered) {
+        k_sort_hist<<<gstream, 256, 0, L.stream>>>(s, ctr);
+        k_sort_pass<0><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        k_sort_pass<1><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        k_sort_pass<2><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        k_sort_pass<3><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        if (L.timing) cudaEventRecord(L.ev[4], L.stream);
+        const int ga = occ_grid(k_apply, kApplyBlock, L.num_sms);
+        const u64 ub_apply = (b.n_ops + kApplyTile - 1) / kApplyTile;
+        const int gapp = (int)((u64)ga < ub_apply ? (u64)ga : (ub_apply ? ub_apply : 1));
+        k_apply<<<gapp, kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
+        if (L.timing) cudaEventRecord(L.ev[5], L.stream);
+    } else {
+        if (L.timing) cudaEventRecord(L.ev[4], L.stream);
+        k_r1_minw<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        k_r1_abort<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        k_r1_exec<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        if (L.timing) cudaEventRecord(L.ev[5], L.stream);
+    }
+    k_finish<<<gstream, 256, 0, L.stream>>>(b, s, ctr, L.rule, L.tune.block * L.tune.ipt);
+    if (L.timing) cudaEventRecord(L.ev[6], L.stream);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s) {
+    cudaMemsetAsync(s.touch, 0, s.n_words * 4, st);
+    cudaMemsetAsync(s.multi, 0, s.n_words * 4, st);
+    cudaMemsetAsync(s.wbits, 0, s.n_words * 4, st);
+    cudaMemsetAsync(s.st_sort[0], 0, s.cap_sort_tiles * 256 * 4, st);
+    cudaMemsetAsync(s.st_sort[1], 0, s.cap_sort_tiles * 256 * 4, st);
+    cudaMemsetAsync(s.st_ids, 0, s.cap_tiles * 8, st);
+    cudaMemsetAsync(s.st_cls, 0, s.cap_tiles * 8, st);
+    cudaMemsetAsync(s.st_apply, 0, s.cap_tiles * 8, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_seeded(cudaStream_t st, const TableDev &t, u64 seed) {
+    k_fill_seeded<<<1024, 256, 0, st>>>(t, seed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_expand_op_txn(cudaStream_t st, const u32 *txn_first, u64 n_txns, u32 *op_txn) {
+    if (n_txns == 0) return cudaSuccess;
+    u64 blocks = (n_txns + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    k_expand_op_txn<<<(unsigned)blocks, 256, 0, st>>>(txn_first, n_txns, op_txn);
+    return cudaGetLastError();
+}
+
+}  // namespace ltp

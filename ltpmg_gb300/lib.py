@@ -1,0 +1,312 @@
+"""ctypes binding of libltpmg_gb300.so (the C ABI in include/ltpmg_gb300.h).
+
+There is no fallback: if the shared library is missing or fails to load,
+every entry point raises.  Build it with ``python -c "import
+__graft_entry__ as g; g.build()"`` (or ``python ltpmg_gb300/_build.py``).
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libltpmg_gb300.so")
+HEADER = os.path.join(os.path.dirname(PKG), "include", "ltpmg_gb300.h")
+
+LTP_OK = 0
+LTP_E_CUDA, LTP_E_CAPACITY, LTP_E_TIMEOUT, LTP_E_BADARG = -1, -2, -3, -4
+LTP_E_DEVICE_ASSERT, LTP_E_NOMEM, LTP_E_STATE = -5, -6, -7
+RULE_ORDERED, RULE_PRIORITY = 0, 1
+OP_READ, OP_ADD = 0, 1
+FLAG_STAGE_TIMING = 1
+STAGE_NAMES = ["mark", "ids", "classify", "sort", "apply", "finish", "unused", "total"]
+
+
+class LtpError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"ltpmg_gb300 error {status}: {msg}")
+        self.status = status
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("rule", ctypes.c_int32), ("reserve_ops", ctypes.c_uint64),
+                ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class Schema(ctypes.Structure):
+    _fields_ = [("n_cols", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("txns", ctypes.c_uint64), ("ops", ctypes.c_uint64), ("committed", ctypes.c_uint64),
+                ("aborted", ctypes.c_uint64), ("contended_ops", ctypes.c_uint64),
+                ("contended_cells", ctypes.c_uint64), ("touched_words", ctypes.c_uint64),
+                ("bytes_algorithmic", ctypes.c_uint64), ("ms_stage", ctypes.c_float * 8)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "ms_stage"}
+        d["ms_stage"] = dict(zip(STAGE_NAMES, list(self.ms_stage)))
+        return d
+
+
+class YcsbParams(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_uint64), ("n_rows", ctypes.c_uint64), ("n_cols", ctypes.c_uint32),
+                ("ops_min", ctypes.c_uint32), ("ops_max", ctypes.c_uint32), ("rmw_delta", ctypes.c_int32),
+                ("read_frac", ctypes.c_double), ("theta", ctypes.c_double)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("block", ctypes.c_uint32), ("ipt", ctypes.c_uint32), ("word_bits", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+_lib = None
+
+
+def load():
+    """Loads the shared library (raises if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise LtpError(LTP_E_STATE, f"{LIB_PATH} is missing: build the CUDA extension first")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, u64, u32, i32, ci = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int
+    pp = ctypes.POINTER(ctypes.c_void_p)
+    sig = {
+        "ltp_version": (ctypes.c_char_p, []),
+        "ltp_status_string": (ctypes.c_char_p, [ci]),
+        "ltp_last_error": (ctypes.c_char_p, [vp]),
+        "ltp_init": (ci, [ctypes.POINTER(Config), pp]),
+        "ltp_shutdown": (ci, [vp]),
+        "ltp_default_stream": (vp, [vp]),
+        "ltp_sync": (ci, [vp, vp]),
+        "ltp_table_create": (ci, [vp, ctypes.POINTER(Schema), u64, ctypes.POINTER(u32)]),
+        "ltp_table_upload": (ci, [vp, u32, u32, u64, u64, vp]),
+        "ltp_table_download": (ci, [vp, u32, u32, u64, u64, vp]),
+        "ltp_table_fill_seeded": (ci, [vp, u32, u64, vp]),
+        "ltp_table_fingerprint": (ci, [vp, u32, ctypes.POINTER(u64)]),
+        "ltp_batch_create": (ci, [vp, u64, u64, pp]),
+        "ltp_batch_free": (ci, [vp, vp]),
+        "ltp_batch_load": (ci, [vp, vp, u64, vp, u32, u64, vp, vp, vp]),
+        "ltp_batch_execute": (ci, [vp, vp, vp]),
+        "ltp_batch_fetch": (ci, [vp, vp, vp, vp, vp]),
+        "ltp_batch_finish": (ci, [vp, vp, ctypes.POINTER(Stats), vp]),
+        "ltp_batch_results": (ci, [vp, vp, vp, vp, ctypes.POINTER(Stats)]),
+        "ltp_batch_device_ptrs": (ci, [vp, pp, pp, pp, pp, pp]),
+        "ltp_host_alloc": (vp, [ctypes.c_size_t]),
+        "ltp_host_free": (None, [vp]),
+        "ltp_gen_ycsb": (u64, [ctypes.POINTER(YcsbParams), u64, u64, vp, vp, vp, u64, ci]),
+        "ltp_table_value": (i32, [u64, u64, u32, u32]),
+        "ltp_set_tuning": (ci, [vp, u32, ctypes.POINTER(Tuning)]),
+        "ltp_get_tuning": (ci, [vp, u32, ctypes.POINTER(Tuning)]),
+        "ltp_debug_stall_next": (ci, [vp, u32]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def header_functions(path=HEADER):
+    """Names of every function declared in the public header."""
+    txt = open(path).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(ltp_[a-z0-9_]+)\s*\(", txt)) - {"ltp_ctx", "ltp_batch"})
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return ctypes.c_void_p(s)
+    return ctypes.c_void_p(int(getattr(s, "cuda_stream", s)))
+
+
+class PinnedArray:
+    """numpy view over pinned (page-locked) host memory from ltp_host_alloc."""
+
+    def __init__(self, shape, dtype):
+        L = load()
+        dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) if shape else 1
+        nbytes = max(n * dtype.itemsize, 1)
+        self._ptr = L.ltp_host_alloc(nbytes)
+        if not self._ptr:
+            raise LtpError(LTP_E_NOMEM, "pinned host allocation failed")
+        buf = (ctypes.c_uint8 * nbytes).from_address(self._ptr)
+        self.array = np.frombuffer(buf, dtype=dtype, count=n).reshape(shape)
+
+    def __del__(self):
+        if getattr(self, "_ptr", None):
+            load().ltp_host_free(self._ptr)
+            self._ptr = None
+
+
+def gen_ycsb(seed, n_rows, n_cols, ops_min, ops_max, read_frac, theta, batch, n_txns, rmw_delta=1, threads=0,
+             out=None):
+    """Seeded batch from the library's host generator.  Returns
+    (txn_first uint32[n_txns+1], keys uint64[n_ops], opw uint32[n_ops]);
+    `out` may supply preallocated (txn_first, keys, opw) arrays."""
+    L = load()
+    p = YcsbParams(seed, n_rows, n_cols, ops_min, ops_max, rmw_delta, read_frac, theta)
+    cap = n_txns * ops_max
+    if out is None:
+        tf = np.zeros(n_txns + 1, np.uint32)
+        keys = np.zeros(max(cap, 1), np.uint64)
+        opw = np.zeros(max(cap, 1), np.uint32)
+    else:
+        tf, keys, opw = out
+        cap = min(len(keys), len(opw))
+    n = L.ltp_gen_ycsb(ctypes.byref(p), batch, n_txns, _p(tf), _p(keys), _p(opw), cap, threads)
+    if n == 2 ** 64 - 1:
+        raise LtpError(LTP_E_BADARG, "generator rejected the parameters")
+    return tf[: n_txns + 1], keys[:n], opw[:n]
+
+
+def opword(kind, col, table=0, imm=0):
+    return (kind | (col << 2) | (table << 8) | ((imm & 0xFFFFF) << 12)) & 0xFFFFFFFF
+
+
+class Context:
+    """One GPU, its tables and scratch (the C-ABI ltp_ctx)."""
+
+    def __init__(self, device=0, rule=RULE_ORDERED, reserve_ops=0, stage_timing=False):
+        self.L = load()
+        cfg = Config(device, rule, reserve_ops, FLAG_STAGE_TIMING if stage_timing else 0, 0)
+        h = ctypes.c_void_p()
+        rc = self.L.ltp_init(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != LTP_OK:
+            raise LtpError(rc, self.L.ltp_status_string(rc).decode())
+        self.h = h
+        self.rule = rule
+        self.tables = []
+
+    def check(self, rc):
+        if rc != LTP_OK:
+            raise LtpError(rc, self.L.ltp_last_error(self.h).decode() or self.L.ltp_status_string(rc).decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ltp_shutdown(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def stream(self):
+        return self.L.ltp_default_stream(self.h)
+
+    def sync(self, stream=None):
+        self.check(self.L.ltp_sync(self.h, _stream(stream)))
+
+    def create_table(self, rows, cols):
+        tid = ctypes.c_uint32()
+        self.check(self.L.ltp_table_create(self.h, ctypes.byref(Schema(cols, 0)), rows, ctypes.byref(tid)))
+        self.tables.append((rows, cols))
+        return tid.value
+
+    def upload(self, table, colmajor):
+        """colmajor: int32[n_cols, n_rows]."""
+        a = np.ascontiguousarray(colmajor, np.int32)
+        for c in range(a.shape[0]):
+            self.check(self.L.ltp_table_upload(self.h, table, c, 0, a.shape[1], _p(a[c])))
+
+    def download(self, table):
+        rows, cols = self.tables[table]
+        out = np.empty((cols, rows), np.int32)
+        for c in range(cols):
+            self.check(self.L.ltp_table_download(self.h, table, c, 0, rows, _p(out[c])))
+        return out
+
+    def fill_seeded(self, table, seed, stream=None):
+        self.check(self.L.ltp_table_fill_seeded(self.h, table, seed, _stream(stream)))
+
+    def fingerprint(self, table):
+        v = ctypes.c_uint64()
+        self.check(self.L.ltp_table_fingerprint(self.h, table, ctypes.byref(v)))
+        return v.value
+
+    def batch(self, max_txns, max_ops):
+        return Batch(self, max_txns, max_ops)
+
+    def set_tuning(self, bucket, block, ipt, word_bits=32):
+        self.check(self.L.ltp_set_tuning(self.h, bucket, ctypes.byref(Tuning(block, ipt, word_bits, 0))))
+
+    def get_tuning(self, bucket):
+        t = Tuning()
+        self.check(self.L.ltp_get_tuning(self.h, bucket, ctypes.byref(t)))
+        return (t.block, t.ipt, t.word_bits)
+
+    def stall_next(self, ms):
+        self.check(self.L.ltp_debug_stall_next(self.h, ms))
+
+
+class Batch:
+    """Device-resident batch (the C-ABI ltp_batch)."""
+
+    def __init__(self, ctx, max_txns, max_ops):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        ctx.check(ctx.L.ltp_batch_create(ctx.h, max_txns, max_ops, ctypes.byref(h)))
+        self.h = h
+        self.n_txns = 0
+        self.n_ops = 0
+
+    def free(self):
+        if getattr(self, "h", None) and self.ctx.h:
+            self.ctx.L.ltp_batch_free(self.ctx.h, self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def load(self, txn_first, keys, opw, ops_per_txn=0, stream=None):
+        """txn_first may be None when every transaction has ops_per_txn ops."""
+        keys = np.ascontiguousarray(keys, np.uint64)
+        opw = np.ascontiguousarray(opw, np.uint32)
+        if txn_first is not None:
+            txn_first = np.ascontiguousarray(txn_first, np.uint32)
+            n_txns = len(txn_first) - 1
+        else:
+            n_txns = len(keys) // ops_per_txn if ops_per_txn else 0
+        self._keep = (txn_first, keys, opw)  # asynchronous copy: keep the sources alive
+        self.ctx.check(self.ctx.L.ltp_batch_load(self.ctx.h, self.h, n_txns, _p(txn_first), ops_per_txn, len(keys),
+                                                 _p(keys), _p(opw), _stream(stream)))
+        self.n_txns, self.n_ops = n_txns, len(keys)
+
+    def execute(self, stream=None):
+        self.ctx.check(self.ctx.L.ltp_batch_execute(self.ctx.h, self.h, _stream(stream)))
+
+    def fetch(self, commit=None, vals=None, stream=None):
+        self.ctx.check(self.ctx.L.ltp_batch_fetch(self.ctx.h, self.h, _p(commit), _p(vals), _stream(stream)))
+
+    def finish(self, stream=None):
+        st = Stats()
+        self.ctx.check(self.ctx.L.ltp_batch_finish(self.ctx.h, self.h, ctypes.byref(st), _stream(stream)))
+        return st
+
+    def results(self):
+        commit = np.zeros(max(self.n_txns, 1), np.uint8)
+        vals = np.zeros(max(self.n_ops, 1), np.int32)
+        st = Stats()
+        self.ctx.check(self.ctx.L.ltp_batch_results(self.ctx.h, self.h, _p(commit), _p(vals), ctypes.byref(st)))
+        return commit[: self.n_txns], vals[: self.n_ops], st

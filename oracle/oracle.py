@@ -1,0 +1,142 @@
+"""ctypes front end of the CPU oracle (oracle/ltp_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
+the checker and by bench.py's CPU-baseline leg.  The shipped library never
+imports it.  Parity status: the replay restates the reference's per-row
+ascending-TID rule; value parity is unpinned by the reference (its operators
+do not write); the reference-generator restatements are pinned by
+tests/golden/.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libltp_oracle.so")
+REF_LIB_PATH = os.path.join(HERE, "_ref", "libltpmg_ref_random.so")
+
+OPW_READ, OPW_ADD, OPW_INSERT = 0, 1, 2
+
+
+def build(verbose=False):
+    """Compile the oracle restatement (gcc; same bits on x86-64 and aarch64)."""
+    cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared",
+           os.path.join(HERE, "ltp_oracle.c"), "-o", LIB_PATH, "-lm", "-lpthread"]
+    subprocess.run(cmd, check=True, capture_output=not verbose)
+    return LIB_PATH
+
+
+def build_ref(verbose=False):
+    """Compile the reference's own generator code into oracle/_ref when the
+    reference tree is present (no-op elsewhere)."""
+    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True, capture_output=not verbose)
+    return REF_LIB_PATH if os.path.exists(REF_LIB_PATH) else None
+
+
+class YcsbParams(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_uint64), ("n_rows", ctypes.c_uint64), ("n_cols", ctypes.c_uint32),
+                ("ops_min", ctypes.c_uint32), ("ops_max", ctypes.c_uint32), ("rmw_delta", ctypes.c_int32),
+                ("read_frac", ctypes.c_double), ("theta", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        u64, u32, i32, dbl, vp = ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32, ctypes.c_double, ctypes.c_void_p
+        L.ltpo_mix64.restype = u64
+        L.ltpo_mix64.argtypes = [u64]
+        L.ltpo_stream_seed.restype = u64
+        L.ltpo_stream_seed.argtypes = [u64, u64, u64]
+        L.ltpo_feistel_perm.restype = u64
+        L.ltpo_feistel_perm.argtypes = [u64, u64, u64]
+        L.ltpo_det_log.restype = dbl
+        L.ltpo_det_log.argtypes = [dbl]
+        L.ltpo_det_exp.restype = dbl
+        L.ltpo_det_exp.argtypes = [dbl]
+        L.ltpo_zipf_draw.restype = u64
+        L.ltpo_zipf_draw.argtypes = [u64, dbl, ctypes.POINTER(u64)]
+        L.ltpo_table_value.restype = i32
+        L.ltpo_table_value.argtypes = [u64, u64, u32, u32]
+        L.ltpo_gen_ycsb_batch.restype = u64
+        L.ltpo_gen_ycsb_batch.argtypes = [ctypes.POINTER(YcsbParams), u64, u64, vp, vp, vp, u64]
+        L.ltpo_table_init.restype = None
+        L.ltpo_table_init.argtypes = [u64, u64, u32, vp]
+        L.ltpo_replay.restype = ctypes.c_int
+        L.ltpo_replay.argtypes = [ctypes.c_int, u64, u32, vp, u64, vp, vp, vp, vp, vp]
+        L.ltpo_replay_r0_mt.restype = ctypes.c_int
+        L.ltpo_replay_r0_mt.argtypes = [u64, u32, vp, u64, vp, vp, vp, vp, vp, ctypes.c_int]
+        L.ltpo_fnv1a.restype = u64
+        L.ltpo_fnv1a.argtypes = [vp, u64]
+        L.ltpo_ref_zipf_table.restype = u32
+        L.ltpo_ref_zipf_table.argtypes = [u64, dbl, vp]
+        L.ltpo_ref_zipf_pick.restype = u32
+        L.ltpo_ref_zipf_pick.argtypes = [vp, u32, u32, u32]
+        L.ltpo_ref_nurand.restype = u64
+        L.ltpo_ref_nurand.argtypes = [u64, u64, u64, u64, u64]
+        L.ltpo_ref_ycsb_op_type.restype = u32
+        L.ltpo_ref_ycsb_op_type.argtypes = [u32, u32]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def opword(kind, col, table=0, imm=0):
+    return (kind | (col << 2) | (table << 8) | ((imm & 0xFFFFF) << 12)) & 0xFFFFFFFF
+
+
+def ycsb_params(seed, n_rows, n_cols, ops_min, ops_max, read_frac, theta, rmw_delta=1):
+    return YcsbParams(seed, n_rows, n_cols, ops_min, ops_max, rmw_delta, read_frac, theta)
+
+
+def gen_ycsb_batch(p, batch, n_txns):
+    """Returns (txn_first uint32[n_txns+1], keys uint64[n_ops], opw uint32[n_ops])."""
+    cap = n_txns * p.ops_max
+    tf = np.zeros(n_txns + 1, np.uint32)
+    keys = np.zeros(max(cap, 1), np.uint64)
+    opw = np.zeros(max(cap, 1), np.uint32)
+    n = lib().ltpo_gen_ycsb_batch(ctypes.byref(p), batch, n_txns, _p(tf), _p(keys), _p(opw), cap)
+    if n == 2 ** 64 - 1:
+        raise ValueError("generator rejected the parameters")
+    return tf, keys[:n].copy(), opw[:n].copy()
+
+
+def table_init(seed, n_rows, n_cols):
+    tab = np.empty((n_cols, n_rows), np.int32)
+    lib().ltpo_table_init(seed, n_rows, n_cols, _p(tab))
+    return tab
+
+
+def replay(rule, tab, txn_first, keys, opw, threads=0):
+    """Serial replay on a copy of the column-major table; returns
+    (table_after, commit uint8[n_txns], out int32[n_ops])."""
+    tab = np.ascontiguousarray(tab, np.int32).copy()
+    n_cols, n_rows = tab.shape
+    n_txns = len(txn_first) - 1
+    commit = np.zeros(max(n_txns, 1), np.uint8)
+    out = np.zeros(max(len(keys), 1), np.int32)
+    tf = np.ascontiguousarray(txn_first, np.uint32)
+    k = np.ascontiguousarray(keys, np.uint64)
+    w = np.ascontiguousarray(opw, np.uint32)
+    if threads and rule == 0:
+        rc = lib().ltpo_replay_r0_mt(n_rows, n_cols, _p(tab), n_txns, _p(tf), _p(k), _p(w), _p(commit), _p(out), threads)
+    else:
+        rc = lib().ltpo_replay(rule, n_rows, n_cols, _p(tab), n_txns, _p(tf), _p(k), _p(w), _p(commit), _p(out))
+    if rc != 0:
+        raise ValueError("oracle rejected the batch (malformed op)")
+    return tab, commit[:n_txns], out[:len(keys)]
+
+
+def fnv1a(a):
+    a = np.ascontiguousarray(a)
+    return int(lib().ltpo_fnv1a(_p(a), a.nbytes))

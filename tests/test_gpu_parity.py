@@ -1,0 +1,279 @@
+"""CUDA path vs the CPU oracle, through the C ABI (libltpmg_gb300.so).
+
+Bit-exact comparison of the commit vector, every per-op value and the final
+table for seeded workloads at reduced sizes, the full-size plain batch
+(2^20 rows, 16 batches of 2^16 transactions x 10 ops) and full-size Zipf
+batches (2^24 rows, 2^20 transactions x 16 ops), plus the edge cases the
+reference's per-row ordering implies (one hot row, one hot cell, read-only,
+write-only, single transaction, empty batch) and error paths.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import ltpmg_gb300 as G
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "seeded_workloads.json")
+SEED = 0x4C54504D47
+
+
+@pytest.fixture(scope="module")
+def lib_loaded():
+    return G.load()
+
+
+def run_and_check(rule, rows, cols, batches, seed=SEED, fixed=0, ctx_kwargs=None, tab0=None, threads=0):
+    """Executes the batches in order on a fresh context and compares each
+    batch's outputs and the final table with the oracle."""
+    with G.Context(device=0, rule=rule, **(ctx_kwargs or {})) as ctx:
+        t = ctx.create_table(rows, cols)
+        if tab0 is None:
+            ctx.fill_seeded(t, seed)
+            ref = O.table_init(seed, rows, cols)
+        else:
+            ctx.upload(t, tab0)
+            ref = tab0.copy()
+        maxops = max([len(k) for _, k, _ in batches] + [1])
+        maxtx = max([len(tf) - 1 for tf, _, _ in batches] + [1])
+        b = ctx.batch(maxtx, maxops)
+        stats = []
+        for tf, keys, opw in batches:
+            if fixed:
+                b.load(None, keys, opw, ops_per_txn=fixed)
+            else:
+                b.load(tf, keys, opw)
+            b.execute()
+            commit, vals, st = b.results()
+            ref, rc, ro = O.replay(rule, ref, tf, keys, opw, threads=threads)
+            assert np.array_equal(commit, rc), "commit vector differs"
+            bad = np.nonzero(vals != ro)[0]
+            assert len(bad) == 0, f"{len(bad)} op values differ, first at {bad[:5]}: {vals[bad[:5]]} vs {ro[bad[:5]]}"
+            stats.append(st.as_dict())
+        final = ctx.download(t)
+        assert np.array_equal(final, ref), f"final table differs in {(final != ref).sum()} cells"
+        return stats
+
+
+def gen(seed, rows, cols, omin, omax, rf, th, b, n):
+    return G.gen_ycsb(seed, rows, cols, omin, omax, rf, th, batch=b, n_txns=n)
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+def test_golden_workloads(lib_loaded, rule):
+    doc = json.load(open(GOLDEN))
+    for w in doc["workloads"]:
+        tf, keys, opw = gen(w["seed"], w["rows"], w["cols"], w["ops_min"], w["ops_max"], w["read_frac"], w["theta"],
+                            w["batch"], w["txns"])
+        assert O.fnv1a(keys) == w["fnv_keys"] and O.fnv1a(opw) == w["fnv_opw"]
+        with G.Context(device=0, rule=rule) as ctx:
+            t = ctx.create_table(w["rows"], w["cols"])
+            ctx.fill_seeded(t, w["seed"])
+            assert O.fnv1a(ctx.download(t)) == w["fnv_table_init"]
+            b = ctx.batch(w["txns"], len(keys))
+            b.load(tf, keys, opw)
+            b.execute()
+            commit, vals, st = b.results()
+            exp = w[f"r{rule}"]
+            assert O.fnv1a(commit) == exp["fnv_commit"], w["name"]
+            assert O.fnv1a(vals) == exp["fnv_out"], w["name"]
+            assert O.fnv1a(ctx.download(t)) == exp["fnv_table"], w["name"]
+            assert st.committed == exp["committed"]
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+@pytest.mark.parametrize("shape", [
+    # rows, cols, ops_min, ops_max, read_frac, theta, txns, batches
+    (1 << 12, 10, 10, 10, 0.5, 0.0, 4096, 3),
+    (1 << 14, 10, 16, 16, 0.8, 0.99, 4096, 3),
+    (1 << 14, 10, 1, 32, 0.7, 0.75, 3000, 3),
+    (64, 4, 1, 32, 0.3, 1.2, 2000, 2),
+    (1 << 16, 1, 8, 8, 0.5, 0.99, 8192, 2),
+    (1 << 10, 64, 4, 12, 0.2, 0.9, 5000, 2),
+])
+def test_seeded_sequences(lib_loaded, rule, shape):
+    rows, cols, omin, omax, rf, th, txns, nb = shape
+    batches = [gen(SEED + 11, rows, cols, omin, omax, rf, th, b, txns) for b in range(nb)]
+    run_and_check(rule, rows, cols, batches, seed=SEED + 11)
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+def test_fixed_length_path(lib_loaded, rule):
+    rows, cols = 1 << 13, 10
+    batches = [gen(3, rows, cols, 16, 16, 0.8, 0.99, b, 4096) for b in range(2)]
+    run_and_check(rule, rows, cols, batches, seed=3, fixed=16)
+
+
+def _manual(txn_ops):
+    """txn_ops: list of transactions, each a list of (key, kind, col, imm)."""
+    tf = [0]
+    keys, opw = [], []
+    for ops in txn_ops:
+        for key, kind, col, imm in ops:
+            keys.append(key)
+            opw.append(O.opword(kind, col, 0, imm))
+        tf.append(len(keys))
+    return np.array(tf, np.uint32), np.array(keys, np.uint64), np.array(opw, np.uint32)
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+def test_edge_cases(lib_loaded, rule):
+    rows, cols = 256, 3
+    rng = np.random.default_rng(5)
+    cases = []
+    # one hot cell: every op of every transaction on (row 7, col 1)
+    cases.append(_manual([[(7, int(rng.random() < 0.5), 1, int(rng.integers(-5, 6)))] for _ in range(5000)]))
+    # one hot row, all columns, all RMW
+    cases.append(_manual([[(3, 1, c, 1) for c in range(3)] for _ in range(3000)]))
+    # read only
+    cases.append(_manual([[(int(r), 0, int(r) % 3, 0) for r in rng.choice(rows, 8, replace=False)] for _ in range(500)]))
+    # write only, large immediates (wrap-around)
+    cases.append(_manual([[(int(r), 1, 0, 524287 if r % 2 else -524288) for r in rng.choice(rows, 4, replace=False)]
+                          for _ in range(2000)]))
+    # a single transaction
+    cases.append(_manual([[(1, 1, 0, 3), (2, 0, 1, 0), (3, 1, 2, -1)]]))
+    # transactions with no ops in between
+    cases.append(_manual([[], [(5, 1, 0, 1)], [], [(5, 0, 0, 0)], []]))
+    tab0 = np.arange(rows * cols, dtype=np.int64).reshape(cols, rows).astype(np.int32) * 7 - 100
+    tab0[0, 10] = 2 ** 31 - 1
+    run_and_check(rule, rows, cols, cases, tab0=tab0)
+
+
+def test_empty_batch(lib_loaded):
+    with G.Context(device=0) as ctx:
+        t = ctx.create_table(100, 2)
+        ctx.fill_seeded(t, 1)
+        before = ctx.download(t)
+        b = ctx.batch(4, 16)
+        b.load(np.zeros(1, np.uint32), np.zeros(0, np.uint64), np.zeros(0, np.uint32))
+        b.execute()
+        commit, vals, st = b.results()
+        assert len(commit) == 0 and len(vals) == 0 and st.ops == 0
+        assert np.array_equal(before, ctx.download(t))
+
+
+@pytest.mark.parametrize("block,ipt", [(b, i) for b in (128, 256, 512) for i in (1, 2, 4, 8)])
+def test_tuning_variants(lib_loaded, block, ipt):
+    rows, cols = 1 << 12, 10
+    tf, keys, opw = gen(21, rows, cols, 1, 32, 0.7, 0.95, 0, 3000)
+    ref_tab, rc, ro = O.replay(0, O.table_init(21, rows, cols), tf, keys, opw)
+    with G.Context(device=0) as ctx:
+        t = ctx.create_table(rows, cols)
+        ctx.fill_seeded(t, 21)
+        for bucket in range(64):
+            ctx.set_tuning(bucket, block, ipt)
+        b = ctx.batch(3000, len(keys))
+        b.load(tf, keys, opw)
+        b.execute()
+        commit, vals, st = b.results()
+        assert np.array_equal(vals, ro) and np.array_equal(ctx.download(t), ref_tab)
+
+
+def test_malformed_op_rejected_and_context_survives(lib_loaded):
+    rows, cols = 128, 2
+    with G.Context(device=0) as ctx:
+        t = ctx.create_table(rows, cols)
+        ctx.fill_seeded(t, 9)
+        before = ctx.download(t)
+        b = ctx.batch(8, 64)
+        tf, keys, opw = _manual([[(1, 1, 0, 1), (rows + 5, 1, 1, 1)], [(2, 1, 1, 1)]])
+        b.load(tf, keys, opw)
+        b.execute()
+        with pytest.raises(G.LtpError) as ei:
+            b.results()
+        assert ei.value.status == G.lib.LTP_E_BADARG and "index 1" in str(ei.value)
+        assert np.array_equal(before, ctx.download(t)), "a rejected batch must not change the table"
+        tf, keys, opw = _manual([[(1, 1, 0, 1)], [(1, 0, 0, 0)]])
+        b.load(tf, keys, opw)
+        b.execute()
+        commit, vals, _ = b.results()
+        assert vals.tolist() == [int(before[0, 1]) + 1, int(before[0, 1]) + 1]
+
+
+def test_bad_column_and_table(lib_loaded):
+    with G.Context(device=0) as ctx:
+        t = ctx.create_table(64, 2)
+        ctx.fill_seeded(t, 2)
+        b = ctx.batch(4, 4)
+        for w in (O.opword(0, 5, 0, 0), O.opword(0, 0, 3, 0), 3):
+            b.load(np.array([0, 1], np.uint32), np.array([1], np.uint64), np.array([w], np.uint32))
+            b.execute()
+            with pytest.raises(G.LtpError):
+                b.results()
+
+
+def test_timeout_status_and_recovery(lib_loaded):
+    """The debug stall makes the first stage poll a flag nothing sets; it gives
+    up after ~200 ms and the batch reports LTP_E_TIMEOUT.  No GPU fault."""
+    rows, cols = 1 << 10, 4
+    tf, keys, opw = gen(4, rows, cols, 4, 4, 0.5, 0.9, 0, 500)
+    with G.Context(device=0) as ctx:
+        t = ctx.create_table(rows, cols)
+        ctx.fill_seeded(t, 4)
+        b = ctx.batch(500, len(keys))
+        b.load(tf, keys, opw)
+        ctx.stall_next(200)
+        b.execute()
+        with pytest.raises(G.LtpError) as ei:
+            b.results()
+        assert ei.value.status == G.lib.LTP_E_TIMEOUT
+        # the context is still usable and the failed batch changed nothing
+        b.execute()
+        commit, vals, _ = b.results()
+        ref_tab, rc, ro = O.replay(0, O.table_init(4, rows, cols), tf, keys, opw)
+        assert np.array_equal(vals, ro) and np.array_equal(ctx.download(t), ref_tab)
+
+
+def test_two_tables(lib_loaded):
+    with G.Context(device=0) as ctx:
+        a = ctx.create_table(1000, 3)
+        bt = ctx.create_table(77, 5)
+        ctx.fill_seeded(a, 1)
+        ctx.fill_seeded(bt, 2)
+        ta, tb = O.table_init(1, 1000, 3), O.table_init(2, 77, 5)
+        rng = np.random.default_rng(3)
+        keys, opw, tf = [], [], [0]
+        for t in range(3000):
+            for j in range(4):
+                if rng.random() < 0.5:
+                    keys.append(int(rng.integers(0, 1000))); opw.append(O.opword(int(rng.random() < 0.4), int(rng.integers(0, 3)), 0, 1))
+                else:
+                    keys.append(int(rng.integers(0, 77))); opw.append(O.opword(int(rng.random() < 0.4), int(rng.integers(0, 5)), 1, 2))
+            tf.append(len(keys))
+        b = ctx.batch(3000, len(keys))
+        b.load(np.array(tf, np.uint32), np.array(keys, np.uint64), np.array(opw, np.uint32))
+        b.execute()
+        commit, vals, _ = b.results()
+        # serial replay over two tables
+        exp = np.zeros(len(keys), np.int32)
+        tabs = [ta.copy(), tb.copy()]
+        for i, (k, w) in enumerate(zip(keys, opw)):
+            tt, col, kind, imm = (w >> 8) & 15, (w >> 2) & 63, w & 3, ((w >> 12) ^ 0x80000) - 0x80000
+            v = int(tabs[tt][col, k])
+            if kind == 1:
+                v = ((v + imm + 2 ** 31) % 2 ** 32) - 2 ** 31
+                tabs[tt][col, k] = v
+            exp[i] = v
+        assert np.array_equal(vals, exp)
+        assert np.array_equal(ctx.download(a), tabs[0]) and np.array_equal(ctx.download(bt), tabs[1])
+
+
+def test_full_size_plain_batches(lib_loaded):
+    """Plain batch workload at full size: 2^20 rows x 10 int32, 16 batches of
+    2^16 transactions x 10 ops, uniform keys, 50% read / 50% +1 RMW."""
+    rows, cols = 1 << 20, 10
+    batches = [gen(SEED, rows, cols, 10, 10, 0.5, 0.0, b, 1 << 16) for b in range(16)]
+    run_and_check(0, rows, cols, batches, fixed=10, threads=8)
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+def test_full_size_zipf_batches(lib_loaded, rule):
+    """High-contention workload at full size: 2^24 rows x 10 int32, batches of
+    2^20 transactions x 16 ops, Zipf 0.99 keys, 80% read / 20% RMW."""
+    rows, cols = 1 << 24, 10
+    batches = [gen(SEED + 2, rows, cols, 16, 16, 0.8, 0.99, b, 1 << 20) for b in range(2 if rule == 0 else 1)]
+    stats = run_and_check(rule, rows, cols, batches, seed=SEED + 2, fixed=16, threads=8 if rule == 0 else 0)
+    assert stats[0]["contended_ops"] > 0
