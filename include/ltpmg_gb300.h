@@ -80,14 +80,19 @@ typedef struct {
     uint32_t reserved;
 } ltp_schema;
 
-#define LTP_N_STAGES 8
+#define LTP_N_STAGES 12
 typedef struct {
     uint64_t txns, ops, committed, aborted;
     uint64_t contended_ops;   /* ops on cells touched >1 time with >=1 write */
     uint64_t contended_cells;
     uint64_t touched_words;   /* 32-cell bitmap words touched by the batch */
     uint64_t bytes_algorithmic;
-    float ms_stage[LTP_N_STAGES]; /* mark, ids, classify, sort, apply, finish, priority, total */
+    /* with LTP_FLAG_STAGE_TIMING, milliseconds per kernel of the batch:
+     * ordered rule:  0 mark, 1 ids, 2 classify, 3 sort histogram,
+     *                4-7 radix passes, 8 apply, 9 finish
+     * priority rule: 0 mark, 1 ids, 2 min-writer, 3 abort, 4 execute, 9 finish
+     * and 11 the whole batch */
+    float ms_stage[LTP_N_STAGES];
 } ltp_stats;
 
 typedef struct {

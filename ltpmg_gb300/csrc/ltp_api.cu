@@ -32,8 +32,6 @@ struct ltp_ctx {
     Counters *ctr = nullptr;
     std::string last_error;
     Tuning tuning[64];
-    cudaEvent_t ev[LTP_N_STAGES + 1];
-    bool have_events = false;
     uint32_t stall_ms_next = 0;
     bool dirty = false;  // scratch must be reset before the next batch
 };
@@ -49,6 +47,8 @@ struct ltp_batch {
     bool loaded = false, executed = false;
     int rule = 0;
     Counters *snap = nullptr;  // device copy of the counters after this batch
+    cudaEvent_t ev[LTP_N_STAGES];
+    bool have_events = false;
 };
 
 namespace {
@@ -212,12 +212,10 @@ int ltp_init(const ltp_config *cfg, ltp_ctx **out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->ctr, sizeof(Counters));
     if (e == cudaSuccess) e = cudaMemset(ctx->ctr, 0, sizeof(Counters));
-    for (int i = 0; e == cudaSuccess && i <= LTP_N_STAGES; i++) e = cudaEventCreate(&ctx->ev[i]);
     if (e != cudaSuccess) {
         ltp_shutdown(ctx);
         return e == cudaErrorMemoryAllocation ? LTP_E_NOMEM : LTP_E_CUDA;
     }
-    ctx->have_events = true;
     if (cfg->reserve_ops) {
         int rc = ensure_scratch(ctx, cfg->reserve_ops);
         if (rc) {
@@ -237,8 +235,6 @@ int ltp_shutdown(ltp_ctx *ctx) {
     free_scratch_ops(ctx->s);
     free_scratch_words(ctx->s);
     cudaFree(ctx->ctr);
-    if (ctx->have_events)
-        for (int i = 0; i <= LTP_N_STAGES; i++) cudaEventDestroy(ctx->ev[i]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return LTP_OK;
@@ -350,6 +346,10 @@ int ltp_batch_create(ltp_ctx *ctx, uint64_t max_txns, uint64_t max_ops, ltp_batc
     if (e == cudaSuccess) e = dalloc(&b->txn_first, max_txns + 1);
     if (e == cudaSuccess) e = dalloc(&b->commit, max_txns);
     if (e == cudaSuccess) e = dalloc(&b->snap, 1);
+    if (e == cudaSuccess && (ctx->flags & LTP_FLAG_STAGE_TIMING)) {
+        for (int i = 0; e == cudaSuccess && i < LTP_N_STAGES; i++) e = cudaEventCreate(&b->ev[i]);
+        b->have_events = e == cudaSuccess;
+    }
     if (e != cudaSuccess) {
         ltp_batch_free(ctx, b);
         return cuda_fail(ctx, e, "ltp_batch_create");
@@ -373,6 +373,8 @@ int ltp_batch_free(ltp_ctx *ctx, ltp_batch *b) {
     cudaFree(b->txn_first);
     cudaFree(b->commit);
     cudaFree(b->snap);
+    if (b->have_events)
+        for (int i = 0; i < LTP_N_STAGES; i++) cudaEventDestroy(b->ev[i]);
     delete b;
     return LTP_OK;
 }
@@ -441,8 +443,8 @@ int ltp_batch_execute(ltp_ctx *ctx, ltp_batch *b, void *stream) {
     L.stall = ctx->stall_ms_next != 0;
     L.stall_ms = ctx->stall_ms_next;
     ctx->stall_ms_next = 0;
-    L.timing = (ctx->flags & LTP_FLAG_STAGE_TIMING) != 0;
-    for (int i = 0; i <= LTP_N_STAGES; i++) L.ev[i] = ctx->ev[i];
+    L.timing = b->have_events;
+    L.ev = b->ev;
     if (b->n_ops) CK(launch_execute(L, bd, tables_dev(ctx), ctx->s, ctx->ctr));
     CK(cudaMemcpyAsync(b->snap, ctx->ctr, sizeof(Counters), cudaMemcpyDeviceToDevice, st));
     b->rule = ctx->rule;
@@ -478,15 +480,15 @@ int ltp_batch_finish(ltp_ctx *ctx, ltp_batch *b, ltp_stats *stats, void *stream)
         stats->contended_cells = c.M;
         stats->touched_words = c.n_tw;
         stats->bytes_algorithmic = 28ull * b->n_ops + 4ull * b->n_txns;
-        if ((ctx->flags & LTP_FLAG_STAGE_TIMING) && b->n_ops) {
-            float total = 0;
-            for (int i = 0; i < 6; i++) {
+        if (b->have_events && b->n_ops) {
+            for (int i = 0; i < 10; i++) {
                 float ms = 0;
-                cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);
+                cudaEventElapsedTime(&ms, b->ev[i], b->ev[i + 1]);
                 stats->ms_stage[i] = ms;
-                total += ms;
             }
-            stats->ms_stage[7] = total;
+            float total = 0;
+            cudaEventElapsedTime(&total, b->ev[0], b->ev[10]);
+            stats->ms_stage[11] = total;
         }
     }
     if (c.err) {

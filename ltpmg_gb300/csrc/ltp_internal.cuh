@@ -111,7 +111,7 @@ struct Launch {
     Tuning tune;
     bool stall;
     u32 stall_ms;
-    cudaEvent_t ev[LTP_N_STAGES + 1];
+    cudaEvent_t *ev;  // LTP_N_STAGES events of the batch when timing
     bool timing;
 };
 

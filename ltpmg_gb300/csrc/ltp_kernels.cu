@@ -632,16 +632,19 @@ __global__ void __launch_bounds__(256) k_r1_minw(BatchDev b, TablesDev T, Scratc
     if (ctr->err) return;
     const u64 n = b.n_ops;
     for (u64 i = (u64)blockIdx.x * 256 + threadIdx.x; i - threadIdx.x < n; i += (u64)gridDim.x * 256) {
-        bool act = false;
+        bool act = false, con = false;
         u32 m = 0, tid = 0;
         if (i < n) {
             const u32 w = b.opw[i];
             OpRef r = decode_op(T, b.keys[i], w);
-            if (r.valid && opw_kind(w) == LTP_OP_ADD && contended_id(s, r.cell, &m)) {
+            con = r.valid && contended_id(s, r.cell, &m);
+            if (con && opw_kind(w) == LTP_OP_ADD) {
                 act = true;
                 tid = op_tid(b, i);
             }
         }
+        const u32 nc = __popc(__ballot_sync(FULL_MASK, con));
+        if ((threadIdx.x & 31) == 0 && nc) atomicAdd(&ctr->n_c, (u64)nc);
         const u32 peers = __match_any_sync(FULL_MASK, act ? m : 0xFFFFFFFFu);
         const u32 mn = __reduce_min_sync(peers, act ? tid : 0xFFFFFFFFu);
         if (act && (threadIdx.x & 31) == (u32)(__ffs(peers) - 1)) atomicMin(&s.dminw[m], mn);
@@ -768,81 +771,106 @@ static int occ_grid(K kernel, int block, int num_sms) {
 }
 
 template <int BLOCK, int IPT>
-static cudaError_t launch_front(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s,
-                                Counters *ctr, bool classify) {
-    const u64 tile = (u64)BLOCK * IPT;
-    const u64 tiles = (b.n_ops + tile - 1) / tile;
-    static int g_mark = 0, g_cls = 0;
-    static int dev_sms = 0;
-    if (dev_sms != L.num_sms) {
-        g_mark = occ_grid(k_mark<BLOCK, IPT>, BLOCK, L.num_sms);
-        g_cls = occ_grid(k_classify<BLOCK, IPT>, BLOCK, L.num_sms);
-        dev_sms = L.num_sms;
+struct Front {
+    static int g_mark, g_cls, sms;
+    static void grids(int num_sms) {
+        if (sms != num_sms) {
+            g_mark = occ_grid(k_mark<BLOCK, IPT>, BLOCK, num_sms);
+            g_cls = occ_grid(k_classify<BLOCK, IPT>, BLOCK, num_sms);
+            sms = num_sms;
+        }
     }
-    int gm = (int)(tiles < (u64)g_mark ? tiles : (u64)g_mark);
-    if (gm < 1) gm = 1;
-    k_mark<BLOCK, IPT><<<gm, BLOCK, 0, L.stream>>>(b, T, s, ctr);
-    if (L.timing) cudaEventRecord(L.ev[1], L.stream);
-    {
-        int gi = occ_grid(k_ids<false>, kIdsBlock, L.num_sms);
-        u64 ub = (b.n_ops + kIdsTile - 1) / kIdsTile;
-        if ((u64)gi > ub) gi = (int)(ub ? ub : 1);
-        if (L.rule == LTP_RULE_PRIORITY) k_ids<true><<<gi, kIdsBlock, 0, L.stream>>>(T, s, ctr);
-        else k_ids<false><<<gi, kIdsBlock, 0, L.stream>>>(T, s, ctr);
+    static void mark(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+        grids(L.num_sms);
+        const u64 tiles = (b.n_ops + (u64)BLOCK * IPT - 1) / ((u64)BLOCK * IPT);
+        const int g = (int)(tiles < (u64)g_mark ? (tiles ? tiles : 1) : (u64)g_mark);
+        k_mark<BLOCK, IPT><<<g, BLOCK, 0, L.stream>>>(b, T, s, ctr);
     }
-    if (L.timing) cudaEventRecord(L.ev[2], L.stream);
-    if (classify) {
-        int gc = (int)(tiles < (u64)g_cls ? tiles : (u64)g_cls);
-        if (gc < 1) gc = 1;
-        k_classify<BLOCK, IPT><<<gc, BLOCK, 0, L.stream>>>(b, T, s, ctr);
+    static void classify(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+        grids(L.num_sms);
+        const u64 tiles = (b.n_ops + (u64)BLOCK * IPT - 1) / ((u64)BLOCK * IPT);
+        const int g = (int)(tiles < (u64)g_cls ? (tiles ? tiles : 1) : (u64)g_cls);
+        k_classify<BLOCK, IPT><<<g, BLOCK, 0, L.stream>>>(b, T, s, ctr);
     }
-    return cudaGetLastError();
-}
+};
+template <int BLOCK, int IPT> int Front<BLOCK, IPT>::g_mark = 0;
+template <int BLOCK, int IPT> int Front<BLOCK, IPT>::g_cls = 0;
+template <int BLOCK, int IPT> int Front<BLOCK, IPT>::sms = 0;
 
-typedef cudaError_t (*front_fn)(const Launch &, const BatchDev &, const TablesDev &, const Scratch &, Counters *, bool);
+typedef void (*front_fn)(const Launch &, const BatchDev &, const TablesDev &, const Scratch &, Counters *);
 
-static front_fn pick_front(const Tuning &t) {
-#define LTP_FRONT(B, I) \
-    if (t.block == B && t.ipt == I) return launch_front<B, I>;
+static void pick_front(const Tuning &t, front_fn *mark, front_fn *classify) {
+#define LTP_FRONT(B, I)                        \
+    if (t.block == B && t.ipt == I) {          \
+        *mark = Front<B, I>::mark;             \
+        *classify = Front<B, I>::classify;     \
+        return;                                \
+    }
     LTP_FRONT(128, 1) LTP_FRONT(128, 2) LTP_FRONT(128, 4) LTP_FRONT(128, 8)
     LTP_FRONT(256, 1) LTP_FRONT(256, 2) LTP_FRONT(256, 4) LTP_FRONT(256, 8)
     LTP_FRONT(512, 1) LTP_FRONT(512, 2) LTP_FRONT(512, 4) LTP_FRONT(512, 8)
 #undef LTP_FRONT
-    return launch_front<256, 4>;
+    *mark = Front<256, 4>::mark;
+    *classify = Front<256, 4>::classify;
 }
 
+static int capped(int grid, u64 upper) { return (int)((u64)grid < upper ? (u64)grid : (upper ? upper : 1)); }
+
 cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
-    if (L.timing) cudaEventRecord(L.ev[0], L.stream);
+    // stage event i is recorded after kernel i; event 0 of the batch precedes everything
+    auto mark_ev = [&](int i) {
+        if (L.timing) cudaEventRecord(L.ev[i], L.stream);
+    };
+    mark_ev(0);
     if (L.stall) k_stall<<<1, 1, 0, L.stream>>>(ctr, L.stall_ms);
-    const bool ordered = L.rule != LTP_RULE_PRIORITY;
-    cudaError_t e = pick_front(L.tune)(L, b, T, s, ctr, ordered);
-    if (e != cudaSuccess) return e;
-    if (L.timing) cudaEventRecord(L.ev[3], L.stream);
-    const int gs = occ_grid(k_sort_pass<0>, kSortBlock, L.num_sms);
-    const u64 ub_sort = (b.n_ops + kSortTile - 1) / kSortTile;
-    const int gsort = (int)((u64)gs < ub_sort ? (u64)gs : (ub_sort ? ub_sort : 1));
+    front_fn f_mark, f_cls;
+    pick_front(L.tune, &f_mark, &f_cls);
+    f_mark(L, b, T, s, ctr);
+    mark_ev(1);
+    {
+        static int gi = 0, sms = 0;
+        if (sms != L.num_sms) {
+            gi = occ_grid(k_ids<false>, kIdsBlock, L.num_sms);
+            sms = L.num_sms;
+        }
+        const int g = capped(gi, (b.n_ops + kIdsTile - 1) / kIdsTile);
+        if (L.rule == LTP_RULE_PRIORITY) k_ids<true><<<g, kIdsBlock, 0, L.stream>>>(T, s, ctr);
+        else k_ids<false><<<g, kIdsBlock, 0, L.stream>>>(T, s, ctr);
+    }
+    mark_ev(2);
     const int gstream = L.num_sms * 8;
-    if (ordered) {
+    if (L.rule != LTP_RULE_PRIORITY) {
+        f_cls(L, b, T, s, ctr);
+        mark_ev(3);
+        static int gs = 0, ga = 0, sms = 0;
+        if (sms != L.num_sms) {
+            gs = occ_grid(k_sort_pass<0>, kSortBlock, L.num_sms);
+            ga = occ_grid(k_apply, kApplyBlock, L.num_sms);
+            sms = L.num_sms;
+        }
+        const int gsort = capped(gs, (b.n_ops + kSortTile - 1) / kSortTile);
         k_sort_hist<<<gstream, 256, 0, L.stream>>>(s, ctr);
+        mark_ev(4);
         k_sort_pass<0><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        mark_ev(5);
         k_sort_pass<1><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        mark_ev(6);
         k_sort_pass<2><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        mark_ev(7);
         k_sort_pass<3><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
-        if (L.timing) cudaEventRecord(L.ev[4], L.stream);
-        const int ga = occ_grid(k_apply, kApplyBlock, L.num_sms);
-        const u64 ub_apply = (b.n_ops + kApplyTile - 1) / kApplyTile;
-        const int gapp = (int)((u64)ga < ub_apply ? (u64)ga : (ub_apply ? ub_apply : 1));
-        k_apply<<<gapp, kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
-        if (L.timing) cudaEventRecord(L.ev[5], L.stream);
+        mark_ev(8);
+        k_apply<<<capped(ga, (b.n_ops + kApplyTile - 1) / kApplyTile), kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
+        mark_ev(9);
     } else {
-        if (L.timing) cudaEventRecord(L.ev[4], L.stream);
         k_r1_minw<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        mark_ev(3);
         k_r1_abort<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        mark_ev(4);
         k_r1_exec<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
-        if (L.timing) cudaEventRecord(L.ev[5], L.stream);
+        for (int i = 5; i <= 9; i++) mark_ev(i);
     }
     k_finish<<<gstream, 256, 0, L.stream>>>(b, s, ctr, L.rule, L.tune.block * L.tune.ipt);
-    if (L.timing) cudaEventRecord(L.ev[6], L.stream);
+    mark_ev(10);
     return cudaGetLastError();
 }
 

@@ -20,7 +20,8 @@ LTP_E_DEVICE_ASSERT, LTP_E_NOMEM, LTP_E_STATE = -5, -6, -7
 RULE_ORDERED, RULE_PRIORITY = 0, 1
 OP_READ, OP_ADD = 0, 1
 FLAG_STAGE_TIMING = 1
-STAGE_NAMES = ["mark", "ids", "classify", "sort", "apply", "finish", "unused", "total"]
+STAGE_NAMES = ["mark", "ids", "classify", "sort_hist", "sort_pass0", "sort_pass1", "sort_pass2", "sort_pass3",
+               "apply", "finish", "unused", "total"]
 
 
 class LtpError(RuntimeError):
@@ -42,7 +43,7 @@ class Stats(ctypes.Structure):
     _fields_ = [("txns", ctypes.c_uint64), ("ops", ctypes.c_uint64), ("committed", ctypes.c_uint64),
                 ("aborted", ctypes.c_uint64), ("contended_ops", ctypes.c_uint64),
                 ("contended_cells", ctypes.c_uint64), ("touched_words", ctypes.c_uint64),
-                ("bytes_algorithmic", ctypes.c_uint64), ("ms_stage", ctypes.c_float * 8)]
+                ("bytes_algorithmic", ctypes.c_uint64), ("ms_stage", ctypes.c_float * 12)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "ms_stage"}

@@ -276,4 +276,4 @@ def test_full_size_zipf_batches(lib_loaded, rule):
     rows, cols = 1 << 24, 10
     batches = [gen(SEED + 2, rows, cols, 16, 16, 0.8, 0.99, b, 1 << 20) for b in range(2 if rule == 0 else 1)]
     stats = run_and_check(rule, rows, cols, batches, seed=SEED + 2, fixed=16, threads=8 if rule == 0 else 0)
-    assert stats[0]["contended_ops"] > 0
+    assert stats[0]["contended_ops"] > 0 and stats[0]["contended_cells"] > 0
