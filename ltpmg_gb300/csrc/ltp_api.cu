@@ -106,12 +106,8 @@ void free_scratch_ops(Scratch &s) {
 }
 
 void free_scratch_words(Scratch &s) {
-    cudaFree(s.touch);
-    cudaFree(s.multi);
-    cudaFree(s.wbits);
-    cudaFree(s.cwx);
-    s.touch = s.multi = s.wbits = nullptr;
-    s.cwx = nullptr;
+    cudaFree(s.words);
+    s.words = nullptr;
 }
 
 // Sizes the bitmaps to the cell space and the per-op scratch to n_ops.
@@ -121,13 +117,8 @@ int ensure_scratch(ltp_ctx *ctx, uint64_t n_ops) {
     if (words > ctx->alloc_words) {
         CK(cudaStreamSynchronize(ctx->stream));
         free_scratch_words(s);
-        CK(dalloc(&s.touch, words));
-        CK(dalloc(&s.multi, words));
-        CK(dalloc(&s.wbits, words));
-        CK(dalloc(&s.cwx, words));
-        CK(cudaMemset(s.touch, 0, words * 4));
-        CK(cudaMemset(s.multi, 0, words * 4));
-        CK(cudaMemset(s.wbits, 0, words * 4));
+        CK(dalloc(&s.words, words));
+        CK(cudaMemset(s.words, 0, words * sizeof(WordState)));
         ctx->alloc_words = words;
     }
     s.n_words = words;

@@ -50,6 +50,8 @@ struct BatchDev {
     u32 pad;
 };
 
+constexpr int kMaxPasses = 4;
+
 // Look-back status slots of the kernels that use decoupled look-back.
 enum TileSlot { SLOT_IDS = 0, SLOT_CLASSIFY = 1, SLOT_SORT0 = 2, SLOT_APPLY = 6, SLOT_R1 = 7, N_SLOTS = 8 };
 
@@ -62,17 +64,23 @@ struct Counters {
     u32 M;             // contended cells
     int err;           // first device-side error status (LTP_E_*), 0 = none
     u32 tile_ctr[N_SLOTS];
-    u32 hist[4][256];  // radix digit histograms of the contended list
+    u32 hist[kMaxPasses][256];  // radix digit histograms of the contended list
     u32 stall;         // polled by the debug stall kernel; never set
     u32 pad;
 };
 
+// Conflict state of 32 consecutive cells, kept together so that building,
+// scanning, reading and clearing it touches one 16-byte sector per word.
+struct __align__(16) WordState {
+    u32 touch;   // cell touched at least once in the batch
+    u32 multi;   // cell touched at least twice
+    u32 wbits;   // cell written (RMW) at least once
+    u32 prefix;  // dense id of the word's first contended cell (multi & wbits)
+};
+
 // Scratch owned by the context, sized by the cell space and the batch capacity.
 struct Scratch {
-    u32 *touch;     // [n_words] cell touched at least once
-    u32 *multi;     // [n_words] cell touched at least twice
-    u32 *wbits;     // [n_words] cell written at least once
-    u64 *cwx;       // [n_words] (contended-id prefix << 32) | contended bits
+    WordState *words; // [n_words]
     u32 *tw_list;   // [cap_ops] touched words
     u64 *list[2];   // [cap_ops] contended-op records, ping-pong for the sort
     u64 *dcell;     // [cap_ops] cell of each contended-cell id

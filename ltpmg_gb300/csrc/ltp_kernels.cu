@@ -138,6 +138,14 @@ __device__ __forceinline__ int32_t *cell_ptr(const TablesDev &T, u64 cell) {
     return t.data + (u64)col * t.rows_cap + row;
 }
 
+// Is the cell contended (touched twice and written)?  If so, *m is its dense id.
+__device__ __forceinline__ bool contended_id(const Scratch &s, u64 cell, u32 *m) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(&s.words[cell >> 5]));
+    const u32 cw = v.y & v.z, bit = 1u << (cell & 31);
+    *m = v.w + __popc(cw & (bit - 1u));
+    return (cw & bit) != 0;
+}
+
 __device__ __forceinline__ u32 op_tid(const BatchDev &b, u64 i) {
     return b.ops_per_txn ? (u32)(i / b.ops_per_txn) : b.op_txn[i];
 }
@@ -181,11 +189,18 @@ __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch
             const int leader = __ffs(peers) - 1;
             bool first = false;
             if (valid && lane == leader) {
-                u32 old = atomicOr(&s.touch[word], obits);
-                first = (old == 0u);
-                u32 m = (old & obits) | dup;
-                if (m) atomicOr(&s.multi[word], m);
-                if (wb) atomicOr(&s.wbits[word], wb);
+                // cached look first: under skew most groups find their bits set
+                // already and skip the atomics (a stale view only costs an atomic)
+                WordState *ws = &s.words[word];
+                const uint4 seen = *reinterpret_cast<const uint4 *>(ws);
+                u32 old = seen.x;
+                if (obits & ~seen.x) {
+                    old = atomicOr(&ws->touch, obits);
+                    first = (old == 0u);
+                }
+                const u32 m = (old & obits) | dup;
+                if (m & ~seen.y) atomicOr(&ws->multi, m);
+                if (wb & ~seen.z) atomicOr(&ws->wbits, wb);
             }
             const u32 fb = __ballot_sync(FULL_MASK, first);
             if (fb) {
@@ -220,7 +235,12 @@ __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Count
         for (int k = 0; k < kIdsIpt; k++) {
             u64 j = t0 + k;
             wd[k] = j < n ? s.tw_list[j] : 0u;
-            cw[k] = j < n ? (s.multi[wd[k]] & s.wbits[wd[k]]) : 0u;
+            if (j < n) {
+                const uint4 v = *reinterpret_cast<const uint4 *>(&s.words[wd[k]]);
+                cw[k] = v.y & v.z;
+            } else {
+                cw[k] = 0u;
+            }
             cnt += __popc(cw[k]);
         }
         // block exclusive scan of cnt
@@ -249,7 +269,7 @@ __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Count
         for (int k = 0; k < kIdsIpt; k++) {
             u64 j = t0 + k;
             if (j < n) {
-                s.cwx[wd[k]] = (pre << 32) | cw[k];
+                s.words[wd[k]].prefix = (u32)pre;
                 u32 bits = cw[k];
                 while (bits) {
                     int bpos = __ffs(bits) - 1;
@@ -267,8 +287,15 @@ __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Count
 }
 
 // ============================================================================
-// classify (ordered rule): execute uncontended ops, compact contended ones
+// classify (ordered rule): execute uncontended ops, compact contended ones,
+// and histogram the contended ids' radix digits for the sort
 // ============================================================================
+__device__ __forceinline__ int sort_passes_dev(u32 M) {
+    if (M <= 1) return 0;
+    const int bits = 32 - __clz(M - 1);
+    return (bits + 7) / 8;
+}
+
 template <int BLOCK, int IPT>
 __global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
     if (ctr->err) return;
@@ -277,8 +304,12 @@ __global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scr
     const u64 n = b.n_ops;
     const u32 tiles = (u32)((n + TILE - 1) / TILE);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int passes = sort_passes_dev(ctr->M);
     __shared__ u32 s_wcnt[NW];
     __shared__ u64 s_prefix;
+    __shared__ u32 s_hist[kMaxPasses][256];
+    for (int i = threadIdx.x; i < kMaxPasses * 256; i += BLOCK) (&s_hist[0][0])[i] = 0;
+    __syncthreads();
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_CLASSIFY);
         if (tile >= tiles) break;
@@ -291,36 +322,51 @@ __global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scr
             key[k] = i < n ? __ldcs(&b.keys[i]) : 0;
             w[k] = i < n ? __ldcs(&b.opw[i]) : 0xFFFFFFFFu;
         }
-        u64 cw[IPT];
         OpRef r[IPT];
+        uint4 ws[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             u64 i = wbase + (u64)k * 32 + lane;
             r[k] = decode_op(T, key[k], w[k]);
             r[k].valid = r[k].valid && i < n;
-            cw[k] = r[k].valid ? s.cwx[r[k].cell >> 5] : 0ull;
+            ws[k] = r[k].valid ? __ldg(reinterpret_cast<const uint4 *>(&s.words[r[k].cell >> 5])) : make_uint4(0, 0, 0, 0);
         }
         u64 rec[IPT];
         u32 wcnt = 0, lpos[IPT];
         bool con[IPT];
+        int32_t val[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             const u32 bit = 1u << (r[k].cell & 31);
-            con[k] = r[k].valid && ((u32)cw[k] & bit);
+            const u32 cw = ws[k].y & ws[k].z;
+            con[k] = r[k].valid && (cw & bit);
+            // an uncontended read's cell is never written in this batch
+            if (r[k].valid && !con[k])
+                val[k] = opw_kind(w[k]) == LTP_OP_ADD ? *r[k].ptr : __ldg(r[k].ptr);
+        }
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            const u32 bit = 1u << (r[k].cell & 31);
+            const u32 cw = ws[k].y & ws[k].z;
             const u64 i = wbase + (u64)k * 32 + lane;
             if (r[k].valid && !con[k]) {
-                int32_t v = *r[k].ptr;
+                int32_t v = val[k];
                 if (opw_kind(w[k]) == LTP_OP_ADD) {
                     v = (int32_t)((u32)v + (u32)opw_imm(w[k]));
                     *r[k].ptr = v;
                 }
                 __stcs(&b.out[i], v);
             }
-            const u32 m = (u32)(cw[k] >> 32) + __popc((u32)cw[k] & (bit - 1u));
+            const u32 m = ws[k].w + __popc(cw & (bit - 1u));
             rec[k] = ((u64)m << 32) | ((u64)(opw_kind(w[k]) == LTP_OP_ADD) << 31) | (u64)(u32)i;
             const u32 bal = __ballot_sync(FULL_MASK, con[k]);
             lpos[k] = wcnt + __popc(bal & lanemask_lt());
             wcnt += __popc(bal);
+            for (int p = 0; p < passes; p++) {  // digit histograms for the radix sort
+                const u32 d = con[k] ? (m >> (8 * p)) & 255u : 256u;
+                const u32 peers = __match_any_sync(FULL_MASK, d);
+                if (con[k] && lane == __ffs(peers) - 1) atomicAdd(&s_hist[p][d], (u32)__popc(peers));
+            }
         }
         if (lane == 0) s_wcnt[warp] = wcnt;
         __syncthreads();
@@ -342,44 +388,18 @@ __global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scr
             if (con[k]) s.list[0][pbase + lpos[k]] = rec[k];
         __syncthreads();
     }
-}
-
-// ============================================================================
-// sort: stable LSD radix sort of the contended records by id (8-bit digits)
-// ============================================================================
-__host__ __device__ __forceinline__ int sort_passes(u32 M) {
-    if (M <= 1) return 0;
-    int bits = 32 - __builtin_clz(M - 1);
-    return (bits + 7) / 8;
-}
-__device__ __forceinline__ int sort_passes_dev(u32 M) {
-    if (M <= 1) return 0;
-    int bits = 32 - __clz(M - 1);
-    return (bits + 7) / 8;
-}
-
-__global__ void __launch_bounds__(256) k_sort_hist(Scratch s, Counters *ctr) {
-    if (ctr->err) return;
-    const int passes = sort_passes_dev(ctr->M);
-    if (passes == 0) return;
-    const u64 n = ctr->n_c;
-    __shared__ u32 sh[4][256];
-    for (int p = 0; p < 4; p++) sh[p][threadIdx.x] = 0;
-    __syncthreads();
-    for (u64 i = (u64)blockIdx.x * 256 + threadIdx.x; i - threadIdx.x < n; i += (u64)gridDim.x * 256) {
-        const bool v = i < n;
-        const u32 id = v ? (u32)(s.list[0][i] >> 32) : 0u;
-        for (int p = 0; p < passes; p++) {
-            u32 d = v ? (id >> (8 * p)) & 255u : 256u;
-            u32 peers = __match_any_sync(FULL_MASK, d);
-            if (v && (threadIdx.x & 31) == (u32)(__ffs(peers) - 1)) atomicAdd(&sh[p][d], (u32)__popc(peers));
-        }
+    for (int i = threadIdx.x; i < passes * 256; i += BLOCK) {
+        const u32 c = (&s_hist[0][0])[i];
+        if (c) atomicAdd(&(&ctr->hist[0][0])[i], c);
     }
-    __syncthreads();
-    for (int p = 0; p < passes; p++)
-        if (sh[p][threadIdx.x]) atomicAdd(&ctr->hist[p][threadIdx.x], sh[p][threadIdx.x]);
 }
 
+// ============================================================================
+// sort: stable LSD radix sort of the contended records by id (8-bit digits);
+// each tile ranks its records per digit, finds its digit offsets by
+// decoupled look-back, stages the records in shared memory in digit order
+// and writes every digit's run with coalesced stores
+// ============================================================================
 template <int P>
 __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *ctr) {
     if (ctr->err) return;
@@ -400,8 +420,10 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
     const u32 tid = threadIdx.x;
     __shared__ u32 s_start[256];
     __shared__ u32 s_whist[NW][256];
-    __shared__ u32 s_base[256];
+    __shared__ u32 s_base[256];   // global position of the tile's first record of each digit
+    __shared__ u32 s_loc[256];    // tile-local position of each digit's first record
     __shared__ u32 s_wsum[NW];
+    __shared__ u64 s_stage[kSortTile];
     {  // global start of every digit: exclusive scan of the histogram
         u32 h = ctr->hist[P][tid];
         u32 incl = h;
@@ -430,7 +452,7 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
 #pragma unroll
         for (int k = 0; k < kSortIpt; k++) {
             u64 i = wbase + (u64)k * 32 + lane;
-            e[k] = i < n ? src[i] : ~0ull;
+            e[k] = i < n ? __ldcs(&src[i]) : ~0ull;
         }
 #pragma unroll
         for (int k = 0; k < kSortIpt; k++) {
@@ -451,6 +473,20 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
             u32 c = s_whist[w][tid];
             s_whist[w][tid] = run;
             run += c;
+        }
+        // tile-local digit starts: exclusive scan of the tile's digit counts
+        {
+            u32 incl = run;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                u32 v = __shfl_up_sync(FULL_MASK, incl, d);
+                if (lane >= d) incl += v;
+            }
+            if (lane == 31) s_wsum[warp] = incl;
+            __syncthreads();
+            u32 off = 0;
+            for (int i = 0; i < warp; i++) off += s_wsum[i];
+            s_loc[tid] = off + incl - run;
         }
         // per-digit decoupled look-back (thread tid owns digit tid)
         u32 excl = 0;
@@ -483,9 +519,16 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
         for (int k = 0; k < kSortIpt; k++) {
             u64 i = wbase + (u64)k * 32 + lane;
             if (i < n) {
-                u32 d = (u32)(e[k] >> shift) & 255u;
-                dst[s_base[d] + s_whist[warp][d] + rank[k]] = e[k];
+                const u32 d = (u32)(e[k] >> shift) & 255u;
+                s_stage[s_loc[d] + s_whist[warp][d] + rank[k]] = e[k];
             }
+        }
+        __syncthreads();
+        const u32 cnt = (u32)min((u64)kSortTile, n - (u64)tile * kSortTile);
+        for (u32 p = tid; p < cnt; p += kSortBlock) {
+            const u64 x = s_stage[p];
+            const u32 d = (u32)(x >> shift) & 255u;
+            dst[s_base[d] + (p - s_loc[d])] = x;
         }
         __syncthreads();
     }
@@ -529,7 +572,7 @@ __global__ void __launch_bounds__(kApplyBlock) k_apply(BatchDev b, TablesDev T, 
             const bool head = v && (i == 0 || (u32)(prev >> 32) != m);
             tail[k] = v && (i + 1 == n || (u32)(next >> 32) != m);
             u32 val = 0;
-            if (v && ((e[k] >> 31) & 1ull)) val = (u32)opw_imm(b.opw[(u32)e[k] & 0x7FFFFFFFu]);
+            if (v && ((e[k] >> 31) & 1ull)) val = (u32)opw_imm(__ldg(&b.opw[(u32)e[k] & 0x7FFFFFFFu]));
             u32 f = head ? 1u : 0u, sum = val;
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
@@ -609,9 +652,9 @@ __global__ void __launch_bounds__(kApplyBlock) k_apply(BatchDev b, TablesDev T, 
             if (i < n) {
                 const u32 m = (u32)(e[k] >> 32);
                 const u32 tot = sf[k] ? sv[k] : sv[k] + carry;
-                const int32_t val = (int32_t)((u32)s.dbase[m] + tot);
+                const int32_t val = (int32_t)((u32)__ldg(&s.dbase[m]) + tot);
                 b.out[(u32)e[k] & 0x7FFFFFFFu] = val;
-                if (tail[k]) *cell_ptr(T, s.dcell[m]) = val;
+                if (tail[k]) *cell_ptr(T, __ldg(&s.dcell[m])) = val;
             }
         }
         __syncthreads();
@@ -621,13 +664,6 @@ __global__ void __launch_bounds__(kApplyBlock) k_apply(BatchDev b, TablesDev T, 
 // ============================================================================
 // priority rule (R1): min writer TID per contended cell, aborts, execute
 // ============================================================================
-__device__ __forceinline__ bool contended_id(const Scratch &s, u64 cell, u32 *m) {
-    const u64 cw = s.cwx[cell >> 5];
-    const u32 bit = 1u << (cell & 31);
-    *m = (u32)(cw >> 32) + __popc((u32)cw & (bit - 1u));
-    return ((u32)cw & bit) != 0;
-}
-
 __global__ void __launch_bounds__(256) k_r1_minw(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
     if (ctr->err) return;
     const u64 n = b.n_ops;
@@ -706,10 +742,7 @@ __global__ void __launch_bounds__(256) k_finish(BatchDev b, Scratch s, Counters 
     const u64 gsz = (u64)gridDim.x * 256, g0 = (u64)blockIdx.x * 256 + threadIdx.x;
     const u64 ntw = ctr->n_tw;
     for (u64 j = g0; j < ntw; j += gsz) {
-        const u32 w = s.tw_list[j];
-        s.touch[w] = 0;
-        s.multi[w] = 0;
-        s.wbits[w] = 0;
+        *reinterpret_cast<uint4 *>(&s.words[s.tw_list[j]]) = make_uint4(0, 0, 0, 0);
     }
     const u64 t_ids = (ntw + kIdsTile - 1) / kIdsTile;
     for (u64 j = g0; j < t_ids; j += gsz) s.st_ids[j] = 0;
@@ -849,7 +882,6 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
             sms = L.num_sms;
         }
         const int gsort = capped(gs, (b.n_ops + kSortTile - 1) / kSortTile);
-        k_sort_hist<<<gstream, 256, 0, L.stream>>>(s, ctr);
         mark_ev(4);
         k_sort_pass<0><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
         mark_ev(5);
@@ -875,9 +907,7 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
 }
 
 cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s) {
-    cudaMemsetAsync(s.touch, 0, s.n_words * 4, st);
-    cudaMemsetAsync(s.multi, 0, s.n_words * 4, st);
-    cudaMemsetAsync(s.wbits, 0, s.n_words * 4, st);
+    cudaMemsetAsync(s.words, 0, s.n_words * sizeof(WordState), st);
     cudaMemsetAsync(s.st_sort[0], 0, s.cap_sort_tiles * 256 * 4, st);
     cudaMemsetAsync(s.st_sort[1], 0, s.cap_sort_tiles * 256 * 4, st);
     cudaMemsetAsync(s.st_ids, 0, s.cap_tiles * 8, st);
