@@ -152,14 +152,35 @@ __device__ __forceinline__ u32 op_tid(const BatchDev &b, u64 i) {
 
 // ============================================================================
 // mark: read/write-set bitmaps
+//
+// Each tile of BLOCK*IPT ops is staged in a shared-memory hash keyed by
+// bitmap word: every op ORs its cell bit into the word's "touched" mask and,
+// when the bit was already there, into its "touched twice" mask; RMW ops also
+// set the "written" mask.  The tile then issues one global atomicOr per
+// distinct word and flag -- under Zipf skew a hot word costs one atomic per
+// tile instead of one per op, which removes the same-address serialisation
+// at L2 that otherwise dominates the batch.
 // ============================================================================
+constexpr u32 kEmptyKey = 0xFFFFFFFFu;
+
+__device__ __forceinline__ u32 hash_word(u32 w) { return (w * 0x9E3779B1u) ^ (w >> 15); }
+
 template <int BLOCK, int IPT>
 __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
     if (ctr->err) return;
+    constexpr u32 TILE = (u32)BLOCK * IPT;
+    constexpr u32 H = 2 * TILE;  // at most TILE distinct words: load factor <= 1/2
+    extern __shared__ u32 mark_smem[];  // 4 * H words (dynamic: up to 128 KB)
+    u32 *hk = mark_smem, *ht = hk + H, *hd = ht + H, *hw = hd + H;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const u64 n = b.n_ops;
-    constexpr u64 TILE = (u64)BLOCK * IPT;
     for (u64 base = (u64)blockIdx.x * TILE; base < n; base += (u64)gridDim.x * TILE) {
+        for (u32 i = threadIdx.x; i < H; i += BLOCK) {
+            hk[i] = kEmptyKey;
+            ht[i] = 0u;
+            hd[i] = 0u;
+            hw[i] = 0u;
+        }
         const u64 wbase = base + (u64)warp * 32 * IPT;
         u64 key[IPT];
         u32 w[IPT];
@@ -169,47 +190,50 @@ __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch
             key[k] = i < n ? b.keys[i] : 0;
             w[k] = i < n ? b.opw[i] : 0xFFFFFFFFu;
         }
+        __syncthreads();
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
-            u64 i = wbase + (u64)k * 32 + lane;
+            const u64 i = wbase + (u64)k * 32 + lane;
+            if (i >= n) continue;
             OpRef r = decode_op(T, key[k], w[k]);
-            bool in = i < n;
-            if (in && !r.valid) {  // record the lowest malformed op (stored inverted)
+            if (!r.valid) {  // record the lowest malformed op (stored inverted)
                 atomicMax(&ctr->bad_op, ~i);
                 set_err(ctr, LTP_E_BADARG);
+                continue;
             }
-            const bool valid = in && r.valid;
-            const u64 word = valid ? (r.cell >> 5) : ~0ull;
-            const u32 bit = 1u << (r.cell & 31);
-            const u32 peers = __match_any_sync(FULL_MASK, word);
-            const u32 same = __match_any_sync(FULL_MASK, valid ? r.cell : ~0ull);
-            const u32 obits = __reduce_or_sync(peers, valid ? bit : 0u);
-            const u32 dup = __reduce_or_sync(peers, (valid && __popc(same) > 1) ? bit : 0u);
-            const u32 wb = __reduce_or_sync(peers, (valid && opw_kind(w[k]) != LTP_OP_READ) ? bit : 0u);
-            const int leader = __ffs(peers) - 1;
+            const u32 word = (u32)(r.cell >> 5), bit = 1u << (r.cell & 31);
+            u32 slot = hash_word(word) & (H - 1);
+            for (u32 probe = 0; probe < H; probe++) {
+                u32 cur = hk[slot];
+                if (cur == kEmptyKey) cur = atomicCAS(&hk[slot], kEmptyKey, word);
+                if (cur == kEmptyKey || cur == word) break;
+                slot = (slot + 1) & (H - 1);
+            }
+            if (atomicOr(&ht[slot], bit) & bit) atomicOr(&hd[slot], bit);
+            if (opw_kind(w[k]) != LTP_OP_READ) atomicOr(&hw[slot], bit);
+        }
+        __syncthreads();
+        for (u32 j = threadIdx.x; j < H; j += BLOCK) {  // uniform trip count per warp
+            const u32 word = hk[j];
             bool first = false;
-            if (valid && lane == leader) {
-                // cached look first: under skew most groups find their bits set
-                // already and skip the atomics (a stale view only costs an atomic)
+            if (word != kEmptyKey) {
                 WordState *ws = &s.words[word];
-                const uint4 seen = *reinterpret_cast<const uint4 *>(ws);
-                u32 old = seen.x;
-                if (obits & ~seen.x) {
-                    old = atomicOr(&ws->touch, obits);
-                    first = (old == 0u);
-                }
-                const u32 m = (old & obits) | dup;
-                if (m & ~seen.y) atomicOr(&ws->multi, m);
-                if (wb & ~seen.z) atomicOr(&ws->wbits, wb);
+                const u32 t = ht[j];
+                const u32 old = atomicOr(&ws->touch, t);
+                first = old == 0u;
+                const u32 m = (old & t) | hd[j];
+                if (m) atomicOr(&ws->multi, m);
+                if (hw[j]) atomicOr(&ws->wbits, hw[j]);
             }
             const u32 fb = __ballot_sync(FULL_MASK, first);
             if (fb) {
                 u64 pos0 = 0;
                 if (lane == 0) pos0 = atomicAdd(&ctr->n_tw, (u64)__popc(fb));
                 pos0 = __shfl_sync(FULL_MASK, pos0, 0);
-                if (first) s.tw_list[pos0 + __popc(fb & lanemask_lt())] = (u32)word;
+                if (first) s.tw_list[pos0 + __popc(fb & lanemask_lt())] = word;
             }
         }
+        __syncthreads();
     }
 }
 
@@ -796,9 +820,9 @@ __global__ void k_expand_op_txn(const u32 *txn_first, u64 n_txns, u32 *op_txn) {
 // host-side launch plans
 // ============================================================================
 template <typename K>
-static int occ_grid(K kernel, int block, int num_sms) {
+static int occ_grid(K kernel, int block, int num_sms, size_t dyn_smem = 0) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, dyn_smem);
     if (per_sm < 1) per_sm = 1;
     return per_sm * num_sms;
 }
@@ -806,9 +830,11 @@ static int occ_grid(K kernel, int block, int num_sms) {
 template <int BLOCK, int IPT>
 struct Front {
     static int g_mark, g_cls, sms;
+    static constexpr size_t kMarkSmem = 4ull * 2 * BLOCK * IPT * sizeof(u32);
     static void grids(int num_sms) {
         if (sms != num_sms) {
-            g_mark = occ_grid(k_mark<BLOCK, IPT>, BLOCK, num_sms);
+            cudaFuncSetAttribute(k_mark<BLOCK, IPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMarkSmem);
+            g_mark = occ_grid(k_mark<BLOCK, IPT>, BLOCK, num_sms, kMarkSmem);
             g_cls = occ_grid(k_classify<BLOCK, IPT>, BLOCK, num_sms);
             sms = num_sms;
         }
@@ -817,7 +843,7 @@ struct Front {
         grids(L.num_sms);
         const u64 tiles = (b.n_ops + (u64)BLOCK * IPT - 1) / ((u64)BLOCK * IPT);
         const int g = (int)(tiles < (u64)g_mark ? (tiles ? tiles : 1) : (u64)g_mark);
-        k_mark<BLOCK, IPT><<<g, BLOCK, 0, L.stream>>>(b, T, s, ctr);
+        k_mark<BLOCK, IPT><<<g, BLOCK, kMarkSmem, L.stream>>>(b, T, s, ctr);
     }
     static void classify(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
         grids(L.num_sms);
