@@ -243,6 +243,10 @@ def run_ours(args, cfg):
     nb = cfg["batches"]
     host = gen_batches(cfg, nb, rank)
     ctx = G.Context(device=local, stage_timing=True)
+    if args.tune:
+        blk, ipt = (int(x) for x in args.tune.split(","))
+        for bucket in range(64):
+            ctx.set_tuning(bucket, blk, ipt)
     t = ctx.create_table(cfg["rows"], cfg["cols"])
     ctx.fill_seeded(t, cfg["seed"] + rank)
     dev = []
@@ -352,6 +356,7 @@ def main():
     ap.add_argument("--config", default="zipf", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batches", type=int, default=0, help="resident batches to cycle (default: the config's)")
+    ap.add_argument("--tune", default="", help="block,ipt for every size bucket (default: library tuning)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

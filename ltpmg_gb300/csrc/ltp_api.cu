@@ -200,6 +200,9 @@ int ltp_init(const ltp_config *cfg, ltp_ctx **out) {
     for (int i = 0; i < 64; i++) ctx->tuning[i] = Tuning{256, 4, 32};
     cudaError_t e = cudaSetDevice(cfg->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, cfg->device);
+    // random 4-16 byte gathers dominate: fetch 32-byte sectors, not 64-byte pairs
+    // (a limit of this process's context only)
+    if (e == cudaSuccess) cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, 32);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->ctr, sizeof(Counters));
     if (e == cudaSuccess) e = cudaMemset(ctx->ctr, 0, sizeof(Counters));

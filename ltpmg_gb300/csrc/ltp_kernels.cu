@@ -213,24 +213,34 @@ __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch
             if (opw_kind(w[k]) != LTP_OP_READ) atomicOr(&hw[slot], bit);
         }
         __syncthreads();
-        for (u32 j = threadIdx.x; j < H; j += BLOCK) {  // uniform trip count per warp
-            const u32 word = hk[j];
-            bool first = false;
-            if (word != kEmptyKey) {
-                WordState *ws = &s.words[word];
-                const u32 t = ht[j];
-                const u32 old = atomicOr(&ws->touch, t);
-                first = old == 0u;
-                const u32 m = (old & t) | hd[j];
-                if (m) atomicOr(&ws->multi, m);
-                if (hw[j]) atomicOr(&ws->wbits, hw[j]);
+        // flush: every thread issues the touch atomics of all its slots before
+        // consuming any result, so the returning atomics overlap
+        constexpr int SPT = H / BLOCK;
+        u32 fw[SPT], ft[SPT], old[SPT];
+#pragma unroll
+        for (int q = 0; q < SPT; q++) {
+            const u32 j = threadIdx.x + q * BLOCK;
+            fw[q] = hk[j];
+            ft[q] = ht[j];
+        }
+#pragma unroll
+        for (int q = 0; q < SPT; q++)
+            old[q] = fw[q] != kEmptyKey ? atomicOr(&s.words[fw[q]].touch, ft[q]) : 1u;
+#pragma unroll
+        for (int q = 0; q < SPT; q++) {
+            const u32 j = threadIdx.x + q * BLOCK;
+            const bool first = old[q] == 0u;
+            if (fw[q] != kEmptyKey) {
+                const u32 m = (old[q] & ft[q]) | hd[j];
+                if (m) atomicOr(&s.words[fw[q]].multi, m);
+                if (hw[j]) atomicOr(&s.words[fw[q]].wbits, hw[j]);
             }
             const u32 fb = __ballot_sync(FULL_MASK, first);
             if (fb) {
                 u64 pos0 = 0;
                 if (lane == 0) pos0 = atomicAdd(&ctr->n_tw, (u64)__popc(fb));
                 pos0 = __shfl_sync(FULL_MASK, pos0, 0);
-                if (first) s.tw_list[pos0 + __popc(fb & lanemask_lt())] = word;
+                if (first) s.tw_list[pos0 + __popc(fb & lanemask_lt())] = fw[q];
             }
         }
         __syncthreads();
@@ -358,29 +368,12 @@ __global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scr
         u64 rec[IPT];
         u32 wcnt = 0, lpos[IPT];
         bool con[IPT];
-        int32_t val[IPT];
-#pragma unroll
-        for (int k = 0; k < IPT; k++) {
-            const u32 bit = 1u << (r[k].cell & 31);
-            const u32 cw = ws[k].y & ws[k].z;
-            con[k] = r[k].valid && (cw & bit);
-            // an uncontended read's cell is never written in this batch
-            if (r[k].valid && !con[k])
-                val[k] = opw_kind(w[k]) == LTP_OP_ADD ? *r[k].ptr : __ldg(r[k].ptr);
-        }
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             const u32 bit = 1u << (r[k].cell & 31);
             const u32 cw = ws[k].y & ws[k].z;
             const u64 i = wbase + (u64)k * 32 + lane;
-            if (r[k].valid && !con[k]) {
-                int32_t v = val[k];
-                if (opw_kind(w[k]) == LTP_OP_ADD) {
-                    v = (int32_t)((u32)v + (u32)opw_imm(w[k]));
-                    *r[k].ptr = v;
-                }
-                __stcs(&b.out[i], v);
-            }
+            con[k] = r[k].valid && (cw & bit);
             const u32 m = ws[k].w + __popc(cw & (bit - 1u));
             rec[k] = ((u64)m << 32) | ((u64)(opw_kind(w[k]) == LTP_OP_ADD) << 31) | (u64)(u32)i;
             const u32 bal = __ballot_sync(FULL_MASK, con[k]);
@@ -394,7 +387,7 @@ __global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scr
         }
         if (lane == 0) s_wcnt[warp] = wcnt;
         __syncthreads();
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0) {  // the look-back overlaps the other warps' execution below
             u32 run = 0;
             for (int i = 0; i < NW; i++) {
                 u32 c = s_wcnt[i];
@@ -404,6 +397,23 @@ __global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scr
             u64 excl = lookback_sum(s.st_cls, tile, run, ctr);
             s_prefix = excl;
             if (tile == tiles - 1) ctr->n_c = excl + run;
+        }
+        // uncontended ops execute in place; an uncontended read's cell is never
+        // written in this batch, an uncontended RMW is its cell's only op
+        int32_t val[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; k++)
+            if (r[k].valid && !con[k]) val[k] = opw_kind(w[k]) == LTP_OP_ADD ? *r[k].ptr : __ldg(r[k].ptr);
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+            if (r[k].valid && !con[k]) {
+                int32_t v = val[k];
+                if (opw_kind(w[k]) == LTP_OP_ADD) {
+                    v = (int32_t)((u32)v + (u32)opw_imm(w[k]));
+                    *r[k].ptr = v;
+                }
+                __stcs(&b.out[wbase + (u64)k * 32 + lane], v);
+            }
         }
         __syncthreads();
         const u64 pbase = s_prefix + s_wcnt[warp];
