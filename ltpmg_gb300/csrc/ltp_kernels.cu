@@ -99,6 +99,7 @@ __device__ u64 lookback_sum(u64 *status, u32 tile, u64 agg, Counters *ctr) {
                 set_err(ctr, LTP_E_TIMEOUT);
                 return 0;
             }
+            __nanosleep(64);
             continue;
         }
         excl += s & kValMask;
@@ -226,23 +227,46 @@ __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch
 #pragma unroll
         for (int q = 0; q < SPT; q++)
             old[q] = fw[q] != kEmptyKey ? atomicOr(&s.words[fw[q]].touch, ft[q]) : 1u;
+        u32 fmask = 0, nfirst = 0;
 #pragma unroll
         for (int q = 0; q < SPT; q++) {
             const u32 j = threadIdx.x + q * BLOCK;
-            const bool first = old[q] == 0u;
             if (fw[q] != kEmptyKey) {
                 const u32 m = (old[q] & ft[q]) | hd[j];
                 if (m) atomicOr(&s.words[fw[q]].multi, m);
                 if (hw[j]) atomicOr(&s.words[fw[q]].wbits, hw[j]);
-            }
-            const u32 fb = __ballot_sync(FULL_MASK, first);
-            if (fb) {
-                u64 pos0 = 0;
-                if (lane == 0) pos0 = atomicAdd(&ctr->n_tw, (u64)__popc(fb));
-                pos0 = __shfl_sync(FULL_MASK, pos0, 0);
-                if (first) s.tw_list[pos0 + __popc(fb & lanemask_lt())] = fw[q];
+                if (old[q] == 0u) {
+                    fmask |= 1u << q;
+                    nfirst++;
+                }
             }
         }
+        // first-touched words go to the touched-word list with one global
+        // atomic per tile (a per-warp counter on one address serialises)
+        u32 incl = nfirst;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const u32 v = __shfl_up_sync(FULL_MASK, incl, d);
+            if (lane >= d) incl += v;
+        }
+        __shared__ u32 s_wtot[BLOCK / 32];
+        __shared__ u64 s_base;
+        if (lane == 31) s_wtot[warp] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            u32 run = 0;
+            for (int i = 0; i < BLOCK / 32; i++) {
+                const u32 c = s_wtot[i];
+                s_wtot[i] = run;
+                run += c;
+            }
+            s_base = run ? atomicAdd(&ctr->n_tw, (u64)run) : 0ull;
+        }
+        __syncthreads();
+        u64 pos = s_base + s_wtot[warp] + (incl - nfirst);
+#pragma unroll
+        for (int q = 0; q < SPT; q++)
+            if (fmask & (1u << q)) s.tw_list[pos++] = fw[q];
         __syncthreads();
     }
 }
@@ -539,6 +563,7 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
                         set_err(ctr, LTP_E_TIMEOUT);
                         break;
                     }
+                    __nanosleep(64);
                     continue;
                 }
                 excl += st & 0x3FFFFFFFu;
@@ -660,6 +685,7 @@ __global__ void __launch_bounds__(kApplyBlock) k_apply(BatchDev b, TablesDev T, 
                             set_err(ctr, LTP_E_TIMEOUT);
                             break;
                         }
+                        __nanosleep(64);
                         continue;
                     }
                     if (!ef) {
