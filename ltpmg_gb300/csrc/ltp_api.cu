@@ -197,7 +197,7 @@ int ltp_init(const ltp_config *cfg, ltp_ctx **out) {
     ctx->rule = cfg->rule;
     ctx->flags = cfg->flags;
     memset(&ctx->s, 0, sizeof(ctx->s));
-    for (int i = 0; i < 64; i++) ctx->tuning[i] = Tuning{256, 4, 32};
+    for (int i = 0; i < 64; i++) ctx->tuning[i] = Tuning{512, 4, 32};
     cudaError_t e = cudaSetDevice(cfg->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, cfg->device);
     // random 4-16 byte gathers dominate: fetch 32-byte sectors, not 64-byte pairs

@@ -96,14 +96,14 @@ struct Scratch {
     u64 cap_sort_tiles;
 };
 
-constexpr u32 kSortBlock = 256;
-constexpr u32 kSortIpt = 16;
+constexpr u32 kSortBlock = 512;
+constexpr u32 kSortIpt = 8;
 constexpr u32 kSortTile = kSortBlock * kSortIpt;
 constexpr u32 kIdsBlock = 256;
 constexpr u32 kIdsIpt = 8;
 constexpr u32 kIdsTile = kIdsBlock * kIdsIpt;
 constexpr u32 kApplyBlock = 256;
-constexpr u32 kApplyIpt = 16;
+constexpr u32 kApplyIpt = 8;
 constexpr u32 kApplyTile = kApplyBlock * kApplyIpt;
 constexpr u32 kMinTile = 128;  // smallest classify tile (block 128 x 1 op)
 

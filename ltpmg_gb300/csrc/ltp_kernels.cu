@@ -476,33 +476,35 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
     constexpr int NW = kSortBlock / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const u32 tid = threadIdx.x;
+    const bool dt = tid < 256;  // threads 0..255 own one digit each
     __shared__ u32 s_start[256];
-    __shared__ u32 s_whist[NW][256];
+    __shared__ unsigned short s_whist[NW][256];  // per-warp digit counts (<= 32 * kSortIpt)
     __shared__ u32 s_base[256];   // global position of the tile's first record of each digit
     __shared__ u32 s_loc[256];    // tile-local position of each digit's first record
-    __shared__ u32 s_wsum[NW];
+    __shared__ u32 s_wsum[8];
     __shared__ u64 s_stage[kSortTile];
     {  // global start of every digit: exclusive scan of the histogram
-        u32 h = ctr->hist[P][tid];
+        u32 h = dt ? ctr->hist[P][tid] : 0u;
         u32 incl = h;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             u32 v = __shfl_up_sync(FULL_MASK, incl, d);
             if (lane >= d) incl += v;
         }
-        if (lane == 31) s_wsum[warp] = incl;
+        if (dt && lane == 31) s_wsum[warp] = incl;
         __syncthreads();
-        u32 off = 0;
-        for (int i = 0; i < warp; i++) off += s_wsum[i];
-        s_start[tid] = off + incl - h;
+        if (dt) {
+            u32 off = 0;
+            for (int i = 0; i < warp; i++) off += s_wsum[i];
+            s_start[tid] = off + incl - h;
+        }
         __syncthreads();
     }
     const int shift = 32 + 8 * P;
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_SORT0 + P);
         if (tile >= tiles) break;
-#pragma unroll
-        for (int w = 0; w < NW; w++) s_whist[w][tid] = 0;
+        for (u32 i = tid; i < NW * 256; i += kSortBlock) (&s_whist[0][0])[i] = 0;
         __syncthreads();
         const u64 wbase = (u64)tile * kSortTile + (u64)warp * 32 * kSortIpt;
         u64 e[kSortIpt];
@@ -520,17 +522,19 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
             const u32 peers = __match_any_sync(FULL_MASK, d);
             const u32 before = v ? s_whist[warp][d] : 0u;
             __syncwarp();
-            if (v && lane == __ffs(peers) - 1) s_whist[warp][d] = before + __popc(peers);
+            if (v && lane == __ffs(peers) - 1) s_whist[warp][d] = (unsigned short)(before + __popc(peers));
             __syncwarp();
             rank[k] = before + __popc(peers & lanemask_lt());
         }
         __syncthreads();
         u32 run = 0;
+        if (dt) {
 #pragma unroll
-        for (int w = 0; w < NW; w++) {
-            u32 c = s_whist[w][tid];
-            s_whist[w][tid] = run;
-            run += c;
+            for (int w = 0; w < NW; w++) {
+                u32 c = s_whist[w][tid];
+                s_whist[w][tid] = (unsigned short)run;
+                run += c;
+            }
         }
         // tile-local digit starts: exclusive scan of the tile's digit counts
         {
@@ -540,39 +544,43 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
                 u32 v = __shfl_up_sync(FULL_MASK, incl, d);
                 if (lane >= d) incl += v;
             }
-            if (lane == 31) s_wsum[warp] = incl;
+            if (dt && lane == 31) s_wsum[warp] = incl;
             __syncthreads();
-            u32 off = 0;
-            for (int i = 0; i < warp; i++) off += s_wsum[i];
-            s_loc[tid] = off + incl - run;
+            if (dt) {
+                u32 off = 0;
+                for (int i = 0; i < warp; i++) off += s_wsum[i];
+                s_loc[tid] = off + incl - run;
+            }
         }
         // per-digit decoupled look-back (thread tid owns digit tid)
-        u32 excl = 0;
-        u32 *slot = &status[(u64)tile * 256 + tid];
-        if (tile == 0) {
-            st_release32(slot, (2u << 30) | run);
-        } else {
-            st_release32(slot, (1u << 30) | run);
-            long long t = (long long)tile - 1;
-            u64 t0 = gtimer();
-            while (t >= 0) {
-                u32 st = ld_acquire32(&status[(u64)t * 256 + tid]);
-                u32 f = st >> 30;
-                if (f == 0) {
-                    if (gtimer() - t0 > kSpinLimitNs) {
-                        set_err(ctr, LTP_E_TIMEOUT);
-                        break;
+        if (dt) {
+            u32 excl = 0;
+            u32 *slot = &status[(u64)tile * 256 + tid];
+            if (tile == 0) {
+                st_release32(slot, (2u << 30) | run);
+            } else {
+                st_release32(slot, (1u << 30) | run);
+                long long t = (long long)tile - 1;
+                u64 t0 = gtimer();
+                while (t >= 0) {
+                    u32 st = ld_acquire32(&status[(u64)t * 256 + tid]);
+                    u32 f = st >> 30;
+                    if (f == 0) {
+                        if (gtimer() - t0 > kSpinLimitNs) {
+                            set_err(ctr, LTP_E_TIMEOUT);
+                            break;
+                        }
+                        __nanosleep(64);
+                        continue;
                     }
-                    __nanosleep(64);
-                    continue;
+                    excl += st & 0x3FFFFFFFu;
+                    if (f == 2) break;
+                    t--;
                 }
-                excl += st & 0x3FFFFFFFu;
-                if (f == 2) break;
-                t--;
+                st_release32(slot, (2u << 30) | (excl + run));
             }
-            st_release32(slot, (2u << 30) | (excl + run));
+            s_base[tid] = s_start[tid] + excl;
         }
-        s_base[tid] = s_start[tid] + excl;
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < kSortIpt; k++) {
