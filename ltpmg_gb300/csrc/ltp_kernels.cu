@@ -348,9 +348,12 @@ __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Count
 // classify (ordered rule): execute uncontended ops, compact contended ones,
 // and histogram the contended ids' radix digits for the sort
 // ============================================================================
+// Radix passes over the contended ids: 8 bits each, at least one pass as soon
+// as there is a contended cell (the first pass also gathers the per-tile
+// regions written by classify into one dense list).
 __device__ __forceinline__ int sort_passes_dev(u32 M) {
-    if (M <= 1) return 0;
-    const int bits = 32 - __clz(M - 1);
+    if (M == 0) return 0;
+    const int bits = M == 1 ? 1 : 32 - __clz(M - 1);
     return (bits + 7) / 8;
 }
 
@@ -364,7 +367,6 @@ __global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scr
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int passes = sort_passes_dev(ctr->M);
     __shared__ u32 s_wcnt[NW];
-    __shared__ u64 s_prefix;
     __shared__ u32 s_hist[kMaxPasses][256];
     for (int i = threadIdx.x; i < kMaxPasses * 256; i += BLOCK) (&s_hist[0][0])[i] = 0;
     __syncthreads();
@@ -411,16 +413,18 @@ __global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scr
         }
         if (lane == 0) s_wcnt[warp] = wcnt;
         __syncthreads();
-        if (threadIdx.x == 0) {  // the look-back overlaps the other warps' execution below
+        if (threadIdx.x == 0) {
+            // the tile's contended records go to its own region of the list
+            // (tile * TILE onward), in op order; the radix sort's first pass
+            // reads the regions in tile order, so no cross-tile scan is needed
             u32 run = 0;
             for (int i = 0; i < NW; i++) {
                 u32 c = s_wcnt[i];
                 s_wcnt[i] = run;
                 run += c;
             }
-            u64 excl = lookback_sum(s.st_cls, tile, run, ctr);
-            s_prefix = excl;
-            if (tile == tiles - 1) ctr->n_c = excl + run;
+            s.st_cls[tile] = run;
+            if (run) atomicAdd(&ctr->n_c, (u64)run);
         }
         // uncontended ops execute in place; an uncontended read's cell is never
         // written in this batch, an uncontended RMW is its cell's only op
@@ -440,7 +444,7 @@ __global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scr
             }
         }
         __syncthreads();
-        const u64 pbase = s_prefix + s_wcnt[warp];
+        const u64 pbase = (u64)tile * TILE + s_wcnt[warp];
 #pragma unroll
         for (int k = 0; k < IPT; k++)
             if (con[k]) s.list[0][pbase + lpos[k]] = rec[k];
@@ -459,18 +463,23 @@ __global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scr
 // and writes every digit's run with coalesced stores
 // ============================================================================
 template <int P>
-__global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *ctr) {
+__global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *ctr, u64 n_ops, u32 seg_tile) {
     if (ctr->err) return;
     const int passes = sort_passes_dev(ctr->M);
     if (P >= passes) return;
     const u64 n = ctr->n_c;
-    const u32 tiles = (u32)((n + kSortTile - 1) / kSortTile);
+    // pass 0 reads classify's per-tile regions: R regions of seg_tile slots per sort tile
+    const u32 R = P == 0 ? kSortTile / seg_tile : 1;
+    const u32 tiles = P == 0 ? (u32)((n_ops + (u64)seg_tile * R - 1) / ((u64)seg_tile * R))
+                             : (u32)((n + kSortTile - 1) / kSortTile);
+    __shared__ u32 s_segoff[kSortTile / kMinTile + 1];
     const u64 *src = s.list[P & 1];
     u64 *dst = s.list[(P + 1) & 1];
     u32 *status = s.st_sort[P & 1];
     if (P >= 1) {  // the previous pass is complete: recycle its look-back slots
         u32 *other = s.st_sort[(P + 1) & 1];
-        for (u64 j = (u64)blockIdx.x * kSortBlock + threadIdx.x; j < (u64)tiles * 256; j += (u64)gridDim.x * kSortBlock)
+        const u64 prev_tiles = P == 1 ? (n_ops + kSortTile - 1) / kSortTile + 1 : tiles;
+        for (u64 j = (u64)blockIdx.x * kSortBlock + threadIdx.x; j < prev_tiles * 256; j += (u64)gridDim.x * kSortBlock)
             other[j] = 0;
     }
     constexpr int NW = kSortBlock / 32;
@@ -506,18 +515,48 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
         if (tile >= tiles) break;
         for (u32 i = tid; i < NW * 256; i += kSortBlock) (&s_whist[0][0])[i] = 0;
         __syncthreads();
-        const u64 wbase = (u64)tile * kSortTile + (u64)warp * 32 * kSortIpt;
+        u32 tcnt;
+        if (P == 0) {
+            if (tid == 0) {
+                u32 run = 0;
+                const u64 first = (u64)tile * R;
+                for (u32 r = 0; r < R; r++) {
+                    s_segoff[r] = run;
+                    if ((first + r) * seg_tile < n_ops) run += (u32)s.st_cls[first + r];
+                }
+                s_segoff[R] = run;
+            }
+            __syncthreads();
+            tcnt = s_segoff[R];
+        } else {
+            tcnt = (u32)min((u64)kSortTile, n - (u64)tile * kSortTile);
+        }
+        const u32 lbase = (u32)warp * 32 * kSortIpt;
         u64 e[kSortIpt];
         u32 rank[kSortIpt];
 #pragma unroll
         for (int k = 0; k < kSortIpt; k++) {
-            u64 i = wbase + (u64)k * 32 + lane;
-            e[k] = i < n ? __ldcs(&src[i]) : ~0ull;
+            const u32 li = lbase + (u32)k * 32 + lane;
+            e[k] = ~0ull;
+            if (li < tcnt) {
+                u64 addr;
+                if (P == 0) {  // locate the region holding local element li
+                    u32 lo = 0, hi = R;
+                    while (hi - lo > 1) {
+                        const u32 mid = (lo + hi) >> 1;
+                        if (s_segoff[mid] <= li) lo = mid;
+                        else hi = mid;
+                    }
+                    addr = ((u64)tile * R + lo) * seg_tile + (li - s_segoff[lo]);
+                } else {
+                    addr = (u64)tile * kSortTile + li;
+                }
+                e[k] = __ldcs(&src[addr]);
+            }
         }
 #pragma unroll
         for (int k = 0; k < kSortIpt; k++) {
-            u64 i = wbase + (u64)k * 32 + lane;
-            const bool v = i < n;
+            const bool v = lbase + (u32)k * 32 + lane < tcnt;
             const u32 d = v ? (u32)(e[k] >> shift) & 255u : 256u;
             const u32 peers = __match_any_sync(FULL_MASK, d);
             const u32 before = v ? s_whist[warp][d] : 0u;
@@ -584,15 +623,13 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < kSortIpt; k++) {
-            u64 i = wbase + (u64)k * 32 + lane;
-            if (i < n) {
+            if (lbase + (u32)k * 32 + lane < tcnt) {
                 const u32 d = (u32)(e[k] >> shift) & 255u;
                 s_stage[s_loc[d] + s_whist[warp][d] + rank[k]] = e[k];
             }
         }
         __syncthreads();
-        const u32 cnt = (u32)min((u64)kSortTile, n - (u64)tile * kSortTile);
-        for (u32 p = tid; p < cnt; p += kSortBlock) {
+        for (u32 p = tid; p < tcnt; p += kSortBlock) {
             const u64 x = s_stage[p];
             const u32 d = (u32)(x >> shift) & 255u;
             dst[s_base[d] + (p - s_loc[d])] = x;
@@ -814,15 +851,13 @@ __global__ void __launch_bounds__(256) k_finish(BatchDev b, Scratch s, Counters 
     }
     const u64 t_ids = (ntw + kIdsTile - 1) / kIdsTile;
     for (u64 j = g0; j < t_ids; j += gsz) s.st_ids[j] = 0;
-    const u64 t_cls = (b.n_ops + cls_tile - 1) / cls_tile;
-    for (u64 j = g0; j < t_cls; j += gsz) s.st_cls[j] = 0;
     const u64 nc = ctr->n_c;
     const u64 t_apply = (nc + kApplyTile - 1) / kApplyTile;
     for (u64 j = g0; j < t_apply; j += gsz) s.st_apply[j] = 0;
     const int passes = sort_passes_dev(ctr->M);
     if (passes > 0) {
         u32 *st = s.st_sort[(passes - 1) & 1];
-        const u64 t_sort = (nc + kSortTile - 1) / kSortTile;
+        const u64 t_sort = passes == 1 ? (b.n_ops + kSortTile - 1) / kSortTile + 1 : (nc + kSortTile - 1) / kSortTile;
         for (u64 j = g0; j < t_sort * 256; j += gsz) st[j] = 0;
     }
     if (rule == LTP_RULE_PRIORITY) {
@@ -953,13 +988,13 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
         }
         const int gsort = capped(gs, (b.n_ops + kSortTile - 1) / kSortTile);
         mark_ev(4);
-        k_sort_pass<0><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        k_sort_pass<0><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops, L.tune.block * L.tune.ipt);
         mark_ev(5);
-        k_sort_pass<1><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        k_sort_pass<1><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops, L.tune.block * L.tune.ipt);
         mark_ev(6);
-        k_sort_pass<2><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        k_sort_pass<2><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops, L.tune.block * L.tune.ipt);
         mark_ev(7);
-        k_sort_pass<3><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        k_sort_pass<3><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops, L.tune.block * L.tune.ipt);
         mark_ev(8);
         k_apply<<<capped(ga, (b.n_ops + kApplyTile - 1) / kApplyTile), kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
         mark_ev(9);
