@@ -184,6 +184,31 @@ int ltp_get_tuning(ltp_ctx *ctx, uint32_t bucket, ltp_tuning *t);
  * the context stays usable. */
 int ltp_debug_stall_next(ltp_ctx *ctx, uint32_t ms);
 
+/* ---- execution without allocation -------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory -- their process hands all of it to another allocator or reserves
+ * it up front, or an allocation could stall a latency-critical path -- this
+ * runs one batch against ONE column-major int32 table that the caller owns
+ * (table[col * rows_cap + row]), with the batch arrays, op values and
+ * commit vector all in caller-provided device memory, and calls no
+ * cudaMalloc, cudaFree or allocating library routine.  All scratch lives in
+ * one fixed array of LTP_NOALLOC_SCRATCH_BYTES inside the library image,
+ * which every GPU that loads the library holds until the process exits.
+ * Limits: n_ops <= LTP_NOALLOC_MAX_OPS and n_rows * n_cols <=
+ * LTP_NOALLOC_MAX_CELLS, else LTP_E_CAPACITY.  The first call on a device
+ * looks the array's device address up (make that first call before any
+ * stream capture).  Every call shares the array and clears what it needs at
+ * its start; calls that overlap on the GPU race, so serialise them.  The
+ * call waits for its stream and returns the batch's status.  Semantics and
+ * outputs equal ltp_batch_execute's for the same rule and inputs. */
+#define LTP_NOALLOC_MAX_OPS (1ull << 18)
+#define LTP_NOALLOC_MAX_CELLS (1ull << 23)
+#define LTP_NOALLOC_SCRATCH_BYTES 14869760ull
+int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table, uint64_t rows_cap, uint64_t n_rows,
+                        uint32_t n_cols, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
+                        uint64_t n_ops, const uint64_t *keys, const uint32_t *opw, int32_t *out, uint8_t *commit,
+                        void *stream);
+
 #ifdef __cplusplus
 }
 #endif

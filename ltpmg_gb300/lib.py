@@ -103,6 +103,7 @@ def load():
         "ltp_set_tuning": (ci, [vp, u32, ctypes.POINTER(Tuning)]),
         "ltp_get_tuning": (ci, [vp, u32, ctypes.POINTER(Tuning)]),
         "ltp_debug_stall_next": (ci, [vp, u32]),
+        "ltp_execute_noalloc": (ci, [i32, i32, vp, u64, u64, u32, u64, vp, u32, u64, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
