@@ -59,6 +59,13 @@ extern "C" {
 /* opword: bits 0-1 kind, 2-7 column, 8-11 table, 12-31 signed immediate */
 #define LTP_OP_READ 0u
 #define LTP_OP_ADD 1u /* read-modify-write: cell += immediate (two's-complement wrap) */
+/* Insert: appends one row to the op's table.  The op's key is an offset into
+ * the batch's insert payload (ltp_batch_load_payload) where the new row's
+ * n_cols int32 values start; the column and immediate fields are unused.
+ * The new row's id is the table's row count at batch start plus the number
+ * of committed inserts into that table earlier in (TID, op) order; it is the
+ * op's output value.  A new row cannot be named by other ops of its batch. */
+#define LTP_OP_INSERT 2u
 #define LTP_OPW(kind, col, table, imm) \
     ((uint32_t)(kind) | ((uint32_t)(col) << 2) | ((uint32_t)(table) << 8) | (((uint32_t)(imm) & 0xFFFFFu) << 12))
 
@@ -121,6 +128,9 @@ int ltp_sync(ltp_ctx *ctx, void *stream);
 /* ---- tables (GPUdatabase::malloc_global_row / copy_to_global_row,
  *      cuda/src/gpudatabase.cu:9-238, made column-store) ---------------- */
 int ltp_table_create(ltp_ctx *ctx, const ltp_schema *schema, uint64_t rows, uint32_t *table_id);
+/* Same with room for inserts: rows_cap >= rows rows are allocated. */
+int ltp_table_create_cap(ltp_ctx *ctx, const ltp_schema *schema, uint64_t rows, uint64_t rows_cap,
+                         uint32_t *table_id);
 /* Copies rows [row0, row0+n) of one column from host memory (int32). */
 int ltp_table_upload(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, const int32_t *src);
 /* New: the reference never copies tables back (gpudatabase.cu:240-339). */
@@ -139,6 +149,12 @@ int ltp_batch_free(ltp_ctx *ctx, ltp_batch *b);
  * entries; when it is NULL every transaction has ops_per_txn ops. */
 int ltp_batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
                    uint64_t n_ops, const uint64_t *keys, const uint32_t *opw, void *stream);
+/* Asynchronous host->device copy of the batch's insert payload (n int32
+ * values, read by LTP_OP_INSERT ops through their key).  Call after
+ * ltp_batch_load; a batch loaded without a payload has none. */
+int ltp_batch_load_payload(ltp_ctx *ctx, ltp_batch *b, const int32_t *payload, uint64_t n, void *stream);
+/* Current row count of a table (grows with committed inserts); synchronises. */
+int ltp_table_rows(ltp_ctx *ctx, uint32_t table, uint64_t *rows);
 /* Executes one batch against the context's tables (replaces
  * GPUlauncher::txn_kernel_launcher, cuda/src/gpulauncher.cu:755-1116). */
 int ltp_batch_execute(ltp_ctx *ctx, ltp_batch *b, void *stream);
@@ -200,10 +216,11 @@ int ltp_debug_stall_next(ltp_ctx *ctx, uint32_t ms);
  * stream capture).  Every call shares the array and clears what it needs at
  * its start; calls that overlap on the GPU race, so serialise them.  The
  * call waits for its stream and returns the batch's status.  Semantics and
- * outputs equal ltp_batch_execute's for the same rule and inputs. */
+ * outputs equal ltp_batch_execute's for the same rule and inputs (reads and
+ * read-modify-writes; the call takes no insert payload). */
 #define LTP_NOALLOC_MAX_OPS (1ull << 18)
 #define LTP_NOALLOC_MAX_CELLS (1ull << 23)
-#define LTP_NOALLOC_SCRATCH_BYTES 14869760ull
+#define LTP_NOALLOC_SCRATCH_BYTES 15001344ull
 int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table, uint64_t rows_cap, uint64_t n_rows,
                         uint32_t n_cols, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
                         uint64_t n_ops, const uint64_t *keys, const uint32_t *opw, int32_t *out, uint8_t *commit,

@@ -30,6 +30,7 @@ struct ltp_ctx {
     Scratch s;
     uint64_t alloc_words = 0;  // bitmap words currently allocated
     Counters *ctr = nullptr;
+    u64 *rows_now = nullptr;  // [LTP_MAX_TABLES] device row counts
     std::string last_error;
     Tuning tuning[64];
     uint32_t stall_ms_next = 0;
@@ -47,6 +48,8 @@ struct ltp_batch {
     bool loaded = false, executed = false;
     int rule = 0;
     Counters *snap = nullptr;  // device copy of the counters after this batch
+    int32_t *payload = nullptr;
+    uint64_t payload_cap = 0, payload_len = 0;
     cudaEvent_t ev[LTP_N_STAGES];
     bool have_events = false;
 };
@@ -95,6 +98,8 @@ void free_scratch_ops(Scratch &s) {
     cudaFree(s.st_ids);
     cudaFree(s.st_cls);
     cudaFree(s.st_apply);
+    cudaFree(s.st_ins);
+    s.st_ins = nullptr;
     s.tw_list = nullptr;
     s.list[0] = s.list[1] = nullptr;
     s.dcell = nullptr;
@@ -140,6 +145,7 @@ int ensure_scratch(ltp_ctx *ctx, uint64_t n_ops) {
         CK(dalloc(&s.st_ids, tiles));
         CK(dalloc(&s.st_cls, tiles));
         CK(dalloc(&s.st_apply, tiles));
+        CK(dalloc(&s.st_ins, tiles * LTP_MAX_TABLES));
         s.cap_ops = cap;
         s.cap_tiles = tiles;
         s.cap_sort_tiles = stiles;
@@ -153,6 +159,7 @@ TablesDev tables_dev(const ltp_ctx *ctx) {
     TablesDev T;
     memset(&T, 0, sizeof(T));
     T.n = (uint32_t)ctx->tables.size();
+    T.rows_now = ctx->rows_now;
     for (size_t i = 0; i < ctx->tables.size(); i++) T.t[i] = ctx->tables[i].dev;
     return T;
 }
@@ -206,6 +213,8 @@ int ltp_init(const ltp_config *cfg, ltp_ctx **out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->ctr, sizeof(Counters));
     if (e == cudaSuccess) e = cudaMemset(ctx->ctr, 0, sizeof(Counters));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->rows_now, LTP_MAX_TABLES * sizeof(u64));
+    if (e == cudaSuccess) e = cudaMemset(ctx->rows_now, 0, LTP_MAX_TABLES * sizeof(u64));
     if (e != cudaSuccess) {
         ltp_shutdown(ctx);
         return e == cudaErrorMemoryAllocation ? LTP_E_NOMEM : LTP_E_CUDA;
@@ -229,6 +238,7 @@ int ltp_shutdown(ltp_ctx *ctx) {
     free_scratch_ops(ctx->s);
     free_scratch_words(ctx->s);
     cudaFree(ctx->ctr);
+    cudaFree(ctx->rows_now);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return LTP_OK;
@@ -243,18 +253,24 @@ int ltp_sync(ltp_ctx *ctx, void *stream) {
 }
 
 int ltp_table_create(ltp_ctx *ctx, const ltp_schema *schema, uint64_t rows, uint32_t *table_id) {
+    return ltp_table_create_cap(ctx, schema, rows, rows, table_id);
+}
+
+int ltp_table_create_cap(ltp_ctx *ctx, const ltp_schema *schema, uint64_t rows, uint64_t rows_cap,
+                         uint32_t *table_id) {
     if (!ctx || !schema || !table_id) return LTP_E_BADARG;
+    if (rows_cap < rows) return fail(ctx, LTP_E_BADARG, "rows_cap must be >= rows");
     if (schema->n_cols == 0 || schema->n_cols > LTP_MAX_COLS) return fail(ctx, LTP_E_BADARG, "n_cols must be 1..64");
-    if (rows == 0 || rows > (1ull << 40)) return fail(ctx, LTP_E_BADARG, "rows must be 1..2^40");
+    if (rows_cap == 0 || rows_cap > (1ull << 31)) return fail(ctx, LTP_E_BADARG, "rows_cap must be 1..2^31");
     if (ctx->tables.size() >= LTP_MAX_TABLES) return fail(ctx, LTP_E_CAPACITY, "at most 16 tables");
-    const uint64_t cells = rows * schema->n_cols;
+    const uint64_t cells = rows_cap * schema->n_cols;
     if ((ctx->total_cells + cells + 31) / 32 >= (1ull << 32))
         return fail(ctx, LTP_E_CAPACITY, "cell space exceeds 2^37 cells");
     CK(cudaSetDevice(ctx->device));
     TableHost t;
     memset(&t, 0, sizeof(t));
     t.n_cols = schema->n_cols;
-    t.dev.rows_cap = (rows + 63) & ~63ull;  // 256-byte aligned columns
+    t.dev.rows_cap = (rows_cap + 63) & ~63ull;  // 256-byte aligned columns
     t.dev.n_rows = rows;
     t.dev.n_cols = schema->n_cols;
     t.dev.cell_base = ctx->total_cells;
@@ -263,6 +279,8 @@ int ltp_table_create(ltp_ctx *ctx, const ltp_schema *schema, uint64_t rows, uint
     // keep the next table's cells in a fresh bitmap word
     ctx->total_cells += (cells + 31) & ~31ull;
     *table_id = (uint32_t)ctx->tables.size();
+    const u64 r = rows;
+    CK(cudaMemcpy(ctx->rows_now + *table_id, &r, sizeof(u64), cudaMemcpyHostToDevice));
     ctx->tables.push_back(t);
     return LTP_OK;
 }
@@ -272,7 +290,10 @@ static int check_table(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0
     if (table >= ctx->tables.size()) return fail(ctx, LTP_E_BADARG, "no such table");
     const TableHost &t = ctx->tables[table];
     if (col >= t.n_cols) return fail(ctx, LTP_E_BADARG, "no such column");
-    if (row0 > t.dev.n_rows || n > t.dev.n_rows - row0) return fail(ctx, LTP_E_BADARG, "row range out of bounds");
+    u64 rows = 0;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&rows, ctx->rows_now + table, sizeof(u64), cudaMemcpyDeviceToHost));
+    if (row0 > rows || n > rows - row0) return fail(ctx, LTP_E_BADARG, "row range out of bounds");
     return LTP_OK;
 }
 
@@ -306,16 +327,29 @@ int ltp_table_fill_seeded(ltp_ctx *ctx, uint32_t table, uint64_t seed, void *str
     return LTP_OK;
 }
 
+int ltp_table_rows(ltp_ctx *ctx, uint32_t table, uint64_t *rows) {
+    if (!ctx || !rows || table >= ctx->tables.size()) return LTP_E_BADARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaDeviceSynchronize());
+    u64 r = 0;
+    CK(cudaMemcpy(&r, ctx->rows_now + table, sizeof(u64), cudaMemcpyDeviceToHost));
+    *rows = r;
+    return LTP_OK;
+}
+
 int ltp_table_fingerprint(ltp_ctx *ctx, uint32_t table, uint64_t *out) {
     if (!ctx || !out || table >= ctx->tables.size()) return LTP_E_BADARG;
     const TableHost &t = ctx->tables[table];
-    std::vector<int32_t> buf(t.dev.n_rows);
+    uint64_t nrows = 0;
+    int rc0 = ltp_table_rows(ctx, table, &nrows);
+    if (rc0) return rc0;
+    std::vector<int32_t> buf(nrows);
     uint64_t h = 0xCBF29CE484222325ull;
     for (uint32_t c = 0; c < t.n_cols; c++) {
-        int rc = ltp_table_download(ctx, table, c, 0, t.dev.n_rows, buf.data());
+        int rc = ltp_table_download(ctx, table, c, 0, nrows, buf.data());
         if (rc) return rc;
         const uint8_t *p = (const uint8_t *)buf.data();
-        for (uint64_t i = 0; i < t.dev.n_rows * 4; i++) {
+        for (uint64_t i = 0; i < nrows * 4; i++) {
             h ^= p[i];
             h *= 0x100000001B3ull;
         }
@@ -367,6 +401,7 @@ int ltp_batch_free(ltp_ctx *ctx, ltp_batch *b) {
     cudaFree(b->txn_first);
     cudaFree(b->commit);
     cudaFree(b->snap);
+    cudaFree(b->payload);
     if (b->have_events)
         for (int i = 0; i < LTP_N_STAGES; i++) cudaEventDestroy(b->ev[i]);
     delete b;
@@ -395,12 +430,33 @@ int ltp_batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *
     b->n_txns = n_txns;
     b->n_ops = n_ops;
     b->ops_per_txn = txn_first ? 0u : ops_per_txn;
+    b->payload_len = 0;
     if (txn_first) {
         CK(cudaMemcpyAsync(b->txn_first, txn_first, (n_txns + 1) * 4, cudaMemcpyHostToDevice, st));
         CK(launch_expand_op_txn(st, b->txn_first, n_txns, b->op_txn));
     }
     b->loaded = true;
     b->executed = false;
+    return LTP_OK;
+}
+
+int ltp_batch_load_payload(ltp_ctx *ctx, ltp_batch *b, const int32_t *payload, uint64_t n, void *stream) {
+    if (!ctx || !b || (n && !payload)) return LTP_E_BADARG;
+    if (!b->loaded) return fail(ctx, LTP_E_STATE, "load the batch before its payload");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = pick_stream(ctx, stream);
+    if (n > b->payload_cap) {
+        CK(cudaStreamSynchronize(st));
+        cudaFree(b->payload);
+        b->payload = nullptr;
+        b->payload_cap = 0;
+        uint64_t cap = 1024;
+        while (cap < n) cap <<= 1;
+        CK(dalloc(&b->payload, cap));
+        b->payload_cap = cap;
+    }
+    if (n) CK(cudaMemcpyAsync(b->payload, payload, n * 4, cudaMemcpyHostToDevice, st));
+    b->payload_len = n;
     return LTP_OK;
 }
 
@@ -429,6 +485,8 @@ int ltp_batch_execute(ltp_ctx *ctx, ltp_batch *b, void *stream) {
     bd.n_txns = b->n_txns;
     bd.ops_per_txn = b->ops_per_txn;
     bd.pad = 0;
+    bd.payload = b->payload;
+    bd.payload_len = b->payload_len;
     Launch L;
     L.stream = st;
     L.num_sms = ctx->num_sms;

@@ -32,6 +32,7 @@ struct TableDev {
 
 struct TablesDev {
     TableDev t[LTP_MAX_TABLES];
+    u64 *rows_now;  // [LTP_MAX_TABLES] device-resident row counts (grow with inserts)
     u32 n;
     u32 pad;
 };
@@ -44,6 +45,8 @@ struct BatchDev {
     const u32 *op_txn;     // [n_ops] transaction of each op (variable-length batches)
     int32_t *out;          // [n_ops] value after each op
     uint8_t *commit;       // [n_txns]
+    const int32_t *payload;  // insert row images (LTP_OP_INSERT keys index it)
+    u64 payload_len;
     u64 n_ops;
     u64 n_txns;
     u32 ops_per_txn;       // > 0: fixed-length transactions (op_txn unused)
@@ -53,7 +56,7 @@ struct BatchDev {
 constexpr int kMaxPasses = 4;
 
 // Look-back status slots of the kernels that use decoupled look-back.
-enum TileSlot { SLOT_IDS = 0, SLOT_CLASSIFY = 1, SLOT_SORT0 = 2, SLOT_APPLY = 6, SLOT_R1 = 7, N_SLOTS = 8 };
+enum TileSlot { SLOT_IDS = 0, SLOT_CLASSIFY = 1, SLOT_SORT0 = 2, SLOT_APPLY = 6, SLOT_INSERT = 7, N_SLOTS = 8 };
 
 // Per-batch device counters; zeroed by the host before every batch.
 struct Counters {
@@ -67,6 +70,8 @@ struct Counters {
     u32 hist[kMaxPasses][256];  // radix digit histograms of the contended list
     u32 stall;         // polled by the debug stall kernel; never set
     u32 pad;
+    u32 ins_total[LTP_MAX_TABLES];      // insert ops per table in the batch
+    u32 ins_committed[LTP_MAX_TABLES];  // committed inserts per table
 };
 
 // Conflict state of 32 consecutive cells, kept together so that building,
@@ -90,6 +95,7 @@ struct Scratch {
     u64 *st_ids;    // [tiles] id-scan look-back status
     u64 *st_cls;    // [tiles] classify look-back status
     u64 *st_apply;  // [tiles] segmented-apply look-back status
+    u32 *st_ins;    // [tiles * LTP_MAX_TABLES] insert-slot look-back status
     u64 n_words;
     u64 cap_ops;
     u64 cap_tiles;  // tiles of the smallest look-back tile size at cap_ops
@@ -106,6 +112,9 @@ constexpr u32 kApplyBlock = 256;
 constexpr u32 kApplyIpt = 8;
 constexpr u32 kApplyTile = kApplyBlock * kApplyIpt;
 constexpr u32 kMinTile = 128;  // smallest classify tile (block 128 x 1 op)
+constexpr u32 kInsBlock = 256;
+constexpr u32 kInsIpt = 8;
+constexpr u32 kInsTile = kInsBlock * kInsIpt;
 
 struct Tuning {
     u32 block, ipt, word_bits;
@@ -129,5 +138,6 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
 cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s);
 cudaError_t launch_fill_seeded(cudaStream_t st, const TableDev &t, u64 seed);
 cudaError_t launch_expand_op_txn(cudaStream_t st, const u32 *txn_first, u64 n_txns, u32 *op_txn);
+cudaError_t launch_set_u64(cudaStream_t st, u64 *dst, u64 value);
 
 }  // namespace ltp

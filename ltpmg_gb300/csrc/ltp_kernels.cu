@@ -122,7 +122,7 @@ __device__ __forceinline__ OpRef decode_op(const TablesDev &T, u64 key, u32 w) {
     u32 tb = opw_table(w), col = opw_col(w), kind = opw_kind(w);
     r.valid = tb < T.n && kind <= 1u;
     const TableDev &t = T.t[r.valid ? tb : 0];
-    r.valid = r.valid && key < t.n_rows && col < t.n_cols;
+    r.valid = r.valid && key < __ldg(&T.rows_now[r.valid ? tb : 0]) && col < t.n_cols;
     r.cell = r.valid ? t.cell_base + key * t.n_cols + col : ~0ull;
     r.ptr = r.valid ? t.data + (u64)col * t.rows_cap + key : nullptr;
     return r;
@@ -173,6 +173,7 @@ __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch
     constexpr u32 H = 2 * TILE;  // at most TILE distinct words: load factor <= 1/2
     extern __shared__ u32 mark_smem[];  // 4 * H words (dynamic: up to 128 KB)
     u32 *hk = mark_smem, *ht = hk + H, *hd = ht + H, *hw = hd + H;
+    __shared__ u32 s_ins[LTP_MAX_TABLES];  // insert ops of the tile per table
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const u64 n = b.n_ops;
     for (u64 base = (u64)blockIdx.x * TILE; base < n; base += (u64)gridDim.x * TILE) {
@@ -182,6 +183,7 @@ __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch
             hd[i] = 0u;
             hw[i] = 0u;
         }
+        if (threadIdx.x < LTP_MAX_TABLES) s_ins[threadIdx.x] = 0u;
         const u64 wbase = base + (u64)warp * 32 * IPT;
         u64 key[IPT];
         u32 w[IPT];
@@ -196,6 +198,16 @@ __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch
         for (int k = 0; k < IPT; k++) {
             const u64 i = wbase + (u64)k * 32 + lane;
             if (i >= n) continue;
+            if (opw_kind(w[k]) == LTP_OP_INSERT) {  // appends a row: no existing cell to mark
+                const u32 tb = opw_table(w[k]);
+                if (tb < T.n && key[k] + T.t[tb].n_cols <= b.payload_len) {
+                    atomicAdd(&s_ins[tb], 1u);
+                } else {
+                    atomicMax(&ctr->bad_op, ~i);
+                    set_err(ctr, LTP_E_BADARG);
+                }
+                continue;
+            }
             OpRef r = decode_op(T, key[k], w[k]);
             if (!r.valid) {  // record the lowest malformed op (stored inverted)
                 atomicMax(&ctr->bad_op, ~i);
@@ -214,6 +226,7 @@ __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch
             if (opw_kind(w[k]) != LTP_OP_READ) atomicOr(&hw[slot], bit);
         }
         __syncthreads();
+        if (threadIdx.x < LTP_MAX_TABLES && s_ins[threadIdx.x]) atomicAdd(&ctr->ins_total[threadIdx.x], s_ins[threadIdx.x]);
         // flush: every thread issues the touch atomics of all its slots before
         // consuming any result, so the returning atomics overlap
         constexpr int SPT = H / BLOCK;
@@ -282,6 +295,10 @@ __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Count
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ u32 s_warp[kIdsBlock / 32];
     __shared__ u64 s_prefix;
+    if (blockIdx.x == 0 && threadIdx.x < T.n) {  // room for this batch's inserts?
+        const u32 tb = threadIdx.x;
+        if (T.rows_now[tb] + ctr->ins_total[tb] > T.t[tb].rows_cap) set_err(ctr, LTP_E_CAPACITY);
+    }
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_IDS);
         if (tile >= tiles) break;
@@ -841,10 +858,116 @@ __global__ void __launch_bounds__(256) k_r1_exec(BatchDev b, TablesDev T, Scratc
 }
 
 // ============================================================================
+// insert: slots for committed inserts, per table, in (TID, op) order -- a
+// 16-way ordered prefix sum (warp match_any ranks, per-table decoupled
+// look-back) -- then the payload row is copied into its slot
+// ============================================================================
+__global__ void __launch_bounds__(kInsBlock) k_insert(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    if (ctr->err) return;
+    u32 any = 0;
+    for (u32 k = 0; k < T.n; k++) any |= ctr->ins_total[k];
+    if (!any) return;
+    constexpr int NW = kInsBlock / 32;
+    const u64 n = b.n_ops;
+    const u32 tiles = (u32)((n + kInsTile - 1) / kInsTile);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ u32 s_wcnt[NW][LTP_MAX_TABLES];
+    __shared__ u64 s_base[LTP_MAX_TABLES];
+    for (;;) {
+        const u32 tile = claim_tile(ctr, SLOT_INSERT);
+        if (tile >= tiles) break;
+        for (u32 i = threadIdx.x; i < NW * LTP_MAX_TABLES; i += kInsBlock) (&s_wcnt[0][0])[i] = 0;
+        __syncthreads();
+        const u64 wbase = (u64)tile * kInsTile + (u64)warp * 32 * kInsIpt;
+        u32 tb[kInsIpt], lrank[kInsIpt];
+#pragma unroll
+        for (int k = 0; k < kInsIpt; k++) {
+            const u64 i = wbase + (u64)k * 32 + lane;
+            bool ins = false;
+            u32 t = LTP_MAX_TABLES;
+            if (i < n) {
+                const u32 w = b.opw[i];
+                if (opw_kind(w) == LTP_OP_INSERT) {
+                    t = opw_table(w);
+                    ins = b.commit[op_tid(b, i)] != 0;
+                    if (!ins) b.out[i] = 0;
+                }
+            }
+            tb[k] = ins ? t : LTP_MAX_TABLES;
+            const u32 peers = __match_any_sync(FULL_MASK, tb[k]);
+            const u32 before = ins ? s_wcnt[warp][t] : 0u;
+            __syncwarp();
+            if (ins && lane == __ffs(peers) - 1) s_wcnt[warp][t] = before + __popc(peers);
+            __syncwarp();
+            lrank[k] = before + __popc(peers & lanemask_lt());
+        }
+        __syncthreads();
+        if (threadIdx.x < LTP_MAX_TABLES) {  // thread t owns table t
+            const u32 t = threadIdx.x;
+            u32 run = 0;
+            for (int w = 0; w < NW; w++) {
+                const u32 c = s_wcnt[w][t];
+                s_wcnt[w][t] = run;
+                run += c;
+            }
+            u32 *st = s.st_ins;
+            u32 excl = 0;
+            u32 *slot = &st[(u64)tile * LTP_MAX_TABLES + t];
+            if (tile == 0) {
+                st_release32(slot, (2u << 30) | run);
+            } else {
+                st_release32(slot, (1u << 30) | run);
+                long long q = (long long)tile - 1;
+                const u64 t0 = gtimer();
+                while (q >= 0) {
+                    const u32 v = ld_acquire32(&st[(u64)q * LTP_MAX_TABLES + t]);
+                    const u32 f = v >> 30;
+                    if (f == 0) {
+                        if (gtimer() - t0 > kSpinLimitNs) {
+                            set_err(ctr, LTP_E_TIMEOUT);
+                            break;
+                        }
+                        __nanosleep(64);
+                        continue;
+                    }
+                    excl += v & 0x3FFFFFFFu;
+                    if (f == 2) break;
+                    q--;
+                }
+                st_release32(slot, (2u << 30) | (excl + run));
+            }
+            s_base[t] = (t < T.n ? T.rows_now[t] : 0ull) + excl;
+            if (run) atomicAdd(&ctr->ins_committed[t], run);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kInsIpt; k++) {
+            if (tb[k] < LTP_MAX_TABLES) {
+                const u64 i = wbase + (u64)k * 32 + lane;
+                const TableDev &t = T.t[tb[k]];
+                const u64 row = s_base[tb[k]] + s_wcnt[warp][tb[k]] + lrank[k];
+                const int32_t *src = b.payload + b.keys[i];
+                for (u32 c = 0; c < t.n_cols; c++) t.data[(u64)c * t.rows_cap + row] = src[c];
+                b.out[i] = (int32_t)row;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ============================================================================
 // finish: return the scratch to its clean state, count commits
 // ============================================================================
-__global__ void __launch_bounds__(256) k_finish(BatchDev b, Scratch s, Counters *ctr, int rule, u32 cls_tile) {
+__global__ void __launch_bounds__(256) k_finish(BatchDev b, TablesDev T, Scratch s, Counters *ctr, int rule,
+                                                u32 cls_tile) {
     const u64 gsz = (u64)gridDim.x * 256, g0 = (u64)blockIdx.x * 256 + threadIdx.x;
+    u32 any_ins = 0;
+    for (u32 k = 0; k < T.n; k++) any_ins |= ctr->ins_total[k];
+    if (blockIdx.x == 0 && threadIdx.x < T.n && !ctr->err) T.rows_now[threadIdx.x] += ctr->ins_committed[threadIdx.x];
+    if (any_ins) {
+        const u64 t_ins = (b.n_ops + kInsTile - 1) / kInsTile;
+        for (u64 j = g0; j < t_ins * LTP_MAX_TABLES; j += gsz) s.st_ins[j] = 0;
+    }
     const u64 ntw = ctr->n_tw;
     for (u64 j = g0; j < ntw; j += gsz) {
         *reinterpret_cast<uint4 *>(&s.words[s.tw_list[j]]) = make_uint4(0, 0, 0, 0);
@@ -1006,7 +1129,15 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
         k_r1_exec<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
         for (int i = 5; i <= 9; i++) mark_ev(i);
     }
-    k_finish<<<gstream, 256, 0, L.stream>>>(b, s, ctr, L.rule, L.tune.block * L.tune.ipt);
+    {
+        static int gins = 0, sms = 0;
+        if (sms != L.num_sms) {
+            gins = occ_grid(k_insert, kInsBlock, L.num_sms);
+            sms = L.num_sms;
+        }
+        k_insert<<<capped(gins, (b.n_ops + kInsTile - 1) / kInsTile), kInsBlock, 0, L.stream>>>(b, T, s, ctr);
+    }
+    k_finish<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr, L.rule, L.tune.block * L.tune.ipt);
     mark_ev(10);
     return cudaGetLastError();
 }
@@ -1018,11 +1149,19 @@ cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s) {
     cudaMemsetAsync(s.st_ids, 0, s.cap_tiles * 8, st);
     cudaMemsetAsync(s.st_cls, 0, s.cap_tiles * 8, st);
     cudaMemsetAsync(s.st_apply, 0, s.cap_tiles * 8, st);
+    cudaMemsetAsync(s.st_ins, 0, s.cap_tiles * LTP_MAX_TABLES * 4, st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_fill_seeded(cudaStream_t st, const TableDev &t, u64 seed) {
     k_fill_seeded<<<1024, 256, 0, st>>>(t, seed);
+    return cudaGetLastError();
+}
+
+__global__ void k_set_u64(u64 *dst, u64 value) { *dst = value; }
+
+cudaError_t launch_set_u64(cudaStream_t st, u64 *dst, u64 value) {
+    k_set_u64<<<1, 1, 0, st>>>(dst, value);
     return cudaGetLastError();
 }
 

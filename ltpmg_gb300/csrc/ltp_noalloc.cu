@@ -50,7 +50,9 @@ constexpr u64 kOffSort1 = kOffSort0 + align256(kNaSortTiles * 256 * 4);
 constexpr u64 kOffIds = kOffSort1 + align256(kNaSortTiles * 256 * 4);
 constexpr u64 kOffCls = kOffIds + align256(kNaTiles * 8);
 constexpr u64 kOffApply = kOffCls + align256(kNaTiles * 8);
-constexpr u64 kOffCtr = kOffApply + align256(kNaTiles * 8);
+constexpr u64 kOffIns = kOffApply + align256(kNaTiles * 8);
+constexpr u64 kOffRows = kOffIns + align256(kNaTiles * LTP_MAX_TABLES * 4);
+constexpr u64 kOffCtr = kOffRows + align256(LTP_MAX_TABLES * 8);
 constexpr u64 kScratchBytes = kOffCtr + align256(sizeof(Counters));
 
 static_assert(kScratchBytes == LTP_NOALLOC_SCRATCH_BYTES, "header and layout disagree on the scratch size");
@@ -120,6 +122,7 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     s.st_ids = (u64 *)(base + kOffIds);
     s.st_cls = (u64 *)(base + kOffCls);
     s.st_apply = (u64 *)(base + kOffApply);
+    s.st_ins = (u32 *)(base + kOffIns);
     s.n_words = (n_rows * n_cols + 31) / 32 + 1;
     s.cap_ops = kNaMaxOps;
     s.cap_tiles = kNaTiles;
@@ -130,6 +133,9 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     // what must start at zero: this table's conflict words, look-back slots, counters
     cudaError_t e = launch_reset_scratch(st, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, sizeof(Counters), st);
+    // the caller's table holds n_rows rows for this call (no inserts here)
+    u64 *rows_now = (u64 *)(base + kOffRows);
+    if (e == cudaSuccess) e = launch_set_u64(st, rows_now, n_rows);
     if (e == cudaSuccess && n_txns) e = cudaMemsetAsync(commit, 1, n_txns, st);
     if (e == cudaSuccess && txn_first && n_txns) e = launch_expand_op_txn(st, txn_first, n_txns, op_txn);
     if (e != cudaSuccess) return LTP_E_CUDA;
@@ -137,6 +143,7 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     TablesDev T;
     memset(&T, 0, sizeof(T));
     T.n = 1;
+    T.rows_now = rows_now;
     T.t[0].data = table;
     T.t[0].rows_cap = rows_cap;
     T.t[0].n_rows = n_rows;
@@ -153,6 +160,8 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     b.n_txns = n_txns;
     b.ops_per_txn = txn_first ? 0u : ops_per_txn;
     b.pad = 0;
+    b.payload = nullptr;
+    b.payload_len = 0;
     Launch L;
     memset(&L, 0, sizeof(L));
     L.stream = st;

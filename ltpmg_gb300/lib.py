@@ -18,7 +18,7 @@ LTP_OK = 0
 LTP_E_CUDA, LTP_E_CAPACITY, LTP_E_TIMEOUT, LTP_E_BADARG = -1, -2, -3, -4
 LTP_E_DEVICE_ASSERT, LTP_E_NOMEM, LTP_E_STATE = -5, -6, -7
 RULE_ORDERED, RULE_PRIORITY = 0, 1
-OP_READ, OP_ADD = 0, 1
+OP_READ, OP_ADD, OP_INSERT = 0, 1, 2
 FLAG_STAGE_TIMING = 1
 STAGE_NAMES = ["mark", "ids", "classify", "sort_hist", "sort_pass0", "sort_pass1", "sort_pass2", "sort_pass3",
                "apply", "finish", "unused", "total"]
@@ -103,6 +103,11 @@ def load():
         "ltp_set_tuning": (ci, [vp, u32, ctypes.POINTER(Tuning)]),
         "ltp_get_tuning": (ci, [vp, u32, ctypes.POINTER(Tuning)]),
         "ltp_debug_stall_next": (ci, [vp, u32]),
+        "ltp_table_create_cap": (ci, [vp, ctypes.POINTER(Schema), u64, u64, ctypes.POINTER(u32)]),
+        "ltp_table_rows": (ci, [vp, u32, ctypes.POINTER(u64)]),
+        "ltp_batch_load_payload": (ci, [vp, vp, vp, u64, vp]),
+        "ltp_compat_last_status": (ci, []),
+        "ltp_compat_last_error": (ctypes.c_char_p, []),
         "ltp_execute_noalloc": (ci, [i32, i32, vp, u64, u64, u32, u64, vp, u32, u64, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
@@ -217,11 +222,17 @@ class Context:
     def sync(self, stream=None):
         self.check(self.L.ltp_sync(self.h, _stream(stream)))
 
-    def create_table(self, rows, cols):
+    def create_table(self, rows, cols, rows_cap=None):
         tid = ctypes.c_uint32()
-        self.check(self.L.ltp_table_create(self.h, ctypes.byref(Schema(cols, 0)), rows, ctypes.byref(tid)))
+        cap = rows if rows_cap is None else rows_cap
+        self.check(self.L.ltp_table_create_cap(self.h, ctypes.byref(Schema(cols, 0)), rows, cap, ctypes.byref(tid)))
         self.tables.append((rows, cols))
         return tid.value
+
+    def table_rows(self, table):
+        v = ctypes.c_uint64()
+        self.check(self.L.ltp_table_rows(self.h, table, ctypes.byref(v)))
+        return v.value
 
     def upload(self, table, colmajor):
         """colmajor: int32[n_cols, n_rows]."""
@@ -230,7 +241,8 @@ class Context:
             self.check(self.L.ltp_table_upload(self.h, table, c, 0, a.shape[1], _p(a[c])))
 
     def download(self, table):
-        rows, cols = self.tables[table]
+        _, cols = self.tables[table]
+        rows = self.table_rows(table)
         out = np.empty((cols, rows), np.int32)
         for c in range(cols):
             self.check(self.L.ltp_table_download(self.h, table, c, 0, rows, _p(out[c])))
@@ -294,6 +306,11 @@ class Batch:
         self.ctx.check(self.ctx.L.ltp_batch_load(self.ctx.h, self.h, n_txns, _p(txn_first), ops_per_txn, len(keys),
                                                  _p(keys), _p(opw), _stream(stream)))
         self.n_txns, self.n_ops = n_txns, len(keys)
+
+    def load_payload(self, payload, stream=None):
+        payload = np.ascontiguousarray(payload, np.int32)
+        self._keep_payload = payload
+        self.ctx.check(self.ctx.L.ltp_batch_load_payload(self.ctx.h, self.h, _p(payload), len(payload), _stream(stream)))
 
     def execute(self, stream=None):
         self.ctx.check(self.ctx.L.ltp_batch_execute(self.ctx.h, self.h, _stream(stream)))

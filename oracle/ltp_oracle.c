@@ -366,6 +366,80 @@ int ltpo_replay_r0_mt(uint64_t n_rows, uint32_t n_cols, int32_t *tab, uint64_t n
     return 0;
 }
 
+/* General replay: several tables, inserts.  The same serial rule as
+ * ltpo_replay; inserts never conflict (a new row cannot be named by another
+ * op of the same batch) and take the next slot of their table in serial
+ * order, which is "table count + rank among earlier committed inserts". */
+static int check_op_t(uint32_t n_tables, const ltpo_table *T, uint64_t key, uint32_t w, uint64_t payload_len) {
+    uint32_t tb = LTPO_TABLE(w), kind = LTPO_KIND(w);
+    if (tb >= n_tables) return -1;
+    if (kind == 2) return key + T[tb].n_cols <= payload_len ? 0 : -1;
+    if (kind > 2) return -1;
+    if (key >= T[tb].n_rows || LTPO_COL(w) >= T[tb].n_cols) return -1;
+    return 0;
+}
+
+int ltpo_replay_tables(int rule, uint32_t n_tables, ltpo_table *T, uint64_t n_txns, const uint32_t *txn_first,
+                       const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
+                       uint8_t *commit, int32_t *out) {
+    const uint64_t n_ops = txn_first[n_txns];
+    uint64_t ins[16] = {0};
+    for (uint64_t i = 0; i < n_ops; i++) {
+        if (check_op_t(n_tables, T, keys[i], opw[i], payload_len)) return -1;
+        if (LTPO_KIND(opw[i]) == 2) ins[LTPO_TABLE(opw[i])]++;
+    }
+    for (uint32_t k = 0; k < n_tables && k < 16; k++)
+        if (T[k].n_rows + ins[k] > T[k].rows_cap) return -2;
+    if (rule != 0 && rule != 1) return -1;
+    for (uint64_t t = 0; t < n_txns; t++) commit[t] = 1;
+    if (rule == 1) {
+        /* cells are (table, row, col); key them as one 64-bit id per table */
+        minmap_t m;
+        if (minmap_init(&m, n_ops)) return -1;
+        for (uint64_t t = 0; t < n_txns; t++)
+            for (uint64_t i = txn_first[t]; i < txn_first[t + 1]; i++)
+                if (LTPO_KIND(opw[i]) == 1) {
+                    const uint32_t tb = LTPO_TABLE(opw[i]);
+                    uint64_t cid = ((uint64_t)tb << 58) | (keys[i] * T[tb].n_cols + LTPO_COL(opw[i]));
+                    uint32_t *v = minmap_slot(&m, cid, 1);
+                    if ((uint32_t)t < *v) *v = (uint32_t)t;
+                }
+        for (uint64_t t = 0; t < n_txns; t++)
+            for (uint64_t i = txn_first[t]; i < txn_first[t + 1]; i++) {
+                if (LTPO_KIND(opw[i]) == 2) continue;
+                const uint32_t tb = LTPO_TABLE(opw[i]);
+                uint64_t cid = ((uint64_t)tb << 58) | (keys[i] * T[tb].n_cols + LTPO_COL(opw[i]));
+                uint32_t *v = minmap_slot(&m, cid, 0);
+                if (v && *v < (uint32_t)t) commit[t] = 0;
+            }
+        free(m.key);
+        free(m.val);
+    }
+    for (uint64_t t = 0; t < n_txns; t++)
+        for (uint64_t i = txn_first[t]; i < txn_first[t + 1]; i++) {
+            const uint32_t w = opw[i], tb = LTPO_TABLE(w);
+            ltpo_table *tab = &T[tb];
+            if (!commit[t]) {
+                out[i] = 0;
+                continue;
+            }
+            if (LTPO_KIND(w) == 2) {
+                const uint64_t slot = tab->n_rows++;
+                for (uint32_t c = 0; c < tab->n_cols; c++) tab->data[(uint64_t)c * tab->rows_cap + slot] = payload[keys[i] + c];
+                out[i] = (int32_t)slot;
+                continue;
+            }
+            int32_t *cell = &tab->data[(uint64_t)LTPO_COL(w) * tab->rows_cap + keys[i]];
+            int32_t v = *cell;
+            if (LTPO_KIND(w) == 1) {
+                v = (int32_t)((uint32_t)v + (uint32_t)LTPO_IMM(w));
+                *cell = v;
+            }
+            out[i] = v;
+        }
+    return 0;
+}
+
 uint64_t ltpo_fnv1a(const void *data, uint64_t bytes) {
     const uint8_t *p = (const uint8_t *)data;
     uint64_t h = 0xCBF29CE484222325ULL;

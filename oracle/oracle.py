@@ -41,6 +41,11 @@ class YcsbParams(ctypes.Structure):
                 ("read_frac", ctypes.c_double), ("theta", ctypes.c_double)]
 
 
+class OTable(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("rows_cap", ctypes.c_uint64), ("n_rows", ctypes.c_uint64),
+                ("n_cols", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+
+
 _lib = None
 
 
@@ -73,6 +78,8 @@ def lib():
         L.ltpo_replay.argtypes = [ctypes.c_int, u64, u32, vp, u64, vp, vp, vp, vp, vp]
         L.ltpo_replay_r0_mt.restype = ctypes.c_int
         L.ltpo_replay_r0_mt.argtypes = [u64, u32, vp, u64, vp, vp, vp, vp, vp, ctypes.c_int]
+        L.ltpo_replay_tables.restype = ctypes.c_int
+        L.ltpo_replay_tables.argtypes = [ctypes.c_int, u32, ctypes.POINTER(OTable), u64, vp, vp, vp, vp, u64, vp, vp]
         L.ltpo_fnv1a.restype = u64
         L.ltpo_fnv1a.argtypes = [vp, u64]
         L.ltpo_ref_zipf_table.restype = u32
@@ -135,6 +142,27 @@ def replay(rule, tab, txn_first, keys, opw, threads=0):
     if rc != 0:
         raise ValueError("oracle rejected the batch (malformed op)")
     return tab, commit[:n_txns], out[:len(keys)]
+
+
+def replay_tables(rule, tables, txn_first, keys, opw, payload=None):
+    """Multi-table replay with inserts.  tables: list of (data int32[n_cols,
+    rows_cap], n_rows); returns (list of (data, n_rows) after, commit, out)."""
+    datas = [np.ascontiguousarray(d, np.int32).copy() for d, _ in tables]
+    T = (OTable * max(len(tables), 1))()
+    for k, ((_, n), d) in enumerate(zip(tables, datas)):
+        T[k] = OTable(d.ctypes.data, d.shape[1], n, d.shape[0], 0)
+    n_txns = len(txn_first) - 1
+    commit = np.zeros(max(n_txns, 1), np.uint8)
+    out = np.zeros(max(len(keys), 1), np.int32)
+    tf = np.ascontiguousarray(txn_first, np.uint32)
+    k = np.ascontiguousarray(keys, np.uint64)
+    w = np.ascontiguousarray(opw, np.uint32)
+    pl = np.ascontiguousarray(payload if payload is not None else np.zeros(1, np.int32), np.int32)
+    rc = lib().ltpo_replay_tables(rule, len(tables), T, n_txns, _p(tf), _p(k), _p(w), _p(pl),
+                                  0 if payload is None else len(pl), _p(commit), _p(out))
+    if rc != 0:
+        raise ValueError(f"oracle rejected the batch ({rc})")
+    return [(d, T[i].n_rows) for i, d in enumerate(datas)], commit[:n_txns], out[:len(keys)]
 
 
 def fnv1a(a):

@@ -277,3 +277,90 @@ def test_full_size_zipf_batches(lib_loaded, rule):
     batches = [gen(SEED + 2, rows, cols, 16, 16, 0.8, 0.99, b, 1 << 20) for b in range(2 if rule == 0 else 1)]
     stats = run_and_check(rule, rows, cols, batches, seed=SEED + 2, fixed=16, threads=8 if rule == 0 else 0)
     assert stats[0]["contended_ops"] > 0 and stats[0]["contended_cells"] > 0
+
+
+def _insert_batch(rng, tables, n_txns, p_ins=0.3, max_ops=8):
+    """Random multi-table batch mixing reads, RMWs and inserts (payload rows)."""
+    tf, keys, opw, payload = [0], [], [], []
+    for _ in range(n_txns):
+        used = set()
+        for _ in range(int(rng.integers(1, max_ops + 1))):
+            tb = int(rng.integers(0, len(tables)))
+            rows, cols = tables[tb]
+            if rng.random() < p_ins:
+                keys.append(len(payload))
+                opw.append(O.opword(2, 0, tb, 0))
+                payload += [int(x) for x in rng.integers(-1000, 1000, cols)]
+                continue
+            r = int(rng.integers(0, min(rows, 24)) if rng.random() < 0.5 else rng.integers(0, rows))
+            c = int(rng.integers(0, cols))
+            if (tb, r, c) in used:
+                continue
+            used.add((tb, r, c))
+            keys.append(r)
+            opw.append(O.opword(int(rng.random() < 0.4), c, tb, int(rng.integers(-3, 4))))
+        tf.append(len(keys))
+    return (np.array(tf, np.uint32), np.array(keys, np.uint64), np.array(opw, np.uint32),
+            np.array(payload or [0], np.int32))
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+def test_inserts_two_tables_sequence(lib_loaded, rule):
+    rng = np.random.default_rng(42 + rule)
+    shapes = [(500, 3), (64, 5)]
+    with G.Context(device=0, rule=rule) as ctx:
+        ids, ref = [], []
+        for k, (rows, cols) in enumerate(shapes):
+            tid = ctx.create_table(rows, cols, rows_cap=rows + 20000)
+            ctx.fill_seeded(tid, 7 + k)
+            data = np.zeros((cols, rows + 20000), np.int32)
+            data[:, :rows] = O.table_init(7 + k, rows, cols)
+            ids.append(tid)
+            ref.append((data, rows))
+        b = ctx.batch(4000, 4000 * 8)
+        cur = list(shapes)
+        for step in range(3):
+            tf, keys, opw, payload = _insert_batch(rng, cur, 3000)
+            b.load(tf, keys, opw)
+            b.load_payload(payload)
+            b.execute()
+            commit, vals, st = b.results()
+            ref, rc, ro = O.replay_tables(rule, ref, tf, keys, opw, payload)
+            assert np.array_equal(commit, rc)
+            assert np.array_equal(vals, ro)
+            cur = [(ref[k][1], shapes[k][1]) for k in range(2)]
+            for k, tid in enumerate(ids):
+                assert ctx.table_rows(tid) == ref[k][1]
+                assert np.array_equal(ctx.download(tid), ref[k][0][:, :ref[k][1]])
+
+
+def test_insert_capacity_and_payload_errors(lib_loaded):
+    with G.Context(device=0) as ctx:
+        t = ctx.create_table(10, 2, rows_cap=12)
+        ctx.fill_seeded(t, 1)
+        before = ctx.download(t)
+        b = ctx.batch(8, 8)
+        ins = O.opword(2, 0, 0, 0)
+        # three inserts into a table with room for two: rejected, table unchanged
+        b.load(np.array([0, 1, 2, 3], np.uint32), np.array([0, 2, 4], np.uint64), np.array([ins] * 3, np.uint32))
+        b.load_payload(np.arange(6, dtype=np.int32))
+        b.execute()
+        with pytest.raises(G.LtpError) as ei:
+            b.results()
+        assert ei.value.status == G.lib.LTP_E_CAPACITY
+        assert ctx.table_rows(t) == 10 and np.array_equal(ctx.download(t), before)
+        # payload too short for the row: malformed
+        b.load(np.array([0, 1], np.uint32), np.array([5], np.uint64), np.array([ins], np.uint32))
+        b.load_payload(np.arange(6, dtype=np.int32))
+        b.execute()
+        with pytest.raises(G.LtpError) as ei:
+            b.results()
+        assert ei.value.status == G.lib.LTP_E_BADARG
+        # two inserts fit
+        b.load(np.array([0, 1, 2], np.uint32), np.array([0, 2], np.uint64), np.array([ins] * 2, np.uint32))
+        b.load_payload(np.array([5, 6, 7, 8], np.int32))
+        b.execute()
+        commit, vals, _ = b.results()
+        assert vals.tolist() == [10, 11]
+        after = ctx.download(t)
+        assert after.shape == (2, 12) and after[:, 10].tolist() == [5, 6] and after[:, 11].tolist() == [7, 8]
