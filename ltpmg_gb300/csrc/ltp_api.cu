@@ -271,6 +271,7 @@ int ltp_table_create_cap(ltp_ctx *ctx, const ltp_schema *schema, uint64_t rows, 
     memset(&t, 0, sizeof(t));
     t.n_cols = schema->n_cols;
     t.dev.rows_cap = (rows_cap + 63) & ~63ull;  // 256-byte aligned columns
+    t.dev.row_limit = rows_cap;
     t.dev.n_rows = rows;
     t.dev.n_cols = schema->n_cols;
     t.dev.cell_base = ctx->total_cells;

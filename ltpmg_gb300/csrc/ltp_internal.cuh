@@ -23,7 +23,8 @@ __host__ __device__ __forceinline__ int32_t opw_imm(u32 w) { return ((int32_t)w)
 // that the cells of one row share a bitmap word.
 struct TableDev {
     int32_t *data;
-    u64 rows_cap;
+    u64 rows_cap;   // column stride (rows allocated, padded)
+    u64 row_limit;  // rows the table may grow to (requested capacity)
     u64 n_rows;
     u64 cell_base;
     u32 n_cols;

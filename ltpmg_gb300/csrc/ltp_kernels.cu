@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Count
     __shared__ u64 s_prefix;
     if (blockIdx.x == 0 && threadIdx.x < T.n) {  // room for this batch's inserts?
         const u32 tb = threadIdx.x;
-        if (T.rows_now[tb] + ctr->ins_total[tb] > T.t[tb].rows_cap) set_err(ctr, LTP_E_CAPACITY);
+        if (T.rows_now[tb] + ctr->ins_total[tb] > T.t[tb].row_limit) set_err(ctr, LTP_E_CAPACITY);
     }
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_IDS);

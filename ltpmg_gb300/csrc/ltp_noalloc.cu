@@ -146,6 +146,7 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     T.rows_now = rows_now;
     T.t[0].data = table;
     T.t[0].rows_cap = rows_cap;
+    T.t[0].row_limit = rows_cap;
     T.t[0].n_rows = n_rows;
     T.t[0].cell_base = 0;
     T.t[0].n_cols = n_cols;
