@@ -1,21 +1,22 @@
 #!/usr/bin/env python3
 """Benchmark of the batched transaction-processing hot path.
 
-Default workload (N=1): the high-contention YCSB-style configuration --
+Default workload (N=1), the high-contention YCSB-style configuration:
 2^24 rows x 10 int32 columns, 32 resident batches of 2^20 transactions x 16
-ops, Zipf 0.99 keys over a seeded permutation of the rows, 80% reads / 20% +1
-read-modify-writes, ordered rule (every op on a cell in ascending TID order,
-all transactions commit).  A step is one batch; steps cycle over the 32
-batches, so the table evolves exactly as a serial replay would evolve it.
-Inputs are far larger than L2 (201 MB of ops per batch, 640 MB table).
+ops, Zipf 0.99 keys over a seeded permutation of the rows, 80% reads / 20%
++1 read-modify-writes, ordered rule (every op on a cell in ascending TID
+order, all transactions commit).  A step is one multi-batch call over all 32
+batches (CUDA graph or persistent kernel, picked by the autotuner, as are the
+kernel tilings per size bucket).  Inputs are far larger than L2 (201 MB of
+ops per batch, 640 MB table).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--config zipf|plain]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config zipf|plain|uneven]
   python bench.py --impl reference ...   (CPU baseline: the oracle's
                                            multi-threaded serial replay)
 
 Under torchrun every rank drives its own GPU with an independent replica of
-the workload (the path does not shard on one GPU per process: replicas only);
-value = all ranks' transactions / the slowest rank's time.
+the workload (replicas only: no data-path collective); value = all ranks'
+transactions / the slowest rank's time.
 """
 import argparse
 import json
@@ -29,20 +30,19 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-SEED = 0x4C54504D47
-CONFIGS = {
-    "zipf": dict(workload="ycsb-zipf0.99: 2^24 rows x 10 int32, 32 batches x 2^20 txns x 16 ops, 80% read / 20% +1 RMW",
-                 rows=1 << 24, cols=10, txns=1 << 20, ops=16, read=0.8, theta=0.99, batches=32, seed=SEED + 2),
-    "plain": dict(workload="ycsb-uniform: 2^20 rows x 10 int32, 16 batches x 2^16 txns x 10 ops, 50% read / 50% +1 RMW",
-                  rows=1 << 20, cols=10, txns=1 << 16, ops=10, read=0.5, theta=0.0, batches=16, seed=SEED),
-}
 METRIC = "committed txn/s"
-# per-kernel algorithmic bytes: key 8 + opword 4 + bitmap word 4
+DEFAULT_STEPS = {"zipf": 20, "plain": 50, "uneven": 30}
+WORKLOAD_TEXT = {
+    "zipf": "ycsb-zipf0.99: 2^24 rows x 10 int32, 32 batches x 2^20 txns x 16 ops, 80% read / 20% +1 RMW",
+    "plain": "ycsb-uniform: 2^20 rows x 10 int32, 16 batches x 2^16 txns x 10 ops, 50% read / 50% +1 RMW",
+    "uneven": "ycsb-uneven: 2^24 rows x 10 int32, 64 batches x 2^U[10,20] txns x U[1,32] ops, zipf U[0.5,0.99], "
+              "70% read / 30% +1 RMW",
+}
+# algorithmic bytes per kernel launch, from the batch's counters
 KERNEL_BYTES = {
     "mark": lambda st: 16 * st["ops"],
     "ids": lambda st: 20 * st["touched_words"] + 16 * st["contended_cells"],
     "classify": lambda st: 28 * st["ops"],
-    "sort_hist": lambda st: 8 * st["contended_ops"],
     "sort_pass0": lambda st: 16 * st["contended_ops"],
     "sort_pass1": lambda st: 16 * st["contended_ops"],
     "sort_pass2": lambda st: 16 * st["contended_ops"],
@@ -50,6 +50,7 @@ KERNEL_BYTES = {
     "apply": lambda st: 16 * st["contended_ops"] + 12 * st["contended_cells"],
     "finish": lambda st: 12 * st["touched_words"],
 }
+KERNELS_PER_BATCH = 10  # mark, ids, classify, 4 radix passes, apply, insert, finish
 
 
 def dist_env():
@@ -132,107 +133,104 @@ def load_traffic():
     return json.load(open(p)) if os.path.exists(p) else {}
 
 
-def gen_batches(cfg, nb, rank):
-    import ltpmg_gb300 as G
+def gen_batches(config, nb, rank):
+    from ltpmg_gb300 import workloads as W
 
-    out = []
-    for b in range(nb):
-        tf, k, w = G.gen_ycsb(cfg["seed"] + rank, cfg["rows"], cfg["cols"], cfg["ops"], cfg["ops"], cfg["read"],
-                              cfg["theta"], batch=b, n_txns=cfg["txns"])
-        out.append((k, w))
-    return out
+    return [W.generate(config, b, rank=rank) for b in range(nb)]
 
 
-def cpu_baseline(cfg, batches, budget_s=12.0):
+def cpu_baseline(config, host, budget_s=12.0):
     """Single-core serial replay (the oracle port) over whole batches until
     the time budget is spent; returns txn/s and what was sampled."""
-    import ctypes
-
     import numpy as np
+
+    from ltpmg_gb300 import workloads as W
 
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
     L = O.lib()
-    tab = O.table_init(cfg["seed"], cfg["rows"], cfg["cols"])
-    tf = (np.arange(cfg["txns"] + 1, dtype=np.uint32) * cfg["ops"]).astype(np.uint32)
-    commit = np.zeros(cfg["txns"], np.uint8)
-    done, t_used = 0, 0.0
-    for k, w in batches:
-        out = np.zeros(len(k), np.int32)
+    sh = W.SHAPES[config]
+    tab = O.table_init(sh["seed"], sh["rows"], sh["cols"])
+    done_txns, done, t_used = 0, 0, 0.0
+    for tf, keys, opw, n, _ in host:
+        out = np.zeros(len(keys), np.int32)
+        commit = np.zeros(n, np.uint8)
         t0 = time.perf_counter()
-        rc = L.ltpo_replay(0, cfg["rows"], cfg["cols"], tab.ctypes.data, cfg["txns"], tf.ctypes.data, k.ctypes.data,
-                           w.ctypes.data, commit.ctypes.data, out.ctypes.data)
+        rc = L.ltpo_replay(0, sh["rows"], sh["cols"], tab.ctypes.data, n, tf.ctypes.data, keys.ctypes.data,
+                           opw.ctypes.data, commit.ctypes.data, out.ctypes.data)
         t_used += time.perf_counter() - t0
         assert rc == 0
         done += 1
+        done_txns += n
         if t_used >= budget_s:
             break
-    _ = ctypes
-    return {"value": done * cfg["txns"] / t_used, "unit": "txn/s", "cores": 1, "kind": "port",
-            "sample": f"{done} full batch(es) of {cfg['txns']} txns x {cfg['ops']} ops, serial replay (ordered rule), "
-                      f"{t_used:.1f} s"}
+    return {"value": done_txns / t_used, "unit": "txn/s", "cores": 1, "kind": "port",
+            "sample": f"{done} whole batch(es), {done_txns} txns, serial replay (ordered rule), {t_used:.1f} s"}
 
 
-def run_reference(args, cfg):
+def run_reference(args, config):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    import ctypes
-
     import numpy as np
 
-    import ltpmg_gb300 as G  # host generator only (no GPU use)
+    from ltpmg_gb300 import workloads as W
 
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
     threads = os.cpu_count() or 1
-    nb = min(cfg["batches"], 4)
-    batches = gen_batches(cfg, nb, 0)
-    tab = O.table_init(cfg["seed"], cfg["rows"], cfg["cols"])
-    sample_txns = min(cfg["txns"], 1 << 16)
-    per_batch = cfg["txns"] // sample_txns
-    tf = (np.arange(sample_txns + 1, dtype=np.uint32) * cfg["ops"]).astype(np.uint32)
-    commit = np.zeros(sample_txns, np.uint8)
-    out = np.zeros(sample_txns * cfg["ops"], np.int32)
+    sh = W.SHAPES[config]
+    nb = min(sh["batches"], 4)
+    host = gen_batches(config, nb, 0)
+    tab = O.table_init(sh["seed"], sh["rows"], sh["cols"])
     L = O.lib()
+    slice_txns = 1 << 16
+
+    # each step replays a slice of up to 2^16 transactions of the workload
+    slices = []
+    for tf, keys, opw, n, _ in host:
+        for lo in range(0, n, slice_txns):
+            hi = min(n, lo + slice_txns)
+            a, b = int(tf[lo]), int(tf[hi])
+            slices.append(((tf[lo:hi + 1] - tf[lo]).astype(np.uint32), keys[a:b], opw[a:b], hi - lo))
 
     def step(i):
-        k, w = batches[(i // per_batch) % nb]
-        j = i % per_batch
-        lo, hi = j * sample_txns * cfg["ops"], (j + 1) * sample_txns * cfg["ops"]
-        kk, ww = k[lo:hi], w[lo:hi]
-        rc = L.ltpo_replay_r0_mt(cfg["rows"], cfg["cols"], tab.ctypes.data, sample_txns, tf.ctypes.data,
-                                 kk.ctypes.data, ww.ctypes.data, commit.ctypes.data, out.ctypes.data, threads)
+        tfs, k, w, n = slices[i % len(slices)]
+        commit = np.zeros(n, np.uint8)
+        out = np.zeros(len(k), np.int32)
+        rc = L.ltpo_replay_r0_mt(sh["rows"], sh["cols"], tab.ctypes.data, n, tfs.ctypes.data, k.ctypes.data,
+                                 w.ctypes.data, commit.ctypes.data, out.ctypes.data, threads)
         assert rc == 0
+        return n
 
     for i in range(args.warmup):
         step(i)
     t0 = time.perf_counter()
-    for i in range(args.steps):
-        step(args.warmup + i)
+    txns = sum(step(args.warmup + i) for i in range(args.steps))
     dt = time.perf_counter() - t0
-    value = args.steps * sample_txns / dt
-    _ = (ctypes, G)
+    value = txns / dt
     line = {"metric": METRIC, "value": value, "unit": "txn/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
-            "config": {"workload": cfg["workload"], "step": f"{sample_txns} txns x {cfg['ops']} ops",
+            "config": {"workload": WORKLOAD_TEXT[config], "step": f"up to {slice_txns} txns of the workload",
                        "l2": "inputs larger than L2"},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "txn/s", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} slices of {sample_txns} txns from {nb} batches, "
+                             "sample": f"{args.steps} slices of up to {slice_txns} txns from {nb} batches, "
                                        f"cell-partitioned serial replay on {threads} threads"},
             "e2e": {"value": value, "unit": "txn/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args, cfg):
+def run_ours(args, config):
     import numpy as np
     import torch
 
     import ltpmg_gb300 as G
+    from ltpmg_gb300 import autotune as AT
+    from ltpmg_gb300 import workloads as W
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -240,24 +238,33 @@ def run_ours(args, cfg):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    nb = cfg["batches"]
-    host = gen_batches(cfg, nb, rank)
+    sh = W.SHAPES[config]
+    nb = args.batches or sh["batches"]
+    host = gen_batches(config, nb, rank)
     ctx = G.Context(device=local, stage_timing=True)
-    if args.tune:
-        blk, ipt = (int(x) for x in args.tune.split(","))
-        for bucket in range(64):
-            ctx.set_tuning(bucket, blk, ipt)
-    t = ctx.create_table(cfg["rows"], cfg["cols"])
-    ctx.fill_seeded(t, cfg["seed"] + rank)
+    t = ctx.create_table(sh["rows"], sh["cols"])
+    ctx.fill_seeded(t, sh["seed"] + rank)
     dev = []
-    for k, w in host:
-        b = ctx.batch(cfg["txns"], len(k))
-        b.load(None, k, w, ops_per_txn=cfg["ops"])
+    for tf, keys, opw, n, opt in host:
+        b = ctx.batch(n, len(keys))
+        b.load(None if opt else tf, keys, opw, ops_per_txn=opt)
         dev.append(b)
     ctx.sync()
+
+    # autotuning (untimed): tilings per size bucket, then the multi-batch mode
+    tiles = AT.tune_buckets(ctx, dev, reps=2)
+    if args.mode == "auto":
+        mode, mode_ms = AT.tune_mode(ctx, dev)
+    else:
+        mode = {"graph": G.MODE_GRAPH, "persistent": G.MODE_PERSISTENT, "stream": G.MODE_STREAM}[args.mode]
+        mode_ms = {}
+    mode_name = {G.MODE_STREAM: "stream", G.MODE_GRAPH: "graph", G.MODE_PERSISTENT: "persistent"}[mode]
+    if args.tuning_out:
+        AT.save(args.tuning_out, tiles, mode_name)
+
     stream = torch.cuda.ExternalStream(ctx.stream)
-    for i in range(args.warmup):
-        dev[i % nb].execute()
+    for _ in range(args.warmup):
+        ctx.execute_many(dev, mode=mode)
     ctx.sync()
     barrier(world)
     clocks = ClockSampler(local)
@@ -265,108 +272,125 @@ def run_ours(args, cfg):
     time.sleep(0.15)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for i in range(args.steps):
-        dev[(args.warmup + i) % nb].execute()
+    for _ in range(args.steps):
+        ctx.execute_many(dev, mode=mode)
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     ms = reduce_max(ms, world)
-    # per-kernel times of the last execution of every batch (events on the launching stream)
-    stats = [b.finish().as_dict() for b in dev]
-    total_txns = args.steps * cfg["txns"] * world
-    value = total_txns / (ms / 1e3)
+    stats = [b.finish().as_dict() for b in dev]  # per-kernel event times of each batch's last run
+    txns_per_step = sum(h[3] for h in host)
+    ops_per_step = sum(len(h[1]) for h in host)
+    value = args.steps * txns_per_step * world / (ms / 1e3)
 
-    # end to end through the C ABI: pinned host inputs, H2D, execute, D2H of
-    # the commit vector and per-op values, every step
-    n_e2e = min(args.steps, 64)
-    pk = [G.PinnedArray((len(host[i][0]),), np.uint64) for i in range(2)]
-    pw = [G.PinnedArray((len(host[i][1]),), np.uint32) for i in range(2)]
-    for i in range(2):
-        pk[i].array[:] = host[i][0]
-        pw[i].array[:] = host[i][1]
-    pc = G.PinnedArray((cfg["txns"],), np.uint8)
-    pv = G.PinnedArray((cfg["txns"] * cfg["ops"],), np.int32)
-    eb = dev[0]
-    for i in range(2):
-        eb.load(None, pk[i].array, pw[i].array, ops_per_txn=cfg["ops"])
+    # end to end through the C ABI: every step copies one batch from pinned
+    # host memory, executes it and copies back its commit vector and values
+    n_e2e = min(64, max(8, args.steps))
+    hb = [max(range(nb), key=lambda i: host[i][3])]
+    hb.append((hb[0] + 1) % nb)
+    pins = []
+    for i in hb:
+        tf, keys, opw, n, opt = host[i]
+        pk, pw = G.PinnedArray((len(keys),), np.uint64), G.PinnedArray((len(opw),), np.uint32)
+        pk.array[:] = keys
+        pw.array[:] = opw
+        ptf = G.PinnedArray((len(tf),), np.uint32)
+        ptf.array[:] = tf
+        pins.append((ptf, pk, pw, n, opt))
+    maxn = max(p[3] for p in pins)
+    maxops = max(len(p[1].array) for p in pins)
+    pc, pv = G.PinnedArray((maxn,), np.uint8), G.PinnedArray((maxops,), np.int32)
+    eb = ctx.batch(maxn, maxops)
+    h2d = d2h = 0
+
+    def e2e_step(i):
+        ptf, pk, pw, n, opt = pins[i % 2]
+        eb.load(None if opt else ptf.array, pk.array, pw.array, ops_per_txn=opt)
         eb.execute()
         eb.fetch(pc.array, pv.array)
+        return n, len(pk.array)
+
+    for i in range(2):
+        e2e_step(i)
     ctx.sync()
     barrier(world)
     t0 = time.perf_counter()
+    e2e_txns = 0
     for i in range(n_e2e):
-        eb.load(None, pk[i % 2].array, pw[i % 2].array, ops_per_txn=cfg["ops"])
-        eb.execute()
-        eb.fetch(pc.array, pv.array)
+        n, nops = e2e_step(i)
+        e2e_txns += n
+        h2d += 12 * nops + (0 if pins[i % 2][4] else 4 * (n + 1))
+        d2h += 4 * nops + n
     ctx.sync()
     e2e_s = reduce_max(time.perf_counter() - t0, world)
     eb.finish()
-    n_ops = cfg["txns"] * cfg["ops"]
-    e2e = {"value": n_e2e * cfg["txns"] * world / e2e_s, "unit": "txn/s", "h2d_bytes_per_step": 12 * n_ops,
-           "d2h_bytes_per_step": 4 * n_ops + cfg["txns"], "steps": n_e2e}
+    e2e = {"value": e2e_txns * world / e2e_s, "unit": "txn/s", "h2d_bytes_per_step": h2d // n_e2e,
+           "d2h_bytes_per_step": d2h // n_e2e, "steps": n_e2e,
+           "note": "one batch per step, sequential copy / execute / copy on one stream"}
 
     if rank != 0:
         return
     peak, peak_kind = load_peaks()
-    avg = {}
-    for name in KERNEL_BYTES:
-        vals = [s["ms_stage"][name] for s in stats]
-        avg[name] = sum(vals) / len(vals)
-    dom = max(avg, key=avg.get)
+    alg = W.algorithmic_bytes(ops_per_step, txns_per_step)
+    step_ms = ms / args.steps
+    roof = {"bound": "hbm", "peak": peak, "unit": "GB/s", "peak_kind": peak_kind,
+            "pipeline": {"algorithmic_bytes_per_step": alg, "avg_step_ms": step_ms,
+                         "achieved": alg / (step_ms / 1e3) / 1e9, "frac": alg / (step_ms / 1e3) / 1e9 / peak}}
     mean_stats = {k: sum(s[k] for s in stats) / len(stats) for k in ("ops", "touched_words", "contended_cells",
                                                                      "contended_ops")}
-    dom_bytes = KERNEL_BYTES[dom](mean_stats)
-    achieved = dom_bytes / (avg[dom] / 1e3) / 1e9
-    traffic = load_traffic().get(dom)
-    traffic_b = None
-    if traffic:
-        units = mean_stats["contended_ops"] if traffic.get("unit") == "contended_op" else mean_stats["ops"]
-        traffic_b = traffic["bytes_per_unit"] * units
-    batch_ms = statistics.mean(s["ms_stage"]["total"] for s in stats)
-    alg_batch = 28 * n_ops + 4 * cfg["txns"]
+    if mode != G.MODE_PERSISTENT:
+        avg = {name: sum(s["ms_stage"][name] for s in stats) / len(stats) for name in KERNEL_BYTES}
+        dom = max(avg, key=avg.get)
+        dom_bytes = KERNEL_BYTES[dom](mean_stats)
+        achieved = dom_bytes / (avg[dom] / 1e3) / 1e9
+        traffic = load_traffic().get(dom)
+        traffic_b = None
+        if traffic:
+            units = mean_stats["contended_ops"] if traffic.get("unit") == "contended_op" else mean_stats["ops"]
+            traffic_b = traffic["bytes_per_unit"] * units
+        roof.update({"kernel": dom, "achieved": achieved, "frac": achieved / peak, "traffic": traffic_b,
+                     "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": avg[dom], "kernel_ms": avg})
+    else:
+        roof.update({"kernel": "k_persist (whole pipeline, one launch per step)", "achieved":
+                     roof["pipeline"]["achieved"], "frac": roof["pipeline"]["frac"], "traffic": None,
+                     "algorithmic_bytes_per_launch": alg, "avg_launch_ms": step_ms})
+    launches = args.steps * (1 if mode == G.MODE_PERSISTENT else KERNELS_PER_BATCH * nb)
     line = {"metric": METRIC, "value": value, "unit": "txn/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
-            "config": {"workload": cfg["workload"], "rule": "ordered (ascending TID per cell, all commit)",
-                       "l2": "inputs larger than L2 (201 MB ops/batch, 640 MB table)",
-                       "parallelism": f"replicas x{world}"},
-            "gpu_launches": 10 * args.steps,
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic_b, "peak_kind": peak_kind,
-                         "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": avg[dom],
-                         "pipeline": {"algorithmic_bytes_per_batch": alg_batch, "avg_batch_ms": batch_ms,
-                                      "achieved": alg_batch / (batch_ms / 1e3) / 1e9,
-                                      "frac": alg_batch / (batch_ms / 1e3) / 1e9 / peak},
-                         "kernel_ms": avg},
-            "clocks": clk, "e2e": e2e,
+            "config": {"workload": WORKLOAD_TEXT[config], "batches_per_step": nb, "txns_per_step": txns_per_step,
+                       "rule": "ordered (ascending TID per cell, all commit)", "mode": mode_name,
+                       "mode_ms": {str(k): v for k, v in mode_ms.items()},
+                       "tuning": {str(k): f"{v['block']}x{v['ipt']}" for k, v in tiles.items()},
+                       "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
+            "gpu_launches": launches, "roofline": roof, "clocks": clk, "e2e": e2e,
             "contention": {"contended_ops_per_batch": mean_stats["contended_ops"],
                            "contended_cells_per_batch": mean_stats["contended_cells"]}}
     if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(cfg, host)
+        line["cpu_baseline"] = cpu_baseline(config, host)
     print(json.dumps(line), flush=True)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=0)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="zipf", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="zipf", choices=sorted(DEFAULT_STEPS))
+    ap.add_argument("--mode", default="auto", choices=["auto", "graph", "persistent", "stream"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--batches", type=int, default=0, help="resident batches to cycle (default: the config's)")
-    ap.add_argument("--tune", default="", help="block,ipt for every size bucket (default: library tuning)")
+    ap.add_argument("--batches", type=int, default=0, help="resident batches (default: the config's)")
+    ap.add_argument("--tuning-out", default="", help="write the autotuner's choices to this JSON file")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
-    cfg = dict(CONFIGS[args.config])
-    if args.batches:
-        cfg["batches"] = args.batches
+    args.warmup = max(args.warmup, 3)
+    if not args.steps:
+        args.steps = DEFAULT_STEPS[args.config]
     if args.impl == "reference":
-        run_reference(args, cfg)
+        run_reference(args, args.config)
     else:
-        run_ours(args, cfg)
+        run_ours(args, args.config)
 
 
 if __name__ == "__main__":

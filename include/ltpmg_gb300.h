@@ -158,6 +158,22 @@ int ltp_table_rows(ltp_ctx *ctx, uint32_t table, uint64_t *rows);
 /* Executes one batch against the context's tables (replaces
  * GPUlauncher::txn_kernel_launcher, cuda/src/gpulauncher.cu:755-1116). */
 int ltp_batch_execute(ltp_ctx *ctx, ltp_batch *b, void *stream);
+/* Many batches in order, against the context's tables, with no host round
+ * trip between them:
+ *  LTP_MODE_STREAM     every batch's kernels launched in order on the stream;
+ *  LTP_MODE_GRAPH      the same launch sequence captured once into a CUDA
+ *                      graph (re-captured when a batch's size, pointers or
+ *                      tuning change) and replayed with one graph launch;
+ *  LTP_MODE_PERSISTENT one cooperative persistent kernel runs every batch
+ *                      through all phases with bounded grid-wide barriers;
+ *                      returns after the kernel completes.
+ * Per-batch results and status come from ltp_batch_fetch / ltp_batch_finish
+ * as for ltp_batch_execute.  Replaces the reference's per-epoch
+ * execute_on_GPU loop (src/scheduler.cpp:44-59). */
+#define LTP_MODE_STREAM 0
+#define LTP_MODE_GRAPH 1
+#define LTP_MODE_PERSISTENT 2
+int ltp_batches_execute(ltp_ctx *ctx, ltp_batch *const *batches, uint32_t n, int32_t mode, void *stream);
 /* Asynchronous device->host copy of the outputs (commit may be NULL, vals
  * may be NULL). */
 int ltp_batch_fetch(ltp_ctx *ctx, ltp_batch *b, uint8_t *commit, int32_t *vals, void *stream);

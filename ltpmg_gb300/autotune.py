@@ -1,0 +1,108 @@
+"""Project-written autotuner for the batch kernels.
+
+Per size bucket (floor(log2(ops in the batch))) it times every candidate
+tiling of the streaming kernels -- threads per block x ops per thread, the
+knobs that set how many ops a tile stages in shared memory -- on a
+representative batch with CUDA events, and keeps the fastest.  For a list of
+batches it also times the multi-batch execution modes (CUDA graph vs the
+persistent cooperative kernel) and keeps the faster one.  Choices persist as
+JSON and are applied with Context.set_tuning.
+
+Tuning runs execute real batches: they advance the table they run on, so
+run them on a context whose table may change (a scratch copy, or before the
+workload's measured or checked part).
+"""
+import json
+import math
+import time
+
+from . import lib as L
+
+BLOCKS = (128, 256, 512)
+IPTS = (1, 2, 4, 8)
+
+
+def bucket_of(n_ops):
+    return max(0, int(math.floor(math.log2(n_ops)))) if n_ops > 0 else 0
+
+
+def _time_batch(ctx, batch, reps):
+    import torch
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ms = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.execute()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    batch.finish()
+    ms.sort()
+    return ms[len(ms) // 2]
+
+
+def tune_tiles(ctx, batch, reps=3, blocks=BLOCKS, ipts=IPTS):
+    """Times every (block, ipt) on one loaded batch; sets and returns the best
+    for the batch's size bucket as {"block", "ipt", "ms", "candidates"}."""
+    bucket = bucket_of(batch.n_ops)
+    results = {}
+    batch.execute()  # warm-up
+    batch.finish()
+    for blk in blocks:
+        for ipt in ipts:
+            ctx.set_tuning(bucket, blk, ipt)
+            results[f"{blk}x{ipt}"] = _time_batch(ctx, batch, reps)
+    best = min(results, key=results.get)
+    blk, ipt = (int(x) for x in best.split("x"))
+    ctx.set_tuning(bucket, blk, ipt)
+    return {"bucket": bucket, "block": blk, "ipt": ipt, "ms": results[best], "candidates": results}
+
+
+def tune_mode(ctx, batches, reps=2, modes=(L.MODE_GRAPH, L.MODE_PERSISTENT)):
+    """Times whole multi-batch calls in each mode; returns (best_mode, {mode: ms})."""
+    import torch
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    out = {}
+    for m in modes:
+        ctx.execute_many(batches, mode=m)  # warm-up (captures the graph)
+        ctx.sync()
+        ms = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.execute_many(batches, mode=m)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        out[m] = min(ms)
+    for b in batches:
+        b.finish()
+    return min(out, key=out.get), out
+
+
+def tune_buckets(ctx, batches, reps=3):
+    """One representative batch per size bucket; returns {bucket: choice}."""
+    seen = {}
+    for b in batches:
+        k = bucket_of(b.n_ops)
+        if k not in seen or b.n_ops > seen[k].n_ops:
+            seen[k] = b
+    return {k: tune_tiles(ctx, b, reps) for k, b in sorted(seen.items())}
+
+
+def save(path, choices, mode=None):
+    doc = {"buckets": {str(k): {"block": v["block"], "ipt": v["ipt"], "ms": v["ms"]} for k, v in choices.items()},
+           "mode": mode, "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
+    with open(path, "w") as f:
+        json.dump(doc, f, indent=1)
+
+
+def load(ctx, path):
+    """Applies a saved tuning file to a context; returns its multi-batch mode."""
+    doc = json.load(open(path))
+    for k, v in doc["buckets"].items():
+        ctx.set_tuning(int(k), int(v["block"]), int(v["ipt"]))
+    return doc.get("mode")

@@ -35,6 +35,14 @@ struct ltp_ctx {
     Tuning tuning[64];
     uint32_t stall_ms_next = 0;
     bool dirty = false;  // scratch must be reset before the next batch
+    // multi-batch execution: cached CUDA graph and persistent-kernel buffers
+    std::vector<uint64_t> graph_key;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaStream_t graph_stream = nullptr;
+    BatchDev *p_batches = nullptr;
+    Counters **p_snaps = nullptr;
+    uint32_t p_cap = 0;
+    u32 *p_bar = nullptr;
 };
 
 struct ltp_batch {
@@ -239,6 +247,10 @@ int ltp_shutdown(ltp_ctx *ctx) {
     free_scratch_words(ctx->s);
     cudaFree(ctx->ctr);
     cudaFree(ctx->rows_now);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    cudaFree(ctx->p_batches);
+    cudaFree(ctx->p_snaps);
+    cudaFree(ctx->p_bar);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return LTP_OK;
@@ -461,20 +473,9 @@ int ltp_batch_load_payload(ltp_ctx *ctx, ltp_batch *b, const int32_t *payload, u
     return LTP_OK;
 }
 
-int ltp_batch_execute(ltp_ctx *ctx, ltp_batch *b, void *stream) {
-    if (!ctx || !b) return LTP_E_BADARG;
-    if (!b->loaded) return fail(ctx, LTP_E_STATE, "batch not loaded");
-    if (ctx->tables.empty()) return fail(ctx, LTP_E_STATE, "no tables");
-    CK(cudaSetDevice(ctx->device));
-    int rc = ensure_scratch(ctx, b->n_ops);
-    if (rc) return rc;
-    cudaStream_t st = pick_stream(ctx, stream);
-    if (ctx->dirty) {
-        CK(launch_reset_scratch(st, ctx->s));
-        ctx->dirty = false;
-    }
-    CK(cudaMemsetAsync(ctx->ctr, 0, sizeof(Counters), st));
-    if (b->n_txns) CK(cudaMemsetAsync(b->commit, 1, b->n_txns, st));
+namespace {
+
+BatchDev batch_dev(const ltp_batch *b) {
     BatchDev bd;
     bd.keys = (const u64 *)b->keys;
     bd.opw = b->opw;
@@ -488,20 +489,140 @@ int ltp_batch_execute(ltp_ctx *ctx, ltp_batch *b, void *stream) {
     bd.pad = 0;
     bd.payload = b->payload;
     bd.payload_len = b->payload_len;
+    return bd;
+}
+
+// Stream-ordered launches of one batch (scratch already sized and clean).
+int execute_one(ltp_ctx *ctx, ltp_batch *b, cudaStream_t st, bool allow_stall) {
+    CK(cudaMemsetAsync(ctx->ctr, 0, sizeof(Counters), st));
+    if (b->n_txns) CK(cudaMemsetAsync(b->commit, 1, b->n_txns, st));
     Launch L;
     L.stream = st;
     L.num_sms = ctx->num_sms;
     L.rule = ctx->rule;
     L.tune = ctx->tuning[bucket_of(b->n_ops)];
-    L.stall = ctx->stall_ms_next != 0;
+    L.stall = allow_stall && ctx->stall_ms_next != 0;
     L.stall_ms = ctx->stall_ms_next;
-    ctx->stall_ms_next = 0;
+    if (allow_stall) ctx->stall_ms_next = 0;
     L.timing = b->have_events;
     L.ev = b->ev;
-    if (b->n_ops) CK(launch_execute(L, bd, tables_dev(ctx), ctx->s, ctx->ctr));
+    if (b->n_ops) CK(launch_execute(L, batch_dev(b), tables_dev(ctx), ctx->s, ctx->ctr));
     CK(cudaMemcpyAsync(b->snap, ctx->ctr, sizeof(Counters), cudaMemcpyDeviceToDevice, st));
     b->rule = ctx->rule;
     b->executed = true;
+    return LTP_OK;
+}
+
+int prepare(ltp_ctx *ctx, ltp_batch *const *bs, uint32_t n, cudaStream_t st) {
+    uint64_t max_ops = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        if (!bs[i]) return fail(ctx, LTP_E_BADARG, "null batch");
+        if (!bs[i]->loaded) return fail(ctx, LTP_E_STATE, "batch not loaded");
+        if (bs[i]->n_ops > max_ops) max_ops = bs[i]->n_ops;
+    }
+    if (ctx->tables.empty()) return fail(ctx, LTP_E_STATE, "no tables");
+    int rc = ensure_scratch(ctx, max_ops);
+    if (rc) return rc;
+    if (ctx->dirty) {
+        CK(launch_reset_scratch(st, ctx->s));
+        ctx->dirty = false;
+    }
+    return LTP_OK;
+}
+
+}  // namespace
+
+int ltp_batch_execute(ltp_ctx *ctx, ltp_batch *b, void *stream) {
+    if (!ctx || !b) return LTP_E_BADARG;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = pick_stream(ctx, stream);
+    int rc = prepare(ctx, &b, 1, st);
+    if (rc) return rc;
+    return execute_one(ctx, b, st, true);
+}
+
+int ltp_batches_execute(ltp_ctx *ctx, ltp_batch *const *batches, uint32_t n, int32_t mode, void *stream) {
+    if (!ctx || (n && !batches)) return LTP_E_BADARG;
+    if (mode != LTP_MODE_STREAM && mode != LTP_MODE_GRAPH && mode != LTP_MODE_PERSISTENT)
+        return fail(ctx, LTP_E_BADARG, "unknown execution mode");
+    if (n == 0) return LTP_OK;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = pick_stream(ctx, stream);
+    int rc = prepare(ctx, batches, n, st);
+    if (rc) return rc;
+    if (mode == LTP_MODE_STREAM) {
+        for (uint32_t i = 0; i < n; i++)
+            if ((rc = execute_one(ctx, batches[i], st, false))) return rc;
+        return LTP_OK;
+    }
+    if (mode == LTP_MODE_GRAPH) {
+        // the captured launch sequence bakes in pointers, sizes and tuning
+        std::vector<uint64_t> key;
+        key.push_back((uint64_t)ctx->rule);
+        key.push_back((uint64_t)(uintptr_t)st);
+        for (uint32_t i = 0; i < n; i++) {
+            const ltp_batch *b = batches[i];
+            const Tuning &t = ctx->tuning[bucket_of(b->n_ops)];
+            key.insert(key.end(), {(uint64_t)(uintptr_t)b, b->n_ops, b->n_txns, b->ops_per_txn,
+                                   (uint64_t)(uintptr_t)b->payload, b->payload_len,
+                                   ((uint64_t)t.block << 32) | t.ipt, (uint64_t)b->have_events});
+        }
+        if (!ctx->graph_exec || key != ctx->graph_key) {
+            if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+            ctx->graph_exec = nullptr;
+            cudaGraph_t graph = nullptr;
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+            for (uint32_t i = 0; i < n && !rc; i++) rc = execute_one(ctx, batches[i], st, false);
+            cudaError_t e = cudaStreamEndCapture(st, &graph);
+            if (rc) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
+            e = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) {
+                ctx->graph_exec = nullptr;
+                return cuda_fail(ctx, e, "cudaGraphInstantiate");
+            }
+            ctx->graph_key = key;
+        }
+        CK(cudaGraphLaunch(ctx->graph_exec, st));
+        for (uint32_t i = 0; i < n; i++) {
+            batches[i]->rule = ctx->rule;
+            batches[i]->executed = true;
+        }
+        return LTP_OK;
+    }
+    // persistent: one cooperative kernel over all batches
+    if (n > ctx->p_cap) {
+        CK(cudaStreamSynchronize(st));
+        cudaFree(ctx->p_batches);
+        cudaFree(ctx->p_snaps);
+        ctx->p_batches = nullptr;
+        ctx->p_snaps = nullptr;
+        ctx->p_cap = 0;
+        CK(dalloc(&ctx->p_batches, n));
+        CK(dalloc(&ctx->p_snaps, n));
+        ctx->p_cap = n;
+    }
+    if (!ctx->p_bar) CK(dalloc(&ctx->p_bar, 2));
+    std::vector<BatchDev> hb(n);
+    std::vector<Counters *> hs(n);
+    for (uint32_t i = 0; i < n; i++) {
+        hb[i] = batch_dev(batches[i]);
+        hs[i] = batches[i]->snap;
+    }
+    CK(cudaMemcpyAsync(ctx->p_batches, hb.data(), n * sizeof(BatchDev), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->p_snaps, hs.data(), n * sizeof(Counters *), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(ctx->ctr, 0, sizeof(Counters), st));
+    CK(launch_persistent(st, ctx->num_sms, ctx->rule, ctx->p_batches, ctx->p_snaps, n, tables_dev(ctx), ctx->s,
+                         ctx->ctr, ctx->p_bar));
+    CK(cudaStreamSynchronize(st));  // the descriptor arrays are host staging above
+    for (uint32_t i = 0; i < n; i++) {
+        batches[i]->rule = ctx->rule;
+        batches[i]->executed = true;
+    }
     return LTP_OK;
 }
 

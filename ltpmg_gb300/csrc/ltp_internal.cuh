@@ -140,5 +140,10 @@ cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s);
 cudaError_t launch_fill_seeded(cudaStream_t st, const TableDev &t, u64 seed);
 cudaError_t launch_expand_op_txn(cudaStream_t st, const u32 *txn_first, u64 n_txns, u32 *op_txn);
 cudaError_t launch_set_u64(cudaStream_t st, u64 *dst, u64 value);
+// One cooperative launch over n_batches device-resident batch descriptors.
+cudaError_t launch_persistent(cudaStream_t st, int num_sms, int rule, const BatchDev *d_batches,
+                              Counters *const *d_snaps, u32 n_batches, const TablesDev &T, const Scratch &s,
+                              Counters *ctr, u32 *bar);
+int persistent_grid(int num_sms);
 
 }  // namespace ltp

@@ -68,6 +68,16 @@ __device__ __forceinline__ u64 mix64(u64 z) {
     return z ^ (z >> 31);
 }
 
+// One view of the device error word for the whole block: every thread takes
+// the same early exit, so no barrier or full-warp collective is left short.
+__device__ __forceinline__ bool block_err(Counters *ctr) {
+    __shared__ int s_err;
+    __syncthreads();
+    if (threadIdx.x == 0) s_err = *(volatile int *)&ctr->err;
+    __syncthreads();
+    return s_err != 0;
+}
+
 // Claims the next tile for the whole block (tiles are handed out in order,
 // which is what makes decoupled look-back safe without co-residency).
 __device__ __forceinline__ u32 claim_tile(Counters *ctr, int slot) {
@@ -167,8 +177,8 @@ constexpr u32 kEmptyKey = 0xFFFFFFFFu;
 __device__ __forceinline__ u32 hash_word(u32 w) { return (w * 0x9E3779B1u) ^ (w >> 15); }
 
 template <int BLOCK, int IPT>
-__global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
-    if (ctr->err) return;
+__device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+    if (block_err(ctr)) return;
     constexpr u32 TILE = (u32)BLOCK * IPT;
     constexpr u32 H = 2 * TILE;  // at most TILE distinct words: load factor <= 1/2
     extern __shared__ u32 mark_smem[];  // 4 * H words (dynamic: up to 128 KB)
@@ -284,16 +294,22 @@ __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch
     }
 }
 
+template <int BLOCK, int IPT>
+__global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    phase_mark<BLOCK, IPT>(b, T, s, ctr);
+}
+
 // ============================================================================
 // ids: dense ids of contended cells (touched twice and written)
 // ============================================================================
-template <bool PRIORITY>
-__global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Counters *ctr) {
-    if (ctr->err) return;
+template <bool PRIORITY, int BLK>
+__device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, Counters *ctr) {
+    constexpr u32 IPT = kIdsTile / BLK;
+    if (block_err(ctr)) return;
     const u64 n = ctr->n_tw;
     const u32 tiles = (u32)((n + kIdsTile - 1) / kIdsTile);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __shared__ u32 s_warp[kIdsBlock / 32];
+    __shared__ u32 s_warp[BLK / 32];
     __shared__ u64 s_prefix;
     if (blockIdx.x == 0 && threadIdx.x < T.n) {  // room for this batch's inserts?
         const u32 tb = threadIdx.x;
@@ -302,12 +318,12 @@ __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Count
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_IDS);
         if (tile >= tiles) break;
-        u32 wd[kIdsIpt], cw[kIdsIpt];
+        u32 wd[IPT], cw[IPT];
         u32 cnt = 0;
-        // blocked arrangement: thread owns kIdsIpt consecutive entries
-        const u64 t0 = (u64)tile * kIdsTile + (u64)threadIdx.x * kIdsIpt;
+        // blocked arrangement: thread owns IPT consecutive entries
+        const u64 t0 = (u64)tile * kIdsTile + (u64)threadIdx.x * IPT;
 #pragma unroll
-        for (int k = 0; k < kIdsIpt; k++) {
+        for (int k = 0; k < IPT; k++) {
             u64 j = t0 + k;
             wd[k] = j < n ? s.tw_list[j] : 0u;
             if (j < n) {
@@ -329,7 +345,7 @@ __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Count
         __syncthreads();
         if (threadIdx.x == 0) {
             u32 run = 0;
-            for (int i = 0; i < kIdsBlock / 32; i++) {
+            for (int i = 0; i < BLK / 32; i++) {
                 u32 c = s_warp[i];
                 s_warp[i] = run;
                 run += c;
@@ -341,7 +357,7 @@ __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Count
         __syncthreads();
         u64 pre = s_prefix + s_warp[warp] + (incl - cnt);
 #pragma unroll
-        for (int k = 0; k < kIdsIpt; k++) {
+        for (int k = 0; k < IPT; k++) {
             u64 j = t0 + k;
             if (j < n) {
                 s.words[wd[k]].prefix = (u32)pre;
@@ -361,6 +377,11 @@ __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Count
     }
 }
 
+template <bool PRIORITY>
+__global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Counters *ctr) {
+    phase_ids<PRIORITY, kIdsBlock>(T, s, ctr);
+}
+
 // ============================================================================
 // classify (ordered rule): execute uncontended ops, compact contended ones,
 // and histogram the contended ids' radix digits for the sort
@@ -375,8 +396,8 @@ __device__ __forceinline__ int sort_passes_dev(u32 M) {
 }
 
 template <int BLOCK, int IPT>
-__global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
-    if (ctr->err) return;
+__device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+    if (block_err(ctr)) return;
     constexpr int NW = BLOCK / 32;
     constexpr u64 TILE = (u64)BLOCK * IPT;
     const u64 n = b.n_ops;
@@ -473,15 +494,22 @@ __global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scr
     }
 }
 
+template <int BLOCK, int IPT>
+__global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    phase_classify<BLOCK, IPT>(b, T, s, ctr);
+}
+
 // ============================================================================
 // sort: stable LSD radix sort of the contended records by id (8-bit digits);
 // each tile ranks its records per digit, finds its digit offsets by
 // decoupled look-back, stages the records in shared memory in digit order
 // and writes every digit's run with coalesced stores
 // ============================================================================
-template <int P>
-__global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *ctr, u64 n_ops, u32 seg_tile) {
-    if (ctr->err) return;
+template <int BLK>
+__device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, Counters *ctr, u64 n_ops, u32 seg_tile) {
+    static_assert(BLK >= 256, "one thread per radix digit");
+    constexpr u32 SIPT = kSortTile / BLK;
+    if (block_err(ctr)) return;
     const int passes = sort_passes_dev(ctr->M);
     if (P >= passes) return;
     const u64 n = ctr->n_c;
@@ -496,15 +524,15 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
     if (P >= 1) {  // the previous pass is complete: recycle its look-back slots
         u32 *other = s.st_sort[(P + 1) & 1];
         const u64 prev_tiles = P == 1 ? (n_ops + kSortTile - 1) / kSortTile + 1 : tiles;
-        for (u64 j = (u64)blockIdx.x * kSortBlock + threadIdx.x; j < prev_tiles * 256; j += (u64)gridDim.x * kSortBlock)
+        for (u64 j = (u64)blockIdx.x * BLK + threadIdx.x; j < prev_tiles * 256; j += (u64)gridDim.x * BLK)
             other[j] = 0;
     }
-    constexpr int NW = kSortBlock / 32;
+    constexpr int NW = BLK / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const u32 tid = threadIdx.x;
     const bool dt = tid < 256;  // threads 0..255 own one digit each
     __shared__ u32 s_start[256];
-    __shared__ unsigned short s_whist[NW][256];  // per-warp digit counts (<= 32 * kSortIpt)
+    __shared__ unsigned short s_whist[NW][256];  // per-warp digit counts (<= 32 * SIPT)
     __shared__ u32 s_base[256];   // global position of the tile's first record of each digit
     __shared__ u32 s_loc[256];    // tile-local position of each digit's first record
     __shared__ u32 s_wsum[8];
@@ -530,7 +558,7 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_SORT0 + P);
         if (tile >= tiles) break;
-        for (u32 i = tid; i < NW * 256; i += kSortBlock) (&s_whist[0][0])[i] = 0;
+        for (u32 i = tid; i < NW * 256; i += BLK) (&s_whist[0][0])[i] = 0;
         __syncthreads();
         u32 tcnt;
         if (P == 0) {
@@ -548,11 +576,11 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
         } else {
             tcnt = (u32)min((u64)kSortTile, n - (u64)tile * kSortTile);
         }
-        const u32 lbase = (u32)warp * 32 * kSortIpt;
-        u64 e[kSortIpt];
-        u32 rank[kSortIpt];
+        const u32 lbase = (u32)warp * 32 * SIPT;
+        u64 e[SIPT];
+        u32 rank[SIPT];
 #pragma unroll
-        for (int k = 0; k < kSortIpt; k++) {
+        for (int k = 0; k < SIPT; k++) {
             const u32 li = lbase + (u32)k * 32 + lane;
             e[k] = ~0ull;
             if (li < tcnt) {
@@ -572,7 +600,7 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
             }
         }
 #pragma unroll
-        for (int k = 0; k < kSortIpt; k++) {
+        for (int k = 0; k < SIPT; k++) {
             const bool v = lbase + (u32)k * 32 + lane < tcnt;
             const u32 d = v ? (u32)(e[k] >> shift) & 255u : 256u;
             const u32 peers = __match_any_sync(FULL_MASK, d);
@@ -639,14 +667,14 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
         }
         __syncthreads();
 #pragma unroll
-        for (int k = 0; k < kSortIpt; k++) {
+        for (int k = 0; k < SIPT; k++) {
             if (lbase + (u32)k * 32 + lane < tcnt) {
                 const u32 d = (u32)(e[k] >> shift) & 255u;
                 s_stage[s_loc[d] + s_whist[warp][d] + rank[k]] = e[k];
             }
         }
         __syncthreads();
-        for (u32 p = tid; p < tcnt; p += kSortBlock) {
+        for (u32 p = tid; p < tcnt; p += BLK) {
             const u64 x = s_stage[p];
             const u32 d = (u32)(x >> shift) & 255u;
             dst[s_base[d] + (p - s_loc[d])] = x;
@@ -655,36 +683,43 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
     }
 }
 
+template <int P>
+__global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *ctr, u64 n_ops, u32 seg_tile) {
+    phase_sort_pass<kSortBlock>(P, s, ctr, n_ops, seg_tile);
+}
+
 // ============================================================================
 // apply: segmented scan of RMW immediates per contended cell, write-back
 // ============================================================================
 // look-back status: bits 62-63 flag, bit 61 "tile holds a segment head",
 // bits 0-31 sum since the last head (wrapping int32 arithmetic)
-__global__ void __launch_bounds__(kApplyBlock) k_apply(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
-    if (ctr->err) return;
+template <int BLK>
+__device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+    constexpr u32 AIPT = kApplyTile / BLK;
+    if (block_err(ctr)) return;
     const u64 n = ctr->n_c;
     const u32 tiles = (u32)((n + kApplyTile - 1) / kApplyTile);
     const u64 *list = s.list[sort_passes_dev(ctr->M) & 1];
-    constexpr int NW = kApplyBlock / 32;
+    constexpr int NW = BLK / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ u32 s_wf[NW], s_ws[NW];
     __shared__ u32 s_tf, s_ts;
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_APPLY);
         if (tile >= tiles) break;
-        const u64 wbase = (u64)tile * kApplyTile + (u64)warp * 32 * kApplyIpt;
-        u64 e[kApplyIpt];
-        u32 sv[kApplyIpt];
-        bool sf[kApplyIpt];
-        bool tail[kApplyIpt];
+        const u64 wbase = (u64)tile * kApplyTile + (u64)warp * 32 * AIPT;
+        u64 e[AIPT];
+        u32 sv[AIPT];
+        bool sf[AIPT];
+        bool tail[AIPT];
 #pragma unroll
-        for (int k = 0; k < kApplyIpt; k++) {
+        for (int k = 0; k < AIPT; k++) {
             u64 i = wbase + (u64)k * 32 + lane;
             e[k] = i < n ? list[i] : ~0ull;
         }
         u32 cf = 0, cs = 0;  // running carry within the warp
 #pragma unroll
-        for (int k = 0; k < kApplyIpt; k++) {
+        for (int k = 0; k < AIPT; k++) {
             const u64 i = wbase + (u64)k * 32 + lane;
             const bool v = i < n;
             const u32 m = (u32)(e[k] >> 32);
@@ -769,7 +804,7 @@ __global__ void __launch_bounds__(kApplyBlock) k_apply(BatchDev b, TablesDev T, 
         const u32 wf = s_wf[warp], ws = s_ws[warp];
         const u32 carry = wf ? ws : s_ts + ws;
 #pragma unroll
-        for (int k = 0; k < kApplyIpt; k++) {
+        for (int k = 0; k < AIPT; k++) {
             const u64 i = wbase + (u64)k * 32 + lane;
             if (i < n) {
                 const u32 m = (u32)(e[k] >> 32);
@@ -783,13 +818,17 @@ __global__ void __launch_bounds__(kApplyBlock) k_apply(BatchDev b, TablesDev T, 
     }
 }
 
+__global__ void __launch_bounds__(kApplyBlock) k_apply(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    phase_apply<kApplyBlock>(b, T, s, ctr);
+}
+
 // ============================================================================
 // priority rule (R1): min writer TID per contended cell, aborts, execute
 // ============================================================================
-__global__ void __launch_bounds__(256) k_r1_minw(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
-    if (ctr->err) return;
+__device__ __forceinline__ void phase_r1_minw(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+    if (block_err(ctr)) return;
     const u64 n = b.n_ops;
-    for (u64 i = (u64)blockIdx.x * 256 + threadIdx.x; i - threadIdx.x < n; i += (u64)gridDim.x * 256) {
+    for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i - threadIdx.x < n; i += (u64)gridDim.x * blockDim.x) {
         bool act = false, con = false;
         u32 m = 0, tid = 0;
         if (i < n) {
@@ -809,10 +848,14 @@ __global__ void __launch_bounds__(256) k_r1_minw(BatchDev b, TablesDev T, Scratc
     }
 }
 
-__global__ void __launch_bounds__(256) k_r1_abort(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
-    if (ctr->err) return;
+__global__ void __launch_bounds__(256) k_r1_minw(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    phase_r1_minw(b, T, s, ctr);
+}
+
+__device__ __forceinline__ void phase_r1_abort(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+    if (block_err(ctr)) return;
     const u64 n = b.n_ops;
-    for (u64 i = (u64)blockIdx.x * 256 + threadIdx.x; i < n; i += (u64)gridDim.x * 256) {
+    for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
         const u32 w = b.opw[i];
         OpRef r = decode_op(T, b.keys[i], w);
         u32 m;
@@ -823,10 +866,14 @@ __global__ void __launch_bounds__(256) k_r1_abort(BatchDev b, TablesDev T, Scrat
     }
 }
 
-__global__ void __launch_bounds__(256) k_r1_exec(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
-    if (ctr->err) return;
+__global__ void __launch_bounds__(256) k_r1_abort(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    phase_r1_abort(b, T, s, ctr);
+}
+
+__device__ __forceinline__ void phase_r1_exec(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+    if (block_err(ctr)) return;
     const u64 n = b.n_ops;
-    for (u64 i = (u64)blockIdx.x * 256 + threadIdx.x; i < n; i += (u64)gridDim.x * 256) {
+    for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
         const u32 w = b.opw[i];
         OpRef r = decode_op(T, b.keys[i], w);
         if (!r.valid) continue;
@@ -857,17 +904,23 @@ __global__ void __launch_bounds__(256) k_r1_exec(BatchDev b, TablesDev T, Scratc
     }
 }
 
+__global__ void __launch_bounds__(256) k_r1_exec(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    phase_r1_exec(b, T, s, ctr);
+}
+
 // ============================================================================
 // insert: slots for committed inserts, per table, in (TID, op) order -- a
 // 16-way ordered prefix sum (warp match_any ranks, per-table decoupled
 // look-back) -- then the payload row is copied into its slot
 // ============================================================================
-__global__ void __launch_bounds__(kInsBlock) k_insert(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
-    if (ctr->err) return;
+template <int BLK>
+__device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+    constexpr u32 IIPT = kInsTile / BLK;
+    if (block_err(ctr)) return;
     u32 any = 0;
     for (u32 k = 0; k < T.n; k++) any |= ctr->ins_total[k];
     if (!any) return;
-    constexpr int NW = kInsBlock / 32;
+    constexpr int NW = BLK / 32;
     const u64 n = b.n_ops;
     const u32 tiles = (u32)((n + kInsTile - 1) / kInsTile);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -876,12 +929,12 @@ __global__ void __launch_bounds__(kInsBlock) k_insert(BatchDev b, TablesDev T, S
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_INSERT);
         if (tile >= tiles) break;
-        for (u32 i = threadIdx.x; i < NW * LTP_MAX_TABLES; i += kInsBlock) (&s_wcnt[0][0])[i] = 0;
+        for (u32 i = threadIdx.x; i < NW * LTP_MAX_TABLES; i += BLK) (&s_wcnt[0][0])[i] = 0;
         __syncthreads();
-        const u64 wbase = (u64)tile * kInsTile + (u64)warp * 32 * kInsIpt;
-        u32 tb[kInsIpt], lrank[kInsIpt];
+        const u64 wbase = (u64)tile * kInsTile + (u64)warp * 32 * IIPT;
+        u32 tb[IIPT], lrank[IIPT];
 #pragma unroll
-        for (int k = 0; k < kInsIpt; k++) {
+        for (int k = 0; k < IIPT; k++) {
             const u64 i = wbase + (u64)k * 32 + lane;
             bool ins = false;
             u32 t = LTP_MAX_TABLES;
@@ -941,7 +994,7 @@ __global__ void __launch_bounds__(kInsBlock) k_insert(BatchDev b, TablesDev T, S
         }
         __syncthreads();
 #pragma unroll
-        for (int k = 0; k < kInsIpt; k++) {
+        for (int k = 0; k < IIPT; k++) {
             if (tb[k] < LTP_MAX_TABLES) {
                 const u64 i = wbase + (u64)k * 32 + lane;
                 const TableDev &t = T.t[tb[k]];
@@ -955,12 +1008,16 @@ __global__ void __launch_bounds__(kInsBlock) k_insert(BatchDev b, TablesDev T, S
     }
 }
 
+__global__ void __launch_bounds__(kInsBlock) k_insert(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    phase_insert<kInsBlock>(b, T, s, ctr);
+}
+
 // ============================================================================
 // finish: return the scratch to its clean state, count commits
 // ============================================================================
-__global__ void __launch_bounds__(256) k_finish(BatchDev b, TablesDev T, Scratch s, Counters *ctr, int rule,
-                                                u32 cls_tile) {
-    const u64 gsz = (u64)gridDim.x * 256, g0 = (u64)blockIdx.x * 256 + threadIdx.x;
+__device__ __forceinline__ void phase_finish(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr,
+                                             int rule) {
+    const u64 gsz = (u64)gridDim.x * blockDim.x, g0 = (u64)blockIdx.x * blockDim.x + threadIdx.x;
     u32 any_ins = 0;
     for (u32 k = 0; k < T.n; k++) any_ins |= ctr->ins_total[k];
     if (blockIdx.x == 0 && threadIdx.x < T.n && !ctr->err) T.rows_now[threadIdx.x] += ctr->ins_committed[threadIdx.x];
@@ -989,6 +1046,10 @@ __global__ void __launch_bounds__(256) k_finish(BatchDev b, TablesDev T, Scratch
         c = __reduce_add_sync(FULL_MASK, c);
         if ((threadIdx.x & 31) == 0 && c) atomicAdd(&ctr->committed, (u64)c);
     }
+}
+
+__global__ void __launch_bounds__(256) k_finish(BatchDev b, TablesDev T, Scratch s, Counters *ctr, int rule) {
+    phase_finish(b, T, s, ctr, rule);
 }
 
 __global__ void k_stall(Counters *ctr, u32 ms) {
@@ -1137,9 +1198,140 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
         }
         k_insert<<<capped(gins, (b.n_ops + kInsTile - 1) / kInsTile), kInsBlock, 0, L.stream>>>(b, T, s, ctr);
     }
-    k_finish<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr, L.rule, L.tune.block * L.tune.ipt);
+    k_finish<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr, L.rule);
     mark_ev(10);
     return cudaGetLastError();
+}
+
+// ============================================================================
+// persistent fused kernel: one cooperative launch runs a list of batches
+// through every phase (bitmap build -> ids -> classify -> sort -> apply ->
+// inserts -> clean-up) with grid-wide barriers in between and no host round
+// trip.  Each barrier is a bounded spin; a timeout or any device error ends
+// the run for every block.
+// ============================================================================
+__device__ __forceinline__ void grid_sync(u32 *bar, u32 nblocks, Counters *ctr) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const u32 gen = ld_acquire32(bar + 1);
+        __threadfence();
+        const u32 arrived = atomicAdd(bar, 1u);
+        if (arrived == nblocks - 1) {
+            bar[0] = 0;
+            __threadfence();
+            st_release32(bar + 1, gen + 1);
+        } else {
+            const u64 t0 = gtimer();
+            volatile int *err = &ctr->err;
+            while (ld_acquire32(bar + 1) == gen) {
+                if (*err) break;
+                if (gtimer() - t0 > kSpinLimitNs) {
+                    set_err(ctr, LTP_E_TIMEOUT);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+    }
+    __syncthreads();
+}
+
+struct PersistArgs {
+    const BatchDev *batches;
+    Counters *const *snaps;  // [n_batches] where each batch's counters go after it ran
+    u32 n_batches;
+    int rule;
+    TablesDev T;
+    Scratch s;
+    Counters *ctr;
+    u32 *bar;  // [2] barrier arrival count and generation
+};
+
+constexpr int kPBlock = 256, kPIpt = 4;
+
+__global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
+    const u32 nb = gridDim.x;
+    for (u32 j = 0; j < a.n_batches; j++) {
+        const BatchDev b = a.batches[j];
+        if (blockIdx.x == 0) {  // fresh counters; a device error stays sticky for the run
+            const int keep = a.ctr->err;
+            __syncthreads();
+            u32 *w = reinterpret_cast<u32 *>(a.ctr);
+            for (u32 i = threadIdx.x; i < sizeof(Counters) / 4; i += blockDim.x) w[i] = 0u;
+            __syncthreads();
+            if (threadIdx.x == 0) a.ctr->err = keep;
+        }
+        for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < b.n_txns; t += (u64)nb * blockDim.x) b.commit[t] = 1;
+        grid_sync(a.bar, nb, a.ctr);
+        if (block_err(a.ctr)) break;
+        phase_mark<kPBlock, kPIpt>(b, a.T, a.s, a.ctr);
+        grid_sync(a.bar, nb, a.ctr);
+        if (a.rule == LTP_RULE_PRIORITY) phase_ids<true, kPBlock>(a.T, a.s, a.ctr);
+        else phase_ids<false, kPBlock>(a.T, a.s, a.ctr);
+        grid_sync(a.bar, nb, a.ctr);
+        if (a.rule != LTP_RULE_PRIORITY) {
+            phase_classify<kPBlock, kPIpt>(b, a.T, a.s, a.ctr);
+            grid_sync(a.bar, nb, a.ctr);
+            phase_sort_pass<kPBlock>(0, a.s, a.ctr, b.n_ops, kPBlock * kPIpt);
+            grid_sync(a.bar, nb, a.ctr);
+            phase_sort_pass<kPBlock>(1, a.s, a.ctr, b.n_ops, kPBlock * kPIpt);
+            grid_sync(a.bar, nb, a.ctr);
+            phase_sort_pass<kPBlock>(2, a.s, a.ctr, b.n_ops, kPBlock * kPIpt);
+            grid_sync(a.bar, nb, a.ctr);
+            phase_sort_pass<kPBlock>(3, a.s, a.ctr, b.n_ops, kPBlock * kPIpt);
+            grid_sync(a.bar, nb, a.ctr);
+            phase_apply<kPBlock>(b, a.T, a.s, a.ctr);
+        } else {
+            phase_r1_minw(b, a.T, a.s, a.ctr);
+            grid_sync(a.bar, nb, a.ctr);
+            phase_r1_abort(b, a.T, a.s, a.ctr);
+            grid_sync(a.bar, nb, a.ctr);
+            phase_r1_exec(b, a.T, a.s, a.ctr);
+        }
+        grid_sync(a.bar, nb, a.ctr);
+        phase_insert<kPBlock>(b, a.T, a.s, a.ctr);
+        grid_sync(a.bar, nb, a.ctr);
+        phase_finish(b, a.T, a.s, a.ctr, a.rule);
+        grid_sync(a.bar, nb, a.ctr);
+        if (blockIdx.x == 0) {
+            const u32 *src = reinterpret_cast<const u32 *>(a.ctr);
+            u32 *dst = reinterpret_cast<u32 *>(a.snaps[j]);
+            for (u32 i = threadIdx.x; i < sizeof(Counters) / 4; i += blockDim.x) dst[i] = src[i];
+        }
+        if (block_err(a.ctr)) break;
+        grid_sync(a.bar, nb, a.ctr);
+    }
+}
+
+cudaError_t launch_persistent(cudaStream_t st, int num_sms, int rule, const BatchDev *d_batches,
+                              Counters *const *d_snaps, u32 n_batches, const TablesDev &T, const Scratch &s,
+                              Counters *ctr, u32 *bar) {
+    constexpr size_t smem = 4ull * 2 * kPBlock * kPIpt * sizeof(u32);
+    static int grid = 0, sms = 0;
+    if (sms != num_sms) {
+        cudaFuncSetAttribute(k_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        grid = occ_grid(k_persist, kPBlock, num_sms, smem);
+        sms = num_sms;
+    }
+    cudaError_t e = cudaMemsetAsync(bar, 0, 2 * sizeof(u32), st);
+    if (e != cudaSuccess) return e;
+    PersistArgs a;
+    a.batches = d_batches;
+    a.snaps = d_snaps;
+    a.n_batches = n_batches;
+    a.rule = rule;
+    a.T = T;
+    a.s = s;
+    a.ctr = ctr;
+    a.bar = bar;
+    void *args[] = {&a};
+    return cudaLaunchCooperativeKernel((const void *)k_persist, dim3(grid), dim3(kPBlock), args, smem, st);
+}
+
+int persistent_grid(int num_sms) {
+    constexpr size_t smem = 4ull * 2 * kPBlock * kPIpt * sizeof(u32);
+    cudaFuncSetAttribute(k_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return occ_grid(k_persist, kPBlock, num_sms, smem);
 }
 
 cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s) {

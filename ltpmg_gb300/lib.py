@@ -20,6 +20,7 @@ LTP_E_DEVICE_ASSERT, LTP_E_NOMEM, LTP_E_STATE = -5, -6, -7
 RULE_ORDERED, RULE_PRIORITY = 0, 1
 OP_READ, OP_ADD, OP_INSERT = 0, 1, 2
 FLAG_STAGE_TIMING = 1
+MODE_STREAM, MODE_GRAPH, MODE_PERSISTENT = 0, 1, 2
 STAGE_NAMES = ["mark", "ids", "classify", "sort_hist", "sort_pass0", "sort_pass1", "sort_pass2", "sort_pass3",
                "apply", "finish", "unused", "total"]
 
@@ -108,6 +109,7 @@ def load():
         "ltp_batch_load_payload": (ci, [vp, vp, vp, u64, vp]),
         "ltp_compat_last_status": (ci, []),
         "ltp_compat_last_error": (ctypes.c_char_p, []),
+        "ltp_batches_execute": (ci, [vp, vp, u32, i32, vp]),
         "ltp_execute_noalloc": (ci, [i32, i32, vp, u64, u64, u32, u64, vp, u32, u64, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
@@ -266,6 +268,11 @@ class Context:
         t = Tuning()
         self.check(self.L.ltp_get_tuning(self.h, bucket, ctypes.byref(t)))
         return (t.block, t.ipt, t.word_bits)
+
+    def execute_many(self, batches, mode=0, stream=None):
+        """Executes batches in order: mode 0 stream, 1 CUDA graph, 2 persistent kernel."""
+        arr = (ctypes.c_void_p * max(len(batches), 1))(*[b.h.value for b in batches])
+        self.check(self.L.ltp_batches_execute(self.h, arr, len(batches), mode, _stream(stream)))
 
     def stall_next(self, ms):
         self.check(self.L.ltp_debug_stall_next(self.h, ms))

@@ -1,0 +1,71 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+They stand in for YCSB / TPC-C inputs (no suite items are used): the
+library's generator draws keys, op kinds and columns from per-transaction
+SplitMix64 streams, so every batch is reproducible from (seed, batch index).
+
+plain   2^20 rows x 10 int32, batches of 2^16 transactions x 10 ops, uniform
+        keys, 50% reads / 50% +1 read-modify-writes, 16 batches
+zipf    2^24 rows x 10 int32, batches of 2^20 transactions x 16 ops, Zipf 0.99
+        keys over a seeded permutation, 80% / 20%, 32 batches
+uneven  2^24 rows x 10 int32, 64 batches of 2^U[10,20] transactions (log-
+        uniform), 1-32 ops per transaction, Zipf theta ~ U[0.5, 0.99] per
+        batch, 70% / 30%
+"""
+import math
+
+from . import lib as L
+
+SEED = 0x4C54504D47
+
+SHAPES = {
+    "plain": dict(rows=1 << 20, cols=10, batches=16, seed=SEED),
+    "zipf": dict(rows=1 << 24, cols=10, batches=32, seed=SEED + 2),
+    "uneven": dict(rows=1 << 24, cols=10, batches=64, seed=SEED + 4),
+}
+
+
+def _mix(z):
+    z &= 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    return z ^ (z >> 31)
+
+
+def batch_params(name, b, seed=None):
+    """(n_txns, ops_min, ops_max, read_frac, theta) of batch b."""
+    s = SHAPES[name]["seed"] if seed is None else seed
+    if name == "plain":
+        return 1 << 16, 10, 10, 0.5, 0.0
+    if name == "zipf":
+        return 1 << 20, 16, 16, 0.8, 0.99
+    u = _mix(s ^ (0xC4 << 40) ^ b)
+    v = _mix(u)
+    n = int(round(2.0 ** (10 + 10 * ((u >> 11) / float(1 << 53)))))
+    theta = 0.5 + 0.49 * ((v >> 11) / float(1 << 53))
+    return n, 1, 32, 0.7, theta
+
+
+def generate(name, b, seed=None, rank=0):
+    """(txn_first, keys, opw, n_txns, ops_per_txn) of batch b; ops_per_txn is
+    0 when transactions vary in length."""
+    sh = SHAPES[name]
+    s = (sh["seed"] if seed is None else seed) + rank
+    n, omin, omax, rf, th = batch_params(name, b, s)
+    tf, keys, opw = L.gen_ycsb(s, sh["rows"], sh["cols"], omin, omax, rf, th, batch=b, n_txns=n)
+    return tf, keys, opw, n, (omin if omin == omax else 0)
+
+
+def algorithmic_bytes(n_ops, n_txns):
+    """28 B per op (key 8, opword 4, value read 4, value written 4, conflict
+    state 8) + 4 B per transaction (commit word / descriptor)."""
+    return 28 * n_ops + 4 * n_txns
+
+
+def expected_txns(name):
+    if name != "uneven":
+        return SHAPES[name]["batches"] * batch_params(name, 0)[0]
+    return sum(batch_params(name, b)[0] for b in range(SHAPES[name]["batches"]))
+
+
+_ = math

@@ -364,3 +364,58 @@ def test_insert_capacity_and_payload_errors(lib_loaded):
         assert vals.tolist() == [10, 11]
         after = ctx.download(t)
         assert after.shape == (2, 12) and after[:, 10].tolist() == [5, 6] and after[:, 11].tolist() == [7, 8]
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+@pytest.mark.parametrize("mode", [G.lib.MODE_STREAM, G.lib.MODE_GRAPH, G.lib.MODE_PERSISTENT])
+def test_multi_batch_modes(lib_loaded, rule, mode):
+    """Uneven batches (sizes, ops per transaction and skew vary per batch) run
+    through one multi-batch call, twice with new contents of the same sizes
+    (the second call replays the cached graph), against the oracle."""
+    rows, cols, seed = 1 << 14, 10, 99
+    shapes = [(1 << 10, 1, 32, 0.5), (3000, 1, 32, 0.99), (200, 4, 4, 0.8), (1 << 12, 16, 16, 0.7), (1, 1, 1, 0.9)]
+    with G.Context(device=0, rule=rule) as ctx:
+        t = ctx.create_table(rows, cols)
+        ctx.fill_seeded(t, seed)
+        ref = O.table_init(seed, rows, cols)
+        bs = [ctx.batch(n, n * omax) for n, omin, omax, th in shapes]
+        for rep in range(2):
+            data = []
+            for k, ((n, omin, omax, th), b) in enumerate(zip(shapes, bs)):
+                tf, keys, opw = gen(seed + rep, rows, cols, omin, omax, 0.7, th, k, n)
+                b.load(tf, keys, opw)
+                data.append((tf, keys, opw))
+            ctx.execute_many(bs, mode=mode)
+            for (tf, keys, opw), b in zip(data, bs):
+                commit, vals, st = b.results()
+                ref, rc, ro = O.replay(rule, ref, tf, keys, opw)
+                assert np.array_equal(commit, rc)
+                assert np.array_equal(vals, ro)
+            assert np.array_equal(ctx.download(t), ref)
+
+
+def test_persistent_mode_with_inserts(lib_loaded):
+    rng = np.random.default_rng(5)
+    with G.Context(device=0) as ctx:
+        t = ctx.create_table(300, 4, rows_cap=300 + 5000)
+        ctx.fill_seeded(t, 3)
+        data = np.zeros((4, 5300), np.int32)
+        data[:, :300] = O.table_init(3, 300, 4)
+        ref = [(data, 300)]
+        bs, batches = [], []
+        cur = [(300, 4)]
+        for k in range(3):
+            tf, keys, opw, payload = _insert_batch(rng, cur, 800, p_ins=0.2)
+            # keys of reads/RMWs must name rows that exist before this batch
+            b = ctx.batch(800, len(keys))
+            b.load(tf, keys, opw)
+            b.load_payload(payload)
+            bs.append(b)
+            batches.append((tf, keys, opw, payload))
+        ctx.execute_many(bs, mode=G.lib.MODE_PERSISTENT)
+        for (tf, keys, opw, payload), b in zip(batches, bs):
+            commit, vals, _ = b.results()
+            ref, rc, ro = O.replay_tables(0, ref, tf, keys, opw, payload)
+            assert np.array_equal(vals, ro)
+        assert ctx.table_rows(t) == ref[0][1]
+        assert np.array_equal(ctx.download(t), ref[0][0][:, :ref[0][1]])
