@@ -655,13 +655,20 @@ int ltp_batch_finish(ltp_ctx *ctx, ltp_batch *b, ltp_stats *stats, void *stream)
         stats->touched_words = c.n_tw;
         stats->bytes_algorithmic = 28ull * b->n_ops + 4ull * b->n_txns;
         if (b->have_events && b->n_ops) {
+            // stage events are absent for batches run by the persistent kernel
             for (int i = 0; i < 10; i++) {
                 float ms = 0;
-                cudaEventElapsedTime(&ms, b->ev[i], b->ev[i + 1]);
+                if (cudaEventElapsedTime(&ms, b->ev[i], b->ev[i + 1]) != cudaSuccess) {
+                    (void)cudaGetLastError();
+                    ms = -1.0f;
+                }
                 stats->ms_stage[i] = ms;
             }
             float total = 0;
-            cudaEventElapsedTime(&total, b->ev[0], b->ev[10]);
+            if (cudaEventElapsedTime(&total, b->ev[0], b->ev[10]) != cudaSuccess) {
+                (void)cudaGetLastError();
+                total = -1.0f;
+            }
             stats->ms_stage[11] = total;
         }
     }

@@ -1085,7 +1085,10 @@ __global__ void k_expand_op_txn(const u32 *txn_first, u64 n_txns, u32 *op_txn) {
 template <typename K>
 static int occ_grid(K kernel, int block, int num_sms, size_t dyn_smem = 0) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, dyn_smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, dyn_smem) != cudaSuccess) {
+        (void)cudaGetLastError();
+        per_sm = 1;
+    }
     if (per_sm < 1) per_sm = 1;
     return per_sm * num_sms;
 }
@@ -1096,7 +1099,9 @@ struct Front {
     static constexpr size_t kMarkSmem = 4ull * 2 * BLOCK * IPT * sizeof(u32);
     static void grids(int num_sms) {
         if (sms != num_sms) {
-            cudaFuncSetAttribute(k_mark<BLOCK, IPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMarkSmem);
+            if (cudaFuncSetAttribute(k_mark<BLOCK, IPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kMarkSmem) != cudaSuccess)
+                return;  // the launch below then reports the error
             g_mark = occ_grid(k_mark<BLOCK, IPT>, BLOCK, num_sms, kMarkSmem);
             g_cls = occ_grid(k_classify<BLOCK, IPT>, BLOCK, num_sms);
             sms = num_sms;
@@ -1139,6 +1144,7 @@ static void pick_front(const Tuning &t, front_fn *mark, front_fn *classify) {
 static int capped(int grid, u64 upper) { return (int)((u64)grid < upper ? (u64)grid : (upper ? upper : 1)); }
 
 cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+    (void)cudaGetLastError();  // report only the launches below
     // stage event i is recorded after kernel i; event 0 of the batch precedes everything
     auto mark_ev = [&](int i) {
         if (L.timing) cudaEventRecord(L.ev[i], L.stream);
@@ -1309,10 +1315,12 @@ cudaError_t launch_persistent(cudaStream_t st, int num_sms, int rule, const Batc
     constexpr size_t smem = 4ull * 2 * kPBlock * kPIpt * sizeof(u32);
     static int grid = 0, sms = 0;
     if (sms != num_sms) {
-        cudaFuncSetAttribute(k_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t fe = cudaFuncSetAttribute(k_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (fe != cudaSuccess) return fe;
         grid = occ_grid(k_persist, kPBlock, num_sms, smem);
         sms = num_sms;
     }
+    (void)cudaGetLastError();
     cudaError_t e = cudaMemsetAsync(bar, 0, 2 * sizeof(u32), st);
     if (e != cudaSuccess) return e;
     PersistArgs a;
