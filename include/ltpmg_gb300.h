@@ -186,6 +186,30 @@ int ltp_batch_results(ltp_ctx *ctx, ltp_batch *b, uint8_t *commit, int32_t *vals
 int ltp_batch_device_ptrs(ltp_batch *b, uint64_t **keys, uint32_t **opw, uint32_t **txn_first, int32_t **vals,
                           uint8_t **commit);
 
+/* ---- pipelined submission ---------------------------------------------- */
+/* A pipeline keeps `depth` device batch slots and three streams: batch k+1's
+ * host->device copy and batch k-1's device->host copy overlap batch k's
+ * execution.  Batches execute one after another in submission order against
+ * the context's tables (the serial order of the whole stream of batches).
+ * Host buffers should be pinned (ltp_host_alloc) for the copies to overlap.
+ * Replaces the reference's synchronous per-epoch transfer_query_to_GPU /
+ * execute_on_GPU sequence (src/scheduler.cpp:44-59).  After a batch reports
+ * an error the pipeline must be drained and freed. */
+typedef struct ltp_pipe ltp_pipe;
+int ltp_pipe_create(ltp_ctx *ctx, uint32_t depth, uint64_t max_txns, uint64_t max_ops, ltp_pipe **out);
+int ltp_pipe_free(ltp_pipe *p);
+/* Enqueues one batch (txn_first may be NULL for fixed-length transactions;
+ * payload may be NULL).  commit_out / vals_out receive the results (either
+ * may be NULL).  Blocks only while all slots are in flight.  *ticket numbers
+ * the batch for ltp_pipe_wait. */
+int ltp_pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
+                    const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
+                    uint8_t *commit_out, int32_t *vals_out, uint64_t *ticket);
+/* Waits until the ticket's results are in its host buffers; returns its status. */
+int ltp_pipe_wait(ltp_pipe *p, uint64_t ticket, ltp_stats *stats);
+/* LTP_OK when the ticket's results are ready, 1 while it is in flight. */
+int ltp_pipe_poll(ltp_pipe *p, uint64_t ticket);
+
 /* ---- pinned host memory ------------------------------------------------ */
 void *ltp_host_alloc(size_t bytes);
 void ltp_host_free(void *p);

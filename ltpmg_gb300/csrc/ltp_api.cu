@@ -85,6 +85,12 @@ int cuda_fail(ltp_ctx *ctx, cudaError_t e, const char *where) {
         if (_e != cudaSuccess) return cuda_fail(ctx, _e, #call); \
     } while (0)
 
+#define CK_CTX(c, call)                                          \
+    do {                                                         \
+        cudaError_t _e = (call);                                 \
+        if (_e != cudaSuccess) return cuda_fail((c), _e, #call); \
+    } while (0)
+
 cudaStream_t pick_stream(ltp_ctx *ctx, void *stream) { return stream ? (cudaStream_t)stream : ctx->stream; }
 
 template <typename T>
@@ -735,6 +741,158 @@ int ltp_get_tuning(ltp_ctx *ctx, uint32_t bucket, ltp_tuning *t) {
 int ltp_debug_stall_next(ltp_ctx *ctx, uint32_t ms) {
     if (!ctx || ms == 0 || ms > 10000) return LTP_E_BADARG;
     ctx->stall_ms_next = ms;
+    return LTP_OK;
+}
+
+}  // extern "C"
+
+// ============================================================================
+// pipelined submission
+// ============================================================================
+namespace {
+
+struct PipeSlot {
+    ltp_batch *b = nullptr;
+    cudaEvent_t in = nullptr, exec = nullptr, out = nullptr;
+    Counters *host_ctr = nullptr;  // pinned copy of the batch's counters
+    uint64_t ticket = UINT64_MAX;
+    bool waited = true;
+    int status = LTP_OK;
+};
+
+}  // namespace
+
+struct ltp_pipe {
+    ltp_ctx *ctx = nullptr;
+    std::vector<PipeSlot> slots;
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    uint64_t next = 0;
+};
+
+static int pipe_finalize(ltp_pipe *p, PipeSlot &sl) {
+    ltp_ctx *ctx = p->ctx;
+    CK(cudaEventSynchronize(sl.out));
+    if (!sl.waited) {
+        sl.status = sl.host_ctr->err;
+        if (sl.status) ctx->dirty = true;
+        sl.waited = true;
+    }
+    return LTP_OK;
+}
+
+extern "C" {
+
+int ltp_pipe_create(ltp_ctx *ctx, uint32_t depth, uint64_t max_txns, uint64_t max_ops, ltp_pipe **out) {
+    if (!ctx || !out || depth < 2 || depth > 64) return LTP_E_BADARG;
+    *out = nullptr;
+    CK(cudaSetDevice(ctx->device));
+    int rc = ensure_scratch(ctx, max_ops);
+    if (rc) return rc;
+    ltp_pipe *p = new ltp_pipe();
+    p->ctx = ctx;
+    p->slots.resize(depth);
+    cudaError_t e = cudaStreamCreateWithFlags(&p->s_in, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->s_out, cudaStreamNonBlocking);
+    for (auto &sl : p->slots) {
+        if (e != cudaSuccess) break;
+        if ((rc = ltp_batch_create(ctx, max_txns, max_ops, &sl.b))) break;
+        e = cudaEventCreateWithFlags(&sl.in, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.exec, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.out, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaMallocHost((void **)&sl.host_ctr, sizeof(Counters));
+    }
+    if (rc || e != cudaSuccess) {
+        ltp_pipe_free(p);
+        return rc ? rc : cuda_fail(ctx, e, "ltp_pipe_create");
+    }
+    *out = p;
+    return LTP_OK;
+}
+
+int ltp_pipe_free(ltp_pipe *p) {
+    if (!p) return LTP_E_BADARG;
+    ltp_ctx *ctx = p->ctx;
+    cudaSetDevice(ctx->device);
+    for (auto &sl : p->slots) {
+        if (sl.out) cudaEventSynchronize(sl.out);
+        if (sl.b) ltp_batch_free(ctx, sl.b);
+        if (sl.in) cudaEventDestroy(sl.in);
+        if (sl.exec) cudaEventDestroy(sl.exec);
+        if (sl.out) cudaEventDestroy(sl.out);
+        if (sl.host_ctr) cudaFreeHost(sl.host_ctr);
+    }
+    if (p->s_in) cudaStreamDestroy(p->s_in);
+    if (p->s_out) cudaStreamDestroy(p->s_out);
+    delete p;
+    return LTP_OK;
+}
+
+int ltp_pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
+                    const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
+                    uint8_t *commit_out, int32_t *vals_out, uint64_t *ticket) {
+    if (!p) return LTP_E_BADARG;
+    ltp_ctx *ctx = p->ctx;
+    CK(cudaSetDevice(ctx->device));
+    const uint64_t t = p->next;
+    PipeSlot &sl = p->slots[t % p->slots.size()];
+    if (sl.ticket != UINT64_MAX) {  // the slot's previous batch must be out
+        int rc = pipe_finalize(p, sl);
+        if (rc) return rc;
+    }
+    if (ctx->dirty) return fail(ctx, LTP_E_STATE, "an earlier batch of this pipeline failed");
+    int rc = ltp_batch_load(ctx, sl.b, n_txns, txn_first, ops_per_txn, n_ops, keys, opw, p->s_in);
+    if (rc) return rc;
+    if (payload && payload_len) {
+        if (payload_len > sl.b->payload_cap) CK(cudaStreamSynchronize(p->s_in));
+        if ((rc = ltp_batch_load_payload(ctx, sl.b, payload, payload_len, p->s_in))) return rc;
+    }
+    CK(cudaEventRecord(sl.in, p->s_in));
+    cudaStream_t sx = ctx->stream;
+    CK(cudaStreamWaitEvent(sx, sl.in, 0));
+    if ((rc = execute_one(ctx, sl.b, sx, false))) return rc;
+    CK(cudaMemcpyAsync(sl.host_ctr, sl.b->snap, sizeof(Counters), cudaMemcpyDeviceToHost, sx));
+    CK(cudaEventRecord(sl.exec, sx));
+    CK(cudaStreamWaitEvent(p->s_out, sl.exec, 0));
+    if ((rc = ltp_batch_fetch(ctx, sl.b, commit_out, vals_out, p->s_out))) return rc;
+    CK(cudaEventRecord(sl.out, p->s_out));
+    sl.ticket = t;
+    sl.waited = false;
+    sl.status = LTP_OK;
+    p->next = t + 1;
+    if (ticket) *ticket = t;
+    return LTP_OK;
+}
+
+int ltp_pipe_wait(ltp_pipe *p, uint64_t ticket, ltp_stats *stats) {
+    if (!p) return LTP_E_BADARG;
+    PipeSlot &sl = p->slots[ticket % p->slots.size()];
+    if (sl.ticket != ticket) return fail(p->ctx, LTP_E_STATE, "ticket no longer held by the pipeline");
+    CK_CTX(p->ctx, cudaSetDevice(p->ctx->device));
+    int rc = pipe_finalize(p, sl);
+    if (rc) return rc;
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        const Counters &c = *sl.host_ctr;
+        stats->txns = sl.b->n_txns;
+        stats->ops = sl.b->n_ops;
+        stats->committed = sl.b->rule == LTP_RULE_PRIORITY ? c.committed : sl.b->n_txns;
+        stats->aborted = sl.b->n_txns - stats->committed;
+        stats->contended_ops = c.n_c;
+        stats->contended_cells = c.M;
+        stats->touched_words = c.n_tw;
+        stats->bytes_algorithmic = 28ull * sl.b->n_ops + 4ull * sl.b->n_txns;
+    }
+    if (sl.status) p->ctx->last_error = ltp_status_string(sl.status);
+    return sl.status;
+}
+
+int ltp_pipe_poll(ltp_pipe *p, uint64_t ticket) {
+    if (!p) return LTP_E_BADARG;
+    PipeSlot &sl = p->slots[ticket % p->slots.size()];
+    if (sl.ticket != ticket) return LTP_E_STATE;
+    cudaError_t e = cudaEventQuery(sl.out);
+    if (e == cudaErrorNotReady) return 1;
+    if (e != cudaSuccess) return cuda_fail(p->ctx, e, "ltp_pipe_poll");
     return LTP_OK;
 }
 

@@ -1146,8 +1146,13 @@ static int capped(int grid, u64 upper) { return (int)((u64)grid < upper ? (u64)g
 cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
     (void)cudaGetLastError();  // report only the launches below
     // stage event i is recorded after kernel i; event 0 of the batch precedes everything
+    // under stream capture the stage events become external event nodes, so
+    // they still carry timestamps when the graph replays
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (L.timing) cudaStreamIsCapturing(L.stream, &cap);
+    const unsigned ev_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
     auto mark_ev = [&](int i) {
-        if (L.timing) cudaEventRecord(L.ev[i], L.stream);
+        if (L.timing) cudaEventRecordWithFlags(L.ev[i], L.stream, ev_flags);
     };
     mark_ev(0);
     if (L.stall) k_stall<<<1, 1, 0, L.stream>>>(ctr, L.stall_ms);

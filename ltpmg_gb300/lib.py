@@ -110,6 +110,11 @@ def load():
         "ltp_compat_last_status": (ci, []),
         "ltp_compat_last_error": (ctypes.c_char_p, []),
         "ltp_batches_execute": (ci, [vp, vp, u32, i32, vp]),
+        "ltp_pipe_create": (ci, [vp, u32, u64, u64, pp]),
+        "ltp_pipe_free": (ci, [vp]),
+        "ltp_pipe_submit": (ci, [vp, u64, vp, u32, u64, vp, vp, vp, u64, vp, vp, ctypes.POINTER(u64)]),
+        "ltp_pipe_wait": (ci, [vp, u64, ctypes.POINTER(Stats)]),
+        "ltp_pipe_poll": (ci, [vp, u64]),
         "ltp_execute_noalloc": (ci, [i32, i32, vp, u64, u64, u32, u64, vp, u32, u64, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
@@ -336,3 +341,49 @@ class Batch:
         st = Stats()
         self.ctx.check(self.ctx.L.ltp_batch_results(self.ctx.h, self.h, _p(commit), _p(vals), ctypes.byref(st)))
         return commit[: self.n_txns], vals[: self.n_ops], st
+
+
+class Pipe:
+    """Pipelined submission (the C-ABI ltp_pipe): copy-in, execution and
+    copy-out of consecutive batches overlap on three streams."""
+
+    def __init__(self, ctx, depth, max_txns, max_ops):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        ctx.check(ctx.L.ltp_pipe_create(ctx.h, depth, max_txns, max_ops, ctypes.byref(h)))
+        self.h = h
+        self._keep = {}
+
+    def submit(self, txn_first, keys, opw, commit_out=None, vals_out=None, ops_per_txn=0, payload=None):
+        """Arrays must stay alive (and unchanged) until wait(ticket)."""
+        if txn_first is not None:
+            n_txns = len(txn_first) - 1
+        else:
+            n_txns = len(keys) // ops_per_txn if ops_per_txn else 0
+        t = ctypes.c_uint64()
+        self.ctx.check(self.ctx.L.ltp_pipe_submit(
+            self.h, n_txns, _p(txn_first), ops_per_txn, len(keys), _p(keys), _p(opw), _p(payload),
+            0 if payload is None else len(payload), _p(commit_out), _p(vals_out), ctypes.byref(t)))
+        self._keep[t.value] = (txn_first, keys, opw, commit_out, vals_out, payload)
+        return t.value
+
+    def wait(self, ticket):
+        st = Stats()
+        rc = self.ctx.L.ltp_pipe_wait(self.h, ticket, ctypes.byref(st))
+        self._keep.pop(ticket, None)
+        self.ctx.check(rc)
+        return st
+
+    def poll(self, ticket):
+        return self.ctx.L.ltp_pipe_poll(self.h, ticket) == 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.ltp_pipe_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

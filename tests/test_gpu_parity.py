@@ -419,3 +419,33 @@ def test_persistent_mode_with_inserts(lib_loaded):
             assert np.array_equal(vals, ro)
         assert ctx.table_rows(t) == ref[0][1]
         assert np.array_equal(ctx.download(t), ref[0][0][:, :ref[0][1]])
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+def test_pipeline_matches_oracle(lib_loaded, rule):
+    """Batches submitted through the 3-deep pipeline (overlapped copy-in,
+    execution, copy-out) give the serial replay of the whole sequence."""
+    rows, cols, seed = 1 << 13, 10, 17
+    with G.Context(device=0, rule=rule) as ctx:
+        t = ctx.create_table(rows, cols)
+        ctx.fill_seeded(t, seed)
+        ref = O.table_init(seed, rows, cols)
+        pipe = G.Pipe(ctx, 3, 4096, 4096 * 32)
+        subs, pinned = [], []
+        for k in range(7):
+            n = [4096, 100, 2000, 1, 3000, 4096, 512][k]
+            tf, keys, opw = gen(seed, rows, cols, 1, 32, 0.7, 0.9, k, n)
+            if k % 2:
+                pinned.append(G.PinnedArray((n,), np.uint8))
+                commit = pinned[-1].array
+            else:
+                commit = np.zeros(n, np.uint8)
+            vals = np.zeros(len(keys), np.int32)
+            subs.append((pipe.submit(tf, keys, opw, commit, vals), tf, keys, opw, commit, vals))
+        for tk, tf, keys, opw, commit, vals in subs:
+            st = pipe.wait(tk)
+            ref, rc, ro = O.replay(rule, ref, tf, keys, opw)
+            assert np.array_equal(commit, rc) and np.array_equal(vals, ro)
+            assert st.ops == len(keys)
+        pipe.close()
+        assert np.array_equal(ctx.download(t), ref)
