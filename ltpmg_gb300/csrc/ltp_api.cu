@@ -8,6 +8,7 @@
 #include <string.h>
 
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "ltp_internal.cuh"
@@ -762,12 +763,31 @@ struct PipeSlot {
 
 }  // namespace
 
+struct PipeDone {
+    int status;
+    ltp_stats stats;
+};
+
 struct ltp_pipe {
     ltp_ctx *ctx = nullptr;
     std::vector<PipeSlot> slots;
     cudaStream_t s_in = nullptr, s_out = nullptr;
     uint64_t next = 0;
+    std::unordered_map<uint64_t, PipeDone> done;  // finished tickets whose slot was reused
 };
+
+static void pipe_stats(const PipeSlot &sl, ltp_stats *stats) {
+    memset(stats, 0, sizeof(*stats));
+    const Counters &c = *sl.host_ctr;
+    stats->txns = sl.b->n_txns;
+    stats->ops = sl.b->n_ops;
+    stats->committed = sl.b->rule == LTP_RULE_PRIORITY ? c.committed : sl.b->n_txns;
+    stats->aborted = sl.b->n_txns - stats->committed;
+    stats->contended_ops = c.n_c;
+    stats->contended_cells = c.M;
+    stats->touched_words = c.n_tw;
+    stats->bytes_algorithmic = 28ull * sl.b->n_ops + 4ull * sl.b->n_txns;
+}
 
 static int pipe_finalize(ltp_pipe *p, PipeSlot &sl) {
     ltp_ctx *ctx = p->ctx;
@@ -836,8 +856,15 @@ int ltp_pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uin
     const uint64_t t = p->next;
     PipeSlot &sl = p->slots[t % p->slots.size()];
     if (sl.ticket != UINT64_MAX) {  // the slot's previous batch must be out
+        const bool unwaited = !sl.waited;
         int rc = pipe_finalize(p, sl);
         if (rc) return rc;
+        if (unwaited) {  // keep its status for a later ltp_pipe_wait
+            PipeDone d;
+            d.status = sl.status;
+            pipe_stats(sl, &d.stats);
+            p->done[sl.ticket] = d;
+        }
     }
     if (ctx->dirty) return fail(ctx, LTP_E_STATE, "an earlier batch of this pipeline failed");
     int rc = ltp_batch_load(ctx, sl.b, n_txns, txn_first, ops_per_txn, n_ops, keys, opw, p->s_in);
@@ -865,29 +892,27 @@ int ltp_pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uin
 
 int ltp_pipe_wait(ltp_pipe *p, uint64_t ticket, ltp_stats *stats) {
     if (!p) return LTP_E_BADARG;
+    auto it = p->done.find(ticket);
+    if (it != p->done.end()) {
+        const PipeDone d = it->second;
+        p->done.erase(it);
+        if (stats) *stats = d.stats;
+        if (d.status) p->ctx->last_error = ltp_status_string(d.status);
+        return d.status;
+    }
     PipeSlot &sl = p->slots[ticket % p->slots.size()];
-    if (sl.ticket != ticket) return fail(p->ctx, LTP_E_STATE, "ticket no longer held by the pipeline");
+    if (sl.ticket != ticket) return fail(p->ctx, LTP_E_STATE, "unknown or already waited ticket");
     CK_CTX(p->ctx, cudaSetDevice(p->ctx->device));
     int rc = pipe_finalize(p, sl);
     if (rc) return rc;
-    if (stats) {
-        memset(stats, 0, sizeof(*stats));
-        const Counters &c = *sl.host_ctr;
-        stats->txns = sl.b->n_txns;
-        stats->ops = sl.b->n_ops;
-        stats->committed = sl.b->rule == LTP_RULE_PRIORITY ? c.committed : sl.b->n_txns;
-        stats->aborted = sl.b->n_txns - stats->committed;
-        stats->contended_ops = c.n_c;
-        stats->contended_cells = c.M;
-        stats->touched_words = c.n_tw;
-        stats->bytes_algorithmic = 28ull * sl.b->n_ops + 4ull * sl.b->n_txns;
-    }
+    if (stats) pipe_stats(sl, stats);
     if (sl.status) p->ctx->last_error = ltp_status_string(sl.status);
     return sl.status;
 }
 
 int ltp_pipe_poll(ltp_pipe *p, uint64_t ticket) {
     if (!p) return LTP_E_BADARG;
+    if (p->done.count(ticket)) return LTP_OK;
     PipeSlot &sl = p->slots[ticket % p->slots.size()];
     if (sl.ticket != ticket) return LTP_E_STATE;
     cudaError_t e = cudaEventQuery(sl.out);
