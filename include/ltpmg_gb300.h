@@ -234,6 +234,10 @@ typedef struct {
 int ltp_set_tuning(ltp_ctx *ctx, uint32_t bucket, const ltp_tuning *t);
 int ltp_get_tuning(ltp_ctx *ctx, uint32_t bucket, ltp_tuning *t);
 
+/* Turns per-kernel event timing on or off for later executions (batches
+ * created while the context had LTP_FLAG_STAGE_TIMING carry the events). */
+int ltp_set_stage_timing(ltp_ctx *ctx, int32_t on);
+
 /* ---- failure injection for tests (host-side; no GPU fault) ------------- */
 /* While set, the next execute's first stage polls a flag that nothing sets,
  * gives up after about `ms` milliseconds and the batch reports LTP_E_TIMEOUT;

@@ -511,7 +511,7 @@ int execute_one(ltp_ctx *ctx, ltp_batch *b, cudaStream_t st, bool allow_stall) {
     L.stall = allow_stall && ctx->stall_ms_next != 0;
     L.stall_ms = ctx->stall_ms_next;
     if (allow_stall) ctx->stall_ms_next = 0;
-    L.timing = b->have_events;
+    L.timing = b->have_events && (ctx->flags & LTP_FLAG_STAGE_TIMING);
     L.ev = b->ev;
     if (b->n_ops) CK(launch_execute(L, batch_dev(b), tables_dev(ctx), ctx->s, ctx->ctr));
     CK(cudaMemcpyAsync(b->snap, ctx->ctr, sizeof(Counters), cudaMemcpyDeviceToDevice, st));
@@ -572,7 +572,8 @@ int ltp_batches_execute(ltp_ctx *ctx, ltp_batch *const *batches, uint32_t n, int
             const Tuning &t = ctx->tuning[bucket_of(b->n_ops)];
             key.insert(key.end(), {(uint64_t)(uintptr_t)b, b->n_ops, b->n_txns, b->ops_per_txn,
                                    (uint64_t)(uintptr_t)b->payload, b->payload_len,
-                                   ((uint64_t)t.block << 32) | t.ipt, (uint64_t)b->have_events});
+                                   ((uint64_t)t.block << 32) | t.ipt,
+                                   (uint64_t)(b->have_events && (ctx->flags & LTP_FLAG_STAGE_TIMING))});
         }
         if (!ctx->graph_exec || key != ctx->graph_key) {
             if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
@@ -661,7 +662,7 @@ int ltp_batch_finish(ltp_ctx *ctx, ltp_batch *b, ltp_stats *stats, void *stream)
         stats->contended_cells = c.M;
         stats->touched_words = c.n_tw;
         stats->bytes_algorithmic = 28ull * b->n_ops + 4ull * b->n_txns;
-        if (b->have_events && b->n_ops) {
+        if (b->have_events && (ctx->flags & LTP_FLAG_STAGE_TIMING) && b->n_ops) {
             // stage events are absent for batches run by the persistent kernel
             for (int i = 0; i < 10; i++) {
                 float ms = 0;
@@ -736,6 +737,13 @@ int ltp_get_tuning(ltp_ctx *ctx, uint32_t bucket, ltp_tuning *t) {
     t->ipt = ctx->tuning[bucket].ipt;
     t->word_bits = ctx->tuning[bucket].word_bits;
     t->reserved = 0;
+    return LTP_OK;
+}
+
+int ltp_set_stage_timing(ltp_ctx *ctx, int32_t on) {
+    if (!ctx) return LTP_E_BADARG;
+    if (on) ctx->flags |= LTP_FLAG_STAGE_TIMING;
+    else ctx->flags &= ~LTP_FLAG_STAGE_TIMING;
     return LTP_OK;
 }
 

@@ -115,6 +115,7 @@ def load():
         "ltp_pipe_submit": (ci, [vp, u64, vp, u32, u64, vp, vp, vp, u64, vp, vp, ctypes.POINTER(u64)]),
         "ltp_pipe_wait": (ci, [vp, u64, ctypes.POINTER(Stats)]),
         "ltp_pipe_poll": (ci, [vp, u64]),
+        "ltp_set_stage_timing": (ci, [vp, i32]),
         "ltp_execute_noalloc": (ci, [i32, i32, vp, u64, u64, u32, u64, vp, u32, u64, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
@@ -278,6 +279,9 @@ class Context:
         """Executes batches in order: mode 0 stream, 1 CUDA graph, 2 persistent kernel."""
         arr = (ctypes.c_void_p * max(len(batches), 1))(*[b.h.value for b in batches])
         self.check(self.L.ltp_batches_execute(self.h, arr, len(batches), mode, _stream(stream)))
+
+    def set_stage_timing(self, on):
+        self.check(self.L.ltp_set_stage_timing(self.h, 1 if on else 0))
 
     def stall_next(self, ms):
         self.check(self.L.ltp_debug_stall_next(self.h, ms))
