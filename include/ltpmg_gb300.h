@@ -210,6 +210,72 @@ int ltp_pipe_wait(ltp_pipe *p, uint64_t ticket, ltp_stats *stats);
 /* LTP_OK when the ticket's results are ready, 1 while it is in flight. */
 int ltp_pipe_poll(ltp_pipe *p, uint64_t ticket);
 
+/* ---- serving loop --------------------------------------------------------- */
+/* Continuous batching over a pipeline: client threads (or the built-in load
+ * generator) submit transactions on numbered streams; a dispatcher thread
+ * closes a batch when its oldest transaction has waited deadline_us, when
+ * its read/write set reaches budget_bytes (12 bytes of key + opword per op)
+ * or the slot capacity, or -- work-conserving -- as soon as the device has
+ * no batch queued; up to `depth` batches are in flight, so arrivals are
+ * admitted while earlier batches execute.  Tables and conflict state stay
+ * on the device.  Transactions aborted by the priority rule are re-queued
+ * at the head of the next batch with their original arrival time (up to
+ * max_attempts tries).  A stream's transactions enter batches in submission
+ * order.  Latency = completion time - arrival time. */
+#define LTP_SERVE_MAX_OPS 64
+typedef struct {
+    uint32_t deadline_us;   /* batch closes this long after its oldest arrival */
+    uint32_t depth;         /* batches in flight (>= 2) */
+    uint64_t budget_bytes;  /* read/write-set budget per batch */
+    uint64_t max_txns;      /* slot capacity */
+    uint64_t max_ops;
+    uint32_t max_attempts;  /* tries before a transaction is reported aborted */
+    uint32_t eager;         /* 1: close early when the device is idle */
+} ltp_serve_config;
+
+typedef struct {
+    uint64_t tag;           /* caller's tag */
+    uint64_t arrival_ns;    /* CLOCK_MONOTONIC */
+    uint64_t done_ns;
+    uint64_t batch_seq;     /* the batch that committed it (or last tried it) */
+    uint32_t pos;           /* its position (TID) in that batch */
+    uint32_t stream;
+    uint32_t n_ops;
+    uint32_t attempts;
+    uint32_t committed;
+    uint32_t pad;
+    int32_t vals[LTP_SERVE_MAX_OPS];
+} ltp_serve_result;
+
+typedef struct {
+    uint64_t submitted, completed, committed, aborted_attempts, batches;
+    uint64_t closed_deadline, closed_budget, closed_idle, ops;
+    double p50_us, p99_us, p999_us, mean_us, max_us;
+    double elapsed_s, committed_per_s;
+} ltp_serve_stats;
+
+typedef struct ltp_server ltp_server;
+int ltp_serve_open(ltp_ctx *ctx, const ltp_serve_config *cfg, ltp_server **out);
+/* Thread-safe.  arrival_ns 0 = now.  Fails with LTP_E_CAPACITY when n_ops
+ * exceeds LTP_SERVE_MAX_OPS or the slot capacity. */
+int ltp_serve_submit(ltp_server *s, uint32_t stream, uint32_t n_ops, const uint64_t *keys, const uint32_t *opw,
+                     uint64_t tag, uint64_t arrival_ns);
+/* Moves up to max completed transactions into out; *n = how many. */
+int ltp_serve_poll(ltp_server *s, ltp_serve_result *out, uint32_t max, uint32_t *n);
+/* Open-loop Poisson load: n_streams clients at `rate` transactions/s in
+ * aggregate for `seconds`, drawing transactions round-robin from the given
+ * pool, on n_threads generator threads.  Returns when the offered load ends;
+ * completions keep arriving until ltp_serve_close. */
+int ltp_serve_loadgen(ltp_server *s, double rate, double seconds, uint32_t n_streams, uint64_t seed,
+                      const uint32_t *txn_first, uint64_t n_pool, const uint64_t *keys, const uint32_t *opw,
+                      uint32_t n_threads);
+/* Statistics so far (latency percentiles over committed transactions). */
+int ltp_serve_stats_now(ltp_server *s, ltp_serve_stats *st);
+/* Drains every admitted transaction, stops the dispatcher, frees. */
+int ltp_serve_close(ltp_server *s, ltp_serve_stats *st);
+/* Current CLOCK_MONOTONIC time in ns (the clock arrivals are stamped with). */
+uint64_t ltp_now_ns(void);
+
 /* ---- pinned host memory ------------------------------------------------ */
 void *ltp_host_alloc(size_t bytes);
 void ltp_host_free(void *p);

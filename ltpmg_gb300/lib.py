@@ -58,6 +58,32 @@ class YcsbParams(ctypes.Structure):
                 ("read_frac", ctypes.c_double), ("theta", ctypes.c_double)]
 
 
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("deadline_us", ctypes.c_uint32), ("depth", ctypes.c_uint32), ("budget_bytes", ctypes.c_uint64),
+                ("max_txns", ctypes.c_uint64), ("max_ops", ctypes.c_uint64), ("max_attempts", ctypes.c_uint32),
+                ("eager", ctypes.c_uint32)]
+
+
+SERVE_MAX_OPS = 64
+
+
+class ServeResult(ctypes.Structure):
+    _fields_ = [("tag", ctypes.c_uint64), ("arrival_ns", ctypes.c_uint64), ("done_ns", ctypes.c_uint64),
+                ("batch_seq", ctypes.c_uint64), ("pos", ctypes.c_uint32), ("stream", ctypes.c_uint32),
+                ("n_ops", ctypes.c_uint32), ("attempts", ctypes.c_uint32), ("committed", ctypes.c_uint32),
+                ("pad", ctypes.c_uint32), ("vals", ctypes.c_int32 * SERVE_MAX_OPS)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_uint64) for k in ("submitted", "completed", "committed", "aborted_attempts", "batches",
+                                               "closed_deadline", "closed_budget", "closed_idle", "ops")] + \
+               [(k, ctypes.c_double) for k in ("p50_us", "p99_us", "p999_us", "mean_us", "max_us", "elapsed_s",
+                                               "committed_per_s")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class Tuning(ctypes.Structure):
     _fields_ = [("block", ctypes.c_uint32), ("ipt", ctypes.c_uint32), ("word_bits", ctypes.c_uint32),
                 ("reserved", ctypes.c_uint32)]
@@ -116,6 +142,13 @@ def load():
         "ltp_pipe_wait": (ci, [vp, u64, ctypes.POINTER(Stats)]),
         "ltp_pipe_poll": (ci, [vp, u64]),
         "ltp_set_stage_timing": (ci, [vp, i32]),
+        "ltp_serve_open": (ci, [vp, ctypes.POINTER(ServeConfig), pp]),
+        "ltp_serve_submit": (ci, [vp, u32, u32, vp, vp, u64, u64]),
+        "ltp_serve_poll": (ci, [vp, ctypes.POINTER(ServeResult), u32, ctypes.POINTER(u32)]),
+        "ltp_serve_loadgen": (ci, [vp, ctypes.c_double, ctypes.c_double, u32, u64, vp, u64, vp, vp, u32]),
+        "ltp_serve_stats_now": (ci, [vp, ctypes.POINTER(ServeStats)]),
+        "ltp_serve_close": (ci, [vp, ctypes.POINTER(ServeStats)]),
+        "ltp_now_ns": (u64, []),
         "ltp_execute_noalloc": (ci, [i32, i32, vp, u64, u64, u32, u64, vp, u32, u64, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
@@ -391,3 +424,47 @@ class Pipe:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """The continuous-batching request loop (the C-ABI ltp_server)."""
+
+    def __init__(self, ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 20, max_ops=1 << 24,
+                 max_attempts=64, eager=True):
+        self.ctx = ctx
+        cfg = ServeConfig(deadline_us, depth, budget_bytes, max_txns, max_ops, max_attempts, 1 if eager else 0)
+        h = ctypes.c_void_p()
+        ctx.check(ctx.L.ltp_serve_open(ctx.h, ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+        self._pool = None
+
+    def submit(self, stream, keys, opw, tag=0, arrival_ns=0):
+        keys = np.ascontiguousarray(keys, np.uint64)
+        opw = np.ascontiguousarray(opw, np.uint32)
+        self.ctx.check(self.ctx.L.ltp_serve_submit(self.h, stream, len(keys), _p(keys), _p(opw), tag, arrival_ns))
+
+    def loadgen(self, rate, seconds, n_streams, txn_first, keys, opw, seed=1, threads=8):
+        self._pool = (np.ascontiguousarray(txn_first, np.uint32), np.ascontiguousarray(keys, np.uint64),
+                      np.ascontiguousarray(opw, np.uint32))
+        tf, k, w = self._pool
+        self.ctx.check(self.ctx.L.ltp_serve_loadgen(self.h, rate, seconds, n_streams, seed, _p(tf), len(tf) - 1,
+                                                    _p(k), _p(w), threads))
+
+    def poll(self, max_results=4096):
+        buf = (ServeResult * max_results)()
+        n = ctypes.c_uint32()
+        self.ctx.check(self.ctx.L.ltp_serve_poll(self.h, buf, max_results, ctypes.byref(n)))
+        return buf[:n.value]
+
+    def stats(self):
+        st = ServeStats()
+        self.ctx.check(self.ctx.L.ltp_serve_stats_now(self.h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def close(self):
+        st = ServeStats()
+        if getattr(self, "h", None):
+            rc = self.ctx.L.ltp_serve_close(self.h, ctypes.byref(st))
+            self.h = None
+            self.ctx.check(rc)
+        return st.as_dict()
