@@ -31,12 +31,14 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "committed txn/s"
-DEFAULT_STEPS = {"zipf": 20, "plain": 50, "uneven": 30}
+DEFAULT_STEPS = {"zipf": 20, "plain": 50, "uneven": 30, "serve": 1}
 WORKLOAD_TEXT = {
     "zipf": "ycsb-zipf0.99: 2^24 rows x 10 int32, 32 batches x 2^20 txns x 16 ops, 80% read / 20% +1 RMW",
     "plain": "ycsb-uniform: 2^20 rows x 10 int32, 16 batches x 2^16 txns x 10 ops, 50% read / 50% +1 RMW",
     "uneven": "ycsb-uneven: 2^24 rows x 10 int32, 64 batches x 2^U[10,20] txns x U[1,32] ops, zipf U[0.5,0.99], "
               "70% read / 30% +1 RMW",
+    "serve": "serving: 256 Poisson client streams over the zipf0.99 YCSB shape (2^24 rows x 10 int32, 16-op txns, "
+             "80/20), offered load swept 1M-50M txn/s, 250 us batch deadline, 4 GB read/write-set budget",
 }
 # algorithmic bytes per kernel launch, from the batch's counters
 KERNEL_BYTES = {
@@ -393,6 +395,59 @@ def run_ours(args, config):
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args):
+    """Offered-load sweep of the serving loop; value = the highest committed
+    txn/s among the loads served at p99 <= 2 ms."""
+    import torch
+
+    import ltpmg_gb300 as G
+    from ltpmg_gb300 import workloads as W
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    sh = W.SHAPES["zipf"]
+    tf, keys, opw, n, _ = W.generate("zipf", 0, rank=rank)
+    txn_first = tf
+    ctx = G.Context(device=local)
+    t = ctx.create_table(sh["rows"], sh["cols"])
+    ctx.fill_seeded(t, sh["seed"] + rank)
+    # the plain batch path on the same GPU and shape, for comparison
+    b = ctx.batch(n, len(keys))
+    b.load(None, keys, opw, ops_per_txn=16)
+    for _ in range(3):
+        b.execute()
+    ctx.sync()
+    t0 = time.perf_counter()
+    for _ in range(10):
+        b.execute()
+    ctx.sync()
+    plain = 10 * n / (time.perf_counter() - t0)
+    del b
+    loads = [float(x) * 1e6 for x in args.loads.split(",")]
+    sweep = []
+    for rate in loads:
+        srv = G.Server(ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 20, max_ops=1 << 24)
+        t_load = max(0.3, min(2.0, 20e6 / rate))
+        srv.loadgen(rate, t_load, 256, txn_first, keys, opw, seed=int(rate), threads=8)
+        st = srv.close()
+        st["offered_txn_per_s"] = rate
+        st["load_seconds"] = t_load
+        st["committed_per_s_offered_window"] = st["committed"] / max(st["elapsed_s"], 1e-9)
+        sweep.append({k: (round(v, 3) if isinstance(v, float) else v) for k, v in st.items()})
+    ok = [p for p in sweep if p["p99_us"] <= 2000.0]
+    best = max(ok, key=lambda p: p["committed_per_s_offered_window"]) if ok else None
+    value = best["committed_per_s_offered_window"] if best else 0.0
+    line = {"metric": METRIC, "value": value, "unit": "txn/s", "n_gpus": world, "steps": len(loads),
+            "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32", "data": "synthetic (seeded generator)",
+            "config": {"workload": WORKLOAD_TEXT["serve"], "selection": "highest committed txn/s with p99 <= 2 ms"},
+            "serving": {"sweep": sweep, "plain_batch_txn_per_s": plain,
+                        "best_p50_us": best["p50_us"] if best else None,
+                        "best_p99_us": best["p99_us"] if best else None,
+                        "best_p999_us": best["p999_us"] if best else None}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -404,12 +459,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batches", type=int, default=0, help="resident batches (default: the config's)")
     ap.add_argument("--tuning-out", default="", help="write the autotuner's choices to this JSON file")
+    ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if not args.steps:
         args.steps = DEFAULT_STEPS[args.config]
     if args.impl == "reference":
-        run_reference(args, args.config)
+        run_reference(args, "zipf" if args.config == "serve" else args.config)
+    elif args.config == "serve":
+        run_serve(args)
     else:
         run_ours(args, args.config)
 
