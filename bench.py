@@ -426,7 +426,8 @@ def run_serve(args):
     loads = [float(x) * 1e6 for x in args.loads.split(",")]
     sweep = []
     for rate in loads:
-        srv = G.Server(ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 20, max_ops=1 << 24)
+        srv = G.Server(ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 20, max_ops=1 << 24,
+                       keep_results=False)
         t_load = max(0.3, min(2.0, 20e6 / rate))
         srv.loadgen(rate, t_load, 256, txn_first, keys, opw, seed=int(rate), threads=8)
         st = srv.close()

@@ -230,8 +230,10 @@ typedef struct {
     uint64_t max_txns;      /* slot capacity */
     uint64_t max_ops;
     uint32_t max_attempts;  /* tries before a transaction is reported aborted */
-    uint32_t eager;         /* 1: close early when the device is idle */
+    uint32_t flags;         /* LTP_SERVE_EAGER | LTP_SERVE_KEEP_RESULTS */
 } ltp_serve_config;
+#define LTP_SERVE_EAGER 1u        /* close a batch as soon as the device has none queued */
+#define LTP_SERVE_KEEP_RESULTS 2u /* keep per-transaction results for ltp_serve_poll */
 
 typedef struct {
     uint64_t tag;           /* caller's tag */

@@ -13,6 +13,11 @@
 //    next batch and keep their arrival time;
 //  * a stream always maps to one admission lane, so its transactions enter
 //    batches in submission order.
+//
+// Admission is in bulk: a lane accumulates transactions (headers and ops in
+// flat arrays) until the dispatcher swaps the whole lane out as a segment;
+// batches copy runs of consecutive transactions with one memcpy per run, and
+// completion walks runs, so the per-transaction cost is a few nanoseconds.
 #include <time.h>
 
 #include <algorithm>
@@ -36,23 +41,44 @@ uint64_t now_ns() {
     return (uint64_t)ts.tv_sec * 1000000000ull + (uint64_t)ts.tv_nsec;
 }
 
-// Ops of admitted transactions live in chunks; a chunk stays alive while any
-// of its transactions is pending or in flight.
-struct Chunk {
+// Transactions of one lane between two drains, in arrival order.
+struct Seg {
+    std::vector<uint64_t> arrival, tag;
+    std::vector<uint32_t> stream, off, attempts;  // off: first op; txn i's ops are [off[i], off[i+1])
     std::vector<uint64_t> keys;
     std::vector<uint32_t> opw;
-};
-
-struct Txn {
-    uint64_t tag, arrival;
-    uint32_t stream, n_ops, attempts, off;
-    std::shared_ptr<Chunk> chunk;
+    size_t head = 0;  // next transaction to batch
+    size_t n() const { return arrival.size(); }
+    void clear() {
+        arrival.clear();
+        tag.clear();
+        stream.clear();
+        off.assign(1, 0);
+        attempts.clear();
+        keys.clear();
+        opw.clear();
+        head = 0;
+    }
+    void push(uint64_t arr, uint64_t tg, uint32_t st, uint32_t att, uint32_t n_ops, const uint64_t *k,
+              const uint32_t *w) {
+        arrival.push_back(arr);
+        tag.push_back(tg);
+        stream.push_back(st);
+        attempts.push_back(att);
+        keys.insert(keys.end(), k, k + n_ops);
+        opw.insert(opw.end(), w, w + n_ops);
+        off.push_back((uint32_t)keys.size());
+    }
 };
 
 struct Lane {
     std::mutex mu;
-    std::shared_ptr<Chunk> chunk = std::make_shared<Chunk>();
-    std::vector<Txn> txns;
+    std::shared_ptr<Seg> seg;
+};
+
+struct Run {  // transactions [first, first+count) of a segment inside a batch
+    std::shared_ptr<Seg> seg;
+    size_t first, count;
 };
 
 struct Slot {
@@ -60,35 +86,43 @@ struct Slot {
     uint32_t *opw = nullptr, *txn_first = nullptr;
     uint8_t *commit = nullptr;
     int32_t *vals = nullptr;
-    std::vector<Txn> txns;
+    std::vector<Run> runs;
     uint64_t ticket = 0, seq = 0;
     bool busy = false;
 };
 
-// Log-scale latency histogram: 1% wide buckets from 100 ns to ~30 s.
+// Latency histogram without floating point: 64 linear sub-buckets per
+// power of two of nanoseconds (~1.6% wide).
 struct Histo {
-    static constexpr double kBase = 100.0, kStep = 1.01;
-    static constexpr int kN = 2000;
-    std::vector<uint64_t> h = std::vector<uint64_t>(kN + 1, 0);
-    uint64_t n = 0;
-    double sum = 0, mx = 0;
-    void add(double ns) {
-        int b = ns <= kBase ? 0 : (int)(std::log(ns / kBase) / std::log(kStep)) + 1;
-        if (b > kN) b = kN;
-        h[b]++;
+    static constexpr int kSub = 64;
+    std::vector<uint64_t> h = std::vector<uint64_t>(64 * kSub, 0);
+    uint64_t n = 0, mx = 0;
+    double sum = 0;
+    static int bucket(uint64_t ns) {
+        if (ns < kSub) return (int)ns;
+        const int e = 63 - __builtin_clzll(ns);  // >= 6
+        return e * kSub + (int)((ns >> (e - 6)) & (kSub - 1));
+    }
+    static double lower(int b) {
+        const int e = b / kSub, m = b % kSub;
+        if (e < 6) return (double)b;
+        return std::ldexp(1.0 + m / (double)kSub, e);
+    }
+    void add(uint64_t ns) {
+        h[bucket(ns)]++;
         n++;
-        sum += ns;
+        sum += (double)ns;
         mx = std::max(mx, ns);
     }
     double pct(double p) const {
         if (!n) return 0;
         const uint64_t want = (uint64_t)std::ceil(p * (double)n);
         uint64_t acc = 0;
-        for (int b = 0; b <= kN; b++) {
+        for (size_t b = 0; b < h.size(); b++) {
             acc += h[b];
-            if (acc >= want) return b == 0 ? kBase : kBase * std::pow(kStep, b);
+            if (acc >= want) return std::min(lower((int)b + 1), (double)mx);
         }
-        return mx;
+        return (double)mx;
     }
 };
 
@@ -97,12 +131,13 @@ struct Histo {
 struct ltp_server {
     ltp_ctx *ctx = nullptr;
     ltp_serve_config cfg;
+    bool keep_results = true;
     ltp_pipe *pipe = nullptr;
     std::vector<std::unique_ptr<Lane>> lanes;
     std::vector<Slot> slots;
-    std::deque<Txn> pending, requeued;
-    uint64_t pending_ops = 0;
-    std::deque<uint32_t> inflight;  // slot indices in submission order
+    std::deque<std::shared_ptr<Seg>> pending;  // requeued segments go to the front
+    uint64_t pending_txns = 0, pending_ops = 0;
+    std::deque<uint32_t> inflight;
     std::thread dispatcher;
     std::atomic<bool> stop{false};
     std::atomic<int> status{0};
@@ -110,27 +145,49 @@ struct ltp_server {
     std::vector<ltp_serve_result> results;
     Histo histo;
     std::atomic<uint64_t> submitted{0};
-    uint64_t completed = 0, committed = 0, aborted_attempts = 0, batches = 0, ops = 0;
+    std::atomic<uint64_t> completed{0}, committed{0};
+    uint64_t aborted_attempts = 0, batches = 0, ops = 0;
     uint64_t closed_deadline = 0, closed_budget = 0, closed_idle = 0;
-    uint64_t t_start = 0, t_last = 0;
-    uint64_t seq = 0;
+    uint64_t t_first = 0, t_last = 0, seq = 0;
+    std::mutex free_mu;
+    std::vector<std::shared_ptr<Seg>> free_segs;
 };
 
 namespace {
 
+std::shared_ptr<Seg> new_seg(ltp_server *s) {
+    std::lock_guard<std::mutex> g(s->free_mu);
+    if (!s->free_segs.empty()) {
+        auto p = s->free_segs.back();
+        s->free_segs.pop_back();
+        return p;
+    }
+    auto p = std::make_shared<Seg>();
+    p->clear();
+    return p;
+}
+
+void recycle(ltp_server *s, std::shared_ptr<Seg> &p) {
+    if (p && p.use_count() == 1) {
+        p->clear();
+        std::lock_guard<std::mutex> g(s->free_mu);
+        if (s->free_segs.size() < 256) s->free_segs.push_back(p);
+    }
+    p.reset();
+}
+
 void drain_lanes(ltp_server *s) {
     for (auto &lp : s->lanes) {
-        std::vector<Txn> got;
+        std::shared_ptr<Seg> got;
         {
             std::lock_guard<std::mutex> g(lp->mu);
-            if (lp->txns.empty()) continue;
-            got.swap(lp->txns);
-            lp->chunk = std::make_shared<Chunk>();
+            if (!lp->seg || lp->seg->n() == 0) continue;
+            got = std::move(lp->seg);
+            lp->seg = nullptr;
         }
-        for (auto &t : got) {
-            s->pending_ops += t.n_ops;
-            s->pending.push_back(std::move(t));
-        }
+        s->pending_txns += got->n();
+        s->pending_ops += got->keys.size();
+        s->pending.push_back(std::move(got));
     }
 }
 
@@ -142,80 +199,110 @@ void complete_batch(ltp_server *s, Slot &sl) {
         return;
     }
     const uint64_t done = now_ns();
+    std::shared_ptr<Seg> again;  // aborted transactions to re-queue
     std::vector<ltp_serve_result> out;
-    out.reserve(sl.txns.size());
-    for (uint32_t i = 0; i < sl.txns.size(); i++) {
-        Txn &t = sl.txns[i];
-        const bool ok = sl.commit[i] != 0;
-        if (!ok && t.attempts + 1 < s->cfg.max_attempts) {
-            s->aborted_attempts++;
-            t.attempts++;
-            s->requeued.push_back(std::move(t));
-            continue;
+    uint32_t pos = 0;
+    uint64_t n_ok = 0, n_done = 0;
+    for (Run &r : sl.runs) {
+        Seg &g = *r.seg;
+        for (size_t i = r.first; i < r.first + r.count; i++, pos++) {
+            const bool ok = sl.commit[pos] != 0;
+            if (!ok && g.attempts[i] + 1 < s->cfg.max_attempts) {
+                s->aborted_attempts++;
+                if (!again) again = new_seg(s);
+                again->push(g.arrival[i], g.tag[i], g.stream[i], g.attempts[i] + 1, g.off[i + 1] - g.off[i],
+                            g.keys.data() + g.off[i], g.opw.data() + g.off[i]);
+                continue;
+            }
+            if (!ok) s->aborted_attempts++;
+            n_done++;
+            if (ok) {
+                n_ok++;
+                s->histo.add(done - g.arrival[i]);
+            }
+            if (s->keep_results) {
+                ltp_serve_result res;
+                memset(&res, 0, sizeof(res));
+                res.tag = g.tag[i];
+                res.arrival_ns = g.arrival[i];
+                res.done_ns = done;
+                res.batch_seq = sl.seq;
+                res.pos = pos;
+                res.stream = g.stream[i];
+                res.n_ops = g.off[i + 1] - g.off[i];
+                res.attempts = g.attempts[i] + 1;
+                res.committed = ok ? 1u : 0u;
+                memcpy(res.vals, sl.vals + sl.txn_first[pos], res.n_ops * sizeof(int32_t));
+                out.push_back(res);
+            }
         }
-        if (!ok) s->aborted_attempts++;
-        ltp_serve_result r;
-        memset(&r, 0, sizeof(r));
-        r.tag = t.tag;
-        r.arrival_ns = t.arrival;
-        r.done_ns = done;
-        r.batch_seq = sl.seq;
-        r.pos = i;
-        r.stream = t.stream;
-        r.n_ops = t.n_ops;
-        r.attempts = t.attempts + 1;
-        r.committed = ok ? 1u : 0u;
-        memcpy(r.vals, sl.vals + sl.txn_first[i], t.n_ops * sizeof(int32_t));
-        s->completed++;
-        if (ok) {
-            s->committed++;
-            s->histo.add((double)(done - t.arrival));
-        }
-        out.push_back(r);
     }
+    for (Run &r : sl.runs) recycle(s, r.seg);
+    sl.runs.clear();
+    if (again) {  // ahead of everything pending: the next batch starts with them
+        s->pending_txns += again->n();
+        s->pending_ops += again->keys.size();
+        s->pending.push_front(std::move(again));
+    }
+    s->completed += n_done;
+    s->committed += n_ok;
     s->t_last = done;
-    sl.txns.clear();
     sl.busy = false;
-    std::lock_guard<std::mutex> g(s->res_mu);
-    s->results.insert(s->results.end(), out.begin(), out.end());
+    if (!out.empty()) {
+        std::lock_guard<std::mutex> g(s->res_mu);
+        s->results.insert(s->results.end(), out.begin(), out.end());
+    }
+}
+
+uint64_t oldest_pending(const ltp_server *s) {
+    uint64_t o = UINT64_MAX;
+    for (const auto &p : s->pending)
+        if (p->head < p->n()) o = std::min(o, p->arrival[p->head]);
+    return o;
 }
 
 bool close_batch(ltp_server *s, uint64_t now) {
-    if (s->inflight.size() >= s->cfg.depth) return false;
-    if (s->pending.empty() && s->requeued.empty()) return false;
-    const uint64_t oldest = std::min(s->requeued.empty() ? UINT64_MAX : s->requeued.front().arrival,
-                                     s->pending.empty() ? UINT64_MAX : s->pending.front().arrival);
+    if (s->inflight.size() >= s->cfg.depth || s->pending_txns == 0) return false;
     const uint64_t cap_ops = std::min<uint64_t>(s->cfg.max_ops, s->cfg.budget_bytes / 12);
-    const bool deadline = now >= oldest + (uint64_t)s->cfg.deadline_us * 1000ull;
-    const bool full = s->pending_ops >= cap_ops || s->pending.size() + s->requeued.size() >= s->cfg.max_txns;
-    const bool idle = s->cfg.eager && s->inflight.empty();
+    const bool deadline = now >= oldest_pending(s) + (uint64_t)s->cfg.deadline_us * 1000ull;
+    const bool full = s->pending_ops >= cap_ops || s->pending_txns >= s->cfg.max_txns;
+    const bool idle = (s->cfg.flags & LTP_SERVE_EAGER) && s->inflight.empty();
     if (!deadline && !full && !idle) return false;
-    if (deadline) s->closed_deadline++;
-    else if (full) s->closed_budget++;
-    else s->closed_idle++;
-    // find a free slot
     uint32_t si = 0;
     while (si < s->slots.size() && s->slots[si].busy) si++;
     if (si == s->slots.size()) return false;
+    if (deadline) s->closed_deadline++;
+    else if (full) s->closed_budget++;
+    else s->closed_idle++;
     Slot &sl = s->slots[si];
     uint64_t nops = 0;
     uint32_t nt = 0;
     sl.txn_first[0] = 0;
-    auto take = [&](std::deque<Txn> &q) {
-        while (!q.empty() && nt < s->cfg.max_txns && nops + q.front().n_ops <= cap_ops) {
-            Txn &t = q.front();
-            memcpy(sl.keys + nops, t.chunk->keys.data() + t.off, t.n_ops * sizeof(uint64_t));
-            memcpy(sl.opw + nops, t.chunk->opw.data() + t.off, t.n_ops * sizeof(uint32_t));
-            nops += t.n_ops;
-            sl.txn_first[++nt] = (uint32_t)nops;
-            sl.txns.push_back(std::move(t));
-            q.pop_front();
+    while (!s->pending.empty() && nt < s->cfg.max_txns) {
+        std::shared_ptr<Seg> &p = s->pending.front();
+        Seg &g = *p;
+        // largest run of this segment that fits
+        size_t k = g.head;
+        while (k < g.n() && nt + (k - g.head) < s->cfg.max_txns && nops + (g.off[k + 1] - g.off[g.head]) <= cap_ops)
+            k++;
+        const size_t cnt = k - g.head;
+        if (cnt) {
+            const uint32_t a = g.off[g.head], b = g.off[k];
+            memcpy(sl.keys + nops, g.keys.data() + a, (size_t)(b - a) * sizeof(uint64_t));
+            memcpy(sl.opw + nops, g.opw.data() + a, (size_t)(b - a) * sizeof(uint32_t));
+            for (size_t i = g.head; i < k; i++) sl.txn_first[++nt] = (uint32_t)(nops + g.off[i + 1] - a);
+            nops += b - a;
+            sl.runs.push_back(Run{p, g.head, cnt});
+            s->pending_txns -= cnt;
+            s->pending_ops -= (b - a);
+            g.head = k;
         }
-    };
-    take(s->requeued);  // aborted transactions first: they keep their arrival time
-    const uint64_t before = nops;
-    take(s->pending);
-    s->pending_ops -= (nops - before);
+        if (g.head == g.n()) {
+            s->pending.pop_front();
+        } else {
+            break;  // the batch is full
+        }
+    }
     if (nt == 0) return false;
     uint64_t ticket = 0;
     const int rc = ltp_pipe_submit(s->pipe, nt, sl.txn_first, 0, nops, sl.keys, sl.opw, nullptr, 0, sl.commit, sl.vals,
@@ -244,9 +331,9 @@ void dispatch_loop(ltp_server *s) {
         }
         if (s->status) break;
         if (close_batch(s, now_ns())) progressed = true;
-        if (s->stop && s->pending.empty() && s->requeued.empty() && s->inflight.empty()) {
+        if (s->stop && s->pending_txns == 0 && s->inflight.empty()) {
             drain_lanes(s);
-            if (s->pending.empty()) break;
+            if (s->pending_txns == 0) break;
         }
         if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(2));
     }
@@ -264,6 +351,7 @@ int ltp_serve_open(ltp_ctx *ctx, const ltp_serve_config *cfg, ltp_server **out) 
     ltp_server *s = new ltp_server();
     s->ctx = ctx;
     s->cfg = *cfg;
+    s->keep_results = (cfg->flags & LTP_SERVE_KEEP_RESULTS) != 0;
     if (s->cfg.max_attempts == 0) s->cfg.max_attempts = 1;
     int rc = ltp_pipe_create(ctx, cfg->depth, cfg->max_txns, cfg->max_ops, &s->pipe);
     if (rc) {
@@ -284,7 +372,6 @@ int ltp_serve_open(ltp_ctx *ctx, const ltp_serve_config *cfg, ltp_server **out) 
             return LTP_E_NOMEM;
         }
     }
-    s->t_start = s->t_last = now_ns();
     s->dispatcher = std::thread(dispatch_loop, s);
     *out = s;
     return LTP_OK;
@@ -296,21 +383,13 @@ int ltp_serve_submit(ltp_server *s, uint32_t stream, uint32_t n_ops, const uint6
     if (n_ops > LTP_SERVE_MAX_OPS || n_ops > s->cfg.max_ops) return LTP_E_CAPACITY;
     if (s->status) return s->status;
     Lane &ln = *s->lanes[stream % s->lanes.size()];
-    Txn t;
-    t.tag = tag;
-    t.arrival = arrival_ns ? arrival_ns : now_ns();
-    t.stream = stream;
-    t.n_ops = n_ops;
-    t.attempts = 0;
+    const uint64_t at = arrival_ns ? arrival_ns : now_ns();
     {
         std::lock_guard<std::mutex> g(ln.mu);
-        t.off = (uint32_t)ln.chunk->keys.size();
-        ln.chunk->keys.insert(ln.chunk->keys.end(), keys, keys + n_ops);
-        ln.chunk->opw.insert(ln.chunk->opw.end(), opw, opw + n_ops);
-        t.chunk = ln.chunk;
-        ln.txns.push_back(std::move(t));
+        if (!ln.seg) ln.seg = new_seg(s);
+        ln.seg->push(at, tag, stream, 0, n_ops, keys, opw);
     }
-    s->submitted++;
+    if (s->submitted.fetch_add(1) == 0) s->t_first = at;
     return LTP_OK;
 }
 
@@ -332,26 +411,26 @@ int ltp_serve_loadgen(ltp_server *s, double rate, double seconds, uint32_t n_str
     const uint64_t t0 = now_ns() + 1000000;  // start 1 ms from now
     const uint64_t t_end = t0 + (uint64_t)(seconds * 1e9);
     std::vector<std::thread> th;
-    std::atomic<uint64_t> next_pool{0};
     for (uint32_t g = 0; g < n_threads; g++) {
-        th.emplace_back([=, &next_pool]() {
-            // this thread's share of the streams: s = g, g + n_threads, ...
+        th.emplace_back([=]() {
+            // this thread's streams: g, g + n_threads, ... ; its own slice of the pool
             const uint32_t my_streams = (n_streams - g + n_threads - 1) / n_threads;
             if (!my_streams) return;
             const double my_rate = rate * (double)my_streams / (double)n_streams;
             std::mt19937_64 rng(seed * 0x9E3779B97F4A7C15ULL + g + 1);
             std::exponential_distribution<double> gap(my_rate / 1e9);
             double t = (double)t0;
+            uint64_t k = (n_pool * g) / n_threads;
             while (true) {
                 t += gap(rng);
                 const uint64_t at = (uint64_t)t;
                 if (at >= t_end || s->status) break;
                 while (now_ns() < at) {
                 }
-                const uint64_t k = next_pool.fetch_add(1) % n_pool;
                 const uint32_t st = g + n_threads * (uint32_t)(rng() % my_streams);
                 const uint32_t a = txn_first[k], n = txn_first[k + 1] - txn_first[k];
                 if (ltp_serve_submit(s, st, n, keys + a, opw + a, k, at)) break;
+                if (++k == n_pool) k = 0;
             }
         });
     }
@@ -375,8 +454,8 @@ int ltp_serve_stats_now(ltp_server *s, ltp_serve_stats *st) {
     st->p99_us = s->histo.pct(0.99) / 1e3;
     st->p999_us = s->histo.pct(0.999) / 1e3;
     st->mean_us = s->histo.n ? s->histo.sum / (double)s->histo.n / 1e3 : 0;
-    st->max_us = s->histo.mx / 1e3;
-    st->elapsed_s = (double)(s->t_last - s->t_start) / 1e9;
+    st->max_us = (double)s->histo.mx / 1e3;
+    st->elapsed_s = s->t_last > s->t_first ? (double)(s->t_last - s->t_first) / 1e9 : 0;
     st->committed_per_s = st->elapsed_s > 0 ? (double)s->committed / st->elapsed_s : 0;
     return s->status;
 }

@@ -61,7 +61,7 @@ class YcsbParams(ctypes.Structure):
 class ServeConfig(ctypes.Structure):
     _fields_ = [("deadline_us", ctypes.c_uint32), ("depth", ctypes.c_uint32), ("budget_bytes", ctypes.c_uint64),
                 ("max_txns", ctypes.c_uint64), ("max_ops", ctypes.c_uint64), ("max_attempts", ctypes.c_uint32),
-                ("eager", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32)]
 
 
 SERVE_MAX_OPS = 64
@@ -430,9 +430,10 @@ class Server:
     """The continuous-batching request loop (the C-ABI ltp_server)."""
 
     def __init__(self, ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 20, max_ops=1 << 24,
-                 max_attempts=64, eager=True):
+                 max_attempts=64, eager=True, keep_results=True):
         self.ctx = ctx
-        cfg = ServeConfig(deadline_us, depth, budget_bytes, max_txns, max_ops, max_attempts, 1 if eager else 0)
+        flags = (1 if eager else 0) | (2 if keep_results else 0)
+        cfg = ServeConfig(deadline_us, depth, budget_bytes, max_txns, max_ops, max_attempts, flags)
         h = ctypes.c_void_p()
         ctx.check(ctx.L.ltp_serve_open(ctx.h, ctypes.byref(cfg), ctypes.byref(h)))
         self.h = h
