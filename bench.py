@@ -10,7 +10,7 @@ batches (CUDA graph or persistent kernel, picked by the autotuner, as are the
 kernel tilings per size bucket).  Inputs are far larger than L2 (201 MB of
 ops per batch, 640 MB table).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--config zipf|plain|uneven]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config zipf|plain|uneven|tpcc|serve]
   python bench.py --impl reference ...   (CPU baseline: the oracle's
                                            multi-threaded serial replay)
 
@@ -31,12 +31,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "committed txn/s"
-DEFAULT_STEPS = {"zipf": 20, "plain": 50, "uneven": 30, "serve": 1}
+DEFAULT_STEPS = {"zipf": 20, "plain": 50, "uneven": 30, "serve": 1, "tpcc": 10}
 WORKLOAD_TEXT = {
     "zipf": "ycsb-zipf0.99: 2^24 rows x 10 int32, 32 batches x 2^20 txns x 16 ops, 80% read / 20% +1 RMW",
     "plain": "ycsb-uniform: 2^20 rows x 10 int32, 16 batches x 2^16 txns x 10 ops, 50% read / 50% +1 RMW",
     "uneven": "ycsb-uneven: 2^24 rows x 10 int32, 64 batches x 2^U[10,20] txns x U[1,32] ops, zipf U[0.5,0.99], "
               "70% read / 30% +1 RMW",
+    "tpcc": "tpcc-shaped order entry: 64 warehouses (10 districts, 30,000 customers, 100,000 stock rows each; "
+            "100,000 items), 4 batches x 2^18 txns, 50% new-order (5-15 lines, NURand items, 1% remote) / 50% payment "
+            "(NURand customers, 15% remote, 60% by last name, int64 cents), 9 tables, int32/int64 columns",
     "serve": "serving: 256 Poisson client streams over the zipf0.99 YCSB shape (2^24 rows x 10 int32, 16-op txns, "
              "80/20), offered load swept 1M-50M txn/s, 250 us batch deadline, 4 GB read/write-set budget",
 }
@@ -395,6 +398,261 @@ def run_ours(args, config):
     print(json.dumps(line), flush=True)
 
 
+def tpcc_setup(seed_offset=0):
+    import ltpmg_gb300 as G
+    from ltpmg_gb300 import workloads as W
+
+    sh = W.SHAPES["tpcc"]
+    return G.Tpcc(sh["warehouses"], seed=sh["seed"] + seed_offset), sh
+
+
+def tpcc_cpu_tables(g, sample_inserts):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    tabs = []
+    for t in range(9):
+        n_cols, mask, rows = g.table(t)
+        tabs.append((g.initial(t, rows + int(sample_inserts[t])), rows, mask))
+    return O.TablesDB(tabs)
+
+
+def tpcc_cpu_baseline(g, host, budget_s=12.0, threads=0, slice_txns=1 << 16):
+    """Replay of whole-batch slices of the workload by the oracle port; only
+    the replay call is timed."""
+    import numpy as np
+
+    sample, t_used, done = [], 0.0, 0
+    for tf, keys, opw, pay, n, ins in host:
+        for lo in range(0, n, slice_txns):
+            hi = min(n, lo + slice_txns)
+            a, b = int(tf[lo]), int(tf[hi])
+            sample.append(((tf[lo:hi + 1] - tf[lo]).astype(np.uint32), keys[a:b], opw[a:b], pay, hi - lo))
+    # room for every slice's inserts (at most one row per op)
+    per = np.zeros(9, np.int64)
+    for tf, keys, opw, pay, n in sample:
+        per += np.bincount(((opw >> 8) & 15)[(opw & 3) == 2], minlength=16)[:9]
+    db = tpcc_cpu_tables(g, per)
+    for tf, keys, opw, pay, n in sample:
+        t0 = time.perf_counter()
+        db.replay(0, tf, keys, opw, pay, threads=threads)
+        t_used += time.perf_counter() - t0
+        done += n
+        if t_used >= budget_s:
+            break
+    return done / t_used, done, t_used
+
+
+def run_tpcc(args):
+    import numpy as np
+    import torch
+
+    import ltpmg_gb300 as G
+    from ltpmg_gb300 import autotune as AT
+    from ltpmg_gb300 import workloads as W
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    g, sh = tpcc_setup(rank)
+    nb = args.batches or sh["batches"]
+    host = []
+    for b in range(nb):
+        tf, keys, opw, pay, n_no, ins = g.gen(b, sh["batch"])
+        host.append((tf, keys, opw, pay, len(tf) - 1, ins))
+    # every execution appends its inserts: size the insert tables for all
+    # executions this run makes (tuning, warm-up, timed steps, the kernel
+    # timing pass and the end-to-end pass)
+    timing_steps = max(1, min(args.steps, 5))
+    n_e2e = min(32, max(8, args.steps))
+    execs_all = 6 + args.warmup * 2 + args.steps + timing_steps
+    per_batch = np.max([h[5] for h in host], axis=0)
+    extra = per_batch * (execs_all * nb + 40 + n_e2e + 3)
+    ctx = G.Context(device=local, stage_timing=True)
+    ctx_tables = g.create_tables(ctx, extra)
+    dev = []
+    for tf, keys, opw, pay, n, _ in host:
+        b = ctx.batch(n, len(keys))
+        b.load(tf, keys, opw)
+        b.load_payload(pay)
+        dev.append(b)
+    ctx.sync()
+    tiles = AT.tune_buckets(ctx, dev[:1], reps=1)
+    if args.mode == "auto":
+        mode, mode_ms = AT.tune_mode(ctx, dev)
+    else:
+        mode = {"graph": G.MODE_GRAPH, "persistent": G.MODE_PERSISTENT, "stream": G.MODE_STREAM}[args.mode]
+        mode_ms = {}
+    mode_name = {G.MODE_STREAM: "stream", G.MODE_GRAPH: "graph", G.MODE_PERSISTENT: "persistent"}[mode]
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def timed_region(steps):
+        for _ in range(args.warmup):
+            ctx.execute_many(dev, mode=mode)
+        ctx.sync()
+        barrier(world)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            ctx.execute_many(dev, mode=mode)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    ctx.set_stage_timing(False)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.15)
+    ms = timed_region(args.steps)
+    clk = clocks.stop()
+    ms = reduce_max(ms, world)
+    for b in dev:
+        b.finish()
+    ctx.set_stage_timing(True)
+    ms_timed = timed_region(timing_steps)
+    stats = [b.finish().as_dict() for b in dev]
+    ctx.set_stage_timing(False)
+    txns_per_step = sum(h[4] for h in host)
+    ops_per_step = sum(len(h[1]) for h in host)
+    value = args.steps * txns_per_step * world / (ms / 1e3)
+
+    # end to end: one batch per step through the 3-slot pipeline (payload too)
+    depth = 3
+    pins = []
+    for tf, keys, opw, pay, n, _ in host[:2]:
+        arrs = []
+        for a, dt in ((tf, np.uint32), (keys, np.uint64), (opw, np.uint32), (pay, np.int32)):
+            p = G.PinnedArray((len(a),), dt)
+            p.array[:] = a
+            arrs.append(p)
+        pins.append((arrs, n))
+    maxn = max(p[1] for p in pins)
+    maxops = max(len(p[0][1].array) for p in pins)
+    outs = [(G.PinnedArray((maxn,), np.uint8), G.PinnedArray((maxops,), np.int32)) for _ in range(depth)]
+    pipe = G.Pipe(ctx, depth, maxn, maxops)
+    h2d = d2h = 0
+
+    def e2e_submit(i):
+        (ptf, pk, pw, pp), n = pins[i % len(pins)]
+        pc, pv = outs[i % depth]
+        tk = pipe.submit(ptf.array, pk.array, pw.array, pc.array[:n], pv.array[:len(pk.array)], payload=pp.array)
+        return tk, n, len(pk.array), len(pp.array)
+
+    for i in range(depth):
+        pipe.wait(e2e_submit(i)[0])
+    ctx.sync()
+    barrier(world)
+    t0 = time.perf_counter()
+    e2e_txns, inflight = 0, []
+    for i in range(n_e2e):
+        tk, n, nops, npay = e2e_submit(i)
+        inflight.append(tk)
+        if len(inflight) >= depth:
+            pipe.wait(inflight.pop(0))
+        e2e_txns += n
+        h2d += 12 * nops + 4 * (n + 1) + 4 * npay
+        d2h += 4 * nops + n
+    for tk in inflight:
+        pipe.wait(tk)
+    e2e_s = reduce_max(time.perf_counter() - t0, world)
+    pipe.close()
+    e2e = {"value": e2e_txns * world / e2e_s, "unit": "txn/s", "h2d_bytes_per_step": h2d // n_e2e,
+           "d2h_bytes_per_step": d2h // n_e2e, "steps": n_e2e,
+           "note": "one batch (+ insert payload) per step through ltp_pipe (3 slots), copies overlapped"}
+    if rank != 0:
+        return
+    peak, peak_kind = load_peaks()
+    alg = sum(W.tpcc_algorithmic_bytes(g, h[1], h[2], h[4]) for h in host)
+    step_ms = ms / args.steps
+    roof = {"bound": "hbm", "peak": peak, "unit": "GB/s", "peak_kind": peak_kind,
+            "kernel_timing_pass_ms_per_step": ms_timed / timing_steps,
+            "pipeline": {"algorithmic_bytes_per_step": alg, "avg_step_ms": step_ms,
+                         "achieved": alg / (step_ms / 1e3) / 1e9, "frac": alg / (step_ms / 1e3) / 1e9 / peak}}
+    mean_stats = {k: sum(s[k] for s in stats) / len(stats) for k in ("ops", "touched_words", "contended_cells",
+                                                                     "contended_ops")}
+    if mode != G.MODE_PERSISTENT:
+        names = list(KERNEL_BYTES) + ["insert"]
+        avg = {nm: sum(s["ms_stage"][nm] for s in stats) / len(stats) for nm in names if nm in stats[0]["ms_stage"]}
+        dom = max((k for k in avg if k in KERNEL_BYTES), key=avg.get)
+        dom_bytes = KERNEL_BYTES[dom](mean_stats)
+        achieved = dom_bytes / (avg[dom] / 1e3) / 1e9
+        roof.update({"kernel": dom, "achieved": achieved, "frac": achieved / peak, "traffic": None,
+                     "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": avg[dom], "kernel_ms": avg})
+    else:
+        roof.update({"kernel": "k_persist (whole pipeline, one launch per step)",
+                     "achieved": roof["pipeline"]["achieved"], "frac": roof["pipeline"]["frac"], "traffic": None,
+                     "algorithmic_bytes_per_launch": alg, "avg_launch_ms": step_ms})
+    launches = args.steps * (1 if mode == G.MODE_PERSISTENT else KERNELS_PER_BATCH * nb)
+    rows = {G.TPCC_TABLES[t]: ctx.table_rows(tid) for t, tid in enumerate(ctx_tables)}
+    line = {"metric": METRIC, "value": value, "unit": "txn/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64", "data": "synthetic (seeded generator)",
+            "config": {"workload": WORKLOAD_TEXT["tpcc"], "batches_per_step": nb, "txns_per_step": txns_per_step,
+                       "ops_per_step": ops_per_step, "rule": "ordered (ascending TID per cell, all commit)",
+                       "mode": mode_name, "mode_ms": {str(k): v for k, v in mode_ms.items()},
+                       "tuning": {str(k): f"{v['block']}x{v['ipt']}" for k, v in tiles.items()},
+                       "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
+            "gpu_launches": launches, "roofline": roof, "clocks": clk, "e2e": e2e,
+            "contention": {"contended_ops_per_batch": mean_stats["contended_ops"],
+                           "contended_cells_per_batch": mean_stats["contended_cells"]},
+            "table_rows_after": rows}
+    if world == 1 and not args.no_cpu_baseline:
+        v, done, t_used = tpcc_cpu_baseline(g, host[:1])
+        line["cpu_baseline"] = {"value": v, "unit": "txn/s", "cores": 1, "kind": "port",
+                                "sample": f"{done} txns of batch 0 in slices of 2^16, serial replay of the 9 tables "
+                                          f"(ordered rule), {t_used:.1f} s"}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_tpcc(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+
+    g, sh = tpcc_setup(0)
+    threads = os.cpu_count() or 1
+    tf, keys, opw, pay, n_no, ins = g.gen(0, sh["batch"])
+    slice_txns = 1 << 16
+    slices = []
+    for lo in range(0, len(tf) - 1, slice_txns):
+        hi = min(len(tf) - 1, lo + slice_txns)
+        a, b = int(tf[lo]), int(tf[hi])
+        slices.append(((tf[lo:hi + 1] - tf[lo]).astype(np.uint32), keys[a:b], opw[a:b], hi - lo))
+    n_steps = args.warmup + args.steps
+    per = np.zeros(9, np.int64)
+    for i in range(n_steps):
+        w = slices[i % len(slices)][2]
+        per += np.bincount(((w >> 8) & 15)[(w & 3) == 2], minlength=16)[:9]
+    db = tpcc_cpu_tables(g, per)
+
+    def step(i):
+        tfs, k, w, n = slices[i % len(slices)]
+        db.replay(0, tfs, k, w, pay, threads=threads)
+        return n
+
+    for i in range(args.warmup):
+        step(i)
+    t0 = time.perf_counter()
+    txns = sum(step(args.warmup + i) for i in range(args.steps))
+    dt = time.perf_counter() - t0
+    value = txns / dt
+    line = {"metric": METRIC, "value": value, "unit": "txn/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64", "data": "synthetic (seeded generator)",
+            "config": {"workload": WORKLOAD_TEXT["tpcc"], "step": f"up to {slice_txns} txns of the workload",
+                       "l2": "inputs larger than L2"},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "txn/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} slices of up to {slice_txns} txns of batch 0, 9 tables, "
+                                       f"cell-partitioned replay on {threads} threads (inserts split by table)"},
+            "e2e": {"value": value, "unit": "txn/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def run_serve(args):
     """Offered-load sweep of the serving loop; value = the highest committed
     txn/s among the loads served at p99 <= 2 ms."""
@@ -466,9 +724,14 @@ def main():
     if not args.steps:
         args.steps = DEFAULT_STEPS[args.config]
     if args.impl == "reference":
-        run_reference(args, "zipf" if args.config == "serve" else args.config)
+        if args.config == "tpcc":
+            run_reference_tpcc(args)
+        else:
+            run_reference(args, "zipf" if args.config == "serve" else args.config)
     elif args.config == "serve":
         run_serve(args)
+    elif args.config == "tpcc":
+        run_tpcc(args)
     else:
         run_ours(args, args.config)
 

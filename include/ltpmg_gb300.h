@@ -13,16 +13,18 @@
  *
  * Data model
  *  - A context owns one CUDA device, its tables and all scratch memory.
- *  - A table is column-store: one contiguous int32 array per column.  Cells
- *    are addressed by (table, row = key, column).
+ *  - A table is column-store: one contiguous array per column, int32 or
+ *    int64 (ltp_schema.wide_cols).  Cells are addressed by (table, row =
+ *    key, column).  Arithmetic on a cell wraps at its own width.
  *  - A batch is a transaction-major list of operations: transaction t owns
  *    ops [txn_first[t], txn_first[t+1]); its TID is t.  Each op is a 64-bit
  *    key (the row id) and a 32-bit opword (LTP_OPW below).
  *  - Outputs per batch: commit[t] (1 committed, 0 aborted) and, per op, the
  *    value of the cell immediately after the op in the serial order (the
  *    value read, or the value the read-modify-write produced; 0 for ops of
- *    aborted transactions).  The table state is read back with
- *    ltp_table_download.
+ *    aborted transactions).  ltp_batch_fetch returns the low 32 bits of
+ *    each value; ltp_batch_fetch64 the full value once the context has an
+ *    int64 column.  The table state is read back with ltp_table_download.
  *
  * Rules (ltp_config.rule)
  *  - LTP_RULE_ORDERED: every op on a cell runs in ascending (TID, op) order
@@ -61,11 +63,19 @@ extern "C" {
 #define LTP_OP_ADD 1u /* read-modify-write: cell += immediate (two's-complement wrap) */
 /* Insert: appends one row to the op's table.  The op's key is an offset into
  * the batch's insert payload (ltp_batch_load_payload) where the new row's
- * n_cols int32 values start; the column and immediate fields are unused.
- * The new row's id is the table's row count at batch start plus the number
- * of committed inserts into that table earlier in (TID, op) order; it is the
- * op's output value.  A new row cannot be named by other ops of its batch. */
+ * values start: one int32 slot per int32 column, two (low word first) per
+ * int64 column.  The new row's id is the table's row count at batch start
+ * plus the number of committed inserts into that table earlier in (TID, op)
+ * order; it is the op's output value.  A new row cannot be named by other
+ * ops of its batch.
+ * Linked insert: when the low 10 bits of the immediate hold a distance d > 0,
+ * column `col` of the new row takes the output of op i - d (a read or
+ * read-modify-write of the same transaction) instead of its payload value --
+ * e.g. an order row taking the order id its transaction just drew from the
+ * district's next-order-id counter.  With d = 0 the column and immediate
+ * fields are unused. */
 #define LTP_OP_INSERT 2u
+#define LTP_INSERT_LINK(col, table, d) LTP_OPW(LTP_OP_INSERT, col, table, (d) & 0x3FF)
 #define LTP_OPW(kind, col, table, imm) \
     ((uint32_t)(kind) | ((uint32_t)(col) << 2) | ((uint32_t)(table) << 8) | (((uint32_t)(imm) & 0xFFFFFu) << 12))
 
@@ -83,8 +93,9 @@ typedef struct {
 } ltp_config;
 
 typedef struct {
-    uint32_t n_cols; /* 1..LTP_MAX_COLS int32 columns */
+    uint32_t n_cols;    /* 1..LTP_MAX_COLS columns */
     uint32_t reserved;
+    uint64_t wide_cols; /* bit c set: column c holds int64, else int32 */
 } ltp_schema;
 
 #define LTP_N_STAGES 12
@@ -131,11 +142,13 @@ int ltp_table_create(ltp_ctx *ctx, const ltp_schema *schema, uint64_t rows, uint
 /* Same with room for inserts: rows_cap >= rows rows are allocated. */
 int ltp_table_create_cap(ltp_ctx *ctx, const ltp_schema *schema, uint64_t rows, uint64_t rows_cap,
                          uint32_t *table_id);
-/* Copies rows [row0, row0+n) of one column from host memory (int32). */
-int ltp_table_upload(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, const int32_t *src);
+/* Copies rows [row0, row0+n) of one column from host memory (n int32 or
+ * int64 values, the column's own width). */
+int ltp_table_upload(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, const void *src);
 /* New: the reference never copies tables back (gpudatabase.cu:240-339). */
-int ltp_table_download(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, int32_t *dst);
-/* Device-side fill with ltp_table_value(seed, row, col, n_cols). */
+int ltp_table_download(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, void *dst);
+/* Device-side fill with ltp_table_value(seed, row, col, n_cols); an int64
+ * column holds that value sign-extended. */
 int ltp_table_fill_seeded(ltp_ctx *ctx, uint32_t table, uint64_t seed, void *stream);
 /* FNV-1a 64 of the whole table (column-major bytes), computed on the host
  * from a download; for checkpoints and tests. */
@@ -177,6 +190,9 @@ int ltp_batches_execute(ltp_ctx *ctx, ltp_batch *const *batches, uint32_t n, int
 /* Asynchronous device->host copy of the outputs (commit may be NULL, vals
  * may be NULL). */
 int ltp_batch_fetch(ltp_ctx *ctx, ltp_batch *b, uint8_t *commit, int32_t *vals, void *stream);
+/* The same for the full 64-bit output values (needs an int64 column in the
+ * context; LTP_E_STATE otherwise). */
+int ltp_batch_fetch64(ltp_ctx *ctx, ltp_batch *b, int64_t *vals, void *stream);
 /* Synchronises the stream, then fills stats (may be NULL) and reports any
  * device-side error of the batch. */
 int ltp_batch_finish(ltp_ctx *ctx, ltp_batch *b, ltp_stats *stats, void *stream);
@@ -291,6 +307,80 @@ uint64_t ltp_gen_ycsb(const ltp_ycsb_params *p, uint64_t batch, uint64_t n_txns,
                       uint32_t *opw, uint64_t cap_ops, int n_threads);
 int32_t ltp_table_value(uint64_t seed, uint64_t row, uint32_t col, uint32_t n_cols);
 
+/* ---- TPC-C-shaped order-entry workload (new-order / payment) ----------
+ * Nine tables with the reference's TPC-C schema (data/TPCC.json) made
+ * columnar: ids and counts int32, money int64 cents, tax and discount int32
+ * basis points, every 24-byte text field six int32 columns.  The op shapes
+ * follow the reference's TPC-C op expansion (parse<Neworder_Query>,
+ * cuda/src/gpuquery.cu:2474-2606: 5 + 3 per order line; parse<Payment_Query>,
+ * gpuquery.cu:2608-2734: 7), with the TPC-C input distributions (NURand
+ * customers and items, 1% remote order lines, 15% remote payments, 60% of
+ * payments by last name) in place of the reference's uniform draws
+ * (src/txn_generator.cpp:231-381).
+ *  new-order: READ W_TAX; RMW D_NEXT_O_ID += 1 (its output is the order id);
+ *    READ C_DISCOUNT; INSERT new-order and order rows linked to the order
+ *    id; per line: INSERT order-line (linked), RMW S_QUANTITY -= qty,
+ *    RMW S_YTD += qty.
+ *  payment: RMW W_YTD += amount; RMW D_YTD += amount; READ C_CREDIT;
+ *    RMW C_BALANCE -= amount; RMW C_YTD_PAYMENT += amount;
+ *    RMW C_PAYMENT_CNT += 1; INSERT history.
+ * A payment by last name resolves the customer on the host through the
+ * static last-name index (the middle customer by id among those with the
+ * name), as the reference resolves it from its index (gpuquery.cu:2641-2650;
+ * index built at src/database.cpp:310-393).  D_NEXT_O_ID holds the last order
+ * id issued.  S_QUANTITY is decremented without TPC-C's +91 wrap. */
+#define LTP_TPCC_N_TABLES 9
+enum {
+    LTP_TPCC_WAREHOUSE = 0, LTP_TPCC_DISTRICT, LTP_TPCC_CUSTOMER, LTP_TPCC_HISTORY, LTP_TPCC_NEW_ORDER,
+    LTP_TPCC_ORDER, LTP_TPCC_ORDER_LINE, LTP_TPCC_ITEM, LTP_TPCC_STOCK
+};
+/* column indices (a 24-byte text field LTPC_X occupies LTPC_X .. LTPC_X+5) */
+enum { LTPC_W_ID = 0, LTPC_W_TAX, LTPC_W_YTD, LTPC_W_NAME, LTPC_W_NCOLS = LTPC_W_NAME + 6 };
+enum { LTPC_D_ID = 0, LTPC_D_W_ID, LTPC_D_TAX, LTPC_D_YTD, LTPC_D_NEXT_O_ID, LTPC_D_NAME, LTPC_D_NCOLS = LTPC_D_NAME + 6 };
+enum {
+    LTPC_C_ID = 0, LTPC_C_D_ID, LTPC_C_W_ID, LTPC_C_LAST, LTPC_C_CREDIT, LTPC_C_DISCOUNT, LTPC_C_BALANCE, LTPC_C_YTD_PAYMENT, LTPC_C_PAYMENT_CNT,
+    LTPC_C_DELIVERY_CNT, LTPC_C_DATA, LTPC_C_NCOLS = LTPC_C_DATA + 6
+};
+enum { LTPC_H_C_ID = 0, LTPC_H_C_D_ID, LTPC_H_C_W_ID, LTPC_H_D_ID, LTPC_H_W_ID, LTPC_H_AMOUNT, LTPC_H_DATA, LTPC_H_NCOLS = LTPC_H_DATA + 6 };
+enum { LTPC_NO_O_ID = 0, LTPC_NO_D_ID, LTPC_NO_W_ID, LTPC_NO_NCOLS };
+enum { LTPC_O_ID = 0, LTPC_O_D_ID, LTPC_O_W_ID, LTPC_O_C_ID, LTPC_O_OL_CNT, LTPC_O_ALL_LOCAL, LTPC_O_CARRIER_ID, LTPC_O_NCOLS };
+enum {
+    LTPC_OL_O_ID = 0, LTPC_OL_D_ID, LTPC_OL_W_ID, LTPC_OL_NUMBER, LTPC_OL_I_ID, LTPC_OL_SUPPLY_W_ID, LTPC_OL_QUANTITY, LTPC_OL_AMOUNT, LTPC_OL_DIST_INFO,
+    LTPC_OL_NCOLS = LTPC_OL_DIST_INFO + 6
+};
+enum { LTPC_I_ID = 0, LTPC_I_IM_ID, LTPC_I_PRICE, LTPC_I_NAME, LTPC_I_NCOLS = LTPC_I_NAME + 6 };
+enum { LTPC_S_I_ID = 0, LTPC_S_W_ID, LTPC_S_QUANTITY, LTPC_S_YTD, LTPC_S_ORDER_CNT, LTPC_S_REMOTE_CNT, LTPC_S_DIST, LTPC_S_NCOLS = LTPC_S_DIST + 6 };
+
+typedef struct {
+    uint64_t seed;
+    uint32_t warehouses;     /* W */
+    uint32_t districts;      /* per warehouse (10) */
+    uint32_t customers;      /* per district (3000) */
+    uint32_t items;          /* items, and stock rows per warehouse (100000) */
+    uint32_t ol_min, ol_max; /* order lines per new-order (5, 15) */
+    double new_order_frac;   /* 0.5 */
+    double remote_line;      /* 0.01: a line's supply warehouse is another one */
+    double remote_payment;   /* 0.15: the paying customer is another warehouse's */
+    double by_last_name;     /* 0.6: payment names the customer by last name */
+} ltp_tpcc_params;
+
+typedef struct ltp_tpcc ltp_tpcc;
+/* Validates the parameters and builds the last-name index. */
+int ltp_tpcc_create(const ltp_tpcc_params *p, ltp_tpcc **out);
+void ltp_tpcc_free(ltp_tpcc *g);
+/* Schema (n_cols, wide_cols) and initial row count of one table; the
+ * insert-only tables (history, new-order, order, order-line) start empty. */
+int ltp_tpcc_table(const ltp_tpcc *g, uint32_t table, ltp_schema *schema, uint64_t *rows);
+/* Initial values of rows [row0, row0+n) of one column, at the column's width. */
+int ltp_tpcc_column(const ltp_tpcc *g, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, void *dst);
+/* Generates batch `batch` of n_txns transactions (TID = position).  With
+ * keys == NULL only the sizes are computed.  n_new_order (may be NULL)
+ * receives the new-order count; inserts[LTP_TPCC_N_TABLES] (may be NULL)
+ * the rows each table gains.  Returns LTP_OK or LTP_E_CAPACITY. */
+int ltp_tpcc_gen(const ltp_tpcc *g, uint64_t batch, uint64_t n_txns, uint32_t *txn_first, uint64_t *keys,
+                 uint32_t *opw, uint64_t cap_ops, int32_t *payload, uint64_t cap_payload, uint64_t *n_ops,
+                 uint64_t *n_payload, uint64_t *n_new_order, uint64_t *inserts, int n_threads);
+
 /* ---- tuning --------------------------------------------------------------- */
 typedef struct {
     uint32_t block;      /* threads per block of the streaming kernels: 128, 256, 512 */
@@ -332,7 +422,7 @@ int ltp_debug_stall_next(ltp_ctx *ctx, uint32_t ms);
  * read-modify-writes; the call takes no insert payload). */
 #define LTP_NOALLOC_MAX_OPS (1ull << 18)
 #define LTP_NOALLOC_MAX_CELLS (1ull << 23)
-#define LTP_NOALLOC_SCRATCH_BYTES 15001344ull
+#define LTP_NOALLOC_SCRATCH_BYTES 16049920ull
 int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table, uint64_t rows_cap, uint64_t n_rows,
                         uint32_t n_cols, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
                         uint64_t n_ops, const uint64_t *keys, const uint32_t *opw, int32_t *out, uint8_t *commit,

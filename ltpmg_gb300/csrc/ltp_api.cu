@@ -18,6 +18,10 @@ using namespace ltp;
 struct TableHost {
     TableDev dev;
     uint32_t n_cols;
+    uint64_t bytes;  // whole allocation (every column over rows_cap rows)
+
+    uint32_t width(uint32_t col) const { return col_wide(dev, col) ? 8u : 4u; }
+    char *col_ptr(uint32_t col, uint64_t row) const { return dev.data + col_off(dev, col) + row * width(col); }
 };
 
 struct ltp_ctx {
@@ -28,6 +32,7 @@ struct ltp_ctx {
     cudaStream_t stream = nullptr;
     std::vector<TableHost> tables;
     uint64_t total_cells = 0;
+    bool any_wide = false;  // some table has an int64 column
     Scratch s;
     uint64_t alloc_words = 0;  // bitmap words currently allocated
     Counters *ctr = nullptr;
@@ -51,6 +56,7 @@ struct ltp_batch {
     uint64_t *keys = nullptr;
     uint32_t *opw = nullptr, *txn_first = nullptr, *op_txn = nullptr;
     int32_t *out = nullptr;
+    long long *out64 = nullptr;  // full outputs, allocated once the context has int64 columns
     uint8_t *commit = nullptr;
     uint64_t n_txns = 0, n_ops = 0;
     uint32_t ops_per_txn = 0;
@@ -175,6 +181,7 @@ TablesDev tables_dev(const ltp_ctx *ctx) {
     memset(&T, 0, sizeof(T));
     T.n = (uint32_t)ctx->tables.size();
     T.rows_now = ctx->rows_now;
+    T.any_wide = ctx->any_wide ? 1u : 0u;
     for (size_t i = 0; i < ctx->tables.size(); i++) T.t[i] = ctx->tables[i].dev;
     return T;
 }
@@ -281,6 +288,8 @@ int ltp_table_create_cap(ltp_ctx *ctx, const ltp_schema *schema, uint64_t rows, 
     if (rows_cap < rows) return fail(ctx, LTP_E_BADARG, "rows_cap must be >= rows");
     if (schema->n_cols == 0 || schema->n_cols > LTP_MAX_COLS) return fail(ctx, LTP_E_BADARG, "n_cols must be 1..64");
     if (rows_cap == 0 || rows_cap > (1ull << 31)) return fail(ctx, LTP_E_BADARG, "rows_cap must be 1..2^31");
+    if (schema->n_cols < 64 && (schema->wide_cols >> schema->n_cols))
+        return fail(ctx, LTP_E_BADARG, "wide_cols names a column beyond n_cols");
     if (ctx->tables.size() >= LTP_MAX_TABLES) return fail(ctx, LTP_E_CAPACITY, "at most 16 tables");
     const uint64_t cells = rows_cap * schema->n_cols;
     if ((ctx->total_cells + cells + 31) / 32 >= (1ull << 32))
@@ -294,8 +303,11 @@ int ltp_table_create_cap(ltp_ctx *ctx, const ltp_schema *schema, uint64_t rows, 
     t.dev.n_rows = rows;
     t.dev.n_cols = schema->n_cols;
     t.dev.cell_base = ctx->total_cells;
-    CK(cudaMalloc((void **)&t.dev.data, t.dev.rows_cap * schema->n_cols * sizeof(int32_t)));
-    CK(cudaMemset(t.dev.data, 0, t.dev.rows_cap * schema->n_cols * sizeof(int32_t)));
+    t.dev.wide = schema->wide_cols;
+    t.bytes = col_off(t.dev, schema->n_cols);  // offset one past the last column
+    CK(cudaMalloc((void **)&t.dev.data, t.bytes));
+    CK(cudaMemset(t.dev.data, 0, t.bytes));
+    if (t.dev.wide) ctx->any_wide = true;
     // keep the next table's cells in a fresh bitmap word
     ctx->total_cells += (cells + 31) & ~31ull;
     *table_id = (uint32_t)ctx->tables.size();
@@ -317,25 +329,25 @@ static int check_table(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0
     return LTP_OK;
 }
 
-int ltp_table_upload(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, const int32_t *src) {
+int ltp_table_upload(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, const void *src) {
     int rc = check_table(ctx, table, col, row0, n);
     if (rc) return rc;
     if (!src && n) return LTP_E_BADARG;
     const TableHost &t = ctx->tables[table];
     CK(cudaSetDevice(ctx->device));
-    CK(cudaMemcpyAsync(t.dev.data + col * t.dev.rows_cap + row0, src, n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(t.col_ptr(col, row0), src, n * t.width(col), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return LTP_OK;
 }
 
-int ltp_table_download(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, int32_t *dst) {
+int ltp_table_download(ltp_ctx *ctx, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, void *dst) {
     int rc = check_table(ctx, table, col, row0, n);
     if (rc) return rc;
     if (!dst && n) return LTP_E_BADARG;
     const TableHost &t = ctx->tables[table];
     CK(cudaSetDevice(ctx->device));
     CK(cudaDeviceSynchronize());
-    CK(cudaMemcpyAsync(dst, t.dev.data + col * t.dev.rows_cap + row0, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(dst, t.col_ptr(col, row0), n * t.width(col), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return LTP_OK;
 }
@@ -363,13 +375,13 @@ int ltp_table_fingerprint(ltp_ctx *ctx, uint32_t table, uint64_t *out) {
     uint64_t nrows = 0;
     int rc0 = ltp_table_rows(ctx, table, &nrows);
     if (rc0) return rc0;
-    std::vector<int32_t> buf(nrows);
+    std::vector<int64_t> buf(nrows);
     uint64_t h = 0xCBF29CE484222325ull;
     for (uint32_t c = 0; c < t.n_cols; c++) {
         int rc = ltp_table_download(ctx, table, c, 0, nrows, buf.data());
         if (rc) return rc;
         const uint8_t *p = (const uint8_t *)buf.data();
-        for (uint64_t i = 0; i < nrows * 4; i++) {
+        for (uint64_t i = 0; i < nrows * t.width(c); i++) {
             h ^= p[i];
             h *= 0x100000001B3ull;
         }
@@ -391,6 +403,7 @@ int ltp_batch_create(ltp_ctx *ctx, uint64_t max_txns, uint64_t max_ops, ltp_batc
     if (e == cudaSuccess) e = dalloc(&b->opw, max_ops);
     if (e == cudaSuccess) e = dalloc(&b->op_txn, max_ops);
     if (e == cudaSuccess) e = dalloc(&b->out, max_ops);
+    if (e == cudaSuccess && ctx->any_wide) e = dalloc(&b->out64, max_ops);
     if (e == cudaSuccess) e = dalloc(&b->txn_first, max_txns + 1);
     if (e == cudaSuccess) e = dalloc(&b->commit, max_txns);
     if (e == cudaSuccess) e = dalloc(&b->snap, 1);
@@ -418,6 +431,7 @@ int ltp_batch_free(ltp_ctx *ctx, ltp_batch *b) {
     cudaFree(b->opw);
     cudaFree(b->op_txn);
     cudaFree(b->out);
+    cudaFree(b->out64);
     cudaFree(b->txn_first);
     cudaFree(b->commit);
     cudaFree(b->snap);
@@ -443,6 +457,10 @@ int ltp_batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *
     }
     CK(cudaSetDevice(ctx->device));
     cudaStream_t st = pick_stream(ctx, stream);
+    if (ctx->any_wide && !b->out64) {  // an int64 column appeared after the batch was made
+        CK(cudaStreamSynchronize(st));
+        CK(dalloc(&b->out64, b->cap_ops));
+    }
     if (n_ops) {
         CK(cudaMemcpyAsync(b->keys, keys, n_ops * 8, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(b->opw, opw, n_ops * 4, cudaMemcpyHostToDevice, st));
@@ -489,6 +507,7 @@ BatchDev batch_dev(const ltp_batch *b) {
     bd.txn_first = b->txn_first;
     bd.op_txn = b->op_txn;
     bd.out = b->out;
+    bd.out64 = b->out64;
     bd.commit = b->commit;
     bd.n_ops = b->n_ops;
     bd.n_txns = b->n_txns;
@@ -641,6 +660,16 @@ int ltp_batch_fetch(ltp_ctx *ctx, ltp_batch *b, uint8_t *commit, int32_t *vals, 
     cudaStream_t st = pick_stream(ctx, stream);
     if (commit && b->n_txns) CK(cudaMemcpyAsync(commit, b->commit, b->n_txns, cudaMemcpyDeviceToHost, st));
     if (vals && b->n_ops) CK(cudaMemcpyAsync(vals, b->out, b->n_ops * 4, cudaMemcpyDeviceToHost, st));
+    return LTP_OK;
+}
+
+int ltp_batch_fetch64(ltp_ctx *ctx, ltp_batch *b, int64_t *vals, void *stream) {
+    if (!ctx || !b) return LTP_E_BADARG;
+    if (!b->executed) return fail(ctx, LTP_E_STATE, "batch not executed");
+    if (!b->out64) return fail(ctx, LTP_E_STATE, "the context has no int64 column");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = pick_stream(ctx, stream);
+    if (vals && b->n_ops) CK(cudaMemcpyAsync(vals, b->out64, b->n_ops * 8, cudaMemcpyDeviceToHost, st));
     return LTP_OK;
 }
 

@@ -22,29 +22,13 @@
 #include <vector>
 
 #include "../../include/ltpmg_gb300.h"
+#include "ltp_rng.h"
 
 namespace {
 
-inline uint64_t mix(uint64_t z) {
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
-    return z ^ (z >> 31);
-}
-
-struct Stream {
-    uint64_t s;
-    uint64_t next() {
-        s += 0x9E3779B97F4A7C15ULL;
-        return mix(s);
-    }
-    uint64_t below(uint64_t n) { return (uint64_t)(((unsigned __int128)next() * n) >> 64); }
-    double unit() { return (double)(next() >> 11) * 0x1.0p-53; }
-};
-
-uint64_t txn_stream(uint64_t seed, uint64_t batch, uint64_t txn) {
-    const uint64_t s = mix(seed ^ mix(batch + 0x4241544348ULL));
-    return mix(s + (txn + 1) * 0x9E3779B97F4A7C15ULL);
-}
+using ltp_rng::mix;
+using ltp_rng::Stream;
+using ltp_rng::txn_stream;
 
 // Seeded permutation of [0, n): balanced 4-round Feistel network on the
 // smallest even bit width >= log2(n), cycle-walking back into range.

@@ -18,24 +18,38 @@ __host__ __device__ __forceinline__ u32 opw_col(u32 w) { return (w >> 2) & 63u; 
 __host__ __device__ __forceinline__ u32 opw_table(u32 w) { return (w >> 8) & 15u; }
 __host__ __device__ __forceinline__ int32_t opw_imm(u32 w) { return ((int32_t)w) >> 12; }
 
-// One column-store table: column c of row r lives at data[c * rows_cap + r].
+// One column-store table.  Columns are int32, or int64 where bit c of
+// `wide` is set; column c starts at byte col_off(c) = rows_cap * (4c + 4 *
+// (wide columns before c)) and row r of it at col_off(c) + r * width(c).
 // Cells are numbered row-major within a table (cell_base + r * n_cols + c) so
 // that the cells of one row share a bitmap word.
 struct TableDev {
-    int32_t *data;
+    char *data;
     u64 rows_cap;   // column stride (rows allocated, padded)
     u64 row_limit;  // rows the table may grow to (requested capacity)
     u64 n_rows;
     u64 cell_base;
+    u64 wide;       // bit c: column c holds int64
     u32 n_cols;
     u32 pad;
 };
+
+__host__ __device__ __forceinline__ u64 col_off(const TableDev &t, u32 c) {
+    const u64 below = c ? (t.wide & ((1ull << c) - 1ull)) : 0ull;
+#ifdef __CUDA_ARCH__
+    const u32 nw = __popcll(below);
+#else
+    const u32 nw = (u32)__builtin_popcountll(below);
+#endif
+    return t.rows_cap * (4ull * c + 4ull * nw);
+}
+__host__ __device__ __forceinline__ bool col_wide(const TableDev &t, u32 c) { return (t.wide >> c) & 1ull; }
 
 struct TablesDev {
     TableDev t[LTP_MAX_TABLES];
     u64 *rows_now;  // [LTP_MAX_TABLES] device-resident row counts (grow with inserts)
     u32 n;
-    u32 pad;
+    u32 any_wide;   // some table has an int64 column
 };
 
 // Device view of one loaded batch.
@@ -44,7 +58,8 @@ struct BatchDev {
     const u32 *opw;        // [n_ops]
     const u32 *txn_first;  // [n_txns + 1]
     const u32 *op_txn;     // [n_ops] transaction of each op (variable-length batches)
-    int32_t *out;          // [n_ops] value after each op
+    int32_t *out;          // [n_ops] value after each op (low 32 bits for int64 cells)
+    long long *out64;      // [n_ops] full value, when the context has int64 columns (else null)
     uint8_t *commit;       // [n_txns]
     const int32_t *payload;  // insert row images (LTP_OP_INSERT keys index it)
     u64 payload_len;
@@ -90,7 +105,7 @@ struct Scratch {
     u32 *tw_list;   // [cap_ops] touched words
     u64 *list[2];   // [cap_ops] contended-op records, ping-pong for the sort
     u64 *dcell;     // [cap_ops] cell of each contended-cell id
-    int32_t *dbase; // [cap_ops] value of each contended cell before the batch
+    long long *dbase; // [cap_ops] value of each contended cell before the batch
     u32 *dminw;     // [cap_ops] smallest writer TID of each contended cell (priority rule)
     u32 *st_sort[2];// [tiles * 256] radix look-back status
     u64 *st_ids;    // [tiles] id-scan look-back status

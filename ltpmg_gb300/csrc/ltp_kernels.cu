@@ -123,8 +123,9 @@ __device__ u64 lookback_sum(u64 *status, u32 tile, u64 agg, Counters *ctr) {
 // ---- table addressing ------------------------------------------------------
 struct OpRef {
     u64 cell;
-    int32_t *ptr;
+    char *ptr;
     bool valid;
+    bool wide;
 };
 
 __device__ __forceinline__ OpRef decode_op(const TablesDev &T, u64 key, u32 w) {
@@ -133,12 +134,30 @@ __device__ __forceinline__ OpRef decode_op(const TablesDev &T, u64 key, u32 w) {
     r.valid = tb < T.n && kind <= 1u;
     const TableDev &t = T.t[r.valid ? tb : 0];
     r.valid = r.valid && key < __ldg(&T.rows_now[r.valid ? tb : 0]) && col < t.n_cols;
+    r.wide = r.valid && col_wide(t, col);
     r.cell = r.valid ? t.cell_base + key * t.n_cols + col : ~0ull;
-    r.ptr = r.valid ? t.data + (u64)col * t.rows_cap + key : nullptr;
+    r.ptr = r.valid ? t.data + col_off(t, col) + key * (r.wide ? 8ull : 4ull) : nullptr;
     return r;
 }
 
-__device__ __forceinline__ int32_t *cell_ptr(const TablesDev &T, u64 cell) {
+// Cell values are handled as 64-bit; int32 cells are sign-extended on load and
+// truncated on store, which is exactly 32-bit two's-complement arithmetic.
+__device__ __forceinline__ long long load_cell(const char *p, bool wide) {
+    return wide ? *reinterpret_cast<const long long *>(p) : (long long)*reinterpret_cast<const int32_t *>(p);
+}
+__device__ __forceinline__ long long load_cell_ro(const char *p, bool wide) {
+    return wide ? __ldg(reinterpret_cast<const long long *>(p)) : (long long)__ldg(reinterpret_cast<const int32_t *>(p));
+}
+__device__ __forceinline__ void store_cell(char *p, bool wide, long long v) {
+    if (wide) *reinterpret_cast<long long *>(p) = v;
+    else *reinterpret_cast<int32_t *>(p) = (int32_t)v;
+}
+__device__ __forceinline__ void store_out(const BatchDev &b, u64 i, long long v) {
+    b.out[i] = (int32_t)v;
+    if (b.out64) b.out64[i] = v;
+}
+
+__device__ __forceinline__ char *cell_ptr(const TablesDev &T, u64 cell, bool *wide) {
     u32 k = 0;
     for (u32 i = 1; i < T.n; i++)
         if (cell >= T.t[i].cell_base) k = i;
@@ -146,7 +165,27 @@ __device__ __forceinline__ int32_t *cell_ptr(const TablesDev &T, u64 cell) {
     u64 local = cell - t.cell_base;
     u64 row = local / t.n_cols;
     u32 col = (u32)(local - row * t.n_cols);
-    return t.data + (u64)col * t.rows_cap + row;
+    *wide = col_wide(t, col);
+    return t.data + col_off(t, col) + row * (*wide ? 8ull : 4ull);
+}
+
+__device__ __forceinline__ u32 op_tid(const BatchDev &b, u64 i);
+
+// An insert's payload row holds one int32 slot per int32 column and two
+// (low word first) per int64 column.
+__device__ __forceinline__ u64 insert_slots(const TableDev &t) { return (u64)t.n_cols + (u64)__popcll(t.wide); }
+
+// A linked insert (link distance d = low 10 bits of the immediate, d > 0)
+// takes column `col` of its new row from the output of op i - d, which must
+// be a read or read-modify-write of the same transaction.
+__device__ __forceinline__ u32 insert_link(u32 w) { return (u32)opw_imm(w) & 0x3FFu; }
+__device__ __forceinline__ bool insert_link_ok(const BatchDev &b, const TableDev &t, u64 i, u32 w) {
+    const u32 d = insert_link(w);
+    if (!d) return true;
+    if (opw_col(w) >= t.n_cols || d > i) return false;
+    const u32 tid = op_tid(b, i);
+    const u64 first = b.txn_first ? (u64)b.txn_first[tid] : (u64)tid * b.ops_per_txn;
+    return i - d >= first && opw_kind(b.opw[i - d]) <= LTP_OP_ADD;
 }
 
 // Is the cell contended (touched twice and written)?  If so, *m is its dense id.
@@ -210,7 +249,7 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
             if (i >= n) continue;
             if (opw_kind(w[k]) == LTP_OP_INSERT) {  // appends a row: no existing cell to mark
                 const u32 tb = opw_table(w[k]);
-                if (tb < T.n && key[k] + T.t[tb].n_cols <= b.payload_len) {
+                if (tb < T.n && key[k] + insert_slots(T.t[tb]) <= b.payload_len && insert_link_ok(b, T.t[tb], i, w[k])) {
                     atomicAdd(&s_ins[tb], 1u);
                 } else {
                     atomicMax(&ctr->bad_op, ~i);
@@ -366,8 +405,10 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
                     int bpos = __ffs(bits) - 1;
                     bits &= bits - 1;
                     u64 cell = ((u64)wd[k] << 5) | (u64)bpos;
-                    s.dcell[pre] = cell;
-                    s.dbase[pre] = *cell_ptr(T, cell);
+                    bool wide_c;
+                    const char *cp = cell_ptr(T, cell, &wide_c);
+                    s.dcell[pre] = cell | (wide_c ? (1ull << 63) : 0ull);  // bit 63: int64 cell
+                    s.dbase[pre] = load_cell(cp, wide_c);
                     if (PRIORITY) s.dminw[pre] = 0xFFFFFFFFu;
                     pre++;
                 }
@@ -466,19 +507,22 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
         }
         // uncontended ops execute in place; an uncontended read's cell is never
         // written in this batch, an uncontended RMW is its cell's only op
-        int32_t val[IPT];
+        long long val[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; k++)
-            if (r[k].valid && !con[k]) val[k] = opw_kind(w[k]) == LTP_OP_ADD ? *r[k].ptr : __ldg(r[k].ptr);
+            if (r[k].valid && !con[k])
+                val[k] = opw_kind(w[k]) == LTP_OP_ADD ? load_cell(r[k].ptr, r[k].wide) : load_cell_ro(r[k].ptr, r[k].wide);
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             if (r[k].valid && !con[k]) {
-                int32_t v = val[k];
+                long long v = val[k];
                 if (opw_kind(w[k]) == LTP_OP_ADD) {
-                    v = (int32_t)((u32)v + (u32)opw_imm(w[k]));
-                    *r[k].ptr = v;
+                    v = (long long)((u64)v + (u64)(long long)opw_imm(w[k]));
+                    store_cell(r[k].ptr, r[k].wide, v);
                 }
-                __stcs(&b.out[wbase + (u64)k * 32 + lane], v);
+                const u64 i = wbase + (u64)k * 32 + lane;
+                __stcs(&b.out[i], (int32_t)v);
+                if (b.out64) b.out64[i] = v;
             }
         }
         __syncthreads();
@@ -495,7 +539,10 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
 }
 
 template <int BLOCK, int IPT>
-__global__ void __launch_bounds__(BLOCK) k_classify(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+// register budget: 64 per thread up to 4 ops per thread, 128 above, so that
+// 64-bit cell values do not halve the resident blocks
+__global__ void __launch_bounds__(BLOCK, 65536 / (BLOCK * (IPT <= 4 ? 64 : 128))) k_classify(BatchDev b, TablesDev T,
+                                                                                          Scratch s, Counters *ctr) {
     phase_classify<BLOCK, IPT>(b, T, s, ctr);
 }
 
@@ -692,24 +739,36 @@ __global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *c
 // apply: segmented scan of RMW immediates per contended cell, write-back
 // ============================================================================
 // look-back status: bits 62-63 flag, bit 61 "tile holds a segment head",
-// bits 0-31 sum since the last head (wrapping int32 arithmetic)
-template <int BLK>
+// bits 0-60 sum since the last head.  S is the scan type: u32 when every
+// column is int32 (wrapping int32 arithmetic), u64 when some column is int64;
+// a 64-bit sum of signed 20-bit immediates over < 2^32 ops stays below 2^52
+// in magnitude, so 61 sign-extended bits hold it exactly.
+constexpr u64 kSum61 = (1ull << 61) - 1ull;
+template <typename S>
+__device__ __forceinline__ S unpack_sum(u64 x) {
+    return (S)(u64)(((long long)(x << 3)) >> 3);
+}
+
+template <int BLK, typename S>
 __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
     constexpr u32 AIPT = kApplyTile / BLK;
+    constexpr bool WIDE = sizeof(S) == 8;
     if (block_err(ctr)) return;
     const u64 n = ctr->n_c;
     const u32 tiles = (u32)((n + kApplyTile - 1) / kApplyTile);
     const u64 *list = s.list[sort_passes_dev(ctr->M) & 1];
     constexpr int NW = BLK / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __shared__ u32 s_wf[NW], s_ws[NW];
-    __shared__ u32 s_tf, s_ts;
+    __shared__ u32 s_wf[NW];
+    __shared__ S s_ws[NW];
+    __shared__ u32 s_tf;
+    __shared__ S s_ts;
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_APPLY);
         if (tile >= tiles) break;
         const u64 wbase = (u64)tile * kApplyTile + (u64)warp * 32 * AIPT;
         u64 e[AIPT];
-        u32 sv[AIPT];
+        S sv[AIPT];
         bool sf[AIPT];
         bool tail[AIPT];
 #pragma unroll
@@ -717,7 +776,8 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
             u64 i = wbase + (u64)k * 32 + lane;
             e[k] = i < n ? list[i] : ~0ull;
         }
-        u32 cf = 0, cs = 0;  // running carry within the warp
+        u32 cf = 0;
+        S cs = 0;  // running carry within the warp
 #pragma unroll
         for (int k = 0; k < AIPT; k++) {
             const u64 i = wbase + (u64)k * 32 + lane;
@@ -727,12 +787,13 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
             const u64 next = (v && i + 1 < n) ? list[i + 1] : ~0ull;
             const bool head = v && (i == 0 || (u32)(prev >> 32) != m);
             tail[k] = v && (i + 1 == n || (u32)(next >> 32) != m);
-            u32 val = 0;
-            if (v && ((e[k] >> 31) & 1ull)) val = (u32)opw_imm(__ldg(&b.opw[(u32)e[k] & 0x7FFFFFFFu]));
-            u32 f = head ? 1u : 0u, sum = val;
+            S val = 0;
+            if (v && ((e[k] >> 31) & 1ull)) val = (S)(long long)opw_imm(__ldg(&b.opw[(u32)e[k] & 0x7FFFFFFFu]));
+            u32 f = head ? 1u : 0u;
+            S sum = val;
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
-                u32 us = __shfl_up_sync(FULL_MASK, sum, d);
+                S us = __shfl_up_sync(FULL_MASK, sum, d);
                 u32 uf = __shfl_up_sync(FULL_MASK, f, d);
                 if (lane >= d) {
                     if (!f) sum += us;
@@ -753,9 +814,11 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
         __syncthreads();
         if (threadIdx.x == 0) {
             // exclusive prefix over warps, then tile look-back
-            u32 af = 0, as = 0;
+            u32 af = 0;
+            S as = 0;
             for (int w = 0; w < NW; w++) {
-                u32 f = s_wf[w], sm = s_ws[w];
+                u32 f = s_wf[w];
+                S sm = s_ws[w];
                 s_wf[w] = af;
                 s_ws[w] = as;
                 if (f) {
@@ -765,9 +828,10 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
                     as += sm;
                 }
             }
-            u64 agg = ((u64)af << 61) | as;
+            u64 agg = ((u64)af << 61) | ((u64)as & kSum61);
             u64 *st = s.st_apply;
-            u32 ef = 0, es = 0;
+            u32 ef = 0;
+            S es = 0;
             if (tile == 0) {
                 st_release(&st[0], kInc | agg);
             } else {
@@ -786,40 +850,61 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
                         continue;
                     }
                     if (!ef) {
-                        es += (u32)x;
+                        es += unpack_sum<S>(x);
                         ef = (u32)((x >> 61) & 1ull);
                     }
                     if (fl == 2 || ef) break;
                     t--;
                 }
                 u32 incf = af ? 1u : ef;
-                u32 incs = af ? as : es + as;
-                st_release(&st[tile], kInc | ((u64)incf << 61) | incs);
+                S incs = af ? as : es + as;
+                st_release(&st[tile], kInc | ((u64)incf << 61) | ((u64)incs & kSum61));
             }
             s_tf = ef;
             s_ts = es;
         }
         __syncthreads();
         // carry into this warp = combine(tile exclusive, warp exclusive)
-        const u32 wf = s_wf[warp], ws = s_ws[warp];
-        const u32 carry = wf ? ws : s_ts + ws;
+        const u32 wf = s_wf[warp];
+        const S ws = s_ws[warp];
+        const S carry = wf ? ws : s_ts + ws;
 #pragma unroll
         for (int k = 0; k < AIPT; k++) {
             const u64 i = wbase + (u64)k * 32 + lane;
             if (i < n) {
                 const u32 m = (u32)(e[k] >> 32);
-                const u32 tot = sf[k] ? sv[k] : sv[k] + carry;
-                const int32_t val = (int32_t)((u32)__ldg(&s.dbase[m]) + tot);
-                b.out[(u32)e[k] & 0x7FFFFFFFu] = val;
-                if (tail[k]) *cell_ptr(T, __ldg(&s.dcell[m])) = val;
+                const S tot = sf[k] ? sv[k] : sv[k] + carry;
+                const u32 op = (u32)e[k] & 0x7FFFFFFFu;
+                if (!WIDE) {
+                    const int32_t val = (int32_t)((u32)__ldg(&s.dbase[m]) + (u32)tot);
+                    b.out[op] = val;
+                    if (b.out64) b.out64[op] = val;
+                    if (tail[k]) {
+                        bool wd;
+                        char *p = cell_ptr(T, __ldg(&s.dcell[m]), &wd);
+                        *reinterpret_cast<int32_t *>(p) = val;
+                    }
+                } else {
+                    // bit 63 of dcell marks an int64 cell
+                    const u64 dc = __ldg(&s.dcell[m]);
+                    long long val = (long long)((u64)__ldg(&s.dbase[m]) + (u64)tot);
+                    if (!(dc >> 63)) val = (int32_t)val;
+                    store_out(b, op, val);
+                    if (tail[k]) {
+                        bool wd;
+                        char *p = cell_ptr(T, dc & ~(1ull << 63), &wd);
+                        store_cell(p, wd, val);
+                    }
+                }
             }
         }
         __syncthreads();
     }
 }
 
+template <typename S>
 __global__ void __launch_bounds__(kApplyBlock) k_apply(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
-    phase_apply<kApplyBlock>(b, T, s, ctr);
+    phase_apply<kApplyBlock, S>(b, T, s, ctr);
 }
 
 // ============================================================================
@@ -879,28 +964,19 @@ __device__ __forceinline__ void phase_r1_exec(const BatchDev &b, const TablesDev
         if (!r.valid) continue;
         const u32 tid = op_tid(b, i);
         if (!b.commit[tid]) {
-            b.out[i] = 0;
+            store_out(b, i, 0);
             continue;
         }
         u32 m;
         const bool add = opw_kind(w) == LTP_OP_ADD;
-        if (contended_id(s, r.cell, &m)) {
-            // a committed op on a contended cell sees the pre-batch value; a
-            // committed RMW here is the cell's only committed writer
-            int32_t v = s.dbase[m];
-            if (add) {
-                v = (int32_t)((u32)v + (u32)opw_imm(w));
-                *r.ptr = v;
-            }
-            b.out[i] = v;
-        } else {
-            int32_t v = *r.ptr;
-            if (add) {
-                v = (int32_t)((u32)v + (u32)opw_imm(w));
-                *r.ptr = v;
-            }
-            b.out[i] = v;
+        // a committed op on a contended cell sees the pre-batch value; a
+        // committed RMW there is the cell's only committed writer
+        long long v = contended_id(s, r.cell, &m) ? s.dbase[m] : load_cell(r.ptr, r.wide);
+        if (add) {
+            v = (long long)((u64)v + (u64)(long long)opw_imm(w));
+            store_cell(r.ptr, r.wide, v);
         }
+        store_out(b, i, v);
     }
 }
 
@@ -943,7 +1019,7 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
                 if (opw_kind(w) == LTP_OP_INSERT) {
                     t = opw_table(w);
                     ins = b.commit[op_tid(b, i)] != 0;
-                    if (!ins) b.out[i] = 0;
+                    if (!ins) store_out(b, i, 0);
                 }
             }
             tb[k] = ins ? t : LTP_MAX_TABLES;
@@ -1000,8 +1076,25 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
                 const TableDev &t = T.t[tb[k]];
                 const u64 row = s_base[tb[k]] + s_wcnt[warp][tb[k]] + lrank[k];
                 const int32_t *src = b.payload + b.keys[i];
-                for (u32 c = 0; c < t.n_cols; c++) t.data[(u64)c * t.rows_cap + row] = src[c];
-                b.out[i] = (int32_t)row;
+                const u32 w = b.opw[i];
+                const u32 d = insert_link(w), lc = d ? opw_col(w) : LTP_MAX_COLS;
+                long long lv = 0;
+                if (d) lv = b.out64 ? b.out64[i - d] : (long long)b.out[i - d];
+                if (!t.wide) {
+                    for (u32 c = 0; c < t.n_cols; c++)
+                        reinterpret_cast<int32_t *>(t.data)[(u64)c * t.rows_cap + row] = c == lc ? (int32_t)lv : src[c];
+                } else {
+                    u32 slot = 0;
+                    for (u32 c = 0; c < t.n_cols; c++) {
+                        const bool wc = col_wide(t, c);
+                        long long v = wc ? (long long)(((u64)(u32)src[slot + 1] << 32) | (u64)(u32)src[slot])
+                                         : (long long)src[slot];
+                        slot += wc ? 2 : 1;
+                        if (c == lc) v = lv;
+                        store_cell(t.data + col_off(t, c) + row * (wc ? 8ull : 4ull), wc, v);
+                    }
+                }
+                store_out(b, i, (long long)row);
             }
         }
         __syncthreads();
@@ -1065,12 +1158,15 @@ __global__ void k_stall(Counters *ctr, u32 ms) {
     }
 }
 
+// int64 columns hold the same seeded int32 value, sign-extended
 __global__ void k_fill_seeded(TableDev t, u64 seed) {
     const u64 base = mix64(seed ^ 0x5441424C45ull);
     const u64 total = t.n_rows * t.n_cols;
     for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < total; j += (u64)gridDim.x * blockDim.x) {
         const u64 col = j / t.n_rows, row = j - col * t.n_rows;
-        t.data[col * t.rows_cap + row] = (int32_t)(u32)mix64(base + row * t.n_cols + col);
+        const bool wc = col_wide(t, (u32)col);
+        store_cell(t.data + col_off(t, (u32)col) + row * (wc ? 8ull : 4ull), wc,
+                   (long long)(int32_t)(u32)mix64(base + row * t.n_cols + col));
     }
 }
 
@@ -1178,7 +1274,7 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
         static int gs = 0, ga = 0, sms = 0;
         if (sms != L.num_sms) {
             gs = occ_grid(k_sort_pass<0>, kSortBlock, L.num_sms);
-            ga = occ_grid(k_apply, kApplyBlock, L.num_sms);
+            ga = occ_grid(k_apply<u64>, kApplyBlock, L.num_sms);
             sms = L.num_sms;
         }
         const int gsort = capped(gs, (b.n_ops + kSortTile - 1) / kSortTile);
@@ -1191,7 +1287,9 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
         mark_ev(7);
         k_sort_pass<3><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops, L.tune.block * L.tune.ipt);
         mark_ev(8);
-        k_apply<<<capped(ga, (b.n_ops + kApplyTile - 1) / kApplyTile), kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
+        const int gapp = capped(ga, (b.n_ops + kApplyTile - 1) / kApplyTile);
+        if (T.any_wide) k_apply<u64><<<gapp, kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
+        else k_apply<u32><<<gapp, kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
         mark_ev(9);
     } else {
         k_r1_minw<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
@@ -1291,7 +1389,8 @@ __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
             grid_sync(a.bar, nb, a.ctr);
             phase_sort_pass<kPBlock>(3, a.s, a.ctr, b.n_ops, kPBlock * kPIpt);
             grid_sync(a.bar, nb, a.ctr);
-            phase_apply<kPBlock>(b, a.T, a.s, a.ctr);
+            if (a.T.any_wide) phase_apply<kPBlock, u64>(b, a.T, a.s, a.ctr);
+            else phase_apply<kPBlock, u32>(b, a.T, a.s, a.ctr);
         } else {
             phase_r1_minw(b, a.T, a.s, a.ctr);
             grid_sync(a.bar, nb, a.ctr);

@@ -43,7 +43,7 @@ constexpr u64 kOffList0 = kOffTw + align256(kNaMaxOps * 4);
 constexpr u64 kOffList1 = kOffList0 + align256(kNaMaxOps * 8);
 constexpr u64 kOffDcell = kOffList1 + align256(kNaMaxOps * 8);
 constexpr u64 kOffDbase = kOffDcell + align256(kNaMaxOps * 8);
-constexpr u64 kOffDminw = kOffDbase + align256(kNaMaxOps * 4);
+constexpr u64 kOffDminw = kOffDbase + align256(kNaMaxOps * 8);
 constexpr u64 kOffOpTxn = kOffDminw + align256(kNaMaxOps * 4);
 constexpr u64 kOffSort0 = kOffOpTxn + align256(kNaMaxOps * 4);
 constexpr u64 kOffSort1 = kOffSort0 + align256(kNaSortTiles * 256 * 4);
@@ -115,7 +115,7 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     s.list[0] = (u64 *)(base + kOffList0);
     s.list[1] = (u64 *)(base + kOffList1);
     s.dcell = (u64 *)(base + kOffDcell);
-    s.dbase = (int32_t *)(base + kOffDbase);
+    s.dbase = (long long *)(base + kOffDbase);
     s.dminw = (u32 *)(base + kOffDminw);
     s.st_sort[0] = (u32 *)(base + kOffSort0);
     s.st_sort[1] = (u32 *)(base + kOffSort1);
@@ -144,7 +144,7 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     memset(&T, 0, sizeof(T));
     T.n = 1;
     T.rows_now = rows_now;
-    T.t[0].data = table;
+    T.t[0].data = reinterpret_cast<char *>(table);
     T.t[0].rows_cap = rows_cap;
     T.t[0].row_limit = rows_cap;
     T.t[0].n_rows = n_rows;
@@ -156,6 +156,7 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     b.txn_first = txn_first;
     b.op_txn = op_txn;
     b.out = out;
+    b.out64 = nullptr;
     b.commit = commit;
     b.n_ops = n_ops;
     b.n_txns = n_txns;

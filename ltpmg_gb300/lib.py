@@ -37,7 +37,7 @@ class Config(ctypes.Structure):
 
 
 class Schema(ctypes.Structure):
-    _fields_ = [("n_cols", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+    _fields_ = [("n_cols", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("wide_cols", ctypes.c_uint64)]
 
 
 class Stats(ctypes.Structure):
@@ -120,12 +120,19 @@ def load():
         "ltp_batch_load": (ci, [vp, vp, u64, vp, u32, u64, vp, vp, vp]),
         "ltp_batch_execute": (ci, [vp, vp, vp]),
         "ltp_batch_fetch": (ci, [vp, vp, vp, vp, vp]),
+        "ltp_batch_fetch64": (ci, [vp, vp, vp, vp]),
         "ltp_batch_finish": (ci, [vp, vp, ctypes.POINTER(Stats), vp]),
         "ltp_batch_results": (ci, [vp, vp, vp, vp, ctypes.POINTER(Stats)]),
         "ltp_batch_device_ptrs": (ci, [vp, pp, pp, pp, pp, pp]),
         "ltp_host_alloc": (vp, [ctypes.c_size_t]),
         "ltp_host_free": (None, [vp]),
         "ltp_gen_ycsb": (u64, [ctypes.POINTER(YcsbParams), u64, u64, vp, vp, vp, u64, ci]),
+        "ltp_tpcc_create": (ci, [ctypes.POINTER(TpccParams), pp]),
+        "ltp_tpcc_free": (None, [vp]),
+        "ltp_tpcc_table": (ci, [vp, u32, ctypes.POINTER(Schema), ctypes.POINTER(u64)]),
+        "ltp_tpcc_column": (ci, [vp, u32, u32, u64, u64, vp]),
+        "ltp_tpcc_gen": (ci, [vp, u64, u64, vp, vp, vp, u64, vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64),
+                              ctypes.POINTER(u64), vp, ci]),
         "ltp_table_value": (i32, [u64, u64, u32, u32]),
         "ltp_set_tuning": (ci, [vp, u32, ctypes.POINTER(Tuning)]),
         "ltp_get_tuning": (ci, [vp, u32, ctypes.POINTER(Tuning)]),
@@ -219,6 +226,104 @@ def gen_ycsb(seed, n_rows, n_cols, ops_min, ops_max, read_frac, theta, batch, n_
     return tf[: n_txns + 1], keys[:n], opw[:n]
 
 
+class TpccParams(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_uint64), ("warehouses", ctypes.c_uint32), ("districts", ctypes.c_uint32),
+                ("customers", ctypes.c_uint32), ("items", ctypes.c_uint32), ("ol_min", ctypes.c_uint32),
+                ("ol_max", ctypes.c_uint32), ("new_order_frac", ctypes.c_double), ("remote_line", ctypes.c_double),
+                ("remote_payment", ctypes.c_double), ("by_last_name", ctypes.c_double)]
+
+
+TPCC_TABLES = ("warehouse", "district", "customer", "history", "new_order", "order", "order_line", "item", "stock")
+TPCC_WAREHOUSE, TPCC_DISTRICT, TPCC_CUSTOMER, TPCC_HISTORY, TPCC_NEW_ORDER, TPCC_ORDER, TPCC_ORDER_LINE, \
+    TPCC_ITEM, TPCC_STOCK = range(9)
+
+
+class Tpcc:
+    """The library's TPC-C-shaped order-entry workload (ltp_tpcc_*): schema,
+    initial table contents and seeded new-order / payment batches."""
+
+    def __init__(self, warehouses, seed=1, districts=10, customers=3000, items=100000, ol_min=5, ol_max=15,
+                 new_order_frac=0.5, remote_line=0.01, remote_payment=0.15, by_last_name=0.6):
+        self.L = load()
+        self.params = TpccParams(seed, warehouses, districts, customers, items, ol_min, ol_max, new_order_frac,
+                                 remote_line, remote_payment, by_last_name)
+        h = ctypes.c_void_p()
+        rc = self.L.ltp_tpcc_create(ctypes.byref(self.params), ctypes.byref(h))
+        if rc:
+            raise LtpError(rc, "ltp_tpcc_create rejected the parameters")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.L.ltp_tpcc_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def table(self, t):
+        """(n_cols, wide_mask, initial rows) of table t."""
+        sc, rows = Schema(), ctypes.c_uint64()
+        rc = self.L.ltp_tpcc_table(self.h, t, ctypes.byref(sc), ctypes.byref(rows))
+        if rc:
+            raise LtpError(rc, "ltp_tpcc_table")
+        return sc.n_cols, sc.wide_cols, rows.value
+
+    def column(self, t, c, row0=0, n=None):
+        n_cols, mask, rows = self.table(t)
+        n = rows - row0 if n is None else n
+        out = np.empty(n, np.int64 if (mask >> c) & 1 else np.int32)
+        rc = self.L.ltp_tpcc_column(self.h, t, c, row0, n, _p(out))
+        if rc:
+            raise LtpError(rc, "ltp_tpcc_column")
+        return out
+
+    def initial(self, t, rows_cap=None):
+        """Column-major initial contents [n_cols, rows_cap] (int64 when the
+        table has an int64 column), zero beyond the initial rows."""
+        n_cols, mask, rows = self.table(t)
+        cap = rows if rows_cap is None else rows_cap
+        out = np.zeros((n_cols, cap), np.int64 if mask else np.int32)
+        for c in range(n_cols):
+            out[c, :rows] = self.column(t, c)
+        return out
+
+    def gen(self, batch, n_txns, threads=0):
+        """(txn_first, keys, opw, payload, n_new_order, inserts[9]) of one batch."""
+        n_ops, n_pay, n_no = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        ins = np.zeros(9, np.uint64)
+        tf = np.zeros(n_txns + 1, np.uint32)
+        rc = self.L.ltp_tpcc_gen(self.h, batch, n_txns, _p(tf), None, None, 0, None, 0, ctypes.byref(n_ops),
+                                 ctypes.byref(n_pay), ctypes.byref(n_no), _p(ins), threads)
+        if rc:
+            raise LtpError(rc, "ltp_tpcc_gen (sizes)")
+        keys = np.zeros(max(n_ops.value, 1), np.uint64)
+        opw = np.zeros(max(n_ops.value, 1), np.uint32)
+        pay = np.zeros(max(n_pay.value, 1), np.int32)
+        rc = self.L.ltp_tpcc_gen(self.h, batch, n_txns, _p(tf), _p(keys), _p(opw), len(keys), _p(pay), len(pay),
+                                 ctypes.byref(n_ops), ctypes.byref(n_pay), ctypes.byref(n_no), _p(ins), threads)
+        if rc:
+            raise LtpError(rc, "ltp_tpcc_gen")
+        return tf, keys[:n_ops.value], opw[:n_ops.value], pay[:n_pay.value], n_no.value, ins
+
+    def create_tables(self, ctx, extra_rows):
+        """Creates the nine tables in ctx, each with room for extra_rows[t]
+        inserted rows, and uploads the initial contents.  Returns the ids."""
+        ids = []
+        for t in range(9):
+            n_cols, mask, rows = self.table(t)
+            wide = [c for c in range(n_cols) if (mask >> c) & 1]
+            tid = ctx.create_table(rows, n_cols, rows_cap=max(1, rows + int(extra_rows[t])), wide=wide)
+            for c in range(n_cols):
+                if rows:
+                    ctx.upload_column(tid, c, self.column(t, c))
+            ids.append(tid)
+        return ids
+
+
 def opword(kind, col, table=0, imm=0):
     return (kind | (col << 2) | (table << 8) | ((imm & 0xFFFFF) << 12)) & 0xFFFFFFFF
 
@@ -263,11 +368,16 @@ class Context:
     def sync(self, stream=None):
         self.check(self.L.ltp_sync(self.h, _stream(stream)))
 
-    def create_table(self, rows, cols, rows_cap=None):
+    def create_table(self, rows, cols, rows_cap=None, wide=()):
+        """wide: indices of the int64 columns (the others are int32)."""
         tid = ctypes.c_uint32()
         cap = rows if rows_cap is None else rows_cap
-        self.check(self.L.ltp_table_create_cap(self.h, ctypes.byref(Schema(cols, 0)), rows, cap, ctypes.byref(tid)))
-        self.tables.append((rows, cols))
+        mask = 0
+        for c in wide:
+            mask |= 1 << int(c)
+        self.check(self.L.ltp_table_create_cap(self.h, ctypes.byref(Schema(cols, 0, mask)), rows, cap,
+                                               ctypes.byref(tid)))
+        self.tables.append((rows, cols, mask))
         return tid.value
 
     def table_rows(self, table):
@@ -275,18 +385,32 @@ class Context:
         self.check(self.L.ltp_table_rows(self.h, table, ctypes.byref(v)))
         return v.value
 
-    def upload(self, table, colmajor):
-        """colmajor: int32[n_cols, n_rows]."""
-        a = np.ascontiguousarray(colmajor, np.int32)
-        for c in range(a.shape[0]):
-            self.check(self.L.ltp_table_upload(self.h, table, c, 0, a.shape[1], _p(a[c])))
+    def upload(self, table, colmajor, row0=0):
+        """colmajor: [n_cols, n] values; each column is stored at its own
+        width (int32 columns take the low 32 bits)."""
+        mask = self.tables[table][2]
+        for c in range(len(colmajor)):
+            a = np.ascontiguousarray(np.asarray(colmajor[c]).astype(np.int64 if (mask >> c) & 1 else np.int32))
+            self.check(self.L.ltp_table_upload(self.h, table, c, row0, a.shape[0], _p(a)))
+
+    def upload_column(self, table, col, values, row0=0):
+        mask = self.tables[table][2]
+        a = np.ascontiguousarray(np.asarray(values).astype(np.int64 if (mask >> col) & 1 else np.int32))
+        self.check(self.L.ltp_table_upload(self.h, table, col, row0, a.shape[0], _p(a)))
 
     def download(self, table):
-        _, cols = self.tables[table]
+        """int32[n_cols, rows], or int64[n_cols, rows] when the table has an
+        int64 column (int32 columns sign-extended)."""
+        _, cols, mask = self.tables[table]
         rows = self.table_rows(table)
-        out = np.empty((cols, rows), np.int32)
+        out = np.empty((cols, rows), np.int64 if mask else np.int32)
+        tmp = np.empty(rows, np.int32)
         for c in range(cols):
-            self.check(self.L.ltp_table_download(self.h, table, c, 0, rows, _p(out[c])))
+            if mask and not (mask >> c) & 1:
+                self.check(self.L.ltp_table_download(self.h, table, c, 0, rows, _p(tmp)))
+                out[c] = tmp
+            else:
+                self.check(self.L.ltp_table_download(self.h, table, c, 0, rows, _p(out[c])))
         return out
 
     def fill_seeded(self, table, seed, stream=None):
@@ -367,6 +491,9 @@ class Batch:
     def fetch(self, commit=None, vals=None, stream=None):
         self.ctx.check(self.ctx.L.ltp_batch_fetch(self.ctx.h, self.h, _p(commit), _p(vals), _stream(stream)))
 
+    def fetch64(self, vals, stream=None):
+        self.ctx.check(self.ctx.L.ltp_batch_fetch64(self.ctx.h, self.h, _p(vals), _stream(stream)))
+
     def finish(self, stream=None):
         st = Stats()
         self.ctx.check(self.ctx.L.ltp_batch_finish(self.ctx.h, self.h, ctypes.byref(st), _stream(stream)))
@@ -377,6 +504,15 @@ class Batch:
         vals = np.zeros(max(self.n_ops, 1), np.int32)
         st = Stats()
         self.ctx.check(self.ctx.L.ltp_batch_results(self.ctx.h, self.h, _p(commit), _p(vals), ctypes.byref(st)))
+        return commit[: self.n_txns], vals[: self.n_ops], st
+
+    def results64(self):
+        """(commit, int64 values, stats); the context must have an int64 column."""
+        commit = np.zeros(max(self.n_txns, 1), np.uint8)
+        vals = np.zeros(max(self.n_ops, 1), np.int64)
+        self.fetch(commit=commit)
+        self.fetch64(vals)
+        st = self.finish()
         return commit[: self.n_txns], vals[: self.n_ops], st
 
 

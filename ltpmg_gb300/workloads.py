@@ -11,6 +11,10 @@ zipf    2^24 rows x 10 int32, batches of 2^20 transactions x 16 ops, Zipf 0.99
 uneven  2^24 rows x 10 int32, 64 batches of 2^U[10,20] transactions (log-
         uniform), 1-32 ops per transaction, Zipf theta ~ U[0.5, 0.99] per
         batch, 70% / 30%
+tpcc    TPC-C-shaped order entry, 64 warehouses (10 districts, 30,000
+        customers, 100,000 stock rows each; 100,000 items), batches of 2^18
+        transactions, 50% new-order (5-15 lines) / 50% payment (the library's
+        ltp_tpcc generator), 4 batches per step
 """
 import math
 
@@ -22,6 +26,7 @@ SHAPES = {
     "plain": dict(rows=1 << 20, cols=10, batches=16, seed=SEED),
     "zipf": dict(rows=1 << 24, cols=10, batches=32, seed=SEED + 2),
     "uneven": dict(rows=1 << 24, cols=10, batches=64, seed=SEED + 4),
+    "tpcc": dict(warehouses=64, batch=1 << 18, batches=4, seed=SEED + 6),
 }
 
 
@@ -60,6 +65,29 @@ def algorithmic_bytes(n_ops, n_txns):
     """28 B per op (key 8, opword 4, value read 4, value written 4, conflict
     state 8) + 4 B per transaction (commit word / descriptor)."""
     return 28 * n_ops + 4 * n_txns
+
+
+def tpcc_algorithmic_bytes(g, keys, opw, n_txns):
+    """Bytes a batch of the TPC-C workload must move at least: per op its key
+    (8), opword (4), output (4) and conflict state (8); a read or RMW reads
+    its cell (4 or 8 B, the column's width) and an RMW writes it back; an
+    insert reads its payload row and writes the new row; 4 B per transaction.
+    """
+    import numpy as np
+
+    kind = opw & 3
+    tb = (opw >> 8) & 15
+    col = (opw >> 2) & 63
+    width = np.zeros((16, 64), np.int64)
+    rowb = np.zeros(16, np.int64)
+    for t in range(9):
+        n_cols, mask, _ = g.table(t)
+        for c in range(n_cols):
+            width[t, c] = 8 if (mask >> c) & 1 else 4
+        rowb[t] = width[t, :n_cols].sum()
+    w = width[tb, col]
+    cell = np.where(kind == 0, w, np.where(kind == 1, 2 * w, 2 * rowb[tb]))
+    return int(24 * len(keys) + cell.sum() + 4 * n_txns)
 
 
 def expected_txns(name):

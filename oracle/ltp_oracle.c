@@ -370,24 +370,53 @@ int ltpo_replay_r0_mt(uint64_t n_rows, uint32_t n_cols, int32_t *tab, uint64_t n
  * ltpo_replay; inserts never conflict (a new row cannot be named by another
  * op of the same batch) and take the next slot of their table in serial
  * order, which is "table count + rank among earlier committed inserts". */
-static int check_op_t(uint32_t n_tables, const ltpo_table *T, uint64_t key, uint32_t w, uint64_t payload_len) {
-    uint32_t tb = LTPO_TABLE(w), kind = LTPO_KIND(w);
+static uint32_t popc64(uint64_t x) {
+    uint32_t n = 0;
+    while (x) {
+        x &= x - 1;
+        n++;
+    }
+    return n;
+}
+
+static int col_is_wide(const ltpo_table *t, uint32_t c) { return (int)((t->wide >> c) & 1u); }
+
+static int64_t cell_get(const ltpo_table *t, uint32_t c, uint64_t row) {
+    return col_is_wide(t, c) ? ((int64_t *)t->cols[c])[row] : (int64_t)((int32_t *)t->cols[c])[row];
+}
+
+static void cell_set(ltpo_table *t, uint32_t c, uint64_t row, int64_t v) {
+    if (col_is_wide(t, c)) ((int64_t *)t->cols[c])[row] = v;
+    else ((int32_t *)t->cols[c])[row] = (int32_t)(uint32_t)(uint64_t)v;
+}
+
+/* Checks op i of transaction t (ops [first, end)). */
+static int check_op_t(uint32_t n_tables, const ltpo_table *T, uint64_t i, uint64_t first, const uint64_t *keys,
+                      const uint32_t *opw, uint64_t payload_len) {
+    const uint32_t w = opw[i], tb = LTPO_TABLE(w), kind = LTPO_KIND(w);
     if (tb >= n_tables) return -1;
-    if (kind == 2) return key + T[tb].n_cols <= payload_len ? 0 : -1;
+    if (kind == 2) {
+        const uint64_t slots = T[tb].n_cols + popc64(T[tb].wide);
+        const uint32_t d = (uint32_t)LTPO_IMM(w) & 0x3FFu;
+        if (keys[i] + slots > payload_len) return -1;
+        if (d && (LTPO_COL(w) >= T[tb].n_cols || d > i - first || LTPO_KIND(opw[i - d]) > 1)) return -1;
+        return 0;
+    }
     if (kind > 2) return -1;
-    if (key >= T[tb].n_rows || LTPO_COL(w) >= T[tb].n_cols) return -1;
+    if (keys[i] >= T[tb].n_rows || LTPO_COL(w) >= T[tb].n_cols) return -1;
     return 0;
 }
 
 int ltpo_replay_tables(int rule, uint32_t n_tables, ltpo_table *T, uint64_t n_txns, const uint32_t *txn_first,
                        const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
-                       uint8_t *commit, int32_t *out) {
+                       uint8_t *commit, int64_t *out) {
     const uint64_t n_ops = txn_first[n_txns];
     uint64_t ins[16] = {0};
-    for (uint64_t i = 0; i < n_ops; i++) {
-        if (check_op_t(n_tables, T, keys[i], opw[i], payload_len)) return -1;
-        if (LTPO_KIND(opw[i]) == 2) ins[LTPO_TABLE(opw[i])]++;
-    }
+    for (uint64_t t = 0; t < n_txns; t++)
+        for (uint64_t i = txn_first[t]; i < txn_first[t + 1]; i++) {
+            if (check_op_t(n_tables, T, i, txn_first[t], keys, opw, payload_len)) return -1;
+            if (LTPO_KIND(opw[i]) == 2) ins[LTPO_TABLE(opw[i])]++;
+        }
     for (uint32_t k = 0; k < n_tables && k < 16; k++)
         if (T[k].n_rows + ins[k] > T[k].rows_cap) return -2;
     if (rule != 0 && rule != 1) return -1;
@@ -425,18 +454,144 @@ int ltpo_replay_tables(int rule, uint32_t n_tables, ltpo_table *T, uint64_t n_tx
             }
             if (LTPO_KIND(w) == 2) {
                 const uint64_t slot = tab->n_rows++;
-                for (uint32_t c = 0; c < tab->n_cols; c++) tab->data[(uint64_t)c * tab->rows_cap + slot] = payload[keys[i] + c];
-                out[i] = (int32_t)slot;
+                const uint32_t d = (uint32_t)LTPO_IMM(w) & 0x3FFu;
+                uint64_t p = keys[i];
+                for (uint32_t c = 0; c < tab->n_cols; c++) {
+                    int64_t v;
+                    if (col_is_wide(tab, c)) {
+                        v = (int64_t)(((uint64_t)(uint32_t)payload[p + 1] << 32) | (uint64_t)(uint32_t)payload[p]);
+                        p += 2;
+                    } else {
+                        v = payload[p];
+                        p += 1;
+                    }
+                    if (d && c == LTPO_COL(w)) v = out[i - d];
+                    cell_set(tab, c, slot, v);
+                }
+                out[i] = (int64_t)slot;
                 continue;
             }
-            int32_t *cell = &tab->data[(uint64_t)LTPO_COL(w) * tab->rows_cap + keys[i]];
-            int32_t v = *cell;
+            const uint32_t c = LTPO_COL(w);
+            int64_t v = cell_get(tab, c, keys[i]);
             if (LTPO_KIND(w) == 1) {
-                v = (int32_t)((uint32_t)v + (uint32_t)LTPO_IMM(w));
-                *cell = v;
+                v = (int64_t)((uint64_t)v + (uint64_t)(int64_t)LTPO_IMM(w));
+                cell_set(tab, c, keys[i], v);
+                v = cell_get(tab, c, keys[i]); /* wrapped at the column's width */
             }
             out[i] = v;
         }
+    return 0;
+}
+
+/* Ordered-rule (R0) replay of ltpo_replay_tables on n_threads threads:
+ * phase 1 splits reads and RMWs by cell (each thread walks the whole batch
+ * in order and executes the ops of the cells it owns), phase 2 splits
+ * inserts by table (they only need phase 1's outputs for their links).
+ * Results equal ltpo_replay_tables(0, ...); the multi-core CPU baseline. */
+typedef struct {
+    uint32_t n_tables;
+    ltpo_table *T;
+    uint64_t n_txns;
+    const uint32_t *txn_first;
+    const uint64_t *keys;
+    const uint32_t *opw;
+    const int32_t *payload;
+    uint64_t payload_len;
+    int64_t *out;
+    int k, n;
+    int err;
+} mtt_arg_t;
+
+static uint32_t owner_of(uint32_t tb, uint64_t cell, int n) {
+    return (uint32_t)((((cell + 1) * 0x9E3779B97F4A7C15ULL) ^ ((uint64_t)tb << 59)) >> 40) % (uint32_t)n;
+}
+
+static void *mtt_cells(void *p) {
+    mtt_arg_t *a = (mtt_arg_t *)p;
+    const uint64_t n_ops = a->txn_first[a->n_txns];
+    for (uint64_t i = 0; i < n_ops; i++) {
+        const uint32_t w = a->opw[i], tb = LTPO_TABLE(w);
+        if (LTPO_KIND(w) == 2) continue;
+        if (tb >= a->n_tables || LTPO_KIND(w) > 2) {
+            a->err = 1;
+            continue;
+        }
+        ltpo_table *tab = &a->T[tb];
+        const uint32_t c = LTPO_COL(w);
+        const uint64_t r = a->keys[i];
+        if (owner_of(tb, r * tab->n_cols + c, a->n) != (uint32_t)a->k) continue;
+        if (r >= tab->n_rows || c >= tab->n_cols) {
+            a->err = 1;
+            continue;
+        }
+        int64_t v = cell_get(tab, c, r);
+        if (LTPO_KIND(w) == 1) {
+            v = (int64_t)((uint64_t)v + (uint64_t)(int64_t)LTPO_IMM(w));
+            cell_set(tab, c, r, v);
+            v = cell_get(tab, c, r);
+        }
+        a->out[i] = v;
+    }
+    return NULL;
+}
+
+static void *mtt_inserts(void *p) {
+    mtt_arg_t *a = (mtt_arg_t *)p;
+    for (uint64_t t = 0; t < a->n_txns; t++)
+        for (uint64_t i = a->txn_first[t]; i < a->txn_first[t + 1]; i++) {
+            const uint32_t w = a->opw[i], tb = LTPO_TABLE(w);
+            if (LTPO_KIND(w) != 2 || tb % (uint32_t)a->n != (uint32_t)a->k) continue;
+            if (check_op_t(a->n_tables, a->T, i, a->txn_first[t], a->keys, a->opw, a->payload_len)) {
+                a->err = 1;
+                continue;
+            }
+            ltpo_table *tab = &a->T[tb];
+            if (tab->n_rows >= tab->rows_cap) {
+                a->err = 2;
+                continue;
+            }
+            const uint64_t slot = tab->n_rows++;
+            const uint32_t d = (uint32_t)LTPO_IMM(w) & 0x3FFu;
+            uint64_t q = a->keys[i];
+            for (uint32_t c = 0; c < tab->n_cols; c++) {
+                int64_t v;
+                if (col_is_wide(tab, c)) {
+                    v = (int64_t)(((uint64_t)(uint32_t)a->payload[q + 1] << 32) | (uint64_t)(uint32_t)a->payload[q]);
+                    q += 2;
+                } else {
+                    v = a->payload[q];
+                    q += 1;
+                }
+                if (d && c == LTPO_COL(w)) v = a->out[i - d];
+                cell_set(tab, c, slot, v);
+            }
+            a->out[i] = (int64_t)slot;
+        }
+    return NULL;
+}
+
+int ltpo_replay_tables_r0_mt(uint32_t n_tables, ltpo_table *T, uint64_t n_txns, const uint32_t *txn_first,
+                             const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
+                             uint8_t *commit, int64_t *out, int n_threads) {
+    if (n_threads < 1) n_threads = 1;
+    if (n_threads > 256) n_threads = 256;
+    pthread_t th[256];
+    mtt_arg_t args[256];
+    int err = 0;
+    for (int phase = 0; phase < 2; phase++) {
+        const int nt = phase == 0 ? n_threads : (n_threads < (int)n_tables ? n_threads : (int)(n_tables ? n_tables : 1));
+        for (int k = 0; k < nt; k++) {
+            mtt_arg_t a = {n_tables, T, n_txns, txn_first, keys, opw, payload, payload_len, out, k, nt, 0};
+            args[k] = a;
+            if (pthread_create(&th[k], NULL, phase == 0 ? mtt_cells : mtt_inserts, &args[k])) return -1;
+        }
+        for (int k = 0; k < nt; k++) {
+            pthread_join(th[k], NULL);
+            if (args[k].err) err = args[k].err;
+        }
+        if (err) return err == 2 ? -2 : -1;
+    }
+    memset(commit, 1, n_txns);
     return 0;
 }
 

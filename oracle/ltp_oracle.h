@@ -85,24 +85,36 @@ int ltpo_replay_r0_mt(uint64_t n_rows, uint32_t n_cols, int32_t *tab, uint64_t n
                       const uint32_t *txn_first, const uint64_t *keys, const uint32_t *opw,
                       uint8_t *commit, int32_t *out, int n_threads);
 
-/* Multi-table replay with inserts.  Tables are column-major with stride
- * rows_cap: data[col * rows_cap + row]; keys of reads/RMWs must be < n_rows
- * as of the batch start.  An insert op (kind 2) appends a row to its table:
- * slot = the table's next row (committed inserts only, in (TID, op) order),
- * its n_cols values are payload[key .. key + n_cols), and out = slot.  Each
- * table's n_rows is advanced by its committed inserts.
+/* Multi-table replay with inserts, int32 and int64 columns.  Column c of a
+ * table is the array cols[c] of rows_cap values, int64 where bit c of `wide`
+ * is set, else int32; cell arithmetic wraps at the column's width.  Keys of
+ * reads/RMWs must be < n_rows as of the batch start.  An insert op (kind 2)
+ * appends a row to its table: slot = the table's next row (committed
+ * inserts only, in (TID, op) order); its values come from payload[key ..]:
+ * one int32 slot per int32 column, two (low word first) per int64 column;
+ * out = slot.  A linked insert (low 10 bits of the immediate = d > 0) sets
+ * column `col` of the new row to out[i - d], which must be a read or RMW of
+ * the same transaction.  Each table's n_rows is advanced by its committed
+ * inserts.  out holds each op's full value.
  * Returns 0, -1 on a malformed batch, -2 when an insert exceeds rows_cap. */
 typedef struct {
-    int32_t *data;
+    void **cols;
     uint64_t rows_cap;
     uint64_t n_rows;
     uint32_t n_cols;
     uint32_t pad;
+    uint64_t wide;
 } ltpo_table;
 
 int ltpo_replay_tables(int rule, uint32_t n_tables, ltpo_table *tables, uint64_t n_txns, const uint32_t *txn_first,
                        const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
-                       uint8_t *commit, int32_t *out);
+                       uint8_t *commit, int64_t *out);
+
+/* The ordered rule of ltpo_replay_tables on n_threads threads (reads and
+ * RMWs split by cell, inserts by table); same results as rule 0 there. */
+int ltpo_replay_tables_r0_mt(uint32_t n_tables, ltpo_table *tables, uint64_t n_txns, const uint32_t *txn_first,
+                             const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
+                             uint8_t *commit, int64_t *out, int n_threads);
 
 /* 64-bit FNV-1a over a byte range (table / result fingerprints). */
 uint64_t ltpo_fnv1a(const void *data, uint64_t bytes);

@@ -42,8 +42,9 @@ class YcsbParams(ctypes.Structure):
 
 
 class OTable(ctypes.Structure):
-    _fields_ = [("data", ctypes.c_void_p), ("rows_cap", ctypes.c_uint64), ("n_rows", ctypes.c_uint64),
-                ("n_cols", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+    _fields_ = [("cols", ctypes.POINTER(ctypes.c_void_p)), ("rows_cap", ctypes.c_uint64),
+                ("n_rows", ctypes.c_uint64), ("n_cols", ctypes.c_uint32), ("pad", ctypes.c_uint32),
+                ("wide", ctypes.c_uint64)]
 
 
 _lib = None
@@ -80,6 +81,9 @@ def lib():
         L.ltpo_replay_r0_mt.argtypes = [u64, u32, vp, u64, vp, vp, vp, vp, vp, ctypes.c_int]
         L.ltpo_replay_tables.restype = ctypes.c_int
         L.ltpo_replay_tables.argtypes = [ctypes.c_int, u32, ctypes.POINTER(OTable), u64, vp, vp, vp, vp, u64, vp, vp]
+        L.ltpo_replay_tables_r0_mt.restype = ctypes.c_int
+        L.ltpo_replay_tables_r0_mt.argtypes = [u32, ctypes.POINTER(OTable), u64, vp, vp, vp, vp, u64, vp, vp,
+                                               ctypes.c_int]
         L.ltpo_fnv1a.restype = u64
         L.ltpo_fnv1a.argtypes = [vp, u64]
         L.ltpo_ref_zipf_table.restype = u32
@@ -144,25 +148,66 @@ def replay(rule, tab, txn_first, keys, opw, threads=0):
     return tab, commit[:n_txns], out[:len(keys)]
 
 
-def replay_tables(rule, tables, txn_first, keys, opw, payload=None):
-    """Multi-table replay with inserts.  tables: list of (data int32[n_cols,
-    rows_cap], n_rows); returns (list of (data, n_rows) after, commit, out)."""
-    datas = [np.ascontiguousarray(d, np.int32).copy() for d, _ in tables]
-    T = (OTable * max(len(tables), 1))()
-    for k, ((_, n), d) in enumerate(zip(tables, datas)):
-        T[k] = OTable(d.ctypes.data, d.shape[1], n, d.shape[0], 0)
-    n_txns = len(txn_first) - 1
-    commit = np.zeros(max(n_txns, 1), np.uint8)
-    out = np.zeros(max(len(keys), 1), np.int32)
-    tf = np.ascontiguousarray(txn_first, np.uint32)
-    k = np.ascontiguousarray(keys, np.uint64)
-    w = np.ascontiguousarray(opw, np.uint32)
-    pl = np.ascontiguousarray(payload if payload is not None else np.zeros(1, np.int32), np.int32)
-    rc = lib().ltpo_replay_tables(rule, len(tables), T, n_txns, _p(tf), _p(k), _p(w), _p(pl),
-                                  0 if payload is None else len(pl), _p(commit), _p(out))
-    if rc != 0:
-        raise ValueError(f"oracle rejected the batch ({rc})")
-    return [(d, T[i].n_rows) for i, d in enumerate(datas)], commit[:n_txns], out[:len(keys)]
+class TablesDB:
+    """Tables held as per-column arrays for repeated multi-table replays
+    (int32 columns, int64 where the table's wide mask says so).  tables:
+    list of (data [n_cols, rows_cap], n_rows) or (data, n_rows, wide_mask)."""
+
+    def __init__(self, tables):
+        self.masks, self.cols, self._ptrs = [], [], []
+        self.T = (OTable * max(len(tables), 1))()
+        for k, tb in enumerate(tables):
+            d, n = np.asarray(tb[0]), tb[1]
+            mask = tb[2] if len(tb) > 2 else 0
+            cols = [np.ascontiguousarray(d[c], np.int64 if (mask >> c) & 1 else np.int32).copy()
+                    for c in range(d.shape[0])]
+            ptrs = (ctypes.c_void_p * len(cols))(*[c.ctypes.data for c in cols])
+            self.masks.append(mask)
+            self.cols.append(cols)
+            self._ptrs.append(ptrs)
+            self.T[k] = OTable(ptrs, d.shape[1], n, d.shape[0], 0, mask)
+        self.n = len(tables)
+
+    def replay(self, rule, txn_first, keys, opw, payload=None, threads=0):
+        """(commit, out int64) of one batch; threads > 0 runs the ordered
+        rule on that many threads."""
+        n_txns = len(txn_first) - 1
+        commit = np.zeros(max(n_txns, 1), np.uint8)
+        out = np.zeros(max(len(keys), 1), np.int64)
+        tf = np.ascontiguousarray(txn_first, np.uint32)
+        k = np.ascontiguousarray(keys, np.uint64)
+        w = np.ascontiguousarray(opw, np.uint32)
+        pl = np.ascontiguousarray(payload if payload is not None else np.zeros(1, np.int32), np.int32)
+        pn = 0 if payload is None else len(pl)
+        if threads > 0:
+            assert rule == 0
+            rc = lib().ltpo_replay_tables_r0_mt(self.n, self.T, n_txns, _p(tf), _p(k), _p(w), _p(pl), pn,
+                                                _p(commit), _p(out), threads)
+        else:
+            rc = lib().ltpo_replay_tables(rule, self.n, self.T, n_txns, _p(tf), _p(k), _p(w), _p(pl), pn,
+                                          _p(commit), _p(out))
+        if rc != 0:
+            raise ValueError(f"oracle rejected the batch ({rc})")
+        return commit[:n_txns], out[:len(keys)]
+
+    def tables(self):
+        """[(data [n_cols, rows_cap], n_rows)], int64 for tables with int64 columns."""
+        res = []
+        for i, cols in enumerate(self.cols):
+            dt = np.int64 if self.masks[i] else np.int32
+            res.append((np.stack([c.astype(dt) for c in cols]), self.T[i].n_rows))
+        return res
+
+
+def replay_tables(rule, tables, txn_first, keys, opw, payload=None, threads=0):
+    """Multi-table replay with inserts.  tables: list of (data [n_cols,
+    rows_cap], n_rows) or (data, n_rows, wide_mask); data is int32, or int64
+    when wide_mask names int64 columns (int32 columns sign-extended).
+    Returns (list of (data, n_rows, wide_mask) after, commit, out int64)."""
+    db = TablesDB(tables)
+    commit, out = db.replay(rule, txn_first, keys, opw, payload, threads)
+    after = [(d, n, m) for (d, n), m in zip(db.tables(), db.masks)]
+    return after, commit, out
 
 
 def fnv1a(a):
