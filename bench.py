@@ -53,6 +53,7 @@ KERNEL_BYTES = {
     "sort_pass2": lambda st: 16 * st["contended_ops"],
     "sort_pass3": lambda st: 16 * st["contended_ops"],
     "apply": lambda st: 16 * st["contended_ops"] + 12 * st["contended_cells"],
+    "insert": lambda st: st.get("insert_bytes", 0),
     "finish": lambda st: 12 * st["touched_words"],
 }
 KERNELS_PER_BATCH = 10  # mark, ids, classify, 4 radix passes, apply, insert, finish
@@ -573,10 +574,10 @@ def run_tpcc(args):
                          "achieved": alg / (step_ms / 1e3) / 1e9, "frac": alg / (step_ms / 1e3) / 1e9 / peak}}
     mean_stats = {k: sum(s[k] for s in stats) / len(stats) for k in ("ops", "touched_words", "contended_cells",
                                                                      "contended_ops")}
+    mean_stats["insert_bytes"] = sum(W.tpcc_insert_bytes(g, h[1], h[2]) for h in host) / len(host)
     if mode != G.MODE_PERSISTENT:
-        names = list(KERNEL_BYTES) + ["insert"]
-        avg = {nm: sum(s["ms_stage"][nm] for s in stats) / len(stats) for nm in names if nm in stats[0]["ms_stage"]}
-        dom = max((k for k in avg if k in KERNEL_BYTES), key=avg.get)
+        avg = {nm: sum(s["ms_stage"][nm] for s in stats) / len(stats) for nm in KERNEL_BYTES}
+        dom = max(avg, key=avg.get)
         dom_bytes = KERNEL_BYTES[dom](mean_stats)
         achieved = dom_bytes / (avg[dom] / 1e3) / 1e9
         roof.update({"kernel": dom, "achieved": achieved, "frac": achieved / peak, "traffic": None,

@@ -106,9 +106,10 @@ typedef struct {
     uint64_t touched_words;   /* 32-cell bitmap words touched by the batch */
     uint64_t bytes_algorithmic;
     /* with LTP_FLAG_STAGE_TIMING, milliseconds per kernel of the batch:
-     * ordered rule:  0 mark, 1 ids, 2 classify, 3 sort histogram,
-     *                4-7 radix passes, 8 apply, 9 finish
-     * priority rule: 0 mark, 1 ids, 2 min-writer, 3 abort, 4 execute, 9 finish
+     * ordered rule:  0 mark, 1 ids, 2 classify, 3-6 radix passes, 7 apply,
+     *                8 insert, 9 finish
+     * priority rule: 0 mark, 1 ids, 2 min-writer, 3 abort, 4 execute,
+     *                8 insert, 9 finish
      * and 11 the whole batch */
     float ms_stage[LTP_N_STAGES];
 } ltp_stats;

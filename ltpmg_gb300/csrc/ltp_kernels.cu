@@ -518,6 +518,7 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
                 long long v = val[k];
                 if (opw_kind(w[k]) == LTP_OP_ADD) {
                     v = (long long)((u64)v + (u64)(long long)opw_imm(w[k]));
+                    if (!r[k].wide) v = (int32_t)v;  // int32 cells wrap at 32 bits
                     store_cell(r[k].ptr, r[k].wide, v);
                 }
                 const u64 i = wbase + (u64)k * 32 + lane;
@@ -969,13 +970,34 @@ __device__ __forceinline__ void phase_r1_exec(const BatchDev &b, const TablesDev
         }
         u32 m;
         const bool add = opw_kind(w) == LTP_OP_ADD;
-        // a committed op on a contended cell sees the pre-batch value; a
-        // committed RMW there is the cell's only committed writer
-        long long v = contended_id(s, r.cell, &m) ? s.dbase[m] : load_cell(r.ptr, r.wide);
-        if (add) {
-            v = (long long)((u64)v + (u64)(long long)opw_imm(w));
-            store_cell(r.ptr, r.wide, v);
+        long long v;
+        bool store = add;
+        if (contended_id(s, r.cell, &m)) {
+            // A committed op on a contended cell sees the pre-batch value,
+            // plus -- when its transaction is the cell's only committed
+            // writer (the smallest writing TID) -- the RMWs its own
+            // transaction made to the cell before it; only the
+            // transaction's last RMW on the cell stores.
+            v = s.dbase[m];
+            if (s.dminw[m] == tid) {
+                const u64 key = b.keys[i];
+                const u32 same = w & 0xFFCu;  // column and table fields
+                const u64 first = b.txn_first ? (u64)b.txn_first[tid] : (u64)tid * b.ops_per_txn;
+                const u64 end = b.txn_first ? (u64)b.txn_first[tid + 1] : first + b.ops_per_txn;
+                for (u64 j = first; j < end; j++) {
+                    if (j == i) continue;
+                    const u32 wj = b.opw[j];
+                    if (opw_kind(wj) != LTP_OP_ADD || (wj & 0xFFCu) != same || b.keys[j] != key) continue;
+                    if (j < i) v = (long long)((u64)v + (u64)(long long)opw_imm(wj));
+                    else store = false;
+                }
+            }
+        } else {
+            v = load_cell(r.ptr, r.wide);
         }
+        if (add) v = (long long)((u64)v + (u64)(long long)opw_imm(w));
+        if (!r.wide) v = (int32_t)v;
+        if (store) store_cell(r.ptr, r.wide, v);
         store_out(b, i, v);
     }
 }
@@ -1278,26 +1300,25 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
             sms = L.num_sms;
         }
         const int gsort = capped(gs, (b.n_ops + kSortTile - 1) / kSortTile);
-        mark_ev(4);
         k_sort_pass<0><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops, L.tune.block * L.tune.ipt);
-        mark_ev(5);
+        mark_ev(4);
         k_sort_pass<1><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops, L.tune.block * L.tune.ipt);
-        mark_ev(6);
+        mark_ev(5);
         k_sort_pass<2><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops, L.tune.block * L.tune.ipt);
-        mark_ev(7);
+        mark_ev(6);
         k_sort_pass<3><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops, L.tune.block * L.tune.ipt);
-        mark_ev(8);
+        mark_ev(7);
         const int gapp = capped(ga, (b.n_ops + kApplyTile - 1) / kApplyTile);
         if (T.any_wide) k_apply<u64><<<gapp, kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
         else k_apply<u32><<<gapp, kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
-        mark_ev(9);
+        mark_ev(8);
     } else {
         k_r1_minw<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
         mark_ev(3);
         k_r1_abort<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
         mark_ev(4);
         k_r1_exec<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
-        for (int i = 5; i <= 9; i++) mark_ev(i);
+        for (int i = 5; i <= 8; i++) mark_ev(i);
     }
     {
         static int gins = 0, sms = 0;
@@ -1307,6 +1328,7 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
         }
         k_insert<<<capped(gins, (b.n_ops + kInsTile - 1) / kInsTile), kInsBlock, 0, L.stream>>>(b, T, s, ctr);
     }
+    mark_ev(9);
     k_finish<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr, L.rule);
     mark_ev(10);
     return cudaGetLastError();

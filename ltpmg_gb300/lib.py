@@ -21,8 +21,10 @@ RULE_ORDERED, RULE_PRIORITY = 0, 1
 OP_READ, OP_ADD, OP_INSERT = 0, 1, 2
 FLAG_STAGE_TIMING = 1
 MODE_STREAM, MODE_GRAPH, MODE_PERSISTENT = 0, 1, 2
-STAGE_NAMES = ["mark", "ids", "classify", "sort_hist", "sort_pass0", "sort_pass1", "sort_pass2", "sort_pass3",
-               "apply", "finish", "unused", "total"]
+# per-kernel stage times of a batch (ordered rule; under the priority rule
+# stages 2-4 are the min-writer, abort and execute kernels)
+STAGE_NAMES = ["mark", "ids", "classify", "sort_pass0", "sort_pass1", "sort_pass2", "sort_pass3", "apply",
+               "insert", "finish", "unused", "total"]
 
 
 class LtpError(RuntimeError):

@@ -90,6 +90,20 @@ def tpcc_algorithmic_bytes(g, keys, opw, n_txns):
     return int(24 * len(keys) + cell.sum() + 4 * n_txns)
 
 
+def tpcc_insert_bytes(g, keys, opw):
+    """Bytes the insert kernel of one batch moves at least: every opword
+    (4 B/op), and per insert its key (8), payload row (read), new row
+    (written) and output (4)."""
+    import numpy as np
+
+    rowb = np.zeros(16, np.int64)
+    for t in range(9):
+        n_cols, mask, _ = g.table(t)
+        rowb[t] = 4 * n_cols + 4 * bin(mask).count("1")
+    ins = (opw & 3) == 2
+    return int(4 * len(opw) + (12 * ins.sum()) + 2 * rowb[((opw >> 8) & 15)[ins]].sum())
+
+
 def expected_txns(name):
     if name != "uneven":
         return SHAPES[name]["batches"] * batch_params(name, 0)[0]

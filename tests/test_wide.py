@@ -183,3 +183,29 @@ def test_bad_link_reported():
             b.results64()
         assert "index 1" in str(e.value)
         assert ctx.table_rows(t) == 4
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rule", [0, 1])
+def test_repeated_cells_in_one_transaction_and_int32_wrap(rule):
+    """A transaction that RMWs one cell twice and reads it in between (the
+    cell is contended: the batch's smallest writing TID is this transaction,
+    later transactions touch it too), and uncontended int32 RMWs that wrap."""
+    with G.Context(device=0, rule=rule) as ctx:
+        t = ctx.create_table(8, 2, wide=[1])
+        init = np.array([[5, 2**31 - 2, -(2**31) + 1, 0, 0, 0, 0, 0], [2**40, 7, 0, 0, 0, 0, 0, 0]], np.int64)
+        ctx.upload(t, init)
+        tf = np.array([0, 5, 7, 8], np.uint32)
+        keys = np.array([0, 0, 0, 0, 1, 0, 0, 2], np.uint64)
+        opw = np.array([O.opword(ADD, 1, 0, 3), O.opword(READ, 1, 0, 0), O.opword(ADD, 1, 0, -7),
+                        O.opword(ADD, 0, 0, 2), O.opword(ADD, 0, 0, 5),
+                        O.opword(READ, 1, 0, 0), O.opword(ADD, 1, 0, 1),
+                        O.opword(ADD, 0, 0, -9)], np.uint32)
+        b = ctx.batch(3, 8)
+        b.load(tf, keys, opw)
+        b.execute()
+        commit, vals, _ = b.results64()
+        ref, rc, ro = O.replay_tables(rule, [(init, 8, 0b10)], tf, keys, opw)
+        assert np.array_equal(commit, rc) and np.array_equal(vals, ro)
+        assert np.array_equal(ctx.download(t), ref[0][0])
+        assert ro[4] == -(2**31) + 3 and ro[7] == 2**31 - 8
