@@ -258,7 +258,7 @@ def run_ours(args, config):
     ctx.sync()
 
     # autotuning (untimed): tilings per size bucket, then the multi-batch mode
-    tiles = AT.tune_buckets(ctx, dev, reps=2)
+    tiles = fixed_tiles(ctx, dev, args.tiles) if args.tiles else AT.tune_buckets(ctx, dev, reps=2)
     if args.mode == "auto":
         mode, mode_ms = AT.tune_mode(ctx, dev)
     else:
@@ -303,57 +303,59 @@ def run_ours(args, config):
     ops_per_step = sum(len(h[1]) for h in host)
     value = args.steps * txns_per_step * world / (ms / 1e3)
 
-    # end to end through the C ABI's pipeline: every step copies one batch
-    # from pinned host memory, executes it and copies its commit vector and
-    # op values back into pinned host memory; copies of neighbouring steps
-    # overlap execution (3-deep pipeline, three streams)
-    depth = 3
-    n_e2e = min(64, max(8, args.steps))
-    hb = [max(range(nb), key=lambda i: host[i][3])]
-    hb.append((hb[0] + 1) % nb)
-    pins = []
-    for i in hb:
-        tf, keys, opw, n, opt = host[i]
-        pk, pw = G.PinnedArray((len(keys),), np.uint64), G.PinnedArray((len(opw),), np.uint32)
-        pk.array[:] = keys
-        pw.array[:] = opw
-        ptf = G.PinnedArray((len(tf),), np.uint32)
-        ptf.array[:] = tf
-        pins.append((ptf, pk, pw, n, opt))
-    maxn = max(p[3] for p in pins)
-    maxops = max(len(p[1].array) for p in pins)
-    outs = [(G.PinnedArray((maxn,), np.uint8), G.PinnedArray((maxops,), np.int32)) for _ in range(depth)]
-    pipe = G.Pipe(ctx, depth, maxn, maxops)
-    h2d = d2h = 0
+    e2e = None
+    if not args.no_e2e:
+        # end to end through the C ABI's pipeline: every step copies one batch
+        # from pinned host memory, executes it and copies its commit vector and
+        # op values back into pinned host memory; copies of neighbouring steps
+        # overlap execution (3-deep pipeline, three streams)
+        depth = 3
+        n_e2e = min(64, max(8, args.steps))
+        hb = [max(range(nb), key=lambda i: host[i][3])]
+        hb.append((hb[0] + 1) % nb)
+        pins = []
+        for i in hb:
+            tf, keys, opw, n, opt = host[i]
+            pk, pw = G.PinnedArray((len(keys),), np.uint64), G.PinnedArray((len(opw),), np.uint32)
+            pk.array[:] = keys
+            pw.array[:] = opw
+            ptf = G.PinnedArray((len(tf),), np.uint32)
+            ptf.array[:] = tf
+            pins.append((ptf, pk, pw, n, opt))
+        maxn = max(p[3] for p in pins)
+        maxops = max(len(p[1].array) for p in pins)
+        outs = [(G.PinnedArray((maxn,), np.uint8), G.PinnedArray((maxops,), np.int32)) for _ in range(depth)]
+        pipe = G.Pipe(ctx, depth, maxn, maxops)
+        h2d = d2h = 0
 
-    def e2e_submit(i):
-        ptf, pk, pw, n, opt = pins[i % 2]
-        pc, pv = outs[i % depth]
-        tk = pipe.submit(None if opt else ptf.array, pk.array, pw.array, pc.array[:n], pv.array[:len(pk.array)],
-                         ops_per_txn=opt)
-        return tk, n, len(pk.array), opt
+        def e2e_submit(i):
+            ptf, pk, pw, n, opt = pins[i % 2]
+            pc, pv = outs[i % depth]
+            tk = pipe.submit(None if opt else ptf.array, pk.array, pw.array, pc.array[:n], pv.array[:len(pk.array)],
+                             ops_per_txn=opt)
+            return tk, n, len(pk.array), opt
 
-    for i in range(depth):
-        pipe.wait(e2e_submit(i)[0])
-    ctx.sync()
-    barrier(world)
-    t0 = time.perf_counter()
-    e2e_txns, inflight = 0, []
-    for i in range(n_e2e):
-        tk, n, nops, opt = e2e_submit(i)
-        inflight.append(tk)
-        if len(inflight) >= depth:
-            pipe.wait(inflight.pop(0))
-        e2e_txns += n
-        h2d += 12 * nops + (0 if opt else 4 * (n + 1))
-        d2h += 4 * nops + n
-    for tk in inflight:
-        pipe.wait(tk)
-    e2e_s = reduce_max(time.perf_counter() - t0, world)
-    pipe.close()
-    e2e = {"value": e2e_txns * world / e2e_s, "unit": "txn/s", "h2d_bytes_per_step": h2d // n_e2e,
-           "d2h_bytes_per_step": d2h // n_e2e, "steps": n_e2e,
-           "note": "one batch per step through ltp_pipe (3 slots): H2D, execute, D2H overlapped across steps"}
+        for i in range(depth):
+            pipe.wait(e2e_submit(i)[0])
+        ctx.sync()
+        barrier(world)
+        t0 = time.perf_counter()
+        e2e_txns, inflight = 0, []
+        for i in range(n_e2e):
+            tk, n, nops, opt = e2e_submit(i)
+            inflight.append(tk)
+            if len(inflight) >= depth:
+                pipe.wait(inflight.pop(0))
+            e2e_txns += n
+            h2d += 12 * nops + (0 if opt else 4 * (n + 1))
+            d2h += 4 * nops + n
+        for tk in inflight:
+            pipe.wait(tk)
+        e2e_s = reduce_max(time.perf_counter() - t0, world)
+        pipe.close()
+        e2e = {"value": e2e_txns * world / e2e_s, "unit": "txn/s", "h2d_bytes_per_step": h2d // n_e2e,
+               "d2h_bytes_per_step": d2h // n_e2e, "steps": n_e2e,
+               "note": "one batch per step through ltp_pipe (3 slots): H2D, execute, D2H overlapped across steps"}
 
     if rank != 0:
         return
@@ -397,6 +399,18 @@ def run_ours(args, config):
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(config, host)
     print(json.dumps(line), flush=True)
+
+
+def fixed_tiles(ctx, dev, spec):
+    from ltpmg_gb300 import autotune as AT
+
+    blk, ipt = (int(x) for x in spec.split("x"))
+    out = {}
+    for b in dev:
+        k = AT.bucket_of(b.n_ops)
+        ctx.set_tuning(k, blk, ipt)
+        out[k] = {"block": blk, "ipt": ipt}
+    return out
 
 
 def tpcc_setup(seed_offset=0):
@@ -469,9 +483,9 @@ def run_tpcc(args):
     # timing pass and the end-to-end pass)
     timing_steps = max(1, min(args.steps, 5))
     n_e2e = min(32, max(8, args.steps))
-    execs_all = 6 + args.warmup * 2 + args.steps + timing_steps
+    execs_all = (6 if args.mode == "auto" else 0) + args.warmup * 2 + args.steps + timing_steps
     per_batch = np.max([h[5] for h in host], axis=0)
-    extra = per_batch * (execs_all * nb + 40 + n_e2e + 3)
+    extra = per_batch * (execs_all * nb + (0 if args.tiles else 40) + (0 if args.no_e2e else n_e2e + 3))
     ctx = G.Context(device=local, stage_timing=True)
     ctx_tables = g.create_tables(ctx, extra)
     dev = []
@@ -481,7 +495,7 @@ def run_tpcc(args):
         b.load_payload(pay)
         dev.append(b)
     ctx.sync()
-    tiles = AT.tune_buckets(ctx, dev[:1], reps=1)
+    tiles = fixed_tiles(ctx, dev, args.tiles) if args.tiles else AT.tune_buckets(ctx, dev[:1], reps=1)
     if args.mode == "auto":
         mode, mode_ms = AT.tune_mode(ctx, dev)
     else:
@@ -520,49 +534,51 @@ def run_tpcc(args):
     ops_per_step = sum(len(h[1]) for h in host)
     value = args.steps * txns_per_step * world / (ms / 1e3)
 
-    # end to end: one batch per step through the 3-slot pipeline (payload too)
-    depth = 3
-    pins = []
-    for tf, keys, opw, pay, n, _ in host[:2]:
-        arrs = []
-        for a, dt in ((tf, np.uint32), (keys, np.uint64), (opw, np.uint32), (pay, np.int32)):
-            p = G.PinnedArray((len(a),), dt)
-            p.array[:] = a
-            arrs.append(p)
-        pins.append((arrs, n))
-    maxn = max(p[1] for p in pins)
-    maxops = max(len(p[0][1].array) for p in pins)
-    outs = [(G.PinnedArray((maxn,), np.uint8), G.PinnedArray((maxops,), np.int32)) for _ in range(depth)]
-    pipe = G.Pipe(ctx, depth, maxn, maxops)
-    h2d = d2h = 0
+    e2e = None
+    if not args.no_e2e:
+        # end to end: one batch per step through the 3-slot pipeline (payload too)
+        depth = 3
+        pins = []
+        for tf, keys, opw, pay, n, _ in host[:2]:
+            arrs = []
+            for a, dt in ((tf, np.uint32), (keys, np.uint64), (opw, np.uint32), (pay, np.int32)):
+                p = G.PinnedArray((len(a),), dt)
+                p.array[:] = a
+                arrs.append(p)
+            pins.append((arrs, n))
+        maxn = max(p[1] for p in pins)
+        maxops = max(len(p[0][1].array) for p in pins)
+        outs = [(G.PinnedArray((maxn,), np.uint8), G.PinnedArray((maxops,), np.int32)) for _ in range(depth)]
+        pipe = G.Pipe(ctx, depth, maxn, maxops)
+        h2d = d2h = 0
 
-    def e2e_submit(i):
-        (ptf, pk, pw, pp), n = pins[i % len(pins)]
-        pc, pv = outs[i % depth]
-        tk = pipe.submit(ptf.array, pk.array, pw.array, pc.array[:n], pv.array[:len(pk.array)], payload=pp.array)
-        return tk, n, len(pk.array), len(pp.array)
+        def e2e_submit(i):
+            (ptf, pk, pw, pp), n = pins[i % len(pins)]
+            pc, pv = outs[i % depth]
+            tk = pipe.submit(ptf.array, pk.array, pw.array, pc.array[:n], pv.array[:len(pk.array)], payload=pp.array)
+            return tk, n, len(pk.array), len(pp.array)
 
-    for i in range(depth):
-        pipe.wait(e2e_submit(i)[0])
-    ctx.sync()
-    barrier(world)
-    t0 = time.perf_counter()
-    e2e_txns, inflight = 0, []
-    for i in range(n_e2e):
-        tk, n, nops, npay = e2e_submit(i)
-        inflight.append(tk)
-        if len(inflight) >= depth:
-            pipe.wait(inflight.pop(0))
-        e2e_txns += n
-        h2d += 12 * nops + 4 * (n + 1) + 4 * npay
-        d2h += 4 * nops + n
-    for tk in inflight:
-        pipe.wait(tk)
-    e2e_s = reduce_max(time.perf_counter() - t0, world)
-    pipe.close()
-    e2e = {"value": e2e_txns * world / e2e_s, "unit": "txn/s", "h2d_bytes_per_step": h2d // n_e2e,
-           "d2h_bytes_per_step": d2h // n_e2e, "steps": n_e2e,
-           "note": "one batch (+ insert payload) per step through ltp_pipe (3 slots), copies overlapped"}
+        for i in range(depth):
+            pipe.wait(e2e_submit(i)[0])
+        ctx.sync()
+        barrier(world)
+        t0 = time.perf_counter()
+        e2e_txns, inflight = 0, []
+        for i in range(n_e2e):
+            tk, n, nops, npay = e2e_submit(i)
+            inflight.append(tk)
+            if len(inflight) >= depth:
+                pipe.wait(inflight.pop(0))
+            e2e_txns += n
+            h2d += 12 * nops + 4 * (n + 1) + 4 * npay
+            d2h += 4 * nops + n
+        for tk in inflight:
+            pipe.wait(tk)
+        e2e_s = reduce_max(time.perf_counter() - t0, world)
+        pipe.close()
+        e2e = {"value": e2e_txns * world / e2e_s, "unit": "txn/s", "h2d_bytes_per_step": h2d // n_e2e,
+               "d2h_bytes_per_step": d2h // n_e2e, "steps": n_e2e,
+               "note": "one batch (+ insert payload) per step through ltp_pipe (3 slots), copies overlapped"}
     if rank != 0:
         return
     peak, peak_kind = load_peaks()
@@ -719,6 +735,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batches", type=int, default=0, help="resident batches (default: the config's)")
     ap.add_argument("--tuning-out", default="", help="write the autotuner's choices to this JSON file")
+    ap.add_argument("--tiles", default="", help="fixed BLOCKxIPT tiling instead of the autotuner's (e.g. 512x4)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
