@@ -134,9 +134,22 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def load_traffic():
-    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    return json.load(open(p)) if os.path.exists(p) else {}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit of work,
+# from one ncu --set full capture of each kernel on one batch of the same
+# workload (profiles/k_mark_classify_apply_zipf.md, profiles/k_mark_insert_tpcc.md);
+# a launch's traffic is this figure times the units it processed
+MEASURED_TRAFFIC = {
+    ("zipf", "classify"): (46.3, "ops"),
+    ("zipf", "mark"): (22.4, "ops"),
+    ("zipf", "apply"): (45.0, "contended_ops"),
+    ("tpcc", "insert"): (73.2, "ops"),
+    ("tpcc", "mark"): (19.9, "ops"),
+}
+
+
+def measured_traffic(config, kernel, stats):
+    t = MEASURED_TRAFFIC.get((config, kernel))
+    return None if t is None else t[0] * stats[t[1]]
 
 
 def gen_batches(config, nb, rank):
@@ -373,11 +386,7 @@ def run_ours(args, config):
         dom = max(avg, key=avg.get)
         dom_bytes = KERNEL_BYTES[dom](mean_stats)
         achieved = dom_bytes / (avg[dom] / 1e3) / 1e9
-        traffic = load_traffic().get(dom)
-        traffic_b = None
-        if traffic:
-            units = mean_stats["contended_ops"] if traffic.get("unit") == "contended_op" else mean_stats["ops"]
-            traffic_b = traffic["bytes_per_unit"] * units
+        traffic_b = measured_traffic(config, dom, mean_stats)
         roof.update({"kernel": dom, "achieved": achieved, "frac": achieved / peak, "traffic": traffic_b,
                      "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": avg[dom], "kernel_ms": avg})
     else:
@@ -596,7 +605,8 @@ def run_tpcc(args):
         dom = max(avg, key=avg.get)
         dom_bytes = KERNEL_BYTES[dom](mean_stats)
         achieved = dom_bytes / (avg[dom] / 1e3) / 1e9
-        roof.update({"kernel": dom, "achieved": achieved, "frac": achieved / peak, "traffic": None,
+        roof.update({"kernel": dom, "achieved": achieved, "frac": achieved / peak,
+                     "traffic": measured_traffic("tpcc", dom, mean_stats),
                      "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": avg[dom], "kernel_ms": avg})
     else:
         roof.update({"kernel": "k_persist (whole pipeline, one launch per step)",
