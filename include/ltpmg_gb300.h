@@ -169,6 +169,12 @@ int ltp_batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *
 int ltp_batch_load_payload(ltp_ctx *ctx, ltp_batch *b, const int32_t *payload, uint64_t n, void *stream);
 /* Current row count of a table (grows with committed inserts); synchronises. */
 int ltp_table_rows(ltp_ctx *ctx, uint32_t table, uint64_t *rows);
+/* Drops the rows at and above `rows` (<= the current count): later inserts
+ * reuse their slots.  Synchronises. */
+int ltp_table_truncate(ltp_ctx *ctx, uint32_t table, uint64_t rows);
+/* 1 when some table of the context has an int64 column (outputs then have a
+ * 64-bit copy, ltp_batch_fetch64), else 0. */
+int ltp_ctx_wide(ltp_ctx *ctx);
 /* Executes one batch against the context's tables (replaces
  * GPUlauncher::txn_kernel_launcher, cuda/src/gpulauncher.cu:755-1116). */
 int ltp_batch_execute(ltp_ctx *ctx, ltp_batch *b, void *stream);
@@ -222,6 +228,10 @@ int ltp_pipe_free(ltp_pipe *p);
 int ltp_pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
                     const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
                     uint8_t *commit_out, int32_t *vals_out, uint64_t *ticket);
+/* The same with the full 64-bit op values (the context must have an int64 column). */
+int ltp_pipe_submit64(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
+                      const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
+                      uint8_t *commit_out, int64_t *vals_out, uint64_t *ticket);
 /* Waits until the ticket's results are in its host buffers; returns its status. */
 int ltp_pipe_wait(ltp_pipe *p, uint64_t ticket, ltp_stats *stats);
 /* LTP_OK when the ticket's results are ready, 1 while it is in flight. */
@@ -232,7 +242,7 @@ int ltp_pipe_poll(ltp_pipe *p, uint64_t ticket);
  * generator) submit transactions on numbered streams; a dispatcher thread
  * closes a batch when its oldest transaction has waited deadline_us, when
  * its read/write set reaches budget_bytes (12 bytes of key + opword per op)
- * or the slot capacity, or -- work-conserving -- as soon as the device has
+ * or the slot capacity (max_txns, max_ops, 6 x max_ops payload slots), or -- work-conserving -- as soon as the device has
  * no batch queued; up to `depth` batches are in flight, so arrivals are
  * admitted while earlier batches execute.  Tables and conflict state stay
  * on the device.  Transactions aborted by the priority rule are re-queued
@@ -263,7 +273,7 @@ typedef struct {
     uint32_t attempts;
     uint32_t committed;
     uint32_t pad;
-    int32_t vals[LTP_SERVE_MAX_OPS];
+    int64_t vals[LTP_SERVE_MAX_OPS]; /* op values (int32 cells sign-extended) */
 } ltp_serve_result;
 
 typedef struct {
@@ -279,6 +289,10 @@ int ltp_serve_open(ltp_ctx *ctx, const ltp_serve_config *cfg, ltp_server **out);
  * exceeds LTP_SERVE_MAX_OPS or the slot capacity. */
 int ltp_serve_submit(ltp_server *s, uint32_t stream, uint32_t n_ops, const uint64_t *keys, const uint32_t *opw,
                      uint64_t tag, uint64_t arrival_ns);
+/* The same for a transaction with inserts: each insert op's key is an offset
+ * into this transaction's own payload (n_payload int32 slots). */
+int ltp_serve_submit_rows(ltp_server *s, uint32_t stream, uint32_t n_ops, const uint64_t *keys, const uint32_t *opw,
+                          uint32_t n_payload, const int32_t *payload, uint64_t tag, uint64_t arrival_ns);
 /* Moves up to max completed transactions into out; *n = how many. */
 int ltp_serve_poll(ltp_server *s, ltp_serve_result *out, uint32_t max, uint32_t *n);
 /* Open-loop Poisson load: n_streams clients at `rate` transactions/s in
@@ -288,6 +302,12 @@ int ltp_serve_poll(ltp_server *s, ltp_serve_result *out, uint32_t max, uint32_t 
 int ltp_serve_loadgen(ltp_server *s, double rate, double seconds, uint32_t n_streams, uint64_t seed,
                       const uint32_t *txn_first, uint64_t n_pool, const uint64_t *keys, const uint32_t *opw,
                       uint32_t n_threads);
+/* The same over a pool with inserts: transaction k's payload is
+ * payload[pay_first[k] .. pay_first[k+1]) and its insert keys are offsets
+ * into the whole payload array. */
+int ltp_serve_loadgen_rows(ltp_server *s, double rate, double seconds, uint32_t n_streams, uint64_t seed,
+                           const uint32_t *txn_first, uint64_t n_pool, const uint64_t *keys, const uint32_t *opw,
+                           const uint64_t *pay_first, const int32_t *payload, uint32_t n_threads);
 /* Statistics so far (latency percentiles over committed transactions). */
 int ltp_serve_stats_now(ltp_server *s, ltp_serve_stats *st);
 /* Drains every admitted transaction, stops the dispatcher, frees. */
@@ -375,12 +395,13 @@ int ltp_tpcc_table(const ltp_tpcc *g, uint32_t table, ltp_schema *schema, uint64
 /* Initial values of rows [row0, row0+n) of one column, at the column's width. */
 int ltp_tpcc_column(const ltp_tpcc *g, uint32_t table, uint32_t col, uint64_t row0, uint64_t n, void *dst);
 /* Generates batch `batch` of n_txns transactions (TID = position).  With
- * keys == NULL only the sizes are computed.  n_new_order (may be NULL)
- * receives the new-order count; inserts[LTP_TPCC_N_TABLES] (may be NULL)
- * the rows each table gains.  Returns LTP_OK or LTP_E_CAPACITY. */
+ * keys == NULL only the sizes are computed.  pay_first[n_txns+1] (may be
+ * NULL) receives where each transaction's payload starts; n_new_order (may
+ * be NULL) the new-order count; inserts[LTP_TPCC_N_TABLES] (may be NULL) the
+ * rows each table gains.  Returns LTP_OK or LTP_E_CAPACITY. */
 int ltp_tpcc_gen(const ltp_tpcc *g, uint64_t batch, uint64_t n_txns, uint32_t *txn_first, uint64_t *keys,
-                 uint32_t *opw, uint64_t cap_ops, int32_t *payload, uint64_t cap_payload, uint64_t *n_ops,
-                 uint64_t *n_payload, uint64_t *n_new_order, uint64_t *inserts, int n_threads);
+                 uint32_t *opw, uint64_t cap_ops, int32_t *payload, uint64_t cap_payload, uint64_t *pay_first,
+                 uint64_t *n_ops, uint64_t *n_payload, uint64_t *n_new_order, uint64_t *inserts, int n_threads);
 
 /* ---- tuning --------------------------------------------------------------- */
 typedef struct {

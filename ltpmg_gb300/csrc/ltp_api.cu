@@ -359,6 +359,18 @@ int ltp_table_fill_seeded(ltp_ctx *ctx, uint32_t table, uint64_t seed, void *str
     return LTP_OK;
 }
 
+int ltp_table_truncate(ltp_ctx *ctx, uint32_t table, uint64_t rows) {
+    uint64_t cur = 0;
+    int rc = ltp_table_rows(ctx, table, &cur);
+    if (rc) return rc;
+    if (rows > cur) return fail(ctx, LTP_E_BADARG, "truncate cannot grow a table");
+    const u64 r = rows;
+    CK(cudaMemcpy(ctx->rows_now + table, &r, sizeof(u64), cudaMemcpyHostToDevice));
+    return LTP_OK;
+}
+
+int ltp_ctx_wide(ltp_ctx *ctx) { return ctx && ctx->any_wide ? 1 : 0; }
+
 int ltp_table_rows(ltp_ctx *ctx, uint32_t table, uint64_t *rows) {
     if (!ctx || !rows || table >= ctx->tables.size()) return LTP_E_BADARG;
     CK(cudaSetDevice(ctx->device));
@@ -884,9 +896,11 @@ int ltp_pipe_free(ltp_pipe *p) {
     return LTP_OK;
 }
 
-int ltp_pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
-                    const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
-                    uint8_t *commit_out, int32_t *vals_out, uint64_t *ticket) {
+}  // extern "C"
+
+static int pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
+                       const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
+                       uint8_t *commit_out, int32_t *vals_out, int64_t *vals64_out, uint64_t *ticket) {
     if (!p) return LTP_E_BADARG;
     ltp_ctx *ctx = p->ctx;
     CK(cudaSetDevice(ctx->device));
@@ -918,6 +932,7 @@ int ltp_pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uin
     CK(cudaEventRecord(sl.exec, sx));
     CK(cudaStreamWaitEvent(p->s_out, sl.exec, 0));
     if ((rc = ltp_batch_fetch(ctx, sl.b, commit_out, vals_out, p->s_out))) return rc;
+    if (vals64_out && (rc = ltp_batch_fetch64(ctx, sl.b, vals64_out, p->s_out))) return rc;
     CK(cudaEventRecord(sl.out, p->s_out));
     sl.ticket = t;
     sl.waited = false;
@@ -925,6 +940,22 @@ int ltp_pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uin
     p->next = t + 1;
     if (ticket) *ticket = t;
     return LTP_OK;
+}
+
+extern "C" {
+
+int ltp_pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
+                    const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
+                    uint8_t *commit_out, int32_t *vals_out, uint64_t *ticket) {
+    return pipe_submit(p, n_txns, txn_first, ops_per_txn, n_ops, keys, opw, payload, payload_len, commit_out, vals_out,
+                       nullptr, ticket);
+}
+
+int ltp_pipe_submit64(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
+                      const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
+                      uint8_t *commit_out, int64_t *vals_out, uint64_t *ticket) {
+    return pipe_submit(p, n_txns, txn_first, ops_per_txn, n_ops, keys, opw, payload, payload_len, commit_out, nullptr,
+                       vals_out, ticket);
 }
 
 int ltp_pipe_wait(ltp_pipe *p, uint64_t ticket, ltp_stats *stats) {

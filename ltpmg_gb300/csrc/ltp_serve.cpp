@@ -41,12 +41,17 @@ uint64_t now_ns() {
     return (uint64_t)ts.tv_sec * 1000000000ull + (uint64_t)ts.tv_nsec;
 }
 
-// Transactions of one lane between two drains, in arrival order.
+inline bool is_insert(uint32_t w) { return (w & 3u) == LTP_OP_INSERT; }
+
+// Transactions of one lane between two drains, in arrival order.  An insert
+// op's key is an offset into the segment's payload array.
 struct Seg {
     std::vector<uint64_t> arrival, tag;
     std::vector<uint32_t> stream, off, attempts;  // off: first op; txn i's ops are [off[i], off[i+1])
     std::vector<uint64_t> keys;
     std::vector<uint32_t> opw;
+    std::vector<uint32_t> poff;  // txn i's payload is [poff[i], poff[i+1])
+    std::vector<int32_t> payload;
     size_t head = 0;  // next transaction to batch
     size_t n() const { return arrival.size(); }
     void clear() {
@@ -54,20 +59,31 @@ struct Seg {
         tag.clear();
         stream.clear();
         off.assign(1, 0);
+        poff.assign(1, 0);
         attempts.clear();
         keys.clear();
         opw.clear();
+        payload.clear();
         head = 0;
     }
+    // key_base: what the caller's insert keys are relative to
     void push(uint64_t arr, uint64_t tg, uint32_t st, uint32_t att, uint32_t n_ops, const uint64_t *k,
-              const uint32_t *w) {
+              const uint32_t *w, uint32_t n_pay, const int32_t *pay, uint64_t key_base) {
         arrival.push_back(arr);
         tag.push_back(tg);
         stream.push_back(st);
         attempts.push_back(att);
+        const size_t k0 = keys.size();
         keys.insert(keys.end(), k, k + n_ops);
         opw.insert(opw.end(), w, w + n_ops);
         off.push_back((uint32_t)keys.size());
+        if (n_pay) {
+            const uint64_t p0 = payload.size();
+            payload.insert(payload.end(), pay, pay + n_pay);
+            for (size_t j = k0; j < keys.size(); j++)
+                if (is_insert(opw[j])) keys[j] = keys[j] - key_base + p0;
+        }
+        poff.push_back((uint32_t)payload.size());
     }
 };
 
@@ -86,6 +102,8 @@ struct Slot {
     uint32_t *opw = nullptr, *txn_first = nullptr;
     uint8_t *commit = nullptr;
     int32_t *vals = nullptr;
+    int64_t *vals64 = nullptr;  // when the context has int64 columns
+    int32_t *payload = nullptr;
     std::vector<Run> runs;
     uint64_t ticket = 0, seq = 0;
     bool busy = false;
@@ -132,6 +150,8 @@ struct ltp_server {
     ltp_ctx *ctx = nullptr;
     ltp_serve_config cfg;
     bool keep_results = true;
+    bool wide = false;
+    uint64_t max_payload = 0;
     ltp_pipe *pipe = nullptr;
     std::vector<std::unique_ptr<Lane>> lanes;
     std::vector<Slot> slots;
@@ -211,7 +231,8 @@ void complete_batch(ltp_server *s, Slot &sl) {
                 s->aborted_attempts++;
                 if (!again) again = new_seg(s);
                 again->push(g.arrival[i], g.tag[i], g.stream[i], g.attempts[i] + 1, g.off[i + 1] - g.off[i],
-                            g.keys.data() + g.off[i], g.opw.data() + g.off[i]);
+                            g.keys.data() + g.off[i], g.opw.data() + g.off[i], g.poff[i + 1] - g.poff[i],
+                            g.payload.data() + g.poff[i], g.poff[i]);
                 continue;
             }
             if (!ok) s->aborted_attempts++;
@@ -232,7 +253,11 @@ void complete_batch(ltp_server *s, Slot &sl) {
                 res.n_ops = g.off[i + 1] - g.off[i];
                 res.attempts = g.attempts[i] + 1;
                 res.committed = ok ? 1u : 0u;
-                memcpy(res.vals, sl.vals + sl.txn_first[pos], res.n_ops * sizeof(int32_t));
+                if (s->wide) {
+                    memcpy(res.vals, sl.vals64 + sl.txn_first[pos], res.n_ops * sizeof(int64_t));
+                } else {
+                    for (uint32_t j = 0; j < res.n_ops; j++) res.vals[j] = sl.vals[sl.txn_first[pos] + j];
+                }
                 out.push_back(res);
             }
         }
@@ -275,7 +300,7 @@ bool close_batch(ltp_server *s, uint64_t now) {
     else if (full) s->closed_budget++;
     else s->closed_idle++;
     Slot &sl = s->slots[si];
-    uint64_t nops = 0;
+    uint64_t nops = 0, npay = 0;
     uint32_t nt = 0;
     sl.txn_first[0] = 0;
     while (!s->pending.empty() && nt < s->cfg.max_txns) {
@@ -283,13 +308,22 @@ bool close_batch(ltp_server *s, uint64_t now) {
         Seg &g = *p;
         // largest run of this segment that fits
         size_t k = g.head;
-        while (k < g.n() && nt + (k - g.head) < s->cfg.max_txns && nops + (g.off[k + 1] - g.off[g.head]) <= cap_ops)
+        while (k < g.n() && nt + (k - g.head) < s->cfg.max_txns && nops + (g.off[k + 1] - g.off[g.head]) <= cap_ops &&
+               npay + (g.poff[k + 1] - g.poff[g.head]) <= s->max_payload)
             k++;
         const size_t cnt = k - g.head;
         if (cnt) {
             const uint32_t a = g.off[g.head], b = g.off[k];
             memcpy(sl.keys + nops, g.keys.data() + a, (size_t)(b - a) * sizeof(uint64_t));
             memcpy(sl.opw + nops, g.opw.data() + a, (size_t)(b - a) * sizeof(uint32_t));
+            const uint32_t pa = g.poff[g.head], pb = g.poff[k];
+            if (pb > pa) {  // move the run's payload and rebase its insert keys
+                memcpy(sl.payload + npay, g.payload.data() + pa, (size_t)(pb - pa) * sizeof(int32_t));
+                const uint64_t delta = npay - pa;
+                for (uint64_t j = nops; j < nops + (b - a); j++)
+                    if (is_insert(sl.opw[j])) sl.keys[j] += delta;
+                npay += pb - pa;
+            }
             for (size_t i = g.head; i < k; i++) sl.txn_first[++nt] = (uint32_t)(nops + g.off[i + 1] - a);
             nops += b - a;
             sl.runs.push_back(Run{p, g.head, cnt});
@@ -305,8 +339,10 @@ bool close_batch(ltp_server *s, uint64_t now) {
     }
     if (nt == 0) return false;
     uint64_t ticket = 0;
-    const int rc = ltp_pipe_submit(s->pipe, nt, sl.txn_first, 0, nops, sl.keys, sl.opw, nullptr, 0, sl.commit, sl.vals,
-                                   &ticket);
+    const int rc = s->wide ? ltp_pipe_submit64(s->pipe, nt, sl.txn_first, 0, nops, sl.keys, sl.opw, sl.payload, npay,
+                                               sl.commit, sl.vals64, &ticket)
+                           : ltp_pipe_submit(s->pipe, nt, sl.txn_first, 0, nops, sl.keys, sl.opw, sl.payload, npay,
+                                             sl.commit, sl.vals, &ticket);
     if (rc) {
         s->status = rc;
         return false;
@@ -352,6 +388,8 @@ int ltp_serve_open(ltp_ctx *ctx, const ltp_serve_config *cfg, ltp_server **out) 
     s->ctx = ctx;
     s->cfg = *cfg;
     s->keep_results = (cfg->flags & LTP_SERVE_KEEP_RESULTS) != 0;
+    s->wide = ltp_ctx_wide(ctx) != 0;
+    s->max_payload = cfg->max_ops * 6;  // int32 slots of insert payload per batch
     if (s->cfg.max_attempts == 0) s->cfg.max_attempts = 1;
     int rc = ltp_pipe_create(ctx, cfg->depth, cfg->max_txns, cfg->max_ops, &s->pipe);
     if (rc) {
@@ -365,9 +403,11 @@ int ltp_serve_open(ltp_ctx *ctx, const ltp_serve_config *cfg, ltp_server **out) 
         sl.keys = (uint64_t *)ltp_host_alloc(cfg->max_ops * 8);
         sl.opw = (uint32_t *)ltp_host_alloc(cfg->max_ops * 4);
         sl.vals = (int32_t *)ltp_host_alloc(cfg->max_ops * 4);
+        sl.vals64 = s->wide ? (int64_t *)ltp_host_alloc(cfg->max_ops * 8) : nullptr;
+        sl.payload = (int32_t *)ltp_host_alloc(s->max_payload * 4);
         sl.txn_first = (uint32_t *)ltp_host_alloc((cfg->max_txns + 1) * 4);
         sl.commit = (uint8_t *)ltp_host_alloc(cfg->max_txns);
-        if (!sl.keys || !sl.opw || !sl.vals || !sl.txn_first || !sl.commit) {
+        if (!sl.keys || !sl.opw || !sl.vals || !sl.txn_first || !sl.commit || !sl.payload || (s->wide && !sl.vals64)) {
             ltp_serve_close(s, nullptr);
             return LTP_E_NOMEM;
         }
@@ -377,20 +417,27 @@ int ltp_serve_open(ltp_ctx *ctx, const ltp_serve_config *cfg, ltp_server **out) 
     return LTP_OK;
 }
 
-int ltp_serve_submit(ltp_server *s, uint32_t stream, uint32_t n_ops, const uint64_t *keys, const uint32_t *opw,
-                     uint64_t tag, uint64_t arrival_ns) {
-    if (!s || (n_ops && (!keys || !opw))) return LTP_E_BADARG;
-    if (n_ops > LTP_SERVE_MAX_OPS || n_ops > s->cfg.max_ops) return LTP_E_CAPACITY;
+int ltp_serve_submit_rows(ltp_server *s, uint32_t stream, uint32_t n_ops, const uint64_t *keys, const uint32_t *opw,
+                          uint32_t n_payload, const int32_t *payload, uint64_t tag, uint64_t arrival_ns) {
+    if (!s || (n_ops && (!keys || !opw)) || (n_payload && !payload)) return LTP_E_BADARG;
+    if (n_ops > LTP_SERVE_MAX_OPS || n_ops > s->cfg.max_ops || n_payload > s->max_payload) return LTP_E_CAPACITY;
+    for (uint32_t j = 0; j < n_ops; j++)  // an insert's payload row must start inside this transaction's payload
+        if (is_insert(opw[j]) && keys[j] >= n_payload) return LTP_E_BADARG;
     if (s->status) return s->status;
     Lane &ln = *s->lanes[stream % s->lanes.size()];
     const uint64_t at = arrival_ns ? arrival_ns : now_ns();
     {
         std::lock_guard<std::mutex> g(ln.mu);
         if (!ln.seg) ln.seg = new_seg(s);
-        ln.seg->push(at, tag, stream, 0, n_ops, keys, opw);
+        ln.seg->push(at, tag, stream, 0, n_ops, keys, opw, n_payload, payload, 0);
     }
     if (s->submitted.fetch_add(1) == 0) s->t_first = at;
     return LTP_OK;
+}
+
+int ltp_serve_submit(ltp_server *s, uint32_t stream, uint32_t n_ops, const uint64_t *keys, const uint32_t *opw,
+                     uint64_t tag, uint64_t arrival_ns) {
+    return ltp_serve_submit_rows(s, stream, n_ops, keys, opw, 0, nullptr, tag, arrival_ns);
 }
 
 int ltp_serve_poll(ltp_server *s, ltp_serve_result *out, uint32_t max, uint32_t *n) {
@@ -406,7 +453,15 @@ int ltp_serve_poll(ltp_server *s, ltp_serve_result *out, uint32_t max, uint32_t 
 int ltp_serve_loadgen(ltp_server *s, double rate, double seconds, uint32_t n_streams, uint64_t seed,
                       const uint32_t *txn_first, uint64_t n_pool, const uint64_t *keys, const uint32_t *opw,
                       uint32_t n_threads) {
+    return ltp_serve_loadgen_rows(s, rate, seconds, n_streams, seed, txn_first, n_pool, keys, opw, nullptr, nullptr,
+                                  n_threads);
+}
+
+int ltp_serve_loadgen_rows(ltp_server *s, double rate, double seconds, uint32_t n_streams, uint64_t seed,
+                           const uint32_t *txn_first, uint64_t n_pool, const uint64_t *keys, const uint32_t *opw,
+                           const uint64_t *pay_first, const int32_t *payload, uint32_t n_threads) {
     if (!s || rate <= 0 || seconds <= 0 || !n_streams || !txn_first || !n_pool || !keys || !opw) return LTP_E_BADARG;
+    if ((pay_first == nullptr) != (payload == nullptr)) return LTP_E_BADARG;
     if (!n_threads) n_threads = 1;
     const uint64_t t0 = now_ns() + 1000000;  // start 1 ms from now
     const uint64_t t_end = t0 + (uint64_t)(seconds * 1e9);
@@ -429,7 +484,18 @@ int ltp_serve_loadgen(ltp_server *s, double rate, double seconds, uint32_t n_str
                 }
                 const uint32_t st = g + n_threads * (uint32_t)(rng() % my_streams);
                 const uint32_t a = txn_first[k], n = txn_first[k + 1] - txn_first[k];
-                if (ltp_serve_submit(s, st, n, keys + a, opw + a, k, at)) break;
+                int rc;
+                if (pay_first && pay_first[k + 1] > pay_first[k]) {
+                    // the pool's insert keys are offsets into the whole payload: make them txn-relative
+                    uint64_t kk[LTP_SERVE_MAX_OPS];
+                    const uint32_t nn = std::min<uint32_t>(n, LTP_SERVE_MAX_OPS);
+                    for (uint32_t j = 0; j < nn; j++) kk[j] = is_insert(opw[a + j]) ? keys[a + j] - pay_first[k] : keys[a + j];
+                    rc = ltp_serve_submit_rows(s, st, n, kk, opw + a, (uint32_t)(pay_first[k + 1] - pay_first[k]),
+                                               payload + pay_first[k], k, at);
+                } else {
+                    rc = ltp_serve_submit(s, st, n, keys + a, opw + a, k, at);
+                }
+                if (rc) break;
                 if (++k == n_pool) k = 0;
             }
         });
@@ -471,6 +537,8 @@ int ltp_serve_close(ltp_server *s, ltp_serve_stats *st) {
         ltp_host_free(sl.keys);
         ltp_host_free(sl.opw);
         ltp_host_free(sl.vals);
+        ltp_host_free(sl.vals64);
+        ltp_host_free(sl.payload);
         ltp_host_free(sl.txn_first);
         ltp_host_free(sl.commit);
     }

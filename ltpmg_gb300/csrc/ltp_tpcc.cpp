@@ -278,8 +278,9 @@ int ltp_tpcc_column(const ltp_tpcc *g, uint32_t table, uint32_t col, uint64_t ro
 }
 
 int ltp_tpcc_gen(const ltp_tpcc *g, uint64_t batch, uint64_t n_txns, uint32_t *txn_first, uint64_t *keys,
-                 uint32_t *opw_out, uint64_t cap_ops, int32_t *payload, uint64_t cap_payload, uint64_t *n_ops_out,
-                 uint64_t *n_payload_out, uint64_t *n_new_order, uint64_t *inserts, int n_threads) {
+                 uint32_t *opw_out, uint64_t cap_ops, int32_t *payload, uint64_t cap_payload, uint64_t *pay_first_out,
+                 uint64_t *n_ops_out, uint64_t *n_payload_out, uint64_t *n_new_order, uint64_t *inserts,
+                 int n_threads) {
     if (!g) return LTP_E_BADARG;
     const ltp_tpcc_params &p = g->p;
     const uint64_t tseed = p.seed ^ 0x54504343ull;
@@ -300,6 +301,7 @@ int ltp_tpcc_gen(const ltp_tpcc *g, uint64_t batch, uint64_t n_txns, uint32_t *t
     }
     pay_first[n_txns] = pay;
     if (txn_first) txn_first[n_txns] = (uint32_t)ops;
+    if (pay_first_out) memcpy(pay_first_out, pay_first.data(), (n_txns + 1) * sizeof(uint64_t));
     if (n_ops_out) *n_ops_out = ops;
     if (n_payload_out) *n_payload_out = pay;
     if (n_new_order) *n_new_order = no;

@@ -73,7 +73,7 @@ class ServeResult(ctypes.Structure):
     _fields_ = [("tag", ctypes.c_uint64), ("arrival_ns", ctypes.c_uint64), ("done_ns", ctypes.c_uint64),
                 ("batch_seq", ctypes.c_uint64), ("pos", ctypes.c_uint32), ("stream", ctypes.c_uint32),
                 ("n_ops", ctypes.c_uint32), ("attempts", ctypes.c_uint32), ("committed", ctypes.c_uint32),
-                ("pad", ctypes.c_uint32), ("vals", ctypes.c_int32 * SERVE_MAX_OPS)]
+                ("pad", ctypes.c_uint32), ("vals", ctypes.c_int64 * SERVE_MAX_OPS)]
 
 
 class ServeStats(ctypes.Structure):
@@ -133,7 +133,7 @@ def load():
         "ltp_tpcc_free": (None, [vp]),
         "ltp_tpcc_table": (ci, [vp, u32, ctypes.POINTER(Schema), ctypes.POINTER(u64)]),
         "ltp_tpcc_column": (ci, [vp, u32, u32, u64, u64, vp]),
-        "ltp_tpcc_gen": (ci, [vp, u64, u64, vp, vp, vp, u64, vp, u64, ctypes.POINTER(u64), ctypes.POINTER(u64),
+        "ltp_tpcc_gen": (ci, [vp, u64, u64, vp, vp, vp, u64, vp, u64, vp, ctypes.POINTER(u64), ctypes.POINTER(u64),
                               ctypes.POINTER(u64), vp, ci]),
         "ltp_table_value": (i32, [u64, u64, u32, u32]),
         "ltp_set_tuning": (ci, [vp, u32, ctypes.POINTER(Tuning)]),
@@ -153,6 +153,11 @@ def load():
         "ltp_set_stage_timing": (ci, [vp, i32]),
         "ltp_serve_open": (ci, [vp, ctypes.POINTER(ServeConfig), pp]),
         "ltp_serve_submit": (ci, [vp, u32, u32, vp, vp, u64, u64]),
+        "ltp_serve_submit_rows": (ci, [vp, u32, u32, vp, vp, u32, vp, u64, u64]),
+        "ltp_serve_loadgen_rows": (ci, [vp, ctypes.c_double, ctypes.c_double, u32, u64, vp, u64, vp, vp, vp, vp, u32]),
+        "ltp_pipe_submit64": (ci, [vp, u64, vp, u32, u64, vp, vp, vp, u64, vp, vp, ctypes.POINTER(u64)]),
+        "ltp_table_truncate": (ci, [vp, u32, u64]),
+        "ltp_ctx_wide": (ci, [vp]),
         "ltp_serve_poll": (ci, [vp, ctypes.POINTER(ServeResult), u32, ctypes.POINTER(u32)]),
         "ltp_serve_loadgen": (ci, [vp, ctypes.c_double, ctypes.c_double, u32, u64, vp, u64, vp, vp, u32]),
         "ltp_serve_stats_now": (ci, [vp, ctypes.POINTER(ServeStats)]),
@@ -293,23 +298,27 @@ class Tpcc:
             out[c, :rows] = self.column(t, c)
         return out
 
-    def gen(self, batch, n_txns, threads=0):
-        """(txn_first, keys, opw, payload, n_new_order, inserts[9]) of one batch."""
+    def gen(self, batch, n_txns, threads=0, with_pay_first=False):
+        """(txn_first, keys, opw, payload, n_new_order, inserts[9]) of one
+        batch, plus pay_first (where each transaction's payload starts) when
+        with_pay_first."""
         n_ops, n_pay, n_no = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
         ins = np.zeros(9, np.uint64)
         tf = np.zeros(n_txns + 1, np.uint32)
-        rc = self.L.ltp_tpcc_gen(self.h, batch, n_txns, _p(tf), None, None, 0, None, 0, ctypes.byref(n_ops),
+        pf = np.zeros(n_txns + 1, np.uint64)
+        rc = self.L.ltp_tpcc_gen(self.h, batch, n_txns, _p(tf), None, None, 0, None, 0, None, ctypes.byref(n_ops),
                                  ctypes.byref(n_pay), ctypes.byref(n_no), _p(ins), threads)
         if rc:
             raise LtpError(rc, "ltp_tpcc_gen (sizes)")
         keys = np.zeros(max(n_ops.value, 1), np.uint64)
         opw = np.zeros(max(n_ops.value, 1), np.uint32)
         pay = np.zeros(max(n_pay.value, 1), np.int32)
-        rc = self.L.ltp_tpcc_gen(self.h, batch, n_txns, _p(tf), _p(keys), _p(opw), len(keys), _p(pay), len(pay),
+        rc = self.L.ltp_tpcc_gen(self.h, batch, n_txns, _p(tf), _p(keys), _p(opw), len(keys), _p(pay), len(pay), _p(pf),
                                  ctypes.byref(n_ops), ctypes.byref(n_pay), ctypes.byref(n_no), _p(ins), threads)
         if rc:
             raise LtpError(rc, "ltp_tpcc_gen")
-        return tf, keys[:n_ops.value], opw[:n_ops.value], pay[:n_pay.value], n_no.value, ins
+        out = (tf, keys[:n_ops.value], opw[:n_ops.value], pay[:n_pay.value], n_no.value, ins)
+        return out + (pf,) if with_pay_first else out
 
     def create_tables(self, ctx, extra_rows):
         """Creates the nine tables in ctx, each with room for extra_rows[t]
@@ -381,6 +390,13 @@ class Context:
                                                ctypes.byref(tid)))
         self.tables.append((rows, cols, mask))
         return tid.value
+
+    def truncate(self, table, rows):
+        self.check(self.L.ltp_table_truncate(self.h, table, rows))
+
+    @property
+    def wide(self):
+        return bool(self.L.ltp_ctx_wide(self.h))
 
     def table_rows(self, table):
         v = ctypes.c_uint64()
@@ -577,17 +593,29 @@ class Server:
         self.h = h
         self._pool = None
 
-    def submit(self, stream, keys, opw, tag=0, arrival_ns=0):
+    def submit(self, stream, keys, opw, tag=0, arrival_ns=0, payload=None):
+        """payload: the transaction's insert rows; its insert ops' keys are
+        offsets into it."""
         keys = np.ascontiguousarray(keys, np.uint64)
         opw = np.ascontiguousarray(opw, np.uint32)
-        self.ctx.check(self.ctx.L.ltp_serve_submit(self.h, stream, len(keys), _p(keys), _p(opw), tag, arrival_ns))
+        if payload is None:
+            self.ctx.check(self.ctx.L.ltp_serve_submit(self.h, stream, len(keys), _p(keys), _p(opw), tag, arrival_ns))
+        else:
+            pl = np.ascontiguousarray(payload, np.int32)
+            self.ctx.check(self.ctx.L.ltp_serve_submit_rows(self.h, stream, len(keys), _p(keys), _p(opw), len(pl),
+                                                            _p(pl), tag, arrival_ns))
 
-    def loadgen(self, rate, seconds, n_streams, txn_first, keys, opw, seed=1, threads=8):
+    def loadgen(self, rate, seconds, n_streams, txn_first, keys, opw, seed=1, threads=8, pay_first=None,
+                payload=None):
+        """Open-loop Poisson load from a pool; with pay_first/payload the pool
+        holds inserts (insert keys are offsets into the whole payload)."""
         self._pool = (np.ascontiguousarray(txn_first, np.uint32), np.ascontiguousarray(keys, np.uint64),
-                      np.ascontiguousarray(opw, np.uint32))
-        tf, k, w = self._pool
-        self.ctx.check(self.ctx.L.ltp_serve_loadgen(self.h, rate, seconds, n_streams, seed, _p(tf), len(tf) - 1,
-                                                    _p(k), _p(w), threads))
+                      np.ascontiguousarray(opw, np.uint32),
+                      None if pay_first is None else np.ascontiguousarray(pay_first, np.uint64),
+                      None if payload is None else np.ascontiguousarray(payload, np.int32))
+        tf, k, w, pf, pl = self._pool
+        self.ctx.check(self.ctx.L.ltp_serve_loadgen_rows(self.h, rate, seconds, n_streams, seed, _p(tf), len(tf) - 1,
+                                                         _p(k), _p(w), _p(pf), _p(pl), threads))
 
     def poll(self, max_results=4096):
         buf = (ServeResult * max_results)()

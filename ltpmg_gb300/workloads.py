@@ -104,6 +104,49 @@ def tpcc_insert_bytes(g, keys, opw):
     return int(4 * len(opw) + (12 * ins.sum()) + 2 * rowb[((opw >> 8) & 15)[ins]].sum())
 
 
+def mixed_pool(ycsb, tpcc, seed, tpcc_table_base=1):
+    """Seeded 50/50 blend of two transaction pools in a random order: ycsb =
+    (txn_first, keys, opw); tpcc = (txn_first, keys, opw, payload, pay_first)
+    whose table ids are shifted by tpcc_table_base.  Returns (txn_first, keys,
+    opw, pay_first, payload, is_tpcc): transaction k's payload is
+    payload[pay_first[k]:pay_first[k+1]] and insert keys index the whole
+    payload."""
+    import numpy as np
+
+    ytf, yk, yw = (np.asarray(a) for a in ycsb)
+    ttf, tk, tw, tpay, tpf = (np.asarray(a) for a in tpcc)
+    tw = tw.astype(np.uint32) + np.uint32(tpcc_table_base << 8)
+    ny, nt = len(ytf) - 1, len(ttf) - 1
+    src = np.concatenate([np.zeros(ny, np.int8), np.ones(nt, np.int8)])
+    np.random.default_rng(seed).shuffle(src)
+    is_t = src == 1
+    idx = np.where(is_t, np.cumsum(is_t) - 1, np.cumsum(~is_t) - 1)
+    ytf64, ttf64, tpf64 = ytf.astype(np.int64), ttf.astype(np.int64), tpf.astype(np.int64)
+    first = np.where(is_t, ttf64[np.minimum(idx, nt)], ytf64[np.minimum(idx, ny)])
+    lens = np.where(is_t, ttf64[np.minimum(idx + 1, nt)] - ttf64[np.minimum(idx, nt)],
+                    ytf64[np.minimum(idx + 1, ny)] - ytf64[np.minimum(idx, ny)])
+    tf = np.concatenate([[0], np.cumsum(lens)])
+    op_src = np.repeat(first - tf[:-1], lens) + np.arange(tf[-1])
+    op_t = np.repeat(is_t, lens)
+    keys = np.empty(tf[-1], np.uint64)
+    opw = np.empty(tf[-1], np.uint32)
+    keys[~op_t] = yk[op_src[~op_t]]
+    opw[~op_t] = yw[op_src[~op_t]]
+    keys[op_t] = tk[op_src[op_t]]
+    opw[op_t] = tw[op_src[op_t]]
+    # payload: TPC-C transactions keep their rows, rebased to the blend
+    pstart = np.where(is_t, tpf64[np.minimum(idx, nt)], 0)
+    plen = np.where(is_t, tpf64[np.minimum(idx + 1, nt)] - tpf64[np.minimum(idx, nt)], 0)
+    pay_first = np.concatenate([[0], np.cumsum(plen)])
+    pay_src = np.repeat(pstart - pay_first[:-1], plen) + np.arange(pay_first[-1])
+    payload = tpay[pay_src] if len(pay_src) else np.zeros(1, np.int32)
+    ins = op_t & ((opw & 3) == 2)
+    delta = np.repeat(pay_first[:-1] - pstart, lens)
+    keys[ins] = (keys[ins].astype(np.int64) + delta[ins]).astype(np.uint64)
+    return (tf.astype(np.uint32), keys, opw, pay_first.astype(np.uint64), payload.astype(np.int32),
+            src.astype(np.int8))
+
+
 def expected_txns(name):
     if name != "uneven":
         return SHAPES[name]["batches"] * batch_params(name, 0)[0]

@@ -111,3 +111,64 @@ def test_serving_priority_rule_requeues_aborts():
     assert max(r.attempts for r in got) > 1
     committed, tab = _verify_history(got, (tf, keys, opw), rows, cols, seed, 1)
     assert np.array_equal(final, tab)
+
+
+def test_serving_mix_of_ycsb_and_tpcc_transactions():
+    """A seeded 50/50 blend of YCSB transactions (table 0) and TPC-C
+    new-order / payment transactions with inserts and int64 columns (tables
+    1-9) through the load generator: every committed transaction's 64-bit
+    values equal its values in the serial replay of the committed history,
+    and so do all ten tables."""
+    from ltpmg_gb300 import workloads as W
+
+    rows, cols, seed = 1 << 12, 10, 41
+    g = G.Tpcc(2, seed=seed)
+    ycsb = _pool(seed, rows, cols, 3000)
+    tf_t, k_t, w_t, pay_t, _, _, pf_t = g.gen(0, 3000, with_pay_first=True)
+    tf, keys, opw, pay_first, payload, src = W.mixed_pool(ycsb, (tf_t, k_t, w_t, pay_t, pf_t), seed=5)
+    extra = np.zeros(9, np.int64)
+    for t, n in enumerate(np.bincount(((w_t >> 8) & 15)[(w_t & 3) == 2], minlength=9)[:9]):
+        extra[t] = n
+    with G.Context(device=0) as ctx:
+        t0 = ctx.create_table(rows, cols)
+        ctx.fill_seeded(t0, seed)
+        ids = g.create_tables(ctx, extra)
+        assert ids == list(range(1, 10)) and ctx.wide
+        srv = G.Server(ctx, deadline_us=200, depth=3, max_txns=2048, max_ops=2048 * 48)
+        srv.loadgen(rate=300000.0, seconds=0.02, n_streams=32, txn_first=tf, keys=keys, opw=opw, seed=3, threads=4,
+                    pay_first=pay_first, payload=payload)
+        got = []
+        while True:
+            got.extend(srv.poll())
+            if len(got) >= srv.stats()["submitted"]:
+                break
+        st = srv.close()
+        finals = [ctx.download(t) for t in [t0] + ids]
+    assert st["submitted"] > 1000 and st["committed"] == st["submitted"]
+    assert {int(src[r.tag]) for r in got} == {0, 1}
+    committed = sorted(got, key=lambda r: (r.batch_seq, r.pos))
+    # the committed history as one serial batch (insert keys rebased to its payload)
+    htf, hk, hw, hp = [0], [], [], []
+    for r in committed:
+        a, b = int(tf[r.tag]), int(tf[r.tag + 1])
+        pa, pb = int(pay_first[r.tag]), int(pay_first[r.tag + 1])
+        k = keys[a:b].copy()
+        ins = (opw[a:b] & 3) == 2
+        k[ins] = k[ins] - np.uint64(pa) + np.uint64(len(hp))
+        hk.extend(k)
+        hw.extend(opw[a:b])
+        hp.extend(payload[pa:pb])
+        htf.append(len(hk))
+    tabs = [(O.table_init(seed, rows, cols), rows)]
+    for t in range(9):
+        n_cols, mask, r0 = g.table(t)
+        tabs.append((g.initial(t, r0 + int(extra[t])), r0, mask))
+    after, rc, out = O.replay_tables(0, tabs, np.array(htf, np.uint32), np.array(hk, np.uint64),
+                                     np.array(hw, np.uint32), np.array(hp or [0], np.int32))
+    for i, r in enumerate(committed):
+        n = htf[i + 1] - htf[i]
+        assert r.n_ops == n
+        assert list(r.vals[:n]) == out[htf[i]:htf[i + 1]].tolist(), (r.tag, r.batch_seq, r.pos)
+    for t, fin in enumerate(finals):
+        data, n = after[t][0], after[t][1]
+        assert np.array_equal(fin, data[:, :n]), t
