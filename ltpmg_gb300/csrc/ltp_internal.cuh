@@ -109,7 +109,7 @@ struct Scratch {
     u32 *dminw;     // [cap_ops] smallest writer TID of each contended cell (priority rule)
     u32 *st_sort[2];// [tiles * 256] radix look-back status
     u64 *st_ids;    // [tiles] id-scan look-back status
-    u64 *st_cls;    // [tiles] classify look-back status
+    u64 *st_cls;    // [tiles] classify look-back status (dense record offsets)
     u64 *st_apply;  // [tiles] segmented-apply look-back status
     u32 *st_ins;    // [tiles * LTP_MAX_TABLES] insert-slot look-back status
     u64 n_words;
@@ -118,8 +118,8 @@ struct Scratch {
     u64 cap_sort_tiles;
 };
 
-constexpr u32 kSortBlock = 512;
-constexpr u32 kSortIpt = 8;
+constexpr u32 kSortBlock = 256;
+constexpr u32 kSortIpt = 12;
 constexpr u32 kSortTile = kSortBlock * kSortIpt;
 constexpr u32 kIdsBlock = 256;
 constexpr u32 kIdsIpt = 8;

@@ -56,6 +56,25 @@ __device__ __forceinline__ u32 ld_acquire32(const u32 *p) {
 __device__ __forceinline__ void st_release32(u32 *p, u32 v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+// Look-back status words pack the flag and the value into one aligned word,
+// so a reader that sees the flag sees the value: relaxed accesses suffice
+// (no other data is published through them).
+__device__ __forceinline__ u64 ld_status(const u64 *p) {
+    u64 v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_status(u64 *p, u64 v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ u32 ld_status32(const u32 *p) {
+    u32 v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_status32(u32 *p, u32 v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 __device__ __forceinline__ u32 lanemask_lt() {
     u32 m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -92,32 +111,47 @@ __device__ __forceinline__ u32 claim_tile(Counters *ctr, int slot) {
 // ---- decoupled look-back, scalar sums (flag in bits 62-63) ---------------
 constexpr u64 kAgg = 1ull << 62, kInc = 2ull << 62, kValMask = (1ull << 62) - 1;
 
-__device__ u64 lookback_sum(u64 *status, u32 tile, u64 agg, Counters *ctr) {
-    if (tile == 0) {
-        st_release(&status[0], kInc | agg);
-        return 0;
-    }
-    st_release(&status[tile], kAgg | agg);
+// Publishes a tile's aggregate (tile 0: its inclusive prefix) early ...
+__device__ __forceinline__ void lookback_publish(u64 *status, u32 tile, u64 agg) {
+    st_status(&status[tile], (tile == 0 ? kInc : kAgg) | agg);
+}
+// ... and later walks back for the exclusive prefix, then publishes the
+// inclusive one.  Bounded: gives up with LTP_E_TIMEOUT after 2 s.
+__device__ u64 lookback_wait(u64 *status, u32 tile, u64 agg, Counters *ctr) {
+    constexpr int WIN = 4;  // predecessors read per round trip
+    if (tile == 0) return 0;
     u64 excl = 0;
     long long t = (long long)tile - 1;
-    u64 t0 = gtimer();
-    while (t >= 0) {
-        u64 s = ld_acquire(&status[t]);
-        u64 f = s >> 62;
-        if (f == 0) {
-            if (gtimer() - t0 > kSpinLimitNs) {
-                set_err(ctr, LTP_E_TIMEOUT);
-                return 0;
+    const u64 t0 = gtimer();
+    for (;;) {
+        u64 st[WIN];
+#pragma unroll
+        for (int j = 0; j < WIN; j++) st[j] = t - j >= 0 ? ld_status(&status[t - j]) : kInc;
+        int j = 0;
+        bool done = false;
+        for (; j < WIN; j++) {
+            const u64 f = st[j] >> 62;
+            if (f == 0) break;
+            excl += st[j] & kValMask;
+            if (f == 2) {
+                done = true;
+                break;
             }
-            __nanosleep(64);
-            continue;
         }
-        excl += s & kValMask;
-        if (f == 2) break;
-        t--;
+        if (done) break;
+        t -= j;
+        if (gtimer() - t0 > kSpinLimitNs) {
+            set_err(ctr, LTP_E_TIMEOUT);
+            return 0;
+        }
     }
-    st_release(&status[tile], kInc | (excl + agg));
+    st_status(&status[tile], kInc | (excl + agg));
     return excl;
+}
+
+__device__ u64 lookback_sum(u64 *status, u32 tile, u64 agg, Counters *ctr) {
+    lookback_publish(status, tile, agg);
+    return lookback_wait(status, tile, agg, ctr);
 }
 
 // ---- table addressing ------------------------------------------------------
@@ -446,6 +480,8 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int passes = sort_passes_dev(ctr->M);
     __shared__ u32 s_wcnt[NW];
+    __shared__ u32 s_run;
+    __shared__ u64 s_pbase;
     __shared__ u32 s_hist[kMaxPasses][256];
     for (int i = threadIdx.x; i < kMaxPasses * 256; i += BLOCK) (&s_hist[0][0])[i] = 0;
     __syncthreads();
@@ -493,16 +529,17 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
         if (lane == 0) s_wcnt[warp] = wcnt;
         __syncthreads();
         if (threadIdx.x == 0) {
-            // the tile's contended records go to its own region of the list
-            // (tile * TILE onward), in op order; the radix sort's first pass
-            // reads the regions in tile order, so no cross-tile scan is needed
+            // the tile's contended records go to the dense list in op order:
+            // its count is published now, its offset is looked back for after
+            // the uncontended ops have executed
             u32 run = 0;
             for (int i = 0; i < NW; i++) {
                 u32 c = s_wcnt[i];
                 s_wcnt[i] = run;
                 run += c;
             }
-            s.st_cls[tile] = run;
+            s_run = run;
+            lookback_publish(s.st_cls, tile, run);
             if (run) atomicAdd(&ctr->n_c, (u64)run);
         }
         // uncontended ops execute in place; an uncontended read's cell is never
@@ -526,8 +563,9 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
                 if (b.out64) b.out64[i] = v;
             }
         }
+        if (threadIdx.x == 0) s_pbase = lookback_wait(s.st_cls, tile, s_run, ctr);
         __syncthreads();
-        const u64 pbase = (u64)tile * TILE + s_wcnt[warp];
+        const u64 pbase = s_pbase + s_wcnt[warp];
 #pragma unroll
         for (int k = 0; k < IPT; k++)
             if (con[k]) s.list[0][pbase + lpos[k]] = rec[k];
@@ -553,172 +591,152 @@ __global__ void __launch_bounds__(BLOCK, 65536 / (BLOCK * (IPT <= 4 ? 64 : 128))
 // decoupled look-back, stages the records in shared memory in digit order
 // and writes every digit's run with coalesced stores
 // ============================================================================
+// Stable LSD radix pass (8-bit digit P) over the dense contended records.
+// Per tile of kSortTile records: warp ranking by ballots (8 ballots give the
+// lanes that share a digit; the group's lowest lane adds the group size to
+// the warp's shared counter, whose old value is the group's offset -- a
+// warp's shared-memory atomics take effect in program order, which keeps
+// the ranks stable), per-digit decoupled look-back over a window of eight
+// predecessor tiles with relaxed loads, shared-memory staging so every
+// digit's run leaves as coalesced stores.
 template <int BLK>
-__device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, Counters *ctr, u64 n_ops, u32 seg_tile) {
-    static_assert(BLK >= 256, "one thread per radix digit");
+__device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, Counters *ctr) {
+    static_assert(BLK == 256, "one thread per radix digit");
     constexpr u32 SIPT = kSortTile / BLK;
+    constexpr int WIN = 8;
     if (block_err(ctr)) return;
     const int passes = sort_passes_dev(ctr->M);
     if (P >= passes) return;
     const u64 n = ctr->n_c;
-    // pass 0 reads classify's per-tile regions: R regions of seg_tile slots per sort tile
-    const u32 R = P == 0 ? kSortTile / seg_tile : 1;
-    const u32 tiles = P == 0 ? (u32)((n_ops + (u64)seg_tile * R - 1) / ((u64)seg_tile * R))
-                             : (u32)((n + kSortTile - 1) / kSortTile);
-    __shared__ u32 s_segoff[kSortTile / kMinTile + 1];
+    const u32 tiles = (u32)((n + kSortTile - 1) / kSortTile);
     const u64 *src = s.list[P & 1];
     u64 *dst = s.list[(P + 1) & 1];
     u32 *status = s.st_sort[P & 1];
     if (P >= 1) {  // the previous pass is complete: recycle its look-back slots
         u32 *other = s.st_sort[(P + 1) & 1];
-        const u64 prev_tiles = P == 1 ? (n_ops + kSortTile - 1) / kSortTile + 1 : tiles;
-        for (u64 j = (u64)blockIdx.x * BLK + threadIdx.x; j < prev_tiles * 256; j += (u64)gridDim.x * BLK)
+        for (u64 j = (u64)blockIdx.x * BLK + threadIdx.x; j < (u64)tiles * 256; j += (u64)gridDim.x * BLK)
             other[j] = 0;
     }
     constexpr int NW = BLK / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const u32 tid = threadIdx.x;
-    const bool dt = tid < 256;  // threads 0..255 own one digit each
     __shared__ u32 s_start[256];
-    __shared__ unsigned short s_whist[NW][256];  // per-warp digit counts (<= 32 * SIPT)
-    __shared__ u32 s_base[256];   // global position of the tile's first record of each digit
-    __shared__ u32 s_loc[256];    // tile-local position of each digit's first record
-    __shared__ u32 s_wsum[8];
+    __shared__ u32 s_cnt[NW][256];  // per-warp digit counts, then per-warp offsets
+    __shared__ u32 s_base[256];     // global position of the tile's first record of each digit
+    __shared__ u32 s_loc[256];      // tile-local position of each digit's first record
+    __shared__ u32 s_wsum[NW];
     __shared__ u64 s_stage[kSortTile];
     {  // global start of every digit: exclusive scan of the histogram
-        u32 h = dt ? ctr->hist[P][tid] : 0u;
+        const u32 h = ctr->hist[P][tid];
         u32 incl = h;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            u32 v = __shfl_up_sync(FULL_MASK, incl, d);
+            const u32 v = __shfl_up_sync(FULL_MASK, incl, d);
             if (lane >= d) incl += v;
         }
-        if (dt && lane == 31) s_wsum[warp] = incl;
+        if (lane == 31) s_wsum[warp] = incl;
         __syncthreads();
-        if (dt) {
-            u32 off = 0;
-            for (int i = 0; i < warp; i++) off += s_wsum[i];
-            s_start[tid] = off + incl - h;
-        }
+        u32 off = 0;
+        for (int i = 0; i < warp; i++) off += s_wsum[i];
+        s_start[tid] = off + incl - h;
         __syncthreads();
     }
     const int shift = 32 + 8 * P;
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_SORT0 + P);
         if (tile >= tiles) break;
-        for (u32 i = tid; i < NW * 256; i += BLK) (&s_whist[0][0])[i] = 0;
-        __syncthreads();
-        u32 tcnt;
-        if (P == 0) {
-            if (tid == 0) {
-                u32 run = 0;
-                const u64 first = (u64)tile * R;
-                for (u32 r = 0; r < R; r++) {
-                    s_segoff[r] = run;
-                    if ((first + r) * seg_tile < n_ops) run += (u32)s.st_cls[first + r];
-                }
-                s_segoff[R] = run;
-            }
-            __syncthreads();
-            tcnt = s_segoff[R];
-        } else {
-            tcnt = (u32)min((u64)kSortTile, n - (u64)tile * kSortTile);
-        }
+        for (u32 i = tid; i < NW * 256; i += BLK) (&s_cnt[0][0])[i] = 0;
+        const u32 tcnt = (u32)min((u64)kSortTile, n - (u64)tile * kSortTile);
         const u32 lbase = (u32)warp * 32 * SIPT;
         u64 e[SIPT];
-        u32 rank[SIPT];
 #pragma unroll
         for (int k = 0; k < SIPT; k++) {
             const u32 li = lbase + (u32)k * 32 + lane;
-            e[k] = ~0ull;
-            if (li < tcnt) {
-                u64 addr;
-                if (P == 0) {  // locate the region holding local element li
-                    u32 lo = 0, hi = R;
-                    while (hi - lo > 1) {
-                        const u32 mid = (lo + hi) >> 1;
-                        if (s_segoff[mid] <= li) lo = mid;
-                        else hi = mid;
-                    }
-                    addr = ((u64)tile * R + lo) * seg_tile + (li - s_segoff[lo]);
-                } else {
-                    addr = (u64)tile * kSortTile + li;
-                }
-                e[k] = __ldcs(&src[addr]);
-            }
+            e[k] = li < tcnt ? __ldcs(&src[(u64)tile * kSortTile + li]) : ~0ull;
         }
+        __syncthreads();
+        u32 rank[SIPT], old[SIPT], lead[SIPT];
 #pragma unroll
         for (int k = 0; k < SIPT; k++) {
             const bool v = lbase + (u32)k * 32 + lane < tcnt;
-            const u32 d = v ? (u32)(e[k] >> shift) & 255u : 256u;
-            const u32 peers = __match_any_sync(FULL_MASK, d);
-            const u32 before = v ? s_whist[warp][d] : 0u;
-            __syncwarp();
-            if (v && lane == __ffs(peers) - 1) s_whist[warp][d] = (unsigned short)(before + __popc(peers));
-            __syncwarp();
-            rank[k] = before + __popc(peers & lanemask_lt());
-        }
-        __syncthreads();
-        u32 run = 0;
-        if (dt) {
+            const u32 d = (u32)(e[k] >> shift) & 255u;
+            u32 peers = __ballot_sync(FULL_MASK, v);
 #pragma unroll
-            for (int w = 0; w < NW; w++) {
-                u32 c = s_whist[w][tid];
-                s_whist[w][tid] = (unsigned short)run;
-                run += c;
+            for (int bit = 0; bit < 8; bit++) {
+                const u32 m = __ballot_sync(FULL_MASK, (d >> bit) & 1u);
+                peers &= ((d >> bit) & 1u) ? m : ~m;
             }
+            const u32 ld = (u32)__ffs(peers) - 1u;
+            u32 o = 0;
+            if (v && (u32)lane == ld) o = atomicAdd(&s_cnt[warp][d], (u32)__popc(peers));
+            old[k] = o;
+            lead[k] = ld & 31u;
+            rank[k] = __popc(peers & lanemask_lt());
         }
-        // tile-local digit starts: exclusive scan of the tile's digit counts
-        {
+#pragma unroll
+        for (int k = 0; k < SIPT; k++) rank[k] += __shfl_sync(FULL_MASK, old[k], lead[k]);
+        __syncthreads();
+        // thread tid owns digit tid: per-warp offsets, the tile's count, and
+        // its aggregate published before the local scan
+        u32 run = 0;
+#pragma unroll
+        for (int w = 0; w < NW; w++) {
+            const u32 c = s_cnt[w][tid];
+            s_cnt[w][tid] = run;
+            run += c;
+        }
+        u32 *slot = &status[(u64)tile * 256 + tid];
+        st_status32(slot, (tile == 0 ? (2u << 30) : (1u << 30)) | run);
+        {  // tile-local digit starts: exclusive scan of the tile's digit counts
             u32 incl = run;
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
-                u32 v = __shfl_up_sync(FULL_MASK, incl, d);
+                const u32 v = __shfl_up_sync(FULL_MASK, incl, d);
                 if (lane >= d) incl += v;
             }
-            if (dt && lane == 31) s_wsum[warp] = incl;
+            if (lane == 31) s_wsum[warp] = incl;
             __syncthreads();
-            if (dt) {
-                u32 off = 0;
-                for (int i = 0; i < warp; i++) off += s_wsum[i];
-                s_loc[tid] = off + incl - run;
-            }
+            u32 off = 0;
+            for (int i = 0; i < warp; i++) off += s_wsum[i];
+            s_loc[tid] = off + incl - run;
         }
-        // per-digit decoupled look-back (thread tid owns digit tid)
-        if (dt) {
-            u32 excl = 0;
-            u32 *slot = &status[(u64)tile * 256 + tid];
-            if (tile == 0) {
-                st_release32(slot, (2u << 30) | run);
-            } else {
-                st_release32(slot, (1u << 30) | run);
-                long long t = (long long)tile - 1;
-                u64 t0 = gtimer();
-                while (t >= 0) {
-                    u32 st = ld_acquire32(&status[(u64)t * 256 + tid]);
-                    u32 f = st >> 30;
-                    if (f == 0) {
-                        if (gtimer() - t0 > kSpinLimitNs) {
-                            set_err(ctr, LTP_E_TIMEOUT);
-                            break;
-                        }
-                        __nanosleep(64);
-                        continue;
+        // per-digit look-back over windows of WIN predecessors
+        u32 excl = 0;
+        if (tile > 0) {
+            long long t = (long long)tile - 1;
+            const u64 t0 = gtimer();
+            bool done = false;
+            while (!done && t >= 0) {
+                u32 st[WIN];
+#pragma unroll
+                for (int j = 0; j < WIN; j++)
+                    st[j] = t - j >= 0 ? ld_status32(&status[(u64)(t - j) * 256 + tid]) : (2u << 30);
+                int j = 0;
+                for (; j < WIN; j++) {
+                    const u32 f = st[j] >> 30;
+                    if (f == 0) break;
+                    excl += st[j] & 0x3FFFFFFFu;
+                    if (f == 2) {
+                        done = true;
+                        break;
                     }
-                    excl += st & 0x3FFFFFFFu;
-                    if (f == 2) break;
-                    t--;
                 }
-                st_release32(slot, (2u << 30) | (excl + run));
+                if (done) break;
+                t -= j;
+                if (gtimer() - t0 > kSpinLimitNs) {
+                    set_err(ctr, LTP_E_TIMEOUT);
+                    break;
+                }
             }
-            s_base[tid] = s_start[tid] + excl;
+            st_status32(slot, (2u << 30) | (excl + run));
         }
+        s_base[tid] = s_start[tid] + excl;
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < SIPT; k++) {
             if (lbase + (u32)k * 32 + lane < tcnt) {
                 const u32 d = (u32)(e[k] >> shift) & 255u;
-                s_stage[s_loc[d] + s_whist[warp][d] + rank[k]] = e[k];
+                s_stage[s_loc[d] + s_cnt[warp][d] + rank[k]] = e[k];
             }
         }
         __syncthreads();
@@ -732,8 +750,8 @@ __device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, C
 }
 
 template <int P>
-__global__ void __launch_bounds__(kSortBlock) k_sort_pass(Scratch s, Counters *ctr, u64 n_ops, u32 seg_tile) {
-    phase_sort_pass<kSortBlock>(P, s, ctr, n_ops, seg_tile);
+__global__ void __launch_bounds__(kSortBlock, 2) k_sort_pass(Scratch s, Counters *ctr) {
+    phase_sort_pass<kSortBlock>(P, s, ctr);
 }
 
 // ============================================================================
@@ -834,13 +852,13 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
             u32 ef = 0;
             S es = 0;
             if (tile == 0) {
-                st_release(&st[0], kInc | agg);
+                st_status(&st[0], kInc | agg);
             } else {
-                st_release(&st[tile], kAgg | agg);
+                st_status(&st[tile], kAgg | agg);
                 long long t = (long long)tile - 1;
                 u64 t0 = gtimer();
                 while (t >= 0) {
-                    u64 x = ld_acquire(&st[t]);
+                    u64 x = ld_status(&st[t]);
                     u64 fl = x >> 62;
                     if (fl == 0) {
                         if (gtimer() - t0 > kSpinLimitNs) {
@@ -859,7 +877,7 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
                 }
                 u32 incf = af ? 1u : ef;
                 S incs = af ? as : es + as;
-                st_release(&st[tile], kInc | ((u64)incf << 61) | ((u64)incs & kSum61));
+                st_status(&st[tile], kInc | ((u64)incf << 61) | ((u64)incs & kSum61));
             }
             s_tf = ef;
             s_ts = es;
@@ -1065,13 +1083,13 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
             u32 excl = 0;
             u32 *slot = &st[(u64)tile * LTP_MAX_TABLES + t];
             if (tile == 0) {
-                st_release32(slot, (2u << 30) | run);
+                st_status32(slot, (2u << 30) | run);
             } else {
-                st_release32(slot, (1u << 30) | run);
+                st_status32(slot, (1u << 30) | run);
                 long long q = (long long)tile - 1;
                 const u64 t0 = gtimer();
                 while (q >= 0) {
-                    const u32 v = ld_acquire32(&st[(u64)q * LTP_MAX_TABLES + t]);
+                    const u32 v = ld_status32(&st[(u64)q * LTP_MAX_TABLES + t]);
                     const u32 f = v >> 30;
                     if (f == 0) {
                         if (gtimer() - t0 > kSpinLimitNs) {
@@ -1085,7 +1103,7 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
                     if (f == 2) break;
                     q--;
                 }
-                st_release32(slot, (2u << 30) | (excl + run));
+                st_status32(slot, (2u << 30) | (excl + run));
             }
             s_base[t] = (t < T.n ? T.rows_now[t] : 0ull) + excl;
             if (run) atomicAdd(&ctr->ins_committed[t], run);
@@ -1152,8 +1170,12 @@ __device__ __forceinline__ void phase_finish(const BatchDev &b, const TablesDev 
     const int passes = sort_passes_dev(ctr->M);
     if (passes > 0) {
         u32 *st = s.st_sort[(passes - 1) & 1];
-        const u64 t_sort = passes == 1 ? (b.n_ops + kSortTile - 1) / kSortTile + 1 : (nc + kSortTile - 1) / kSortTile;
+        const u64 t_sort = (nc + kSortTile - 1) / kSortTile;
         for (u64 j = g0; j < t_sort * 256; j += gsz) st[j] = 0;
+    }
+    if (rule != LTP_RULE_PRIORITY) {  // classify's look-back slots (any tiling: at most one per kMinTile ops)
+        const u64 t_cls = (b.n_ops + kMinTile - 1) / kMinTile;
+        for (u64 j = g0; j < t_cls; j += gsz) s.st_cls[j] = 0;
     }
     if (rule == LTP_RULE_PRIORITY) {
         u32 c = 0;
@@ -1300,13 +1322,13 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
             sms = L.num_sms;
         }
         const int gsort = capped(gs, (b.n_ops + kSortTile - 1) / kSortTile);
-        k_sort_pass<0><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops, L.tune.block * L.tune.ipt);
+        k_sort_pass<0><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
         mark_ev(4);
-        k_sort_pass<1><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops, L.tune.block * L.tune.ipt);
+        k_sort_pass<1><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
         mark_ev(5);
-        k_sort_pass<2><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops, L.tune.block * L.tune.ipt);
+        k_sort_pass<2><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
         mark_ev(6);
-        k_sort_pass<3><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops, L.tune.block * L.tune.ipt);
+        k_sort_pass<3><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
         mark_ev(7);
         const int gapp = capped(ga, (b.n_ops + kApplyTile - 1) / kApplyTile);
         if (T.any_wide) k_apply<u64><<<gapp, kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
@@ -1403,13 +1425,13 @@ __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
         if (a.rule != LTP_RULE_PRIORITY) {
             phase_classify<kPBlock, kPIpt>(b, a.T, a.s, a.ctr);
             grid_sync(a.bar, nb, a.ctr);
-            phase_sort_pass<kPBlock>(0, a.s, a.ctr, b.n_ops, kPBlock * kPIpt);
+            phase_sort_pass<kPBlock>(0, a.s, a.ctr);
             grid_sync(a.bar, nb, a.ctr);
-            phase_sort_pass<kPBlock>(1, a.s, a.ctr, b.n_ops, kPBlock * kPIpt);
+            phase_sort_pass<kPBlock>(1, a.s, a.ctr);
             grid_sync(a.bar, nb, a.ctr);
-            phase_sort_pass<kPBlock>(2, a.s, a.ctr, b.n_ops, kPBlock * kPIpt);
+            phase_sort_pass<kPBlock>(2, a.s, a.ctr);
             grid_sync(a.bar, nb, a.ctr);
-            phase_sort_pass<kPBlock>(3, a.s, a.ctr, b.n_ops, kPBlock * kPIpt);
+            phase_sort_pass<kPBlock>(3, a.s, a.ctr);
             grid_sync(a.bar, nb, a.ctr);
             if (a.T.any_wide) phase_apply<kPBlock, u64>(b, a.T, a.s, a.ctr);
             else phase_apply<kPBlock, u32>(b, a.T, a.s, a.ctr);
