@@ -94,8 +94,8 @@ struct Counters {
 // scanning, reading and clearing it touches one 16-byte sector per word.
 struct __align__(16) WordState {
     u32 touch;   // cell touched at least once in the batch
-    u32 multi;   // cell touched at least twice
     u32 wbits;   // cell written (RMW) at least once
+    u32 multi;   // cell touched at least twice
     u32 prefix;  // dense id of the word's first contended cell (multi & wbits)
 };
 

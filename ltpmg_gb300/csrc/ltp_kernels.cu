@@ -375,11 +375,19 @@ __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch
 // ============================================================================
 // ids: dense ids of contended cells (touched twice and written)
 // ============================================================================
+// When a batch touches more than a quarter of the conflict words, the ids
+// scan and the clean-up stream over every word in address order instead of
+// visiting the touched-word list in first-touch (random) order.
+__device__ __forceinline__ bool ids_dense(const Scratch &s, const Counters *ctr) {
+    return ctr->n_tw * 4 > s.n_words;
+}
+
 template <bool PRIORITY, int BLK>
 __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, Counters *ctr) {
     constexpr u32 IPT = kIdsTile / BLK;
     if (block_err(ctr)) return;
-    const u64 n = ctr->n_tw;
+    const bool dense = ids_dense(s, ctr);
+    const u64 n = dense ? s.n_words : ctr->n_tw;
     const u32 tiles = (u32)((n + kIdsTile - 1) / kIdsTile);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ u32 s_warp[BLK / 32];
@@ -393,12 +401,13 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
         if (tile >= tiles) break;
         u32 wd[IPT], cw[IPT];
         u32 cnt = 0;
-        // blocked arrangement: thread owns IPT consecutive entries
-        const u64 t0 = (u64)tile * kIdsTile + (u64)threadIdx.x * IPT;
+        // striped arrangement (coalesced loads); a thread's entries get
+        // consecutive ids -- any bijection onto 0..M-1 serves as ids
+        const u64 t0 = (u64)tile * kIdsTile + threadIdx.x;
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
-            u64 j = t0 + k;
-            wd[k] = j < n ? s.tw_list[j] : 0u;
+            u64 j = t0 + (u64)k * BLK;
+            wd[k] = j < n ? (dense ? (u32)j : s.tw_list[j]) : 0u;
             if (j < n) {
                 const uint4 v = *reinterpret_cast<const uint4 *>(&s.words[wd[k]]);
                 cw[k] = v.y & v.z;
@@ -431,7 +440,7 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
         u64 pre = s_prefix + s_warp[warp] + (incl - cnt);
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
-            u64 j = t0 + k;
+            u64 j = t0 + (u64)k * BLK;
             if (j < n) {
                 s.words[wd[k]].prefix = (u32)pre;
                 u32 bits = cw[k];
@@ -520,11 +529,8 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
             const u32 bal = __ballot_sync(FULL_MASK, con[k]);
             lpos[k] = wcnt + __popc(bal & lanemask_lt());
             wcnt += __popc(bal);
-            for (int p = 0; p < passes; p++) {  // digit histograms for the radix sort
-                const u32 d = con[k] ? (m >> (8 * p)) & 255u : 256u;
-                const u32 peers = __match_any_sync(FULL_MASK, d);
-                if (con[k] && lane == __ffs(peers) - 1) atomicAdd(&s_hist[p][d], (u32)__popc(peers));
-            }
+            if (con[k])  // digit histograms for the radix sort
+                for (int p = 0; p < passes; p++) atomicAdd(&s_hist[p][(m >> (8 * p)) & 255u], 1u);
         }
         if (lane == 0) s_wcnt[warp] = wcnt;
         __syncthreads();
@@ -797,13 +803,23 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
         }
         u32 cf = 0;
         S cs = 0;  // running carry within the warp
+        // the warp's neighbours outside its own 32 x AIPT run
+        const u64 before_w = (lane == 0 && wbase > 0 && wbase - 1 < n) ? list[wbase - 1] : ~0ull;
+        const u64 wend = wbase + 32ull * AIPT;
+        const u64 after_w = (lane == 31 && wend < n) ? list[wend] : ~0ull;
 #pragma unroll
         for (int k = 0; k < AIPT; k++) {
             const u64 i = wbase + (u64)k * 32 + lane;
             const bool v = i < n;
             const u32 m = (u32)(e[k] >> 32);
-            const u64 prev = (v && i > 0) ? list[i - 1] : ~0ull;
-            const u64 next = (v && i + 1 < n) ? list[i + 1] : ~0ull;
+            // element i - 1 is lane - 1 of this row, or lane 31 of the previous row
+            u64 prev = __shfl_up_sync(FULL_MASK, e[k], 1);
+            const u64 prev_row = __shfl_sync(FULL_MASK, k > 0 ? e[k > 0 ? k - 1 : 0] : before_w, k > 0 ? 31 : 0);
+            if (lane == 0) prev = prev_row;
+            u64 next = __shfl_down_sync(FULL_MASK, e[k], 1);
+            const u64 next_row = __shfl_sync(FULL_MASK, k + 1 < (int)AIPT ? e[k + 1 < (int)AIPT ? k + 1 : k] : after_w,
+                                             k + 1 < (int)AIPT ? 0 : 31);
+            if (lane == 31) next = next_row;
             const bool head = v && (i == 0 || (u32)(prev >> 32) != m);
             tail[k] = v && (i + 1 == n || (u32)(next >> 32) != m);
             S val = 0;
@@ -856,24 +872,29 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
             } else {
                 st_status(&st[tile], kAgg | agg);
                 long long t = (long long)tile - 1;
-                u64 t0 = gtimer();
-                while (t >= 0) {
-                    u64 x = ld_status(&st[t]);
-                    u64 fl = x >> 62;
-                    if (fl == 0) {
-                        if (gtimer() - t0 > kSpinLimitNs) {
-                            set_err(ctr, LTP_E_TIMEOUT);
+                const u64 t0 = gtimer();
+                for (;;) {  // four predecessors per round trip
+                    u64 x[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) x[j] = t - j >= 0 ? ld_status(&st[t - j]) : kInc;
+                    bool stop = false;
+                    int j = 0;
+                    for (; j < 4; j++) {
+                        const u64 fl = x[j] >> 62;
+                        if (fl == 0) break;
+                        es += unpack_sum<S>(x[j]);
+                        ef = (u32)((x[j] >> 61) & 1ull);
+                        if (fl == 2 || ef) {
+                            stop = true;
                             break;
                         }
-                        __nanosleep(64);
-                        continue;
                     }
-                    if (!ef) {
-                        es += unpack_sum<S>(x);
-                        ef = (u32)((x >> 61) & 1ull);
+                    if (stop) break;
+                    t -= j;
+                    if (gtimer() - t0 > kSpinLimitNs) {
+                        set_err(ctr, LTP_E_TIMEOUT);
+                        break;
                     }
-                    if (fl == 2 || ef) break;
-                    t--;
                 }
                 u32 incf = af ? 1u : ef;
                 S incs = af ? as : es + as;
@@ -1159,10 +1180,14 @@ __device__ __forceinline__ void phase_finish(const BatchDev &b, const TablesDev 
         for (u64 j = g0; j < t_ins * LTP_MAX_TABLES; j += gsz) s.st_ins[j] = 0;
     }
     const u64 ntw = ctr->n_tw;
-    for (u64 j = g0; j < ntw; j += gsz) {
-        *reinterpret_cast<uint4 *>(&s.words[s.tw_list[j]]) = make_uint4(0, 0, 0, 0);
+    const bool dense = ids_dense(s, ctr);
+    if (dense) {
+        for (u64 j = g0; j < s.n_words; j += gsz) *reinterpret_cast<uint4 *>(&s.words[j]) = make_uint4(0, 0, 0, 0);
+    } else {
+        for (u64 j = g0; j < ntw; j += gsz)
+            *reinterpret_cast<uint4 *>(&s.words[s.tw_list[j]]) = make_uint4(0, 0, 0, 0);
     }
-    const u64 t_ids = (ntw + kIdsTile - 1) / kIdsTile;
+    const u64 t_ids = ((dense ? s.n_words : ntw) + kIdsTile - 1) / kIdsTile;
     for (u64 j = g0; j < t_ids; j += gsz) s.st_ids[j] = 0;
     const u64 nc = ctr->n_c;
     const u64 t_apply = (nc + kApplyTile - 1) / kApplyTile;
