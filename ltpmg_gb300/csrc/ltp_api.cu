@@ -493,6 +493,7 @@ int ltp_batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *
 int ltp_batch_load_payload(ltp_ctx *ctx, ltp_batch *b, const int32_t *payload, uint64_t n, void *stream) {
     if (!ctx || !b || (n && !payload)) return LTP_E_BADARG;
     if (!b->loaded) return fail(ctx, LTP_E_STATE, "load the batch before its payload");
+    if (n >= (1ull << 32)) return fail(ctx, LTP_E_CAPACITY, "a payload holds fewer than 2^32 slots");
     CK(cudaSetDevice(ctx->device));
     cudaStream_t st = pick_stream(ctx, stream);
     if (n > b->payload_cap) {

@@ -35,6 +35,10 @@ namespace ltp {
 
 constexpr u64 kSpinLimitNs = 2000000000ull;  // 2 s per wait
 
+// The dynamic shared memory of every kernel: the mark phase's tile hash and
+// the insert phase's staging use it in turn.
+extern __shared__ __align__(16) u32 ltp_dyn_smem[];
+
 __device__ __forceinline__ u64 gtimer() {
     u64 t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -254,7 +258,7 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
     if (block_err(ctr)) return;
     constexpr u32 TILE = (u32)BLOCK * IPT;
     constexpr u32 H = 2 * TILE;  // at most TILE distinct words: load factor <= 1/2
-    extern __shared__ u32 mark_smem[];  // 4 * H words (dynamic: up to 128 KB)
+    u32 *mark_smem = ltp_dyn_smem;  // 4 * H words (dynamic: up to 128 KB)
     u32 *hk = mark_smem, *ht = hk + H, *hd = ht + H, *hw = hd + H;
     __shared__ u32 s_ins[LTP_MAX_TABLES];  // insert ops of the tile per table
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1063,6 +1067,11 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ u32 s_wcnt[NW][LTP_MAX_TABLES];
     __shared__ u64 s_base[LTP_MAX_TABLES];
+    __shared__ u32 s_tcnt[LTP_MAX_TABLES], s_toff[LTP_MAX_TABLES];
+    // staging of the tile's inserts in the dynamic shared memory (kInsSmem bytes)
+    u32 *s_off = ltp_dyn_smem;                                                  // [kInsTile] payload offsets
+    long long *s_lv = reinterpret_cast<long long *>(ltp_dyn_smem + kInsTile);  // [kInsTile] link values
+    unsigned char *s_lc = reinterpret_cast<unsigned char *>(s_lv + kInsTile);  // [kInsTile] link columns
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_INSERT);
         if (tile >= tiles) break;
@@ -1117,7 +1126,6 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
                             set_err(ctr, LTP_E_TIMEOUT);
                             break;
                         }
-                        __nanosleep(64);
                         continue;
                     }
                     excl += v & 0x3FFFFFFFu;
@@ -1127,35 +1135,52 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
                 st_status32(slot, (2u << 30) | (excl + run));
             }
             s_base[t] = (t < T.n ? T.rows_now[t] : 0ull) + excl;
+            s_tcnt[t] = run;
             if (run) atomicAdd(&ctr->ins_committed[t], run);
         }
         __syncthreads();
+        if (threadIdx.x == 0) {  // the tile's inserts, grouped by table, in rank order
+            u32 run = 0;
+            for (int t = 0; t < LTP_MAX_TABLES; t++) {
+                s_toff[t] = run;
+                run += s_tcnt[t];
+            }
+        }
+        __syncthreads();
+        // every insert notes its payload row and link; its output is its row id
 #pragma unroll
         for (int k = 0; k < IIPT; k++) {
             if (tb[k] < LTP_MAX_TABLES) {
                 const u64 i = wbase + (u64)k * 32 + lane;
-                const TableDev &t = T.t[tb[k]];
-                const u64 row = s_base[tb[k]] + s_wcnt[warp][tb[k]] + lrank[k];
-                const int32_t *src = b.payload + b.keys[i];
+                const u32 r = s_wcnt[warp][tb[k]] + lrank[k];
+                const u32 e = s_toff[tb[k]] + r;
                 const u32 w = b.opw[i];
-                const u32 d = insert_link(w), lc = d ? opw_col(w) : LTP_MAX_COLS;
-                long long lv = 0;
-                if (d) lv = b.out64 ? b.out64[i - d] : (long long)b.out[i - d];
-                if (!t.wide) {
-                    for (u32 c = 0; c < t.n_cols; c++)
-                        reinterpret_cast<int32_t *>(t.data)[(u64)c * t.rows_cap + row] = c == lc ? (int32_t)lv : src[c];
-                } else {
-                    u32 slot = 0;
-                    for (u32 c = 0; c < t.n_cols; c++) {
-                        const bool wc = col_wide(t, c);
-                        long long v = wc ? (long long)(((u64)(u32)src[slot + 1] << 32) | (u64)(u32)src[slot])
-                                         : (long long)src[slot];
-                        slot += wc ? 2 : 1;
-                        if (c == lc) v = lv;
-                        store_cell(t.data + col_off(t, c) + row * (wc ? 8ull : 4ull), wc, v);
-                    }
+                const u32 d = insert_link(w);
+                s_off[e] = (u32)b.keys[i];
+                s_lc[e] = d ? (unsigned char)opw_col(w) : (unsigned char)0xFF;
+                s_lv[e] = d ? (b.out64 ? b.out64[i - d] : (long long)b.out[i - d]) : 0ll;
+                store_out(b, i, (long long)(s_base[tb[k]] + r));
+            }
+        }
+        __syncthreads();
+        // column by column, consecutive threads store consecutive rows
+        for (u32 t = 0; t < T.n; t++) {
+            const u32 cnt = s_tcnt[t];
+            if (!cnt) continue;
+            const TableDev &tab = T.t[t];
+            const u64 row0 = s_base[t];
+            u32 slot = 0;
+            for (u32 c = 0; c < tab.n_cols; c++) {
+                const bool wc = col_wide(tab, c);
+                char *col = tab.data + col_off(tab, c);
+                for (u32 j = threadIdx.x; j < cnt; j += BLK) {
+                    const u32 e = s_toff[t] + j;
+                    const int32_t *src = b.payload + s_off[e] + slot;
+                    long long v = wc ? (long long)(((u64)(u32)src[1] << 32) | (u64)(u32)src[0]) : (long long)src[0];
+                    if (s_lc[e] == c) v = s_lv[e];
+                    store_cell(col + (row0 + j) * (wc ? 8ull : 4ull), wc, v);
                 }
-                store_out(b, i, (long long)row);
+                slot += wc ? 2 : 1;
             }
         }
         __syncthreads();
@@ -1370,10 +1395,10 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
     {
         static int gins = 0, sms = 0;
         if (sms != L.num_sms) {
-            gins = occ_grid(k_insert, kInsBlock, L.num_sms);
+            gins = occ_grid(k_insert, kInsBlock, L.num_sms, kInsSmem);
             sms = L.num_sms;
         }
-        k_insert<<<capped(gins, (b.n_ops + kInsTile - 1) / kInsTile), kInsBlock, 0, L.stream>>>(b, T, s, ctr);
+        k_insert<<<capped(gins, (b.n_ops + kInsTile - 1) / kInsTile), kInsBlock, kInsSmem, L.stream>>>(b, T, s, ctr);
     }
     mark_ev(9);
     k_finish<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr, L.rule);
@@ -1426,6 +1451,10 @@ struct PersistArgs {
 };
 
 constexpr int kPBlock = 256, kPIpt = 4;
+// dynamic shared memory of the persistent kernel: the larger of the mark
+// phase's hash (4 arrays of 2 x tile words) and the insert staging
+constexpr size_t kPersistSmem = 4ull * 2 * kPBlock * kPIpt * sizeof(u32) > kInsSmem
+                                    ? 4ull * 2 * kPBlock * kPIpt * sizeof(u32) : (size_t)kInsSmem;
 
 __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
     const u32 nb = gridDim.x;
@@ -1485,7 +1514,7 @@ __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
 cudaError_t launch_persistent(cudaStream_t st, int num_sms, int rule, const BatchDev *d_batches,
                               Counters *const *d_snaps, u32 n_batches, const TablesDev &T, const Scratch &s,
                               Counters *ctr, u32 *bar) {
-    constexpr size_t smem = 4ull * 2 * kPBlock * kPIpt * sizeof(u32);
+    constexpr size_t smem = kPersistSmem;
     static int grid = 0, sms = 0;
     if (sms != num_sms) {
         cudaError_t fe = cudaFuncSetAttribute(k_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1510,7 +1539,7 @@ cudaError_t launch_persistent(cudaStream_t st, int num_sms, int rule, const Batc
 }
 
 int persistent_grid(int num_sms) {
-    constexpr size_t smem = 4ull * 2 * kPBlock * kPIpt * sizeof(u32);
+    constexpr size_t smem = kPersistSmem;
     cudaFuncSetAttribute(k_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     return occ_grid(k_persist, kPBlock, num_sms, smem);
 }
