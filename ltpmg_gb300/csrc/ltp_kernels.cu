@@ -477,6 +477,17 @@ __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Count
 // Radix passes over the contended ids: 8 bits each, at least one pass as soon
 // as there is a contended cell (the first pass also gathers the per-tile
 // regions written by classify into one dense list).
+// Contended-op records.  Packed (fewer than 2^20 contended cells and at most
+// 2^24 ops): id << 44 | imm20 << 24 | op -- the RMW immediate travels with
+// the record (a read carries 0, which is what it adds).  Otherwise:
+// id << 32 | rmw << 31 | op, and the immediate is read from the opword.
+__device__ __forceinline__ bool rec_packed(u32 M, u64 n_ops) { return M < (1u << 20) && n_ops <= (1ull << 24); }
+__device__ __forceinline__ int rec_shift(bool packed) { return packed ? 44 : 32; }
+__device__ __forceinline__ u32 rec_id(u64 e, bool packed) { return (u32)(e >> rec_shift(packed)); }
+__device__ __forceinline__ u32 rec_op(u64 e, bool packed) {
+    return packed ? (u32)e & 0xFFFFFFu : (u32)e & 0x7FFFFFFFu;
+}
+
 __device__ __forceinline__ int sort_passes_dev(u32 M) {
     if (M == 0) return 0;
     const int bits = M == 1 ? 1 : 32 - __clz(M - 1);
@@ -492,6 +503,7 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
     const u32 tiles = (u32)((n + TILE - 1) / TILE);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int passes = sort_passes_dev(ctr->M);
+    const bool packed = rec_packed(ctr->M, n);
     __shared__ u32 s_wcnt[NW];
     __shared__ u32 s_run;
     __shared__ u64 s_pbase;
@@ -529,7 +541,10 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
             const u64 i = wbase + (u64)k * 32 + lane;
             con[k] = r[k].valid && (cw & bit);
             const u32 m = ws[k].w + __popc(cw & (bit - 1u));
-            rec[k] = ((u64)m << 32) | ((u64)(opw_kind(w[k]) == LTP_OP_ADD) << 31) | (u64)(u32)i;
+            rec[k] = packed ? ((u64)m << 44) |
+                                  ((u64)(opw_kind(w[k]) == LTP_OP_ADD ? ((u32)opw_imm(w[k]) & 0xFFFFFu) : 0u) << 24) |
+                                  (u64)(u32)i
+                            : ((u64)m << 32) | ((u64)(opw_kind(w[k]) == LTP_OP_ADD) << 31) | (u64)(u32)i;
             const u32 bal = __ballot_sync(FULL_MASK, con[k]);
             lpos[k] = wcnt + __popc(bal & lanemask_lt());
             wcnt += __popc(bal);
@@ -610,7 +625,7 @@ __global__ void __launch_bounds__(BLOCK, 65536 / (BLOCK * (IPT <= 4 ? 64 : 128))
 // predecessor tiles with relaxed loads, shared-memory staging so every
 // digit's run leaves as coalesced stores.
 template <int BLK>
-__device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, Counters *ctr) {
+__device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, Counters *ctr, u64 n_ops) {
     static_assert(BLK == 256, "one thread per radix digit");
     constexpr u32 SIPT = kSortTile / BLK;
     constexpr int WIN = 8;
@@ -651,7 +666,7 @@ __device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, C
         s_start[tid] = off + incl - h;
         __syncthreads();
     }
-    const int shift = 32 + 8 * P;
+    const int shift = rec_shift(rec_packed(ctr->M, n_ops)) + 8 * P;
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_SORT0 + P);
         if (tile >= tiles) break;
@@ -760,8 +775,8 @@ __device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, C
 }
 
 template <int P>
-__global__ void __launch_bounds__(kSortBlock, 2) k_sort_pass(Scratch s, Counters *ctr) {
-    phase_sort_pass<kSortBlock>(P, s, ctr);
+__global__ void __launch_bounds__(kSortBlock, 2) k_sort_pass(Scratch s, Counters *ctr, u64 n_ops) {
+    phase_sort_pass<kSortBlock>(P, s, ctr, n_ops);
 }
 
 // ============================================================================
@@ -786,6 +801,7 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
     const u64 n = ctr->n_c;
     const u32 tiles = (u32)((n + kApplyTile - 1) / kApplyTile);
     const u64 *list = s.list[sort_passes_dev(ctr->M) & 1];
+    const bool packed = rec_packed(ctr->M, b.n_ops);
     constexpr int NW = BLK / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ u32 s_wf[NW];
@@ -803,7 +819,7 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
 #pragma unroll
         for (int k = 0; k < AIPT; k++) {
             u64 i = wbase + (u64)k * 32 + lane;
-            e[k] = i < n ? list[i] : ~0ull;
+            e[k] = i < n ? __ldcs(&list[i]) : ~0ull;
         }
         u32 cf = 0;
         S cs = 0;  // running carry within the warp
@@ -815,7 +831,7 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
         for (int k = 0; k < AIPT; k++) {
             const u64 i = wbase + (u64)k * 32 + lane;
             const bool v = i < n;
-            const u32 m = (u32)(e[k] >> 32);
+            const u32 m = rec_id(e[k], packed);
             // element i - 1 is lane - 1 of this row, or lane 31 of the previous row
             u64 prev = __shfl_up_sync(FULL_MASK, e[k], 1);
             const u64 prev_row = __shfl_sync(FULL_MASK, k > 0 ? e[k > 0 ? k - 1 : 0] : before_w, k > 0 ? 31 : 0);
@@ -824,10 +840,13 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
             const u64 next_row = __shfl_sync(FULL_MASK, k + 1 < (int)AIPT ? e[k + 1 < (int)AIPT ? k + 1 : k] : after_w,
                                              k + 1 < (int)AIPT ? 0 : 31);
             if (lane == 31) next = next_row;
-            const bool head = v && (i == 0 || (u32)(prev >> 32) != m);
-            tail[k] = v && (i + 1 == n || (u32)(next >> 32) != m);
+            const bool head = v && (i == 0 || rec_id(prev, packed) != m);
+            tail[k] = v && (i + 1 == n || rec_id(next, packed) != m);
             S val = 0;
-            if (v && ((e[k] >> 31) & 1ull)) val = (S)(long long)opw_imm(__ldg(&b.opw[(u32)e[k] & 0x7FFFFFFFu]));
+            if (v) {
+                if (packed) val = (S)(long long)(((int)((u32)(e[k] >> 24) << 12)) >> 12);  // sign-extend 20 bits
+                else if ((e[k] >> 31) & 1ull) val = (S)(long long)opw_imm(__ldg(&b.opw[(u32)e[k] & 0x7FFFFFFFu]));
+            }
             u32 f = head ? 1u : 0u;
             S sum = val;
 #pragma unroll
@@ -916,9 +935,9 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
         for (int k = 0; k < AIPT; k++) {
             const u64 i = wbase + (u64)k * 32 + lane;
             if (i < n) {
-                const u32 m = (u32)(e[k] >> 32);
+                const u32 m = rec_id(e[k], packed);
                 const S tot = sf[k] ? sv[k] : sv[k] + carry;
-                const u32 op = (u32)e[k] & 0x7FFFFFFFu;
+                const u32 op = rec_op(e[k], packed);
                 if (!WIDE) {
                     const int32_t val = (int32_t)((u32)__ldg(&s.dbase[m]) + (u32)tot);
                     b.out[op] = val;
@@ -1372,13 +1391,13 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
             sms = L.num_sms;
         }
         const int gsort = capped(gs, (b.n_ops + kSortTile - 1) / kSortTile);
-        k_sort_pass<0><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        k_sort_pass<0><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
         mark_ev(4);
-        k_sort_pass<1><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        k_sort_pass<1><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
         mark_ev(5);
-        k_sort_pass<2><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        k_sort_pass<2><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
         mark_ev(6);
-        k_sort_pass<3><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr);
+        k_sort_pass<3><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
         mark_ev(7);
         const int gapp = capped(ga, (b.n_ops + kApplyTile - 1) / kApplyTile);
         if (T.any_wide) k_apply<u64><<<gapp, kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
@@ -1479,13 +1498,13 @@ __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
         if (a.rule != LTP_RULE_PRIORITY) {
             phase_classify<kPBlock, kPIpt>(b, a.T, a.s, a.ctr);
             grid_sync(a.bar, nb, a.ctr);
-            phase_sort_pass<kPBlock>(0, a.s, a.ctr);
+            phase_sort_pass<kPBlock>(0, a.s, a.ctr, b.n_ops);
             grid_sync(a.bar, nb, a.ctr);
-            phase_sort_pass<kPBlock>(1, a.s, a.ctr);
+            phase_sort_pass<kPBlock>(1, a.s, a.ctr, b.n_ops);
             grid_sync(a.bar, nb, a.ctr);
-            phase_sort_pass<kPBlock>(2, a.s, a.ctr);
+            phase_sort_pass<kPBlock>(2, a.s, a.ctr, b.n_ops);
             grid_sync(a.bar, nb, a.ctr);
-            phase_sort_pass<kPBlock>(3, a.s, a.ctr);
+            phase_sort_pass<kPBlock>(3, a.s, a.ctr, b.n_ops);
             grid_sync(a.bar, nb, a.ctr);
             if (a.T.any_wide) phase_apply<kPBlock, u64>(b, a.T, a.s, a.ctr);
             else phase_apply<kPBlock, u32>(b, a.T, a.s, a.ctr);
