@@ -180,6 +180,41 @@ __device__ __forceinline__ OpRef decode_op(const TablesDev &T, u64 key, u32 w) {
 
 // Cell values are handled as 64-bit; int32 cells are sign-extended on load and
 // truncated on store, which is exactly 32-bit two's-complement arithmetic.
+// ---- L2 eviction-priority hints ---------------------------------------------
+// Conflict words are re-read by later kernels of the batch: keep them in L2.
+// Uncontended table cells are touched once: let them leave L2 first.
+__device__ __forceinline__ u64 pol_evict_last() {
+    u64 p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ u64 pol_evict_first() {
+    u64 p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint4 ld_word_hint(const void *ptr, u64 pol) {
+    uint4 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(ptr), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ long long load_cell_hint(const char *p, bool wide, u64 pol) {
+    if (wide) {
+        long long v;
+        asm volatile("ld.global.L2::cache_hint.b64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(pol) : "memory");
+        return v;
+    }
+    int v;
+    asm volatile("ld.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol) : "memory");
+    return (long long)v;
+}
+__device__ __forceinline__ void store_cell_hint(char *p, bool wide, long long v, u64 pol) {
+    if (wide) asm volatile("st.global.L2::cache_hint.b64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
+    else asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(p), "r"((int)v), "l"(pol) : "memory");
+}
+
 __device__ __forceinline__ long long load_cell(const char *p, bool wide) {
     return wide ? *reinterpret_cast<const long long *>(p) : (long long)*reinterpret_cast<const int32_t *>(p);
 }
@@ -504,6 +539,7 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int passes = sort_passes_dev(ctr->M);
     const bool packed = rec_packed(ctr->M, n);
+    const u64 pol_keep = pol_evict_last(), pol_once = pol_evict_first();
     __shared__ u32 s_wcnt[NW];
     __shared__ u32 s_run;
     __shared__ u64 s_pbase;
@@ -529,7 +565,7 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
             u64 i = wbase + (u64)k * 32 + lane;
             r[k] = decode_op(T, key[k], w[k]);
             r[k].valid = r[k].valid && i < n;
-            ws[k] = r[k].valid ? __ldg(reinterpret_cast<const uint4 *>(&s.words[r[k].cell >> 5])) : make_uint4(0, 0, 0, 0);
+            ws[k] = r[k].valid ? ld_word_hint(&s.words[r[k].cell >> 5], pol_keep) : make_uint4(0, 0, 0, 0);
         }
         u64 rec[IPT];
         u32 wcnt = 0, lpos[IPT];
@@ -573,7 +609,7 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
 #pragma unroll
         for (int k = 0; k < IPT; k++)
             if (r[k].valid && !con[k])
-                val[k] = opw_kind(w[k]) == LTP_OP_ADD ? load_cell(r[k].ptr, r[k].wide) : load_cell_ro(r[k].ptr, r[k].wide);
+                val[k] = load_cell_hint(r[k].ptr, r[k].wide, pol_once);
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             if (r[k].valid && !con[k]) {
@@ -581,7 +617,7 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
                 if (opw_kind(w[k]) == LTP_OP_ADD) {
                     v = (long long)((u64)v + (u64)(long long)opw_imm(w[k]));
                     if (!r[k].wide) v = (int32_t)v;  // int32 cells wrap at 32 bits
-                    store_cell(r[k].ptr, r[k].wide, v);
+                    store_cell_hint(r[k].ptr, r[k].wide, v, pol_once);
                 }
                 const u64 i = wbase + (u64)k * 32 + lane;
                 __stcs(&b.out[i], (int32_t)v);
