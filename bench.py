@@ -401,7 +401,8 @@ def run_ours(args, config):
             "config": {"workload": WORKLOAD_TEXT[config], "batches_per_step": nb, "txns_per_step": txns_per_step,
                        "rule": "ordered (ascending TID per cell, all commit)", "mode": mode_name,
                        "mode_ms": {str(k): v for k, v in mode_ms.items()},
-                       "tuning": {str(k): f"{v['block']}x{v['ipt']}" for k, v in tiles.items()},
+                       "tuning": {str(k): f"{v['block']}x{v['ipt']}" + ("+precheck" if v.get("flags") else "")
+                                  for k, v in tiles.items()},
                        "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
             "gpu_launches": launches, "roofline": roof, "clocks": clk, "e2e": e2e,
             "contention": {"contended_ops_per_batch": mean_stats["contended_ops"],
@@ -414,12 +415,16 @@ def run_ours(args, config):
 def fixed_tiles(ctx, dev, spec):
     from ltpmg_gb300 import autotune as AT
 
-    blk, ipt = (int(x) for x in spec.split("x"))
+    import ltpmg_gb300 as G
+
+    base, _, opt = spec.partition("+")
+    blk, ipt = (int(x) for x in base.split("x"))
+    flags = G.lib.TUNE_MARK_PRECHECK if opt == "precheck" else 0
     out = {}
     for b in dev:
         k = AT.bucket_of(b.n_ops)
-        ctx.set_tuning(k, blk, ipt)
-        out[k] = {"block": blk, "ipt": ipt}
+        ctx.set_tuning(k, blk, ipt, flags=flags)
+        out[k] = {"block": blk, "ipt": ipt, "flags": flags}
     return out
 
 
@@ -621,7 +626,8 @@ def run_tpcc(args):
             "config": {"workload": WORKLOAD_TEXT["tpcc"], "batches_per_step": nb, "txns_per_step": txns_per_step,
                        "ops_per_step": ops_per_step, "rule": "ordered (ascending TID per cell, all commit)",
                        "mode": mode_name, "mode_ms": {str(k): v for k, v in mode_ms.items()},
-                       "tuning": {str(k): f"{v['block']}x{v['ipt']}" for k, v in tiles.items()},
+                       "tuning": {str(k): f"{v['block']}x{v['ipt']}" + ("+precheck" if v.get("flags") else "")
+                                  for k, v in tiles.items()},
                        "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
             "gpu_launches": launches, "roofline": roof, "clocks": clk, "e2e": e2e,
             "contention": {"contended_ops_per_batch": mean_stats["contended_ops"],
@@ -778,7 +784,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batches", type=int, default=0, help="resident batches (default: the config's)")
     ap.add_argument("--tuning-out", default="", help="write the autotuner's choices to this JSON file")
-    ap.add_argument("--tiles", default="", help="fixed BLOCKxIPT tiling instead of the autotuner's (e.g. 512x4)")
+    ap.add_argument("--tiles", default="",
+                    help="fixed BLOCKxIPT[+precheck] tiling instead of the autotuner's (e.g. 512x4)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     args = ap.parse_args()

@@ -407,9 +407,14 @@ int ltp_tpcc_gen(const ltp_tpcc *g, uint64_t batch, uint64_t n_txns, uint32_t *t
 typedef struct {
     uint32_t block;      /* threads per block of the streaming kernels: 128, 256, 512 */
     uint32_t ipt;        /* ops per thread per tile: 1, 2, 4, 8 */
-    uint32_t word_bits;  /* bitmap word granularity: 32 or 64 */
-    uint32_t reserved;
+    uint32_t word_bits;  /* conflict-word granularity: 32 cells (the only one built) */
+    uint32_t flags;      /* LTP_TUNE_* */
 } ltp_tuning;
+/* The mark kernel reads a conflict word it touched more than once in a tile
+ * before its atomics and skips those whose bits are already set: a win when
+ * a few words are hot in every tile (order-entry warehouse and district
+ * rows), a loss when repeated words are still filling up (Zipf tails). */
+#define LTP_TUNE_MARK_PRECHECK 1u
 /* Tuning used for batches whose op count falls in size bucket floor(log2(ops)). */
 int ltp_set_tuning(ltp_ctx *ctx, uint32_t bucket, const ltp_tuning *t);
 int ltp_get_tuning(ltp_ctx *ctx, uint32_t bucket, ltp_tuning *t);

@@ -56,8 +56,14 @@ def tune_tiles(ctx, batch, reps=3, blocks=BLOCKS, ipts=IPTS):
             results[f"{blk}x{ipt}"] = _time_batch(ctx, batch, reps)
     best = min(results, key=results.get)
     blk, ipt = (int(x) for x in best.split("x"))
-    ctx.set_tuning(bucket, blk, ipt)
-    return {"bucket": bucket, "block": blk, "ipt": ipt, "ms": results[best], "candidates": results}
+    # then, for the best tiling, the mark kernel's hot-word pre-check
+    ctx.set_tuning(bucket, blk, ipt, flags=L.TUNE_MARK_PRECHECK)
+    pre_ms = _time_batch(ctx, batch, reps)
+    results[f"{blk}x{ipt}+precheck"] = pre_ms
+    flags = L.TUNE_MARK_PRECHECK if pre_ms < results[best] else 0
+    ctx.set_tuning(bucket, blk, ipt, flags=flags)
+    return {"bucket": bucket, "block": blk, "ipt": ipt, "flags": flags, "ms": min(results[best], pre_ms),
+            "candidates": results}
 
 
 def tune_mode(ctx, batches, reps=2, modes=(L.MODE_GRAPH, L.MODE_PERSISTENT)):
@@ -94,7 +100,8 @@ def tune_buckets(ctx, batches, reps=3):
 
 
 def save(path, choices, mode=None):
-    doc = {"buckets": {str(k): {"block": v["block"], "ipt": v["ipt"], "ms": v["ms"]} for k, v in choices.items()},
+    doc = {"buckets": {str(k): {"block": v["block"], "ipt": v["ipt"], "flags": v.get("flags", 0), "ms": v["ms"]}
+                       for k, v in choices.items()},
            "mode": mode, "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
     with open(path, "w") as f:
         json.dump(doc, f, indent=1)
@@ -104,5 +111,5 @@ def load(ctx, path):
     """Applies a saved tuning file to a context; returns its multi-batch mode."""
     doc = json.load(open(path))
     for k, v in doc["buckets"].items():
-        ctx.set_tuning(int(k), int(v["block"]), int(v["ipt"]))
+        ctx.set_tuning(int(k), int(v["block"]), int(v["ipt"]), flags=int(v.get("flags", 0)))
     return doc.get("mode")

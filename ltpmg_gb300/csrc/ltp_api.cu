@@ -226,7 +226,7 @@ int ltp_init(const ltp_config *cfg, ltp_ctx **out) {
     ctx->rule = cfg->rule;
     ctx->flags = cfg->flags;
     memset(&ctx->s, 0, sizeof(ctx->s));
-    for (int i = 0; i < 64; i++) ctx->tuning[i] = Tuning{512, 4, 32};
+    for (int i = 0; i < 64; i++) ctx->tuning[i] = Tuning{512, 4, 32, 0};
     cudaError_t e = cudaSetDevice(cfg->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, cfg->device);
     // random 4-16 byte gathers dominate: fetch 32-byte sectors, not 64-byte pairs
@@ -525,7 +525,7 @@ BatchDev batch_dev(const ltp_batch *b) {
     bd.n_ops = b->n_ops;
     bd.n_txns = b->n_txns;
     bd.ops_per_txn = b->ops_per_txn;
-    bd.pad = 0;
+    bd.flags = 0;
     bd.payload = b->payload;
     bd.payload_len = b->payload_len;
     return bd;
@@ -651,6 +651,7 @@ int ltp_batches_execute(ltp_ctx *ctx, ltp_batch *const *batches, uint32_t n, int
     std::vector<Counters *> hs(n);
     for (uint32_t i = 0; i < n; i++) {
         hb[i] = batch_dev(batches[i]);
+        hb[i].flags = ctx->tuning[bucket_of(batches[i]->n_ops)].flags;
         hs[i] = batches[i]->snap;
     }
     CK(cudaMemcpyAsync(ctx->p_batches, hb.data(), n * sizeof(BatchDev), cudaMemcpyHostToDevice, st));
@@ -768,8 +769,9 @@ int ltp_set_tuning(ltp_ctx *ctx, uint32_t bucket, const ltp_tuning *t) {
     if (!ctx || !t || bucket >= 64) return LTP_E_BADARG;
     if (t->block != 128 && t->block != 256 && t->block != 512) return fail(ctx, LTP_E_BADARG, "block must be 128/256/512");
     if (t->ipt != 1 && t->ipt != 2 && t->ipt != 4 && t->ipt != 8) return fail(ctx, LTP_E_BADARG, "ipt must be 1/2/4/8");
-    if (t->word_bits != 32 && t->word_bits != 64) return fail(ctx, LTP_E_BADARG, "word_bits must be 32/64");
-    ctx->tuning[bucket] = Tuning{t->block, t->ipt, t->word_bits};
+    if (t->word_bits != 32) return fail(ctx, LTP_E_BADARG, "word_bits must be 32 (32-cell conflict words)");
+    if (t->flags & ~LTP_TUNE_MARK_PRECHECK) return fail(ctx, LTP_E_BADARG, "unknown tuning flag");
+    ctx->tuning[bucket] = Tuning{t->block, t->ipt, t->word_bits, t->flags};
     return LTP_OK;
 }
 
@@ -778,7 +780,7 @@ int ltp_get_tuning(ltp_ctx *ctx, uint32_t bucket, ltp_tuning *t) {
     t->block = ctx->tuning[bucket].block;
     t->ipt = ctx->tuning[bucket].ipt;
     t->word_bits = ctx->tuning[bucket].word_bits;
-    t->reserved = 0;
+    t->flags = ctx->tuning[bucket].flags;
     return LTP_OK;
 }
 

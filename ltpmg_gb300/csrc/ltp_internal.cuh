@@ -66,7 +66,7 @@ struct BatchDev {
     u64 n_ops;
     u64 n_txns;
     u32 ops_per_txn;       // > 0: fixed-length transactions (op_txn unused)
-    u32 pad;
+    u32 flags;             // LTP_TUNE_* flags of the batch's size bucket
 };
 
 constexpr int kMaxPasses = 4;
@@ -134,7 +134,7 @@ constexpr u32 kInsTile = kInsBlock * kInsIpt;
 constexpr u32 kInsSmem = kInsTile * (4 + 8 + 1);  // insert staging: payload offset, link value, link column
 
 struct Tuning {
-    u32 block, ipt, word_bits;
+    u32 block, ipt, word_bits, flags;
 };
 
 // Host-side launch plan for one batch.

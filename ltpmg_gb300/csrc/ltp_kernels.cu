@@ -193,6 +193,14 @@ __device__ __forceinline__ u64 pol_evict_first() {
     asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
     return p;
 }
+__device__ __forceinline__ uint4 ld_word_relaxed(const void *ptr) {
+    uint4 v;
+    asm volatile("ld.relaxed.gpu.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(ptr)
+                 : "memory");
+    return v;
+}
 __device__ __forceinline__ uint4 ld_word_hint(const void *ptr, u64 pol) {
     uint4 v;
     asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
@@ -235,9 +243,10 @@ __device__ __forceinline__ char *cell_ptr(const TablesDev &T, u64 cell, bool *wi
     for (u32 i = 1; i < T.n; i++)
         if (cell >= T.t[i].cell_base) k = i;
     const TableDev &t = T.t[k];
-    u64 local = cell - t.cell_base;
-    u64 row = local / t.n_cols;
-    u32 col = (u32)(local - row * t.n_cols);
+    const u64 local = cell - t.cell_base;
+    // 32-bit division whenever the table's cell numbers fit (the usual case)
+    const u64 row = local < (1ull << 32) ? (u64)((u32)local / t.n_cols) : local / t.n_cols;
+    const u32 col = (u32)(local - row * t.n_cols);
     *wide = col_wide(t, col);
     return t.data + col_off(t, col) + row * (*wide ? 8ull : 4ull);
 }
@@ -291,6 +300,7 @@ __device__ __forceinline__ u32 hash_word(u32 w) { return (w * 0x9E3779B1u) ^ (w 
 template <int BLOCK, int IPT>
 __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
     if (block_err(ctr)) return;
+    const bool precheck = (b.flags & LTP_TUNE_MARK_PRECHECK) != 0u;
     constexpr u32 TILE = (u32)BLOCK * IPT;
     constexpr u32 H = 2 * TILE;  // at most TILE distinct words: load factor <= 1/2
     u32 *mark_smem = ltp_dyn_smem;  // 4 * H words (dynamic: up to 128 KB)
@@ -359,17 +369,36 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
             fw[q] = hk[j];
             ft[q] = ht[j];
         }
+        // a word whose touched, touched-twice and written bits already hold
+        // what this tile adds needs no atomic (hot words, after their first
+        // tiles); the bits only ever grow, so a stale read merely costs an
+        // atomic that was not needed.  Only words this tile touched more than
+        // once are checked first: a word touched once per tile is usually
+        // cold, and the read would only add a round trip before its atomic.
+        uint4 cur[SPT];
 #pragma unroll
-        for (int q = 0; q < SPT; q++)
-            old[q] = fw[q] != kEmptyKey ? atomicOr(&s.words[fw[q]].touch, ft[q]) : 1u;
+        for (int q = 0; q < SPT; q++) {
+            const u32 j = threadIdx.x + q * BLOCK;
+            const bool hot = precheck && fw[q] != kEmptyKey && (hd[j] != 0u || (ft[q] & (ft[q] - 1u)) != 0u);
+            cur[q] = hot ? ld_word_relaxed(&s.words[fw[q]]) : make_uint4(0u, 0u, 0u, 0u);
+        }
+        u32 dmask = 0;  // slots that issued their atomics
+#pragma unroll
+        for (int q = 0; q < SPT; q++) {
+            const u32 j = threadIdx.x + q * BLOCK;
+            // cur: x touch, y wbits, z multi
+            const bool need = fw[q] != kEmptyKey && ((ft[q] & ~cur[q].z) || (hw[j] & ~cur[q].y));
+            old[q] = need ? atomicOr(&s.words[fw[q]].touch, ft[q]) : 0u;
+            if (need) dmask |= 1u << q;
+        }
         u32 fmask = 0, nfirst = 0;
 #pragma unroll
         for (int q = 0; q < SPT; q++) {
             const u32 j = threadIdx.x + q * BLOCK;
-            if (fw[q] != kEmptyKey) {
+            if (dmask & (1u << q)) {
                 const u32 m = (old[q] & ft[q]) | hd[j];
-                if (m) atomicOr(&s.words[fw[q]].multi, m);
-                if (hw[j]) atomicOr(&s.words[fw[q]].wbits, hw[j]);
+                if (m & ~cur[q].z) atomicOr(&s.words[fw[q]].multi, m);
+                if (hw[j] & ~cur[q].y) atomicOr(&s.words[fw[q]].wbits, hw[j]);
                 if (old[q] == 0u) {
                     fmask |= 1u << q;
                     nfirst++;
@@ -1388,7 +1417,10 @@ static void pick_front(const Tuning &t, front_fn *mark, front_fn *classify) {
 
 static int capped(int grid, u64 upper) { return (int)((u64)grid < upper ? (u64)grid : (upper ? upper : 1)); }
 
-cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDev &T, const Scratch &s,
+                           Counters *ctr) {
+    BatchDev b = b_in;
+    b.flags = L.tune.flags;
     (void)cudaGetLastError();  // report only the launches below
     // stage event i is recorded after kernel i; event 0 of the batch precedes everything
     // under stream capture the stage events become external event nodes, so

@@ -161,7 +161,7 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     b.n_ops = n_ops;
     b.n_txns = n_txns;
     b.ops_per_txn = txn_first ? 0u : ops_per_txn;
-    b.pad = 0;
+    b.flags = 0;
     b.payload = nullptr;
     b.payload_len = 0;
     Launch L;
@@ -169,7 +169,7 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     L.stream = st;
     L.num_sms = sms;
     L.rule = rule;
-    L.tune = Tuning{512, 4, 32};
+    L.tune = Tuning{512, 4, 32, 0};
     if (n_ops && launch_execute(L, b, T, s, ctr) != cudaSuccess) return LTP_E_CUDA;
 
     // the device-side status of this call

@@ -88,7 +88,10 @@ class ServeStats(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("block", ctypes.c_uint32), ("ipt", ctypes.c_uint32), ("word_bits", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32)]
+
+
+TUNE_MARK_PRECHECK = 1
 
 
 _lib = None
@@ -442,13 +445,14 @@ class Context:
     def batch(self, max_txns, max_ops):
         return Batch(self, max_txns, max_ops)
 
-    def set_tuning(self, bucket, block, ipt, word_bits=32):
-        self.check(self.L.ltp_set_tuning(self.h, bucket, ctypes.byref(Tuning(block, ipt, word_bits, 0))))
+    def set_tuning(self, bucket, block, ipt, word_bits=32, flags=0):
+        self.check(self.L.ltp_set_tuning(self.h, bucket, ctypes.byref(Tuning(block, ipt, word_bits, flags))))
 
     def get_tuning(self, bucket):
+        """(block, ipt, word_bits, flags) of a size bucket."""
         t = Tuning()
         self.check(self.L.ltp_get_tuning(self.h, bucket, ctypes.byref(t)))
-        return (t.block, t.ipt, t.word_bits)
+        return (t.block, t.ipt, t.word_bits, t.flags)
 
     def execute_many(self, batches, mode=0, stream=None):
         """Executes batches in order: mode 0 stream, 1 CUDA graph, 2 persistent kernel."""

@@ -155,21 +155,32 @@ def test_empty_batch(lib_loaded):
         assert np.array_equal(before, ctx.download(t))
 
 
-@pytest.mark.parametrize("block,ipt", [(b, i) for b in (128, 256, 512) for i in (1, 2, 4, 8)])
-def test_tuning_variants(lib_loaded, block, ipt):
+@pytest.mark.parametrize("block,ipt,flags", [(b, i, 0) for b in (128, 256, 512) for i in (1, 2, 4, 8)] +
+                         [(512, 4, G.lib.TUNE_MARK_PRECHECK), (128, 1, G.lib.TUNE_MARK_PRECHECK)])
+def test_tuning_variants(lib_loaded, block, ipt, flags):
     rows, cols = 1 << 12, 10
-    tf, keys, opw = gen(21, rows, cols, 1, 32, 0.7, 0.95, 0, 3000)
-    ref_tab, rc, ro = O.replay(0, O.table_init(21, rows, cols), tf, keys, opw)
     with G.Context(device=0) as ctx:
         t = ctx.create_table(rows, cols)
         ctx.fill_seeded(t, 21)
         for bucket in range(64):
-            ctx.set_tuning(bucket, block, ipt)
-        b = ctx.batch(3000, len(keys))
-        b.load(tf, keys, opw)
-        b.execute()
-        commit, vals, st = b.results()
-        assert np.array_equal(vals, ro) and np.array_equal(ctx.download(t), ref_tab)
+            ctx.set_tuning(bucket, block, ipt, flags=flags)
+        assert ctx.get_tuning(5) == (block, ipt, 32, flags)
+        b = ctx.batch(3000, 3000 * 32)
+        ref_tab = O.table_init(21, rows, cols)
+        for batch in range(2):  # the second batch sees hot words already marked by the first's tiles
+            tf, keys, opw = gen(21, rows, cols, 1, 32, 0.7, 0.95, batch, 3000)
+            ref_tab, rc, ro = O.replay(0, ref_tab, tf, keys, opw)
+            b.load(tf, keys, opw)
+            b.execute()
+            commit, vals, st = b.results()
+            assert np.array_equal(vals, ro)
+        assert np.array_equal(ctx.download(t), ref_tab)
+
+
+def test_tuning_rejects_unbuilt_word_size(lib_loaded):
+    with G.Context(device=0) as ctx:
+        with pytest.raises(G.LtpError):
+            ctx.set_tuning(3, 512, 4, word_bits=64)
 
 
 def test_malformed_op_rejected_and_context_survives(lib_loaded):
