@@ -137,14 +137,14 @@ def load_peaks():
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit of work,
 # from one ncu --set full capture of each kernel on one batch of the same
-# workload (profiles/k_mark_classify_apply_zipf.md, profiles/k_mark_insert_tpcc.md);
+# workload (profiles/batch_kernels_zipf.md, profiles/k_mark_insert_tpcc.md);
 # a launch's traffic is this figure times the units it processed
 MEASURED_TRAFFIC = {
-    ("zipf", "classify"): (46.3, "ops"),
+    ("zipf", "classify"): (45.2, "ops"),
     ("zipf", "mark"): (22.4, "ops"),
-    ("zipf", "apply"): (45.0, "contended_ops"),
-    ("tpcc", "insert"): (73.2, "ops"),
-    ("tpcc", "mark"): (19.9, "ops"),
+    ("zipf", "apply"): (28.9, "contended_ops"),
+    ("tpcc", "insert"): (64.2, "ops"),
+    ("tpcc", "mark"): (20.1, "ops"),
 }
 
 
