@@ -840,7 +840,7 @@ __device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, C
 }
 
 template <int P>
-__global__ void __launch_bounds__(kSortBlock, 2) k_sort_pass(Scratch s, Counters *ctr, u64 n_ops) {
+__global__ void __launch_bounds__(kSortBlock, 3) k_sort_pass(Scratch s, Counters *ctr, u64 n_ops) {
     phase_sort_pass<kSortBlock>(P, s, ctr, n_ops);
 }
 
@@ -1031,7 +1031,7 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
 }
 
 template <typename S>
-__global__ void __launch_bounds__(kApplyBlock) k_apply(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+__global__ void __launch_bounds__(kApplyBlock, 4) k_apply(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
     phase_apply<kApplyBlock, S>(b, T, s, ctr);
 }
 
