@@ -57,7 +57,7 @@ KERNEL_BYTES = {
     "insert": lambda st: st.get("insert_bytes", 0),
     "finish": lambda st: 12 * st["touched_words"],
 }
-KERNELS_PER_BATCH = 10  # mark, ids, classify, 4 radix passes, apply, insert, finish
+KERNELS_PER_BATCH = 11  # mark, ids, dbase, classify, 4 radix passes, apply, insert, finish
 
 
 def dist_env():

@@ -450,6 +450,25 @@ __device__ __forceinline__ bool ids_dense(const Scratch &s, const Counters *ctr)
     return ctr->n_tw * 4 > s.n_words;
 }
 
+// Per contended cell: its address width (bit 63 of dcell marks an int64
+// cell), its value before the batch, and (priority rule) the min-writer slot.
+__device__ __forceinline__ void phase_dbase(const TablesDev &T, const Scratch &s, Counters *ctr, bool priority) {
+    if (block_err(ctr)) return;
+    const u64 M = ctr->M;
+    for (u64 m = (u64)blockIdx.x * blockDim.x + threadIdx.x; m < M; m += (u64)gridDim.x * blockDim.x) {
+        const u64 cell = s.dcell[m];
+        bool wide_c;
+        const char *cp = cell_ptr(T, cell, &wide_c);
+        if (wide_c) s.dcell[m] = cell | (1ull << 63);
+        s.dbase[m] = load_cell(cp, wide_c);
+        if (priority) s.dminw[m] = 0xFFFFFFFFu;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_dbase(TablesDev T, Scratch s, Counters *ctr, int priority) {
+    phase_dbase(T, s, ctr, priority != 0);
+}
+
 template <bool PRIORITY, int BLK>
 __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, Counters *ctr) {
     constexpr u32 IPT = kIdsTile / BLK;
@@ -512,16 +531,10 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
             if (j < n) {
                 s.words[wd[k]].prefix = (u32)pre;
                 u32 bits = cw[k];
-                while (bits) {
+                while (bits) {  // the cells' values are read by k_dbase, fully parallel
                     int bpos = __ffs(bits) - 1;
                     bits &= bits - 1;
-                    u64 cell = ((u64)wd[k] << 5) | (u64)bpos;
-                    bool wide_c;
-                    const char *cp = cell_ptr(T, cell, &wide_c);
-                    s.dcell[pre] = cell | (wide_c ? (1ull << 63) : 0ull);  // bit 63: int64 cell
-                    s.dbase[pre] = load_cell(cp, wide_c);
-                    if (PRIORITY) s.dminw[pre] = 0xFFFFFFFFu;
-                    pre++;
+                    s.dcell[pre++] = ((u64)wd[k] << 5) | (u64)bpos;
                 }
             }
         }
@@ -1446,6 +1459,7 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDe
         const int g = capped(gi, (b.n_ops + kIdsTile - 1) / kIdsTile);
         if (L.rule == LTP_RULE_PRIORITY) k_ids<true><<<g, kIdsBlock, 0, L.stream>>>(T, s, ctr);
         else k_ids<false><<<g, kIdsBlock, 0, L.stream>>>(T, s, ctr);
+        k_dbase<<<L.num_sms * 8, 256, 0, L.stream>>>(T, s, ctr, L.rule == LTP_RULE_PRIORITY);
     }
     mark_ev(2);
     const int gstream = L.num_sms * 8;
@@ -1562,6 +1576,8 @@ __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
         grid_sync(a.bar, nb, a.ctr);
         if (a.rule == LTP_RULE_PRIORITY) phase_ids<true, kPBlock>(a.T, a.s, a.ctr);
         else phase_ids<false, kPBlock>(a.T, a.s, a.ctr);
+        grid_sync(a.bar, nb, a.ctr);
+        phase_dbase(a.T, a.s, a.ctr, a.rule == LTP_RULE_PRIORITY);
         grid_sync(a.bar, nb, a.ctr);
         if (a.rule != LTP_RULE_PRIORITY) {
             phase_classify<kPBlock, kPIpt>(b, a.T, a.s, a.ctr);
