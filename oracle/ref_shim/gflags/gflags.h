@@ -1,6 +1,6 @@
-// Minimal stand-in for the gflags macros the reference's host headers use,
-// so that individual reference host sources compile for the oracle harness.
-// Test infrastructure only.
+// Minimal stand-in for the gflags macros and calls the reference's host
+// sources use: flags are plain globals with their defaults and the command
+// line is not parsed.  Test infrastructure only.
 #pragma once
 #include <cstdint>
 #include <string>
@@ -10,3 +10,7 @@
 #define DEFINE_string(n, v, d) std::string FLAGS_##n = v
 #define DEFINE_uint32(n, v, d) uint32_t FLAGS_##n = v
 #define DEFINE_double(n, v, d) double FLAGS_##n = v
+namespace gflags {
+inline uint32_t ParseCommandLineFlags(int *, char ***, bool) { return 0; }
+inline void ShutDownCommandLineFlags() {}
+}  // namespace gflags

@@ -101,3 +101,21 @@ def test_scheduler_sequence_matches_oracle(lib, tmp_path, variant):
     assert np.array_equal(final, exp)
     if variant == 4:
         assert tables[0][1] == rows + txns * epochs
+
+
+REF_HOST = os.path.join(ROOT, "oracle", "_ref", "ltpmg_host")
+
+
+def test_reference_host_program_links_against_the_library():
+    """The reference's whole host program (its src/*.cpp, main included,
+    compiled with the gflags/glog stand-ins) links against
+    libltpmg_gb300.so in place of its CUDA library: every GPU entry point it
+    calls resolves here.  Built by oracle/build_ref.sh where the reference
+    tree is present."""
+    if not os.path.exists(REF_HOST):
+        pytest.skip("reference host program not built (reference tree absent)")
+    und = subprocess.run(["nm", "-D", "--undefined-only", REF_HOST], capture_output=True, text=True).stdout
+    for sym in REFERENCE_SYMBOLS:
+        assert sym in und, sym
+    deps = subprocess.run(["ldd", REF_HOST], capture_output=True, text=True).stdout
+    assert "libltpmg_gb300.so" in deps and "not found" not in deps
