@@ -1473,13 +1473,16 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDe
             sms = L.num_sms;
         }
         const int gsort = capped(gs, (b.n_ops + kSortTile - 1) / kSortTile);
+        // at most n_ops contended ids: passes beyond their width are not launched
+        int max_passes = 1;
+        while (max_passes < 4 && ((b.n_ops - 1) >> (8 * max_passes)) != 0) max_passes++;
         k_sort_pass<0><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
         mark_ev(4);
-        k_sort_pass<1><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
+        if (max_passes > 1) k_sort_pass<1><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
         mark_ev(5);
-        k_sort_pass<2><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
+        if (max_passes > 2) k_sort_pass<2><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
         mark_ev(6);
-        k_sort_pass<3><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
+        if (max_passes > 3) k_sort_pass<3><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
         mark_ev(7);
         const int gapp = capped(ga, (b.n_ops + kApplyTile - 1) / kApplyTile);
         if (T.any_wide) k_apply<u64><<<gapp, kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
@@ -1499,7 +1502,8 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDe
             gins = occ_grid(k_insert, kInsBlock, L.num_sms, kInsSmem);
             sms = L.num_sms;
         }
-        k_insert<<<capped(gins, (b.n_ops + kInsTile - 1) / kInsTile), kInsBlock, kInsSmem, L.stream>>>(b, T, s, ctr);
+        if (b.payload_len)  // a batch without payload has no valid insert
+            k_insert<<<capped(gins, (b.n_ops + kInsTile - 1) / kInsTile), kInsBlock, kInsSmem, L.stream>>>(b, T, s, ctr);
     }
     mark_ev(9);
     k_finish<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr, L.rule);
@@ -1582,14 +1586,13 @@ __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
         if (a.rule != LTP_RULE_PRIORITY) {
             phase_classify<kPBlock, kPIpt>(b, a.T, a.s, a.ctr);
             grid_sync(a.bar, nb, a.ctr);
-            phase_sort_pass<kPBlock>(0, a.s, a.ctr, b.n_ops);
-            grid_sync(a.bar, nb, a.ctr);
-            phase_sort_pass<kPBlock>(1, a.s, a.ctr, b.n_ops);
-            grid_sync(a.bar, nb, a.ctr);
-            phase_sort_pass<kPBlock>(2, a.s, a.ctr, b.n_ops);
-            grid_sync(a.bar, nb, a.ctr);
-            phase_sort_pass<kPBlock>(3, a.s, a.ctr, b.n_ops);
-            grid_sync(a.bar, nb, a.ctr);
+            // only the passes the contended ids need (M is the same for every
+            // block after the barrier, so every block skips the same ones)
+            const int passes = sort_passes_dev(*(volatile u32 *)&a.ctr->M);
+            for (int P = 0; P < passes; P++) {
+                phase_sort_pass<kPBlock>(P, a.s, a.ctr, b.n_ops);
+                grid_sync(a.bar, nb, a.ctr);
+            }
             if (a.T.any_wide) phase_apply<kPBlock, u64>(b, a.T, a.s, a.ctr);
             else phase_apply<kPBlock, u32>(b, a.T, a.s, a.ctr);
         } else {
@@ -1600,8 +1603,10 @@ __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
             phase_r1_exec(b, a.T, a.s, a.ctr);
         }
         grid_sync(a.bar, nb, a.ctr);
-        phase_insert<kPBlock>(b, a.T, a.s, a.ctr);
-        grid_sync(a.bar, nb, a.ctr);
+        if (b.payload_len) {  // a batch without payload has no valid insert
+            phase_insert<kPBlock>(b, a.T, a.s, a.ctr);
+            grid_sync(a.bar, nb, a.ctr);
+        }
         phase_finish(b, a.T, a.s, a.ctr, a.rule);
         grid_sync(a.bar, nb, a.ctr);
         if (blockIdx.x == 0) {
