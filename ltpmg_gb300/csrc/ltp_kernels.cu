@@ -683,7 +683,7 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
 template <int BLOCK, int IPT>
 // register budget: 64 per thread up to 4 ops per thread, 128 above, so that
 // 64-bit cell values do not halve the resident blocks
-__global__ void __launch_bounds__(BLOCK, 65536 / (BLOCK * (IPT <= 4 ? 64 : 128))) k_classify(BatchDev b, TablesDev T,
+__global__ void __launch_bounds__(BLOCK, 65536 / (BLOCK * (IPT <= 2 ? 40 : IPT <= 4 ? 48 : 96))) k_classify(BatchDev b, TablesDev T,
                                                                                           Scratch s, Counters *ctr) {
     phase_classify<BLOCK, IPT>(b, T, s, ctr);
 }
