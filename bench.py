@@ -31,7 +31,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "committed txn/s"
-DEFAULT_STEPS = {"zipf": 20, "plain": 50, "uneven": 30, "serve": 1, "tpcc": 10}
+DEFAULT_STEPS = {"zipf": 20, "plain": 50, "uneven": 30, "serve": 1, "tpcc": 10, "gather": 1}
 WORKLOAD_TEXT = {
     "zipf": "ycsb-zipf0.99: 2^24 rows x 10 int32, 32 batches x 2^20 txns x 16 ops, 80% read / 20% +1 RMW",
     "plain": "ycsb-uniform: 2^20 rows x 10 int32, 16 batches x 2^16 txns x 10 ops, 50% read / 50% +1 RMW",
@@ -773,6 +773,37 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_gather(args):
+    """Random-access ceiling of this GPU: uniformly random 4-byte gathers
+    (torch indexing kernel, not this library) from a table of the Zipf
+    workload's size (640 MB, beyond L2) and of its conflict-word array's size
+    (84 MB, L2-resident).  Every random read moves at least one 32-byte
+    sector, so this -- not the copy bandwidth -- bounds kernels whose ops
+    touch random cells."""
+    import torch
+
+    torch.manual_seed(0)
+    out = {}
+    n_idx = 1 << 24
+    for name, nbytes in (("table_640MB", 10 << 26), ("words_84MB", 84 << 20)):
+        src = torch.zeros(nbytes // 4, dtype=torch.int32, device="cuda")
+        idx = torch.randint(0, src.numel(), (n_idx,), device="cuda")
+        for _ in range(3):
+            src[idx]
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        reps = 10
+        for _ in range(reps):
+            src[idx]
+        e1.record()
+        e1.synchronize()
+        s_per = e0.elapsed_time(e1) / 1e3 / reps
+        out[name] = {"gathers_per_s": n_idx / s_per, "sector_GBps": n_idx * 32 / s_per / 1e9}
+        del src, idx
+    print(json.dumps({"metric": "random 4-byte gathers/s", "gather": out}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -796,11 +827,13 @@ def main():
         if args.config == "tpcc":
             run_reference_tpcc(args)
         else:
-            run_reference(args, "zipf" if args.config == "serve" else args.config)
+            run_reference(args, "zipf" if args.config in ("serve", "gather") else args.config)
     elif args.config == "serve":
         run_serve(args)
     elif args.config == "tpcc":
         run_tpcc(args)
+    elif args.config == "gather":
+        run_gather(args)
     else:
         run_ours(args, args.config)
 
