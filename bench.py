@@ -743,15 +743,18 @@ def run_serve(args):
     # one short untimed load first: allocations and first-touch of the
     # server's host buffers happen here, not in the first sweep point
     srv = G.Server(ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 18, max_ops=1 << 22,
-                   keep_results=False)
+                   keep_results=False, persistent=args.serve_mode == "persistent")
     srv.loadgen(1e6, 0.1, 256, ptf, pk, pw, seed=1, threads=8, pay_first=ppf, payload=ppay)
     srv.close()
     truncate()
     sweep = []
     for rate, t_load in zip(loads, t_loads):
         srv = G.Server(ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 18, max_ops=1 << 22,
-                       keep_results=False)
-        srv.loadgen(rate, t_load, 256, ptf, pk, pw, seed=int(rate), threads=8, pay_first=ppf, payload=ppay)
+                       keep_results=False, persistent=args.serve_mode == "persistent")
+        # load-generator threads: every host core but those of the dispatcher,
+        # the completer and this thread
+        srv.loadgen(rate, t_load, 256, ptf, pk, pw, seed=int(rate), threads=max(4, (os.cpu_count() or 8) - 4),
+                    pay_first=ppf, payload=ppay)
         st = srv.close()
         truncate()
         st["offered_txn_per_s"] = rate
@@ -765,7 +768,7 @@ def run_serve(args):
             "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32/int64", "data": "synthetic (seeded generator)",
             "config": {"workload": WORKLOAD_TEXT["serve"], "selection": "highest committed txn/s with p99 <= 2 ms",
-                       "pool_txns": n_pool},
+                       "pool_txns": n_pool, "batch_execution": args.serve_mode},
             "serving": {"sweep": sweep, "plain_batch_txn_per_s": plain,
                         "best_p50_us": best["p50_us"] if best else None,
                         "best_p99_us": best["p99_us"] if best else None,
@@ -819,6 +822,8 @@ def main():
                     help="fixed BLOCKxIPT[+precheck] tiling instead of the autotuner's (e.g. 512x4)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
+    ap.add_argument("--serve-mode", default="persistent", choices=["persistent", "stream"],
+                    help="serving: each batch as one persistent-kernel launch, or as a kernel sequence")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if not args.steps:

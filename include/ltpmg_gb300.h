@@ -220,6 +220,11 @@ int ltp_batch_device_ptrs(ltp_batch *b, uint64_t **keys, uint32_t **opw, uint32_
  * an error the pipeline must be drained and freed. */
 typedef struct ltp_pipe ltp_pipe;
 int ltp_pipe_create(ltp_ctx *ctx, uint32_t depth, uint64_t max_txns, uint64_t max_ops, ltp_pipe **out);
+/* With LTP_PIPE_PERSISTENT every batch runs as one persistent-kernel launch
+ * (no stage timing): fewer launches per batch, for small batches. */
+#define LTP_PIPE_PERSISTENT 1u
+int ltp_pipe_create2(ltp_ctx *ctx, uint32_t depth, uint64_t max_txns, uint64_t max_ops, uint32_t flags,
+                     ltp_pipe **out);
 int ltp_pipe_free(ltp_pipe *p);
 /* Enqueues one batch (txn_first may be NULL for fixed-length transactions;
  * payload may be NULL).  commit_out / vals_out receive the results (either
@@ -261,6 +266,7 @@ typedef struct {
 } ltp_serve_config;
 #define LTP_SERVE_EAGER 1u        /* close a batch as soon as the device has none queued */
 #define LTP_SERVE_KEEP_RESULTS 2u /* keep per-transaction results for ltp_serve_poll */
+#define LTP_SERVE_PERSISTENT 4u   /* execute each batch as one persistent-kernel launch */
 
 typedef struct {
     uint64_t tag;           /* caller's tag */
@@ -281,6 +287,11 @@ typedef struct {
     uint64_t closed_deadline, closed_budget, closed_idle, ops;
     double p50_us, p99_us, p999_us, mean_us, max_us;
     double elapsed_s, committed_per_s;
+    /* where the host time goes: seconds the dispatcher spent forming and
+     * submitting batches, seconds the completer spent on finished batches
+     * (excluding its waits), and the share of load-generator submissions
+     * made more than 100 us after their scheduled arrival */
+    double dispatch_busy_s, complete_busy_s, loadgen_late_frac;
 } ltp_serve_stats;
 
 typedef struct ltp_server ltp_server;

@@ -807,6 +807,9 @@ namespace {
 struct PipeSlot {
     ltp_batch *b = nullptr;
     cudaEvent_t in = nullptr, exec = nullptr, out = nullptr;
+    BatchDev *h_desc = nullptr;    // pinned staging of the batch descriptor (persistent execution)
+    BatchDev *d_desc = nullptr;    // device copy the persistent kernel reads
+    Counters **d_snap = nullptr;   // device array holding b->snap
     Counters *host_ctr = nullptr;  // pinned copy of the batch's counters
     uint64_t ticket = UINT64_MAX;
     bool waited = true;
@@ -822,6 +825,7 @@ struct PipeDone {
 
 struct ltp_pipe {
     ltp_ctx *ctx = nullptr;
+    bool persistent = false;  // each batch runs as one persistent-kernel launch
     std::vector<PipeSlot> slots;
     cudaStream_t s_in = nullptr, s_out = nullptr;
     uint64_t next = 0;
@@ -855,13 +859,19 @@ static int pipe_finalize(ltp_pipe *p, PipeSlot &sl) {
 extern "C" {
 
 int ltp_pipe_create(ltp_ctx *ctx, uint32_t depth, uint64_t max_txns, uint64_t max_ops, ltp_pipe **out) {
-    if (!ctx || !out || depth < 2 || depth > 64) return LTP_E_BADARG;
+    return ltp_pipe_create2(ctx, depth, max_txns, max_ops, 0, out);
+}
+
+int ltp_pipe_create2(ltp_ctx *ctx, uint32_t depth, uint64_t max_txns, uint64_t max_ops, uint32_t flags,
+                     ltp_pipe **out) {
+    if (!ctx || !out || depth < 2 || depth > 64 || (flags & ~LTP_PIPE_PERSISTENT)) return LTP_E_BADARG;
     *out = nullptr;
     CK(cudaSetDevice(ctx->device));
     int rc = ensure_scratch(ctx, max_ops);
     if (rc) return rc;
     ltp_pipe *p = new ltp_pipe();
     p->ctx = ctx;
+    p->persistent = (flags & LTP_PIPE_PERSISTENT) != 0;
     p->slots.resize(depth);
     cudaError_t e = cudaStreamCreateWithFlags(&p->s_in, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->s_out, cudaStreamNonBlocking);
@@ -872,7 +882,14 @@ int ltp_pipe_create(ltp_ctx *ctx, uint32_t depth, uint64_t max_txns, uint64_t ma
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.exec, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.out, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaMallocHost((void **)&sl.host_ctr, sizeof(Counters));
+        if (e == cudaSuccess && p->persistent) {
+            e = cudaMallocHost((void **)&sl.h_desc, sizeof(BatchDev));
+            if (e == cudaSuccess) e = dalloc(&sl.d_desc, 1);
+            if (e == cudaSuccess) e = dalloc(&sl.d_snap, 1);
+            if (e == cudaSuccess) e = cudaMemcpy(sl.d_snap, &sl.b->snap, sizeof(Counters *), cudaMemcpyHostToDevice);
+        }
     }
+    if (!rc && e == cudaSuccess && p->persistent && !ctx->p_bar) e = dalloc(&ctx->p_bar, 2);
     if (rc || e != cudaSuccess) {
         ltp_pipe_free(p);
         return rc ? rc : cuda_fail(ctx, e, "ltp_pipe_create");
@@ -892,6 +909,9 @@ int ltp_pipe_free(ltp_pipe *p) {
         if (sl.exec) cudaEventDestroy(sl.exec);
         if (sl.out) cudaEventDestroy(sl.out);
         if (sl.host_ctr) cudaFreeHost(sl.host_ctr);
+        if (sl.h_desc) cudaFreeHost(sl.h_desc);
+        cudaFree(sl.d_desc);
+        cudaFree(sl.d_snap);
     }
     if (p->s_in) cudaStreamDestroy(p->s_in);
     if (p->s_out) cudaStreamDestroy(p->s_out);
@@ -930,7 +950,20 @@ static int pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, 
     CK(cudaEventRecord(sl.in, p->s_in));
     cudaStream_t sx = ctx->stream;
     CK(cudaStreamWaitEvent(sx, sl.in, 0));
-    if ((rc = execute_one(ctx, sl.b, sx, false))) return rc;
+    if (p->persistent && sl.b->n_ops) {
+        // one cooperative launch runs every phase of the batch; its
+        // descriptor goes up from pinned staging on the execution stream
+        *sl.h_desc = batch_dev(sl.b);
+        sl.h_desc->flags = ctx->tuning[bucket_of(sl.b->n_ops)].flags;
+        CK(cudaMemcpyAsync(sl.d_desc, sl.h_desc, sizeof(BatchDev), cudaMemcpyHostToDevice, sx));
+        CK(cudaMemsetAsync(ctx->ctr, 0, sizeof(Counters), sx));
+        CK(launch_persistent(sx, ctx->num_sms, ctx->rule, sl.d_desc, sl.d_snap, 1, tables_dev(ctx), ctx->s, ctx->ctr,
+                             ctx->p_bar));
+        sl.b->rule = ctx->rule;
+        sl.b->executed = true;
+    } else if ((rc = execute_one(ctx, sl.b, sx, false))) {
+        return rc;
+    }
     CK(cudaMemcpyAsync(sl.host_ctr, sl.b->snap, sizeof(Counters), cudaMemcpyDeviceToHost, sx));
     CK(cudaEventRecord(sl.exec, sx));
     CK(cudaStreamWaitEvent(p->s_out, sl.exec, 0));

@@ -18,11 +18,16 @@
 // flat arrays) until the dispatcher swaps the whole lane out as a segment;
 // batches copy runs of consecutive transactions with one memcpy per run, and
 // completion walks runs, so the per-transaction cost is a few nanoseconds.
+// Two threads drive the loop: the dispatcher admits and submits, the
+// completer waits for finished batches in order, records latencies and hands
+// aborted transactions back to the dispatcher.
 #include <time.h>
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <deque>
 #include <memory>
@@ -106,7 +111,7 @@ struct Slot {
     int32_t *payload = nullptr;
     std::vector<Run> runs;
     uint64_t ticket = 0, seq = 0;
-    bool busy = false;
+    std::atomic<bool> busy{false};  // set by the dispatcher, cleared by the completer
 };
 
 // Latency histogram without floating point: 64 linear sub-buckets per
@@ -154,11 +159,20 @@ struct ltp_server {
     uint64_t max_payload = 0;
     ltp_pipe *pipe = nullptr;
     std::vector<std::unique_ptr<Lane>> lanes;
-    std::vector<Slot> slots;
+    std::unique_ptr<Slot[]> slots;  // [n_slots]
+    uint32_t n_slots = 0;
     std::deque<std::shared_ptr<Seg>> pending;  // requeued segments go to the front
     uint64_t pending_txns = 0, pending_ops = 0;
+    // submitted batches, oldest first: the dispatcher appends, the completer
+    // takes the front; aborted transactions come back through `requeued`
+    std::mutex fl_mu;
+    std::condition_variable fl_cv;
     std::deque<uint32_t> inflight;
-    std::thread dispatcher;
+    std::vector<std::shared_ptr<Seg>> requeued;
+    std::atomic<uint32_t> n_inflight{0};
+    std::atomic<bool> dispatcher_done{false};
+    std::thread dispatcher, completer;
+    std::mutex histo_mu;
     std::atomic<bool> stop{false};
     std::atomic<int> status{0};
     std::mutex res_mu;
@@ -166,6 +180,7 @@ struct ltp_server {
     Histo histo;
     std::atomic<uint64_t> submitted{0};
     std::atomic<uint64_t> completed{0}, committed{0};
+    std::atomic<uint64_t> dispatch_ns{0}, complete_ns{0}, lg_total{0}, lg_late{0};
     uint64_t aborted_attempts = 0, batches = 0, ops = 0;
     uint64_t closed_deadline = 0, closed_budget = 0, closed_idle = 0;
     uint64_t t_first = 0, t_last = 0, seq = 0;
@@ -221,6 +236,8 @@ void complete_batch(ltp_server *s, Slot &sl) {
     const uint64_t done = now_ns();
     std::shared_ptr<Seg> again;  // aborted transactions to re-queue
     std::vector<ltp_serve_result> out;
+    std::vector<uint64_t> lat;
+    lat.reserve(sl.runs.empty() ? 0 : 4096);
     uint32_t pos = 0;
     uint64_t n_ok = 0, n_done = 0;
     for (Run &r : sl.runs) {
@@ -239,7 +256,7 @@ void complete_batch(ltp_server *s, Slot &sl) {
             n_done++;
             if (ok) {
                 n_ok++;
-                s->histo.add(done - g.arrival[i]);
+                lat.push_back(done - g.arrival[i]);
             }
             if (s->keep_results) {
                 ltp_serve_result res;
@@ -264,15 +281,18 @@ void complete_batch(ltp_server *s, Slot &sl) {
     }
     for (Run &r : sl.runs) recycle(s, r.seg);
     sl.runs.clear();
-    if (again) {  // ahead of everything pending: the next batch starts with them
-        s->pending_txns += again->n();
-        s->pending_ops += again->keys.size();
-        s->pending.push_front(std::move(again));
+    if (again) {  // the dispatcher puts them ahead of everything pending
+        std::lock_guard<std::mutex> g(s->fl_mu);
+        s->requeued.push_back(std::move(again));
+    }
+    {
+        std::lock_guard<std::mutex> g(s->histo_mu);
+        for (uint64_t ns : lat) s->histo.add(ns);
     }
     s->completed += n_done;
     s->committed += n_ok;
     s->t_last = done;
-    sl.busy = false;
+    sl.busy.store(false, std::memory_order_release);
     if (!out.empty()) {
         std::lock_guard<std::mutex> g(s->res_mu);
         s->results.insert(s->results.end(), out.begin(), out.end());
@@ -287,15 +307,15 @@ uint64_t oldest_pending(const ltp_server *s) {
 }
 
 bool close_batch(ltp_server *s, uint64_t now) {
-    if (s->inflight.size() >= s->cfg.depth || s->pending_txns == 0) return false;
+    if (s->n_inflight.load() >= s->cfg.depth || s->pending_txns == 0) return false;
     const uint64_t cap_ops = std::min<uint64_t>(s->cfg.max_ops, s->cfg.budget_bytes / 12);
     const bool deadline = now >= oldest_pending(s) + (uint64_t)s->cfg.deadline_us * 1000ull;
     const bool full = s->pending_ops >= cap_ops || s->pending_txns >= s->cfg.max_txns;
-    const bool idle = (s->cfg.flags & LTP_SERVE_EAGER) && s->inflight.empty();
+    const bool idle = (s->cfg.flags & LTP_SERVE_EAGER) && s->n_inflight.load() == 0;
     if (!deadline && !full && !idle) return false;
     uint32_t si = 0;
-    while (si < s->slots.size() && s->slots[si].busy) si++;
-    if (si == s->slots.size()) return false;
+    while (si < s->n_slots && s->slots[si].busy.load(std::memory_order_acquire)) si++;
+    if (si == s->n_slots) return false;
     if (deadline) s->closed_deadline++;
     else if (full) s->closed_budget++;
     else s->closed_idle++;
@@ -349,29 +369,80 @@ bool close_batch(ltp_server *s, uint64_t now) {
     }
     sl.ticket = ticket;
     sl.seq = s->seq++;
-    sl.busy = true;
-    s->inflight.push_back(si);
+    sl.busy.store(true, std::memory_order_release);
+    {
+        std::lock_guard<std::mutex> g(s->fl_mu);
+        s->inflight.push_back(si);
+        s->n_inflight++;
+    }
+    s->fl_cv.notify_one();
     s->batches++;
     s->ops += nops;
     return true;
 }
 
+// Puts transactions re-queued by the completer ahead of everything pending.
+void take_requeued(ltp_server *s) {
+    std::vector<std::shared_ptr<Seg>> got;
+    {
+        std::lock_guard<std::mutex> g(s->fl_mu);
+        got.swap(s->requeued);
+    }
+    for (auto it = got.rbegin(); it != got.rend(); ++it) {
+        s->pending_txns += (*it)->n();
+        s->pending_ops += (*it)->keys.size();
+        s->pending.push_front(std::move(*it));
+    }
+}
+
+// Admission and submission; completion runs on its own thread.
 void dispatch_loop(ltp_server *s) {
     for (;;) {
         drain_lanes(s);
-        bool progressed = false;
-        while (!s->inflight.empty() && ltp_pipe_poll(s->pipe, s->slots[s->inflight.front()].ticket) == 0) {
-            complete_batch(s, s->slots[s->inflight.front()]);
-            s->inflight.pop_front();
-            progressed = true;
-        }
+        take_requeued(s);
+        const uint64_t t0 = now_ns();
+        const bool progressed = close_batch(s, t0);
+        if (progressed) s->dispatch_ns += now_ns() - t0;
         if (s->status) break;
-        if (close_batch(s, now_ns())) progressed = true;
-        if (s->stop && s->pending_txns == 0 && s->inflight.empty()) {
+        if (s->stop && s->pending_txns == 0 && s->n_inflight.load() == 0) {
             drain_lanes(s);
-            if (s->pending_txns == 0) break;
+            take_requeued(s);
+            if (s->pending_txns == 0 && s->n_inflight.load() == 0) break;
         }
         if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(2));
+    }
+    s->dispatcher_done = true;
+    s->fl_cv.notify_all();
+}
+
+// Waits for submitted batches in order and hands their results back.
+void complete_loop(ltp_server *s) {
+    for (;;) {
+        uint32_t si;
+        {
+            std::unique_lock<std::mutex> lk(s->fl_mu);
+            s->fl_cv.wait_for(lk, std::chrono::milliseconds(1),
+                              [&] { return !s->inflight.empty() || s->dispatcher_done.load(); });
+            if (s->inflight.empty()) {
+                if (s->dispatcher_done.load()) break;
+                continue;
+            }
+            si = s->inflight.front();
+        }
+        while (ltp_pipe_poll(s->pipe, s->slots[si].ticket) == 1) std::this_thread::sleep_for(std::chrono::microseconds(2));
+        const uint64_t c0 = now_ns();
+        complete_batch(s, s->slots[si]);  // the batch's results are in host memory
+        s->complete_ns += now_ns() - c0;
+        {
+            std::lock_guard<std::mutex> g(s->fl_mu);
+            s->inflight.pop_front();
+            s->n_inflight--;
+        }
+        if (s->status) {
+            // the dispatcher stops on the status; drop what is still in flight
+            std::lock_guard<std::mutex> g(s->fl_mu);
+            if (s->dispatcher_done.load() && s->inflight.empty()) break;
+        }
     }
 }
 
@@ -391,15 +462,18 @@ int ltp_serve_open(ltp_ctx *ctx, const ltp_serve_config *cfg, ltp_server **out) 
     s->wide = ltp_ctx_wide(ctx) != 0;
     s->max_payload = cfg->max_ops * 6;  // int32 slots of insert payload per batch
     if (s->cfg.max_attempts == 0) s->cfg.max_attempts = 1;
-    int rc = ltp_pipe_create(ctx, cfg->depth, cfg->max_txns, cfg->max_ops, &s->pipe);
+    int rc = ltp_pipe_create2(ctx, cfg->depth, cfg->max_txns, cfg->max_ops,
+                              (cfg->flags & LTP_SERVE_PERSISTENT) ? LTP_PIPE_PERSISTENT : 0u, &s->pipe);
     if (rc) {
         delete s;
         return rc;
     }
     const unsigned n_lanes = 64;
     for (unsigned i = 0; i < n_lanes; i++) s->lanes.emplace_back(new Lane());
-    s->slots.resize(cfg->depth);
-    for (auto &sl : s->slots) {
+    s->slots.reset(new Slot[cfg->depth]);
+    s->n_slots = cfg->depth;
+    for (uint32_t i = 0; i < s->n_slots; i++) {
+        Slot &sl = s->slots[i];
         sl.keys = (uint64_t *)ltp_host_alloc(cfg->max_ops * 8);
         sl.opw = (uint32_t *)ltp_host_alloc(cfg->max_ops * 4);
         sl.vals = (int32_t *)ltp_host_alloc(cfg->max_ops * 4);
@@ -413,6 +487,7 @@ int ltp_serve_open(ltp_ctx *ctx, const ltp_serve_config *cfg, ltp_server **out) 
         }
     }
     s->dispatcher = std::thread(dispatch_loop, s);
+    s->completer = std::thread(complete_loop, s);
     *out = s;
     return LTP_OK;
 }
@@ -476,12 +551,16 @@ int ltp_serve_loadgen_rows(ltp_server *s, double rate, double seconds, uint32_t 
             std::exponential_distribution<double> gap(my_rate / 1e9);
             double t = (double)t0;
             uint64_t k = (n_pool * g) / n_threads;
+            uint64_t local_total = 0, local_late = 0;
             while (true) {
                 t += gap(rng);
                 const uint64_t at = (uint64_t)t;
                 if (at >= t_end || s->status) break;
-                while (now_ns() < at) {
+                uint64_t tn;
+                while ((tn = now_ns()) < at) {
                 }
+                local_total++;
+                if (tn - at > 100000ull) local_late++;
                 const uint32_t st = g + n_threads * (uint32_t)(rng() % my_streams);
                 const uint32_t a = txn_first[k], n = txn_first[k + 1] - txn_first[k];
                 int rc;
@@ -498,6 +577,8 @@ int ltp_serve_loadgen_rows(ltp_server *s, double rate, double seconds, uint32_t 
                 if (rc) break;
                 if (++k == n_pool) k = 0;
             }
+            s->lg_total += local_total;
+            s->lg_late += local_late;
         });
     }
     for (auto &x : th) x.join();
@@ -516,12 +597,18 @@ int ltp_serve_stats_now(ltp_server *s, ltp_serve_stats *st) {
     st->closed_budget = s->closed_budget;
     st->closed_idle = s->closed_idle;
     st->ops = s->ops;
-    st->p50_us = s->histo.pct(0.50) / 1e3;
-    st->p99_us = s->histo.pct(0.99) / 1e3;
-    st->p999_us = s->histo.pct(0.999) / 1e3;
-    st->mean_us = s->histo.n ? s->histo.sum / (double)s->histo.n / 1e3 : 0;
-    st->max_us = (double)s->histo.mx / 1e3;
+    {
+        std::lock_guard<std::mutex> g(s->histo_mu);
+        st->p50_us = s->histo.pct(0.50) / 1e3;
+        st->p99_us = s->histo.pct(0.99) / 1e3;
+        st->p999_us = s->histo.pct(0.999) / 1e3;
+        st->mean_us = s->histo.n ? s->histo.sum / (double)s->histo.n / 1e3 : 0;
+        st->max_us = (double)s->histo.mx / 1e3;
+    }
     st->elapsed_s = s->t_last > s->t_first ? (double)(s->t_last - s->t_first) / 1e9 : 0;
+    st->dispatch_busy_s = (double)s->dispatch_ns.load() / 1e9;
+    st->complete_busy_s = (double)s->complete_ns.load() / 1e9;
+    st->loadgen_late_frac = s->lg_total.load() ? (double)s->lg_late.load() / (double)s->lg_total.load() : 0.0;
     st->committed_per_s = st->elapsed_s > 0 ? (double)s->committed / st->elapsed_s : 0;
     return s->status;
 }
@@ -530,10 +617,12 @@ int ltp_serve_close(ltp_server *s, ltp_serve_stats *st) {
     if (!s) return LTP_E_BADARG;
     s->stop = true;
     if (s->dispatcher.joinable()) s->dispatcher.join();
+    if (s->completer.joinable()) s->completer.join();
     if (st) ltp_serve_stats_now(s, st);
     const int status = s->status;
     if (s->pipe) ltp_pipe_free(s->pipe);
-    for (auto &sl : s->slots) {
+    for (uint32_t i = 0; i < s->n_slots; i++) {
+        Slot &sl = s->slots[i];
         ltp_host_free(sl.keys);
         ltp_host_free(sl.opw);
         ltp_host_free(sl.vals);

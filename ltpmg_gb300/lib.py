@@ -80,7 +80,8 @@ class ServeStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_uint64) for k in ("submitted", "completed", "committed", "aborted_attempts", "batches",
                                                "closed_deadline", "closed_budget", "closed_idle", "ops")] + \
                [(k, ctypes.c_double) for k in ("p50_us", "p99_us", "p999_us", "mean_us", "max_us", "elapsed_s",
-                                               "committed_per_s")]
+                                               "committed_per_s", "dispatch_busy_s", "complete_busy_s",
+                                               "loadgen_late_frac")]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -149,6 +150,7 @@ def load():
         "ltp_compat_last_error": (ctypes.c_char_p, []),
         "ltp_batches_execute": (ci, [vp, vp, u32, i32, vp]),
         "ltp_pipe_create": (ci, [vp, u32, u64, u64, pp]),
+        "ltp_pipe_create2": (ci, [vp, u32, u64, u64, u32, pp]),
         "ltp_pipe_free": (ci, [vp]),
         "ltp_pipe_submit": (ci, [vp, u64, vp, u32, u64, vp, vp, vp, u64, vp, vp, ctypes.POINTER(u64)]),
         "ltp_pipe_wait": (ci, [vp, u64, ctypes.POINTER(Stats)]),
@@ -542,10 +544,10 @@ class Pipe:
     """Pipelined submission (the C-ABI ltp_pipe): copy-in, execution and
     copy-out of consecutive batches overlap on three streams."""
 
-    def __init__(self, ctx, depth, max_txns, max_ops):
+    def __init__(self, ctx, depth, max_txns, max_ops, persistent=False):
         self.ctx = ctx
         h = ctypes.c_void_p()
-        ctx.check(ctx.L.ltp_pipe_create(ctx.h, depth, max_txns, max_ops, ctypes.byref(h)))
+        ctx.check(ctx.L.ltp_pipe_create2(ctx.h, depth, max_txns, max_ops, 1 if persistent else 0, ctypes.byref(h)))
         self.h = h
         self._keep = {}
 
@@ -588,9 +590,9 @@ class Server:
     """The continuous-batching request loop (the C-ABI ltp_server)."""
 
     def __init__(self, ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 20, max_ops=1 << 24,
-                 max_attempts=64, eager=True, keep_results=True):
+                 max_attempts=64, eager=True, keep_results=True, persistent=False):
         self.ctx = ctx
-        flags = (1 if eager else 0) | (2 if keep_results else 0)
+        flags = (1 if eager else 0) | (2 if keep_results else 0) | (4 if persistent else 0)
         cfg = ServeConfig(deadline_us, depth, budget_bytes, max_txns, max_ops, max_attempts, flags)
         h = ctypes.c_void_p()
         ctx.check(ctx.L.ltp_serve_open(ctx.h, ctypes.byref(cfg), ctypes.byref(h)))

@@ -433,15 +433,17 @@ def test_persistent_mode_with_inserts(lib_loaded):
 
 
 @pytest.mark.parametrize("rule", [0, 1])
-def test_pipeline_matches_oracle(lib_loaded, rule):
+@pytest.mark.parametrize("persistent", [False, True])
+def test_pipeline_matches_oracle(lib_loaded, rule, persistent):
     """Batches submitted through the 3-deep pipeline (overlapped copy-in,
-    execution, copy-out) give the serial replay of the whole sequence."""
+    execution, copy-out; each batch as a kernel sequence or as one
+    persistent-kernel launch) give the serial replay of the whole sequence."""
     rows, cols, seed = 1 << 13, 10, 17
     with G.Context(device=0, rule=rule) as ctx:
         t = ctx.create_table(rows, cols)
         ctx.fill_seeded(t, seed)
         ref = O.table_init(seed, rows, cols)
-        pipe = G.Pipe(ctx, 3, 4096, 4096 * 32)
+        pipe = G.Pipe(ctx, 3, 4096, 4096 * 32, persistent=persistent)
         subs, pinned = [], []
         for k in range(7):
             n = [4096, 100, 2000, 1, 3000, 4096, 512][k]

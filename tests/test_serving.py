@@ -38,14 +38,15 @@ def _pool(seed, rows, cols, n, theta=0.99, omax=16):
     return G.gen_ycsb(seed, rows, cols, 1, omax, 0.7, theta, batch=0, n_txns=n)
 
 
-@pytest.mark.parametrize("eager", [True, False])
-def test_serving_ordered_rule_loadgen(eager):
+@pytest.mark.parametrize("eager,persistent", [(True, False), (False, False), (True, True)])
+def test_serving_ordered_rule_loadgen(eager, persistent):
     rows, cols, seed = 1 << 12, 10, 31
     pool = _pool(seed, rows, cols, 20000)
     with G.Context(device=0) as ctx:
         t = ctx.create_table(rows, cols)
         ctx.fill_seeded(t, seed)
-        srv = G.Server(ctx, deadline_us=250, depth=3, max_txns=4096, max_ops=4096 * 16, eager=eager)
+        srv = G.Server(ctx, deadline_us=250, depth=3, max_txns=4096, max_ops=4096 * 16, eager=eager,
+                       persistent=persistent)
         srv.loadgen(rate=400000.0, seconds=0.04, n_streams=64, txn_first=pool[0], keys=pool[1], opw=pool[2],
                     seed=7, threads=4)
         got = []
@@ -134,7 +135,7 @@ def test_serving_mix_of_ycsb_and_tpcc_transactions():
         ctx.fill_seeded(t0, seed)
         ids = g.create_tables(ctx, extra)
         assert ids == list(range(1, 10)) and ctx.wide
-        srv = G.Server(ctx, deadline_us=200, depth=3, max_txns=2048, max_ops=2048 * 48)
+        srv = G.Server(ctx, deadline_us=200, depth=3, max_txns=2048, max_ops=2048 * 48, persistent=True)
         srv.loadgen(rate=300000.0, seconds=0.02, n_streams=32, txn_first=tf, keys=keys, opw=opw, seed=3, threads=4,
                     pay_first=pay_first, payload=payload)
         got = []
