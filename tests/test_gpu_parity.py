@@ -462,3 +462,37 @@ def test_pipeline_matches_oracle(lib_loaded, rule, persistent):
             assert st.ops == len(keys)
         pipe.close()
         assert np.array_equal(ctx.download(t), ref)
+
+
+def test_largest_table_row_ids(lib_loaded):
+    """A table at the row limit (2^31 rows x 1 int32 column, 8 GiB): ops on
+    the last rows and on row 0 share the batch; every index past 2^31 cells
+    stays exact (row ids, cell numbers, conflict words)."""
+    rows = 1 << 31
+    with G.Context(device=0) as ctx:
+        t = ctx.create_table(rows, 1)
+        hi = np.array([rows - 1, rows - 2, rows - 33, 0, 1], np.uint64)
+        init = np.array([7, -5, 2**31 - 1, 11, 0], np.int32)
+        for r, v in zip(hi, init):
+            ctx.upload_column(t, 0, np.array([v], np.int32), row0=int(r))
+        # 3 transactions: RMWs and reads on the boundary rows, some cells shared
+        tf = np.array([0, 3, 6, 8], np.uint32)
+        keys = np.array([rows - 1, rows - 33, 0, rows - 1, rows - 2, 1, rows - 33, rows - 1], np.uint64)
+        opw = np.array([O.opword(1, 0, 0, 3), O.opword(1, 0, 0, 1), O.opword(0, 0, 0, 0),
+                        O.opword(0, 0, 0, 0), O.opword(1, 0, 0, -2), O.opword(1, 0, 0, 9),
+                        O.opword(0, 0, 0, 0), O.opword(1, 0, 0, 100)], np.uint32)
+        b = ctx.batch(3, 8)
+        b.load(tf, keys, opw)
+        b.execute()
+        commit, vals, st = b.results()
+        cells = {int(r): int(v) for r, v in zip(hi, init)}
+        expect = []
+        for k, w in zip(keys, opw):
+            imm = int(np.int32(np.uint32(w) >> np.uint32(12) << np.uint32(12)) >> 12) if (w & 3) == 1 else 0
+            cells[int(k)] = int(np.int32(np.uint32((cells[int(k)] + imm) & 0xFFFFFFFF)))
+            expect.append(cells[int(k)])
+        assert list(vals) == expect and st.contended_cells == 2
+        out = np.zeros(1, np.int32)
+        for r in hi:
+            G.lib.load().ltp_table_download(ctx.h, t, 0, int(r), 1, out.ctypes.data)
+            assert out[0] == cells[int(r)]
