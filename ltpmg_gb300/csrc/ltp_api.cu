@@ -604,9 +604,11 @@ int ltp_batches_execute(ltp_ctx *ctx, ltp_batch *const *batches, uint32_t n, int
             const Tuning &t = ctx->tuning[bucket_of(b->n_ops)];
             key.insert(key.end(), {(uint64_t)(uintptr_t)b, b->n_ops, b->n_txns, b->ops_per_txn,
                                    (uint64_t)(uintptr_t)b->payload, b->payload_len,
-                                   ((uint64_t)t.block << 32) | t.ipt,
+                                   ((uint64_t)t.block << 32) | t.ipt, (uint64_t)t.flags,
                                    (uint64_t)(b->have_events && (ctx->flags & LTP_FLAG_STAGE_TIMING))});
         }
+        key.push_back(ctx->tables.size());
+        key.push_back(ctx->any_wide ? 1u : 0u);
         if (!ctx->graph_exec || key != ctx->graph_key) {
             if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
             ctx->graph_exec = nullptr;
@@ -807,6 +809,9 @@ namespace {
 struct PipeSlot {
     ltp_batch *b = nullptr;
     cudaEvent_t in = nullptr, exec = nullptr, out = nullptr;
+    cudaGraphExec_t gexec = nullptr;   // this slot's captured launch sequence ...
+    std::vector<uint64_t> gkey;        // ... for batches of this shape
+    std::vector<uint64_t> last_key;    // shape of the slot's previous batch
     BatchDev *h_desc = nullptr;    // pinned staging of the batch descriptor (persistent execution)
     BatchDev *d_desc = nullptr;    // device copy the persistent kernel reads
     Counters **d_snap = nullptr;   // device array holding b->snap
@@ -843,6 +848,49 @@ static void pipe_stats(const PipeSlot &sl, ltp_stats *stats) {
     stats->contended_cells = c.M;
     stats->touched_words = c.n_tw;
     stats->bytes_algorithmic = 28ull * sl.b->n_ops + 4ull * sl.b->n_txns;
+}
+
+// Executes the slot's batch on sx.  A slot that sees two batches of the same
+// shape in a row captures their launch sequence as a CUDA graph and replays
+// it while the shape stays (one launch call instead of a dozen).
+static int pipe_execute(ltp_ctx *ctx, PipeSlot &sl, cudaStream_t sx) {
+    const ltp_batch *b = sl.b;
+    const Tuning &t = ctx->tuning[bucket_of(b->n_ops)];
+    const std::vector<uint64_t> key = {b->n_ops, b->n_txns, b->ops_per_txn, (uint64_t)(uintptr_t)b->payload,
+                                       b->payload_len, ((uint64_t)t.block << 32) | t.ipt, (uint64_t)t.flags,
+                                       (uint64_t)ctx->rule,
+                                       (uint64_t)(b->have_events && (ctx->flags & LTP_FLAG_STAGE_TIMING)),
+                                       ctx->tables.size(), ctx->any_wide ? 1u : 0u};
+    if (sl.gexec && key == sl.gkey) {
+        CK(cudaGraphLaunch(sl.gexec, sx));
+        sl.b->rule = ctx->rule;
+        sl.b->executed = true;
+        return LTP_OK;
+    }
+    if (key != sl.last_key) {
+        sl.last_key = key;
+        return execute_one(ctx, sl.b, sx, false);
+    }
+    if (sl.gexec) cudaGraphExecDestroy(sl.gexec);
+    sl.gexec = nullptr;
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(sx, cudaStreamCaptureModeRelaxed));
+    int rc = execute_one(ctx, sl.b, sx, false);
+    cudaError_t e = cudaStreamEndCapture(sx, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&sl.gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        sl.gexec = nullptr;
+        return cuda_fail(ctx, e, "cudaGraphInstantiate");
+    }
+    sl.gkey = key;
+    CK(cudaGraphLaunch(sl.gexec, sx));
+    return LTP_OK;
 }
 
 static int pipe_finalize(ltp_pipe *p, PipeSlot &sl) {
@@ -910,6 +958,7 @@ int ltp_pipe_free(ltp_pipe *p) {
         if (sl.out) cudaEventDestroy(sl.out);
         if (sl.host_ctr) cudaFreeHost(sl.host_ctr);
         if (sl.h_desc) cudaFreeHost(sl.h_desc);
+        if (sl.gexec) cudaGraphExecDestroy(sl.gexec);
         cudaFree(sl.d_desc);
         cudaFree(sl.d_snap);
     }
@@ -961,7 +1010,7 @@ static int pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, 
                              ctx->p_bar));
         sl.b->rule = ctx->rule;
         sl.b->executed = true;
-    } else if ((rc = execute_one(ctx, sl.b, sx, false))) {
+    } else if ((rc = pipe_execute(ctx, sl, sx))) {
         return rc;
     }
     CK(cudaMemcpyAsync(sl.host_ctr, sl.b->snap, sizeof(Counters), cudaMemcpyDeviceToHost, sx));

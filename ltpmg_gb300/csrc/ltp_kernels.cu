@@ -266,7 +266,8 @@ __device__ __forceinline__ bool insert_link_ok(const BatchDev &b, const TableDev
     if (!d) return true;
     if (opw_col(w) >= t.n_cols || d > i) return false;
     const u32 tid = op_tid(b, i);
-    const u64 first = b.txn_first ? (u64)b.txn_first[tid] : (u64)tid * b.ops_per_txn;
+    // fixed-length batches carry ops_per_txn (their txn_first buffer is not loaded)
+    const u64 first = b.ops_per_txn ? (u64)tid * b.ops_per_txn : (u64)b.txn_first[tid];
     return i - d >= first && opw_kind(b.opw[i - d]) <= LTP_OP_ADD;
 }
 
@@ -1122,8 +1123,9 @@ __device__ __forceinline__ void phase_r1_exec(const BatchDev &b, const TablesDev
             if (s.dminw[m] == tid) {
                 const u64 key = b.keys[i];
                 const u32 same = w & 0xFFCu;  // column and table fields
-                const u64 first = b.txn_first ? (u64)b.txn_first[tid] : (u64)tid * b.ops_per_txn;
-                const u64 end = b.txn_first ? (u64)b.txn_first[tid + 1] : first + b.ops_per_txn;
+                // fixed-length batches carry ops_per_txn (their txn_first buffer is not loaded)
+                const u64 first = b.ops_per_txn ? (u64)tid * b.ops_per_txn : (u64)b.txn_first[tid];
+                const u64 end = b.ops_per_txn ? first + b.ops_per_txn : (u64)b.txn_first[tid + 1];
                 for (u64 j = first; j < end; j++) {
                     if (j == i) continue;
                     const u32 wj = b.opw[j];

@@ -496,3 +496,30 @@ def test_largest_table_row_ids(lib_loaded):
         for r in hi:
             G.lib.load().ltp_table_download(ctx.h, t, 0, int(r), 1, out.ctypes.data)
             assert out[0] == cells[int(r)]
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+def test_pipeline_replays_captured_graphs(lib_loaded, rule):
+    """Batches of one shape through the pipeline: from the second batch of
+    that shape on a slot, the slot replays a captured CUDA graph; values and
+    the table still equal the serial replay, and a shape change falls back
+    to launches."""
+    rows, cols, seed = 1 << 13, 10, 18
+    with G.Context(device=0, rule=rule) as ctx:
+        t = ctx.create_table(rows, cols)
+        ctx.fill_seeded(t, seed)
+        ref = O.table_init(seed, rows, cols)
+        pipe = G.Pipe(ctx, 3, 2048, 2048 * 16)
+        subs = []
+        for k in range(11):
+            n = 2048 if k != 7 else 1000  # one shape change in the middle
+            tf, keys, opw = gen(seed, rows, cols, 16, 16, 0.7, 0.9, k, n)
+            commit = np.zeros(n, np.uint8)
+            vals = np.zeros(len(keys), np.int32)
+            subs.append((pipe.submit(None, keys, opw, commit, vals, ops_per_txn=16), tf, keys, opw, commit, vals))
+        for tk, tf, keys, opw, commit, vals in subs:
+            pipe.wait(tk)
+            ref, rc, ro = O.replay(rule, ref, tf, keys, opw)
+            assert np.array_equal(commit, rc) and np.array_equal(vals, ro)
+        pipe.close()
+        assert np.array_equal(ctx.download(t), ref)
