@@ -272,6 +272,7 @@ def run_ours(args, config):
     ctx.sync()
 
     # autotuning (untimed): tilings per size bucket, then the multi-batch mode
+    ctx.set_stage_timing(False)  # tune what the timed region runs: no event nodes
     tiles = fixed_tiles(ctx, dev, args.tiles) if args.tiles else AT.tune_buckets(ctx, dev, reps=2)
     if args.mode == "auto":
         mode, mode_ms = AT.tune_mode(ctx, dev)
@@ -510,6 +511,7 @@ def run_tpcc(args):
         b.load_payload(pay)
         dev.append(b)
     ctx.sync()
+    ctx.set_stage_timing(False)  # tune what the timed region runs: no event nodes
     tiles = fixed_tiles(ctx, dev, args.tiles) if args.tiles else AT.tune_buckets(ctx, dev[:1], reps=1)
     if args.mode == "auto":
         mode, mode_ms = AT.tune_mode(ctx, dev)
