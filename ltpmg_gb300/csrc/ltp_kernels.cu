@@ -648,6 +648,8 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
         }
         // uncontended ops execute in place; an uncontended read's cell is never
         // written in this batch, an uncontended RMW is its cell's only op
+        // (the cell is read only once the word says the op runs here: reading
+        // it speculatively for contended ops costs more than the overlap saves)
         long long val[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; k++)
@@ -682,8 +684,8 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
 }
 
 template <int BLOCK, int IPT>
-// register budget: 64 per thread up to 4 ops per thread, 128 above, so that
-// 64-bit cell values do not halve the resident blocks
+// register budget per thread: 40 up to 2 ops per thread, 48 up to 4, 96
+// above, so that 64-bit cell values do not cut the resident blocks
 __global__ void __launch_bounds__(BLOCK, 65536 / (BLOCK * (IPT <= 2 ? 40 : IPT <= 4 ? 48 : 96))) k_classify(BatchDev b, TablesDev T,
                                                                                           Scratch s, Counters *ctr) {
     phase_classify<BLOCK, IPT>(b, T, s, ctr);
