@@ -5,14 +5,17 @@
 //             written) built with warp-aggregated atomicOr; records every
 //             bitmap word the batch touches
 //   ids       contended cell = touched twice and written; scan over the
-//             touched words gives every contended cell a dense id and
-//             snapshots its value before the batch
+//             touched words gives every contended cell a dense id
+//   dbase     per contended id: the cell's address, width and value before
+//             the batch
 //   classify  uncontended ops execute in place (one toucher, or no writer);
-//             contended ops are compacted in op order as (id, op) records
+//             contended ops are compacted in op order as (id, imm, op)
+//             records at dense positions
 //   sort      stable LSD radix sort of the contended records by id
 //   apply     segmented scan of the RMW immediates per id: every op gets
 //             base + (sum of earlier RMWs on its cell in TID order); the last
 //             op of each cell writes the final value back
+//   insert    committed inserts get their rows (per-table ordered prefix)
 //   finish    clears exactly the bitmap words and look-back slots the batch
 //             used, so the next batch starts clean
 //
@@ -553,8 +556,7 @@ __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Count
 // and histogram the contended ids' radix digits for the sort
 // ============================================================================
 // Radix passes over the contended ids: 8 bits each, at least one pass as soon
-// as there is a contended cell (the first pass also gathers the per-tile
-// regions written by classify into one dense list).
+// as there is a contended cell.
 // Contended-op records.  Packed (fewer than 2^20 contended cells and at most
 // 2^24 ops): id << 44 | imm20 << 24 | op -- the RMW immediate travels with
 // the record (a read carries 0, which is what it adds).  Otherwise:
