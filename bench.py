@@ -753,10 +753,10 @@ def run_serve(args):
     for rate, t_load in zip(loads, t_loads):
         srv = G.Server(ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 18, max_ops=1 << 22,
                        keep_results=False, persistent=args.serve_mode == "persistent")
-        # load-generator threads: every host core but those of the dispatcher,
-        # the completer and this thread
-        srv.loadgen(rate, t_load, 256, ptf, pk, pw, seed=int(rate), threads=max(4, (os.cpu_count() or 8) - 4),
-                    pay_first=ppf, payload=ppay)
+        # eight load-generator threads (half the host cores of the GPU
+        # machine): more of them busy-wait the dispatcher and completer off
+        # their cores
+        srv.loadgen(rate, t_load, 256, ptf, pk, pw, seed=int(rate), threads=8, pay_first=ppf, payload=ppay)
         st = srv.close()
         truncate()
         st["offered_txn_per_s"] = rate
