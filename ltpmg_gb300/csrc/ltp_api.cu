@@ -49,6 +49,10 @@ struct ltp_ctx {
     Counters **p_snaps = nullptr;
     uint32_t p_cap = 0;
     u32 *p_bar = nullptr;
+    std::vector<uint64_t> p_key;          // batch list whose descriptors are on the device
+    cudaGraphExec_t p_exec = nullptr;     // captured persistent launch for that list
+    cudaStream_t p_stream = nullptr;
+    bool p_no_graph = false;              // capture of the cooperative launch failed once: launch directly
 };
 
 struct ltp_batch {
@@ -262,6 +266,7 @@ int ltp_shutdown(ltp_ctx *ctx) {
     cudaFree(ctx->ctr);
     cudaFree(ctx->rows_now);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->p_exec) cudaGraphExecDestroy(ctx->p_exec);
     cudaFree(ctx->p_batches);
     cudaFree(ctx->p_snaps);
     cudaFree(ctx->p_bar);
@@ -636,32 +641,70 @@ int ltp_batches_execute(ltp_ctx *ctx, ltp_batch *const *batches, uint32_t n, int
         }
         return LTP_OK;
     }
-    // persistent: one cooperative kernel over all batches
-    if (n > ctx->p_cap) {
-        CK(cudaStreamSynchronize(st));
-        cudaFree(ctx->p_batches);
-        cudaFree(ctx->p_snaps);
-        ctx->p_batches = nullptr;
-        ctx->p_snaps = nullptr;
-        ctx->p_cap = 0;
-        CK(dalloc(&ctx->p_batches, n));
-        CK(dalloc(&ctx->p_snaps, n));
-        ctx->p_cap = n;
-    }
-    if (!ctx->p_bar) CK(dalloc(&ctx->p_bar, 2));
-    std::vector<BatchDev> hb(n);
-    std::vector<Counters *> hs(n);
+    // persistent: one cooperative kernel over all batches.  The batch
+    // descriptors stay on the device while the list is unchanged, and the
+    // launch (counter reset + cooperative kernel) is a captured CUDA graph.
+    std::vector<uint64_t> key = {(uint64_t)ctx->rule, ctx->tables.size(), ctx->any_wide ? 1u : 0u};
     for (uint32_t i = 0; i < n; i++) {
-        hb[i] = batch_dev(batches[i]);
-        hb[i].flags = ctx->tuning[bucket_of(batches[i]->n_ops)].flags;
-        hs[i] = batches[i]->snap;
+        const ltp_batch *b = batches[i];
+        key.insert(key.end(), {(uint64_t)(uintptr_t)b, b->n_ops, b->n_txns, b->ops_per_txn,
+                               (uint64_t)(uintptr_t)b->payload, b->payload_len,
+                               (uint64_t)ctx->tuning[bucket_of(b->n_ops)].flags});
     }
-    CK(cudaMemcpyAsync(ctx->p_batches, hb.data(), n * sizeof(BatchDev), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(ctx->p_snaps, hs.data(), n * sizeof(Counters *), cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(ctx->ctr, 0, sizeof(Counters), st));
-    CK(launch_persistent(st, ctx->num_sms, ctx->rule, ctx->p_batches, ctx->p_snaps, n, tables_dev(ctx), ctx->s,
-                         ctx->ctr, ctx->p_bar));
-    CK(cudaStreamSynchronize(st));  // the descriptor arrays are host staging above
+    if (key != ctx->p_key) {
+        CK(cudaStreamSynchronize(st));
+        if (ctx->p_exec) cudaGraphExecDestroy(ctx->p_exec);
+        ctx->p_exec = nullptr;
+        ctx->p_key.clear();
+        if (n > ctx->p_cap) {
+            cudaFree(ctx->p_batches);
+            cudaFree(ctx->p_snaps);
+            ctx->p_batches = nullptr;
+            ctx->p_snaps = nullptr;
+            ctx->p_cap = 0;
+            CK(dalloc(&ctx->p_batches, n));
+            CK(dalloc(&ctx->p_snaps, n));
+            ctx->p_cap = n;
+        }
+        if (!ctx->p_bar) CK(dalloc(&ctx->p_bar, 2));
+        std::vector<BatchDev> hb(n);
+        std::vector<Counters *> hs(n);
+        for (uint32_t i = 0; i < n; i++) {
+            hb[i] = batch_dev(batches[i]);
+            hb[i].flags = ctx->tuning[bucket_of(batches[i]->n_ops)].flags;
+            hs[i] = batches[i]->snap;
+        }
+        CK(cudaMemcpy(ctx->p_batches, hb.data(), n * sizeof(BatchDev), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->p_snaps, hs.data(), n * sizeof(Counters *), cudaMemcpyHostToDevice));
+        ctx->p_key = key;
+    }
+    if (ctx->p_exec && ctx->p_stream != st) {
+        cudaGraphExecDestroy(ctx->p_exec);
+        ctx->p_exec = nullptr;
+    }
+    if (!ctx->p_exec) {
+        persistent_grid(ctx->num_sms);  // kernel attributes, outside the capture
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = ctx->p_no_graph ? cudaErrorNotSupported : cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            cudaMemsetAsync(ctx->ctr, 0, sizeof(Counters), st);
+            launch_persistent(st, ctx->num_sms, ctx->rule, ctx->p_batches, ctx->p_snaps, n, tables_dev(ctx), ctx->s,
+                              ctx->ctr, ctx->p_bar);
+            e = cudaStreamEndCapture(st, &graph);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->p_exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {  // a driver without captured cooperative launches: launch directly
+            (void)cudaGetLastError();
+            ctx->p_exec = nullptr;
+            ctx->p_no_graph = true;
+            CK(cudaMemsetAsync(ctx->ctr, 0, sizeof(Counters), st));
+            CK(launch_persistent(st, ctx->num_sms, ctx->rule, ctx->p_batches, ctx->p_snaps, n, tables_dev(ctx),
+                                 ctx->s, ctx->ctr, ctx->p_bar));
+        }
+        ctx->p_stream = st;
+    }
+    if (ctx->p_exec) CK(cudaGraphLaunch(ctx->p_exec, st));
     for (uint32_t i = 0; i < n; i++) {
         batches[i]->rule = ctx->rule;
         batches[i]->executed = true;
