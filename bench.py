@@ -47,7 +47,7 @@ WORKLOAD_TEXT = {
 # algorithmic bytes per kernel launch, from the batch's counters
 KERNEL_BYTES = {
     "mark": lambda st: 16 * st["ops"],
-    "ids": lambda st: 20 * st["touched_words"] + 16 * st["contended_cells"],
+    "ids": lambda st: 20 * st["touched_words"] + 32 * st["contended_cells"],  # id scan + pre-batch values
     "classify": lambda st: 28 * st["ops"],
     "sort_pass0": lambda st: 16 * st["contended_ops"],
     "sort_pass1": lambda st: 16 * st["contended_ops"],

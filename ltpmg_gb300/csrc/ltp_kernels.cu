@@ -229,9 +229,6 @@ __device__ __forceinline__ void store_cell_hint(char *p, bool wide, long long v,
 __device__ __forceinline__ long long load_cell(const char *p, bool wide) {
     return wide ? *reinterpret_cast<const long long *>(p) : (long long)*reinterpret_cast<const int32_t *>(p);
 }
-__device__ __forceinline__ long long load_cell_ro(const char *p, bool wide) {
-    return wide ? __ldg(reinterpret_cast<const long long *>(p)) : (long long)__ldg(reinterpret_cast<const int32_t *>(p));
-}
 __device__ __forceinline__ void store_cell(char *p, bool wide, long long v) {
     if (wide) *reinterpret_cast<long long *>(p) = v;
     else *reinterpret_cast<int32_t *>(p) = (int32_t)v;
@@ -473,7 +470,7 @@ __global__ void __launch_bounds__(256) k_dbase(TablesDev T, Scratch s, Counters 
     phase_dbase(T, s, ctr, priority != 0);
 }
 
-template <bool PRIORITY, int BLK>
+template <int BLK>
 __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, Counters *ctr) {
     constexpr u32 IPT = kIdsTile / BLK;
     if (block_err(ctr)) return;
@@ -546,9 +543,8 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
     }
 }
 
-template <bool PRIORITY>
 __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Counters *ctr) {
-    phase_ids<PRIORITY, kIdsBlock>(T, s, ctr);
+    phase_ids<kIdsBlock>(T, s, ctr);
 }
 
 // ============================================================================
@@ -1459,12 +1455,11 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDe
     {
         static int gi = 0, sms = 0;
         if (sms != L.num_sms) {
-            gi = occ_grid(k_ids<false>, kIdsBlock, L.num_sms);
+            gi = occ_grid(k_ids, kIdsBlock, L.num_sms);
             sms = L.num_sms;
         }
         const int g = capped(gi, (b.n_ops + kIdsTile - 1) / kIdsTile);
-        if (L.rule == LTP_RULE_PRIORITY) k_ids<true><<<g, kIdsBlock, 0, L.stream>>>(T, s, ctr);
-        else k_ids<false><<<g, kIdsBlock, 0, L.stream>>>(T, s, ctr);
+        k_ids<<<g, kIdsBlock, 0, L.stream>>>(T, s, ctr);
         k_dbase<<<L.num_sms * 8, 256, 0, L.stream>>>(T, s, ctr, L.rule == LTP_RULE_PRIORITY);
     }
     mark_ev(2);
@@ -1584,8 +1579,7 @@ __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
         if (block_err(a.ctr)) break;
         phase_mark<kPBlock, kPIpt>(b, a.T, a.s, a.ctr);
         grid_sync(a.bar, nb, a.ctr);
-        if (a.rule == LTP_RULE_PRIORITY) phase_ids<true, kPBlock>(a.T, a.s, a.ctr);
-        else phase_ids<false, kPBlock>(a.T, a.s, a.ctr);
+        phase_ids<kPBlock>(a.T, a.s, a.ctr);
         grid_sync(a.bar, nb, a.ctr);
         phase_dbase(a.T, a.s, a.ctr, a.rule == LTP_RULE_PRIORITY);
         grid_sync(a.bar, nb, a.ctr);
