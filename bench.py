@@ -756,7 +756,8 @@ def run_serve(args):
         # eight load-generator threads (half the host cores of the GPU
         # machine): more of them busy-wait the dispatcher and completer off
         # their cores
-        srv.loadgen(rate, t_load, 256, ptf, pk, pw, seed=int(rate), threads=8, pay_first=ppf, payload=ppay)
+        srv.loadgen(rate, t_load, 256, ptf, pk, pw, seed=int(rate), threads=args.loadgen_threads, pay_first=ppf,
+                    payload=ppay)
         st = srv.close()
         truncate()
         st["offered_txn_per_s"] = rate
@@ -824,6 +825,7 @@ def main():
                     help="fixed BLOCKxIPT[+precheck] tiling instead of the autotuner's (e.g. 512x4)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
+    ap.add_argument("--loadgen-threads", type=int, default=8, help="serving sweep: load-generator threads")
     ap.add_argument("--serve-mode", default="persistent", choices=["persistent", "stream"],
                     help="serving: each batch as one persistent-kernel launch, or as a kernel sequence")
     args = ap.parse_args()

@@ -92,14 +92,40 @@ struct Seg {
     }
 };
 
-struct Lane {
-    std::mutex mu;
+// Lock for sections of a few dozen nanoseconds (a lane's append or swap):
+// waiting threads spin, then yield, instead of sleeping in the kernel.
+struct SpinLock {
+    std::atomic<bool> f{false};
+    void lock() {
+        for (unsigned n = 0; f.exchange(true, std::memory_order_acquire);)
+            while (f.load(std::memory_order_relaxed))
+                if (++n > 64) std::this_thread::yield();
+    }
+    void unlock() { f.store(false, std::memory_order_release); }
+};
+
+// An admission lane.  The dispatcher reads the counters without the lock to
+// decide whether a batch is due, and takes the segment only when it closes
+// one, so segments hold a batch's worth of a lane's arrivals.
+struct alignas(64) Lane {
+    SpinLock mu;
     std::shared_ptr<Seg> seg;
+    std::atomic<uint64_t> oldest{UINT64_MAX};  // earliest arrival in seg
+    std::atomic<uint64_t> n_txns{0}, n_ops{0};  // what seg holds
+    std::atomic<uint64_t> submitted{0};         // written under mu only
 };
 
 struct Run {  // transactions [first, first+count) of a segment inside a batch
     std::shared_ptr<Seg> seg;
     size_t first, count;
+};
+
+// Part of a batch: transactions [i0, i1) of a segment, placed at transaction
+// t0, op o0 and payload slot p0 of the slot's arrays.
+struct Piece {
+    Seg *g;
+    size_t i0, i1;
+    uint64_t t0, o0, p0;
 };
 
 struct Slot {
@@ -178,14 +204,28 @@ struct ltp_server {
     std::mutex res_mu;
     std::vector<ltp_serve_result> results;
     Histo histo;
-    std::atomic<uint64_t> submitted{0};
+    std::atomic<bool> started{false};
     std::atomic<uint64_t> completed{0}, committed{0};
     std::atomic<uint64_t> dispatch_ns{0}, complete_ns{0}, lg_total{0}, lg_late{0};
     uint64_t aborted_attempts = 0, batches = 0, ops = 0;
     uint64_t closed_deadline = 0, closed_budget = 0, closed_idle = 0;
-    uint64_t t_first = 0, t_last = 0, seq = 0;
+    std::atomic<uint64_t> t_first{0};
+    uint64_t t_last = 0, seq = 0;
     std::mutex free_mu;
     std::vector<std::shared_ptr<Seg>> free_segs;
+    // batch assembly: the dispatcher cuts the batch into pieces and copies
+    // them together with the helper threads.  claim = generation << 40 |
+    // piece count << 20 | next piece; a helper claims a piece only while the
+    // generation it saw is current and pieces remain, so a late helper never
+    // reads the list while the dispatcher rebuilds it for the next batch.
+    std::vector<Piece> pieces;
+    Slot *asm_slot = nullptr;
+    std::atomic<uint64_t> claim{0};
+    std::atomic<uint64_t> pieces_done{0};
+    std::atomic<bool> helpers_stop{false};
+    std::mutex asm_mu;
+    std::condition_variable asm_cv;  // a new generation was published
+    std::vector<std::thread> helpers;
 };
 
 namespace {
@@ -213,12 +253,16 @@ void recycle(ltp_server *s, std::shared_ptr<Seg> &p) {
 
 void drain_lanes(ltp_server *s) {
     for (auto &lp : s->lanes) {
+        if (lp->n_txns.load(std::memory_order_relaxed) == 0) continue;
         std::shared_ptr<Seg> got;
         {
-            std::lock_guard<std::mutex> g(lp->mu);
+            std::lock_guard<SpinLock> g(lp->mu);
             if (!lp->seg || lp->seg->n() == 0) continue;
             got = std::move(lp->seg);
             lp->seg = nullptr;
+            lp->oldest.store(UINT64_MAX, std::memory_order_relaxed);
+            lp->n_txns.store(0, std::memory_order_relaxed);
+            lp->n_ops.store(0, std::memory_order_relaxed);
         }
         s->pending_txns += got->n();
         s->pending_ops += got->keys.size();
@@ -306,16 +350,82 @@ uint64_t oldest_pending(const ltp_server *s) {
     return o;
 }
 
+// Copies one piece into the slot: keys, opwords, payload (with insert keys
+// rebased onto the batch payload) and the transactions' op offsets.
+void copy_piece(Slot &sl, const Piece &pc) {
+    const Seg &g = *pc.g;
+    const uint32_t a = g.off[pc.i0], b = g.off[pc.i1];
+    memcpy(sl.keys + pc.o0, g.keys.data() + a, (size_t)(b - a) * sizeof(uint64_t));
+    memcpy(sl.opw + pc.o0, g.opw.data() + a, (size_t)(b - a) * sizeof(uint32_t));
+    const uint32_t pa = g.poff[pc.i0], pb = g.poff[pc.i1];
+    if (pb > pa) {
+        memcpy(sl.payload + pc.p0, g.payload.data() + pa, (size_t)(pb - pa) * sizeof(int32_t));
+        const uint64_t delta = pc.p0 - pa;
+        for (uint64_t j = pc.o0; j < pc.o0 + (b - a); j++)
+            if (is_insert(sl.opw[j])) sl.keys[j] += delta;
+    }
+    for (size_t i = pc.i0; i < pc.i1; i++) sl.txn_first[pc.t0 + (i - pc.i0) + 1] = (uint32_t)(pc.o0 + g.off[i + 1] - a);
+}
+
+constexpr uint64_t kClaimMask = (1u << 20) - 1;
+inline uint64_t claim_gen(uint64_t c) { return c >> 40; }
+
+// Copies pieces of the current generation until none is left unclaimed.
+void copy_pieces(ltp_server *s, uint64_t gen) {
+    for (;;) {
+        uint64_t c = s->claim.load(std::memory_order_acquire);
+        if (claim_gen(c) != gen) return;
+        const uint32_t i = (uint32_t)(c & kClaimMask);
+        if (i >= ((c >> 20) & kClaimMask)) return;
+        if (!s->claim.compare_exchange_weak(c, c + 1, std::memory_order_acq_rel)) continue;
+        copy_piece(*s->asm_slot, s->pieces[i]);
+        s->pieces_done.fetch_add(1, std::memory_order_acq_rel);
+    }
+}
+
+// Sleeps until a batch is published, then helps copy it (the dispatcher
+// starts copying at once, so a helper that wakes late only helps less).
+void helper_loop(ltp_server *s) {
+    uint64_t seen = claim_gen(s->claim.load());
+    for (;;) {
+        uint64_t gen;
+        {
+            std::unique_lock<std::mutex> lk(s->asm_mu);
+            s->asm_cv.wait(lk, [&] {
+                return s->helpers_stop.load() || claim_gen(s->claim.load(std::memory_order_acquire)) != seen;
+            });
+            if (s->helpers_stop.load()) return;
+            gen = claim_gen(s->claim.load(std::memory_order_acquire));
+        }
+        seen = gen;
+        copy_pieces(s, gen);
+    }
+}
+
+constexpr unsigned kHelpers = 3;          // batch-assembly threads besides the dispatcher
+constexpr size_t kPieceTxns = 2048;  // transactions per piece at most
+constexpr uint64_t kParallelOps = 16384;  // smaller batches are copied by the dispatcher alone
+
 bool close_batch(ltp_server *s, uint64_t now) {
-    if (s->n_inflight.load() >= s->cfg.depth || s->pending_txns == 0) return false;
+    if (s->n_inflight.load() >= s->cfg.depth) return false;
+    // what is waiting, pending or still in the lanes (read without locking)
+    uint64_t oldest = oldest_pending(s), w_txns = s->pending_txns, w_ops = s->pending_ops;
+    for (const auto &lp : s->lanes) {
+        oldest = std::min(oldest, lp->oldest.load(std::memory_order_relaxed));
+        w_txns += lp->n_txns.load(std::memory_order_relaxed);
+        w_ops += lp->n_ops.load(std::memory_order_relaxed);
+    }
+    if (w_txns == 0) return false;
     const uint64_t cap_ops = std::min<uint64_t>(s->cfg.max_ops, s->cfg.budget_bytes / 12);
-    const bool deadline = now >= oldest_pending(s) + (uint64_t)s->cfg.deadline_us * 1000ull;
-    const bool full = s->pending_ops >= cap_ops || s->pending_txns >= s->cfg.max_txns;
+    const bool deadline = oldest != UINT64_MAX && now >= oldest + (uint64_t)s->cfg.deadline_us * 1000ull;
+    const bool full = w_ops >= cap_ops || w_txns >= s->cfg.max_txns;
     const bool idle = (s->cfg.flags & LTP_SERVE_EAGER) && s->n_inflight.load() == 0;
     if (!deadline && !full && !idle) return false;
     uint32_t si = 0;
     while (si < s->n_slots && s->slots[si].busy.load(std::memory_order_acquire)) si++;
     if (si == s->n_slots) return false;
+    drain_lanes(s);
+    if (s->pending_txns == 0) return false;
     if (deadline) s->closed_deadline++;
     else if (full) s->closed_budget++;
     else s->closed_idle++;
@@ -323,38 +433,52 @@ bool close_batch(ltp_server *s, uint64_t now) {
     uint64_t nops = 0, npay = 0;
     uint32_t nt = 0;
     sl.txn_first[0] = 0;
+    s->pieces.clear();
     while (!s->pending.empty() && nt < s->cfg.max_txns) {
         std::shared_ptr<Seg> &p = s->pending.front();
         Seg &g = *p;
-        // largest run of this segment that fits
-        size_t k = g.head;
-        while (k < g.n() && nt + (k - g.head) < s->cfg.max_txns && nops + (g.off[k + 1] - g.off[g.head]) <= cap_ops &&
-               npay + (g.poff[k + 1] - g.poff[g.head]) <= s->max_payload)
-            k++;
-        const size_t cnt = k - g.head;
+        // largest run of this segment that fits (offsets are non-decreasing)
+        const size_t h = g.head;
+        size_t k = std::min<size_t>(g.n(), h + (s->cfg.max_txns - nt));
+        k = (size_t)(std::upper_bound(g.off.begin() + h, g.off.begin() + k + 1, g.off[h] + (cap_ops - nops)) -
+                     g.off.begin()) - 1;
+        k = (size_t)(std::upper_bound(g.poff.begin() + h, g.poff.begin() + k + 1,
+                                      g.poff[h] + (s->max_payload - npay)) - g.poff.begin()) - 1;
+        const size_t cnt = k - h;
         if (cnt) {
-            const uint32_t a = g.off[g.head], b = g.off[k];
-            memcpy(sl.keys + nops, g.keys.data() + a, (size_t)(b - a) * sizeof(uint64_t));
-            memcpy(sl.opw + nops, g.opw.data() + a, (size_t)(b - a) * sizeof(uint32_t));
-            const uint32_t pa = g.poff[g.head], pb = g.poff[k];
-            if (pb > pa) {  // move the run's payload and rebase its insert keys
-                memcpy(sl.payload + npay, g.payload.data() + pa, (size_t)(pb - pa) * sizeof(int32_t));
-                const uint64_t delta = npay - pa;
-                for (uint64_t j = nops; j < nops + (b - a); j++)
-                    if (is_insert(sl.opw[j])) sl.keys[j] += delta;
-                npay += pb - pa;
+            for (size_t i0 = h; i0 < k; i0 += kPieceTxns) {
+                const size_t i1 = std::min(k, i0 + kPieceTxns);
+                s->pieces.push_back(Piece{&g, i0, i1, nt + (i0 - h), nops + (g.off[i0] - g.off[h]),
+                                          npay + (g.poff[i0] - g.poff[h])});
             }
-            for (size_t i = g.head; i < k; i++) sl.txn_first[++nt] = (uint32_t)(nops + g.off[i + 1] - a);
-            nops += b - a;
-            sl.runs.push_back(Run{p, g.head, cnt});
+            const uint32_t ops = g.off[k] - g.off[h];
+            nt += (uint32_t)cnt;
+            nops += ops;
+            npay += g.poff[k] - g.poff[h];
+            sl.runs.push_back(Run{p, h, cnt});
             s->pending_txns -= cnt;
-            s->pending_ops -= (b - a);
+            s->pending_ops -= ops;
             g.head = k;
         }
         if (g.head == g.n()) {
             s->pending.pop_front();
         } else {
             break;  // the batch is full
+        }
+    }
+    if (nops < kParallelOps || s->helpers.empty() || s->pieces.size() > kClaimMask) {
+        for (const Piece &pc : s->pieces) copy_piece(sl, pc);
+    } else {
+        s->asm_slot = &sl;
+        s->pieces_done.store(0, std::memory_order_relaxed);
+        const uint64_t gen = (claim_gen(s->claim.load()) + 1) & ((1u << 24) - 1);
+        {
+            std::lock_guard<std::mutex> g(s->asm_mu);
+            s->claim.store(gen << 40 | (uint64_t)s->pieces.size() << 20, std::memory_order_release);
+        }
+        s->asm_cv.notify_all();
+        copy_pieces(s, gen);
+        while (s->pieces_done.load(std::memory_order_acquire) < s->pieces.size()) {
         }
     }
     if (nt == 0) return false;
@@ -398,7 +522,6 @@ void take_requeued(ltp_server *s) {
 // Admission and submission; completion runs on its own thread.
 void dispatch_loop(ltp_server *s) {
     for (;;) {
-        drain_lanes(s);
         take_requeued(s);
         const uint64_t t0 = now_ns();
         const bool progressed = close_batch(s, t0);
@@ -446,6 +569,23 @@ void complete_loop(ltp_server *s) {
     }
 }
 
+// Appends a checked transaction to its stream's lane.  key_base: what the
+// insert ops' keys are relative to (the start of `payload`).
+void admit(ltp_server *s, uint32_t stream, uint64_t at, uint64_t tag, uint32_t n_ops, const uint64_t *keys,
+           const uint32_t *opw, uint32_t n_payload, const int32_t *payload, uint64_t key_base) {
+    Lane &ln = *s->lanes[stream % s->lanes.size()];
+    {
+        std::lock_guard<SpinLock> g(ln.mu);
+        if (!ln.seg) ln.seg = new_seg(s);
+        ln.seg->push(at, tag, stream, 0, n_ops, keys, opw, n_payload, payload, key_base);
+        if (at < ln.oldest.load(std::memory_order_relaxed)) ln.oldest.store(at, std::memory_order_relaxed);
+        ln.n_txns.store(ln.n_txns.load(std::memory_order_relaxed) + 1, std::memory_order_relaxed);
+        ln.n_ops.store(ln.n_ops.load(std::memory_order_relaxed) + n_ops, std::memory_order_relaxed);
+        ln.submitted.store(ln.submitted.load(std::memory_order_relaxed) + 1, std::memory_order_relaxed);
+    }
+    if (!s->started.load(std::memory_order_relaxed) && !s->started.exchange(true)) s->t_first = at;
+}
+
 }  // namespace
 
 extern "C" {
@@ -488,6 +628,7 @@ int ltp_serve_open(ltp_ctx *ctx, const ltp_serve_config *cfg, ltp_server **out) 
     }
     s->dispatcher = std::thread(dispatch_loop, s);
     s->completer = std::thread(complete_loop, s);
+    for (unsigned i = 0; i < kHelpers; i++) s->helpers.emplace_back(helper_loop, s);
     *out = s;
     return LTP_OK;
 }
@@ -499,14 +640,7 @@ int ltp_serve_submit_rows(ltp_server *s, uint32_t stream, uint32_t n_ops, const 
     for (uint32_t j = 0; j < n_ops; j++)  // an insert's payload row must start inside this transaction's payload
         if (is_insert(opw[j]) && keys[j] >= n_payload) return LTP_E_BADARG;
     if (s->status) return s->status;
-    Lane &ln = *s->lanes[stream % s->lanes.size()];
-    const uint64_t at = arrival_ns ? arrival_ns : now_ns();
-    {
-        std::lock_guard<std::mutex> g(ln.mu);
-        if (!ln.seg) ln.seg = new_seg(s);
-        ln.seg->push(at, tag, stream, 0, n_ops, keys, opw, n_payload, payload, 0);
-    }
-    if (s->submitted.fetch_add(1) == 0) s->t_first = at;
+    admit(s, stream, arrival_ns ? arrival_ns : now_ns(), tag, n_ops, keys, opw, n_payload, payload, 0);
     return LTP_OK;
 }
 
@@ -538,43 +672,51 @@ int ltp_serve_loadgen_rows(ltp_server *s, double rate, double seconds, uint32_t 
     if (!s || rate <= 0 || seconds <= 0 || !n_streams || !txn_first || !n_pool || !keys || !opw) return LTP_E_BADARG;
     if ((pay_first == nullptr) != (payload == nullptr)) return LTP_E_BADARG;
     if (!n_threads) n_threads = 1;
+    // the pool is checked once, as ltp_serve_submit_rows checks a transaction
+    for (uint64_t k = 0; k < n_pool; k++) {
+        const uint32_t a = txn_first[k], n = txn_first[k + 1] - txn_first[k];
+        const uint64_t p0 = pay_first ? pay_first[k] : 0, np = pay_first ? pay_first[k + 1] - p0 : 0;
+        if (txn_first[k + 1] < a || (pay_first && pay_first[k + 1] < p0)) return LTP_E_BADARG;
+        if (n > LTP_SERVE_MAX_OPS || n > s->cfg.max_ops || np > s->max_payload) return LTP_E_CAPACITY;
+        for (uint32_t j = 0; j < n; j++)
+            if (is_insert(opw[a + j]) && (keys[a + j] < p0 || keys[a + j] - p0 >= np)) return LTP_E_BADARG;
+    }
+    const uint32_t n_lanes = (uint32_t)s->lanes.size();
     const uint64_t t0 = now_ns() + 1000000;  // start 1 ms from now
     const uint64_t t_end = t0 + (uint64_t)(seconds * 1e9);
     std::vector<std::thread> th;
     for (uint32_t g = 0; g < n_threads; g++) {
         th.emplace_back([=]() {
-            // this thread's streams: g, g + n_threads, ... ; its own slice of the pool
-            const uint32_t my_streams = (n_streams - g + n_threads - 1) / n_threads;
+            // this thread's streams: those whose lane no other generator
+            // thread uses (lane = stream mod lanes); its own slice of the pool
+            std::vector<uint32_t> mine;
+            for (uint32_t st = 0; st < n_streams; st++)
+                if ((st % n_lanes) % n_threads == g) mine.push_back(st);
+            const uint32_t my_streams = (uint32_t)mine.size();
             if (!my_streams) return;
             const double my_rate = rate * (double)my_streams / (double)n_streams;
             std::mt19937_64 rng(seed * 0x9E3779B97F4A7C15ULL + g + 1);
             std::exponential_distribution<double> gap(my_rate / 1e9);
             double t = (double)t0;
             uint64_t k = (n_pool * g) / n_threads;
-            uint64_t local_total = 0, local_late = 0;
+            uint64_t local_total = 0, local_late = 0, tn = 0;
             while (true) {
                 t += gap(rng);
                 const uint64_t at = (uint64_t)t;
                 if (at >= t_end || s->status) break;
-                uint64_t tn;
-                while ((tn = now_ns()) < at) {
-                }
+                if (tn < at)  // not due yet (a generator running behind skips the clock read)
+                    while ((tn = now_ns()) < at) {
+                    }
                 local_total++;
                 if (tn - at > 100000ull) local_late++;
-                const uint32_t st = g + n_threads * (uint32_t)(rng() % my_streams);
+                const uint32_t st = mine[rng() % my_streams];
                 const uint32_t a = txn_first[k], n = txn_first[k + 1] - txn_first[k];
-                int rc;
-                if (pay_first && pay_first[k + 1] > pay_first[k]) {
-                    // the pool's insert keys are offsets into the whole payload: make them txn-relative
-                    uint64_t kk[LTP_SERVE_MAX_OPS];
-                    const uint32_t nn = std::min<uint32_t>(n, LTP_SERVE_MAX_OPS);
-                    for (uint32_t j = 0; j < nn; j++) kk[j] = is_insert(opw[a + j]) ? keys[a + j] - pay_first[k] : keys[a + j];
-                    rc = ltp_serve_submit_rows(s, st, n, kk, opw + a, (uint32_t)(pay_first[k + 1] - pay_first[k]),
-                                               payload + pay_first[k], k, at);
-                } else {
-                    rc = ltp_serve_submit(s, st, n, keys + a, opw + a, k, at);
-                }
-                if (rc) break;
+                if (s->status) break;
+                if (pay_first)  // the pool's insert keys are offsets into the whole payload
+                    admit(s, st, at, k, n, keys + a, opw + a, (uint32_t)(pay_first[k + 1] - pay_first[k]),
+                          payload + pay_first[k], pay_first[k]);
+                else
+                    admit(s, st, at, k, n, keys + a, opw + a, 0, nullptr, 0);
                 if (++k == n_pool) k = 0;
             }
             s->lg_total += local_total;
@@ -588,7 +730,7 @@ int ltp_serve_loadgen_rows(ltp_server *s, double rate, double seconds, uint32_t 
 int ltp_serve_stats_now(ltp_server *s, ltp_serve_stats *st) {
     if (!s || !st) return LTP_E_BADARG;
     memset(st, 0, sizeof(*st));
-    st->submitted = s->submitted;
+    for (const auto &lp : s->lanes) st->submitted += lp->submitted.load(std::memory_order_relaxed);
     st->completed = s->completed;
     st->committed = s->committed;
     st->aborted_attempts = s->aborted_attempts;
@@ -605,7 +747,8 @@ int ltp_serve_stats_now(ltp_server *s, ltp_serve_stats *st) {
         st->mean_us = s->histo.n ? s->histo.sum / (double)s->histo.n / 1e3 : 0;
         st->max_us = (double)s->histo.mx / 1e3;
     }
-    st->elapsed_s = s->t_last > s->t_first ? (double)(s->t_last - s->t_first) / 1e9 : 0;
+    const uint64_t t_first = s->t_first.load();
+    st->elapsed_s = s->t_last > t_first ? (double)(s->t_last - t_first) / 1e9 : 0;
     st->dispatch_busy_s = (double)s->dispatch_ns.load() / 1e9;
     st->complete_busy_s = (double)s->complete_ns.load() / 1e9;
     st->loadgen_late_frac = s->lg_total.load() ? (double)s->lg_late.load() / (double)s->lg_total.load() : 0.0;
@@ -618,6 +761,12 @@ int ltp_serve_close(ltp_server *s, ltp_serve_stats *st) {
     s->stop = true;
     if (s->dispatcher.joinable()) s->dispatcher.join();
     if (s->completer.joinable()) s->completer.join();
+    {
+        std::lock_guard<std::mutex> g(s->asm_mu);
+        s->helpers_stop = true;
+    }
+    s->asm_cv.notify_all();
+    for (auto &h : s->helpers) h.join();
     if (st) ltp_serve_stats_now(s, st);
     const int status = s->status;
     if (s->pipe) ltp_pipe_free(s->pipe);
