@@ -18,7 +18,7 @@
  * Mapping of the reference's operations (cuda/src/gpuquery.cu:2929-3303):
  *  - a YCSB "select" of a row reads every int column of the row; an "update"
  *    adds 1 to every int column of the row (the reference's operators leave
- *    the row unchanged, cuda/src/gpulauncher.cu:79-103; BASELINE's RMW is +1);
+ *    the row unchanged, cuda/src/gpulauncher.cu:79-103; the YCSB workloads here add +1);
  *  - YCSB_E's 9 scans of rows [r, r+2) read those rows; its insert appends a
  *    row whose int columns are the query's ROW_ID[9] (the reference's insert
  *    operator is also an identity on an existing row);

@@ -326,6 +326,39 @@ int ltp_serve_close(ltp_server *s, ltp_serve_stats *st);
 /* Current CLOCK_MONOTONIC time in ns (the clock arrivals are stamped with). */
 uint64_t ltp_now_ns(void);
 
+/* ---- serving from a device-resident request log --------------------------
+ * Requests are already in HBM when they arrive -- the way a NIC writing by
+ * GPUDirect RDMA places them -- and carry arrival times; the host touches no
+ * request.  One host thread admits, by the clock, every request whose arrival
+ * time has passed, closes batches with the rules of ltp_serve_config
+ * (deadline, max_txns / max_ops / 6 x max_ops payload slots, read/write-set
+ * budget, LTP_SERVE_EAGER), keeps `depth` batches in flight, and re-queues
+ * transactions the priority rule aborted at the head of the next batch it
+ * closes (up to max_attempts tries).  Batches are gathered on the device:
+ * re-queued transactions first, then the newly arrived requests in arrival
+ * order; a batch of new requests only (no wrap of the pool) is executed in
+ * place from the log.  Latency = the host time the batch was seen complete -
+ * arrival time.
+ *
+ * The log is a pool of n_pool transactions (txn_first[n_pool + 1] op
+ * offsets; optional payload as in ltp_serve_loadgen_rows); request i of a run
+ * is pool transaction i mod n_pool. */
+typedef struct ltp_ingest ltp_ingest;
+int ltp_ingest_open(ltp_ctx *ctx, const ltp_serve_config *cfg, uint64_t n_pool, const uint32_t *txn_first,
+                    const uint64_t *keys, const uint32_t *opw, const uint64_t *pay_first, const int32_t *payload,
+                    ltp_ingest **out);
+/* Serves n_txns requests; arrival_ns[i] = request i's arrival, in ns after
+ * the run's start (non-decreasing).  Returns when every request is committed
+ * or has used its tries.  Tables keep the effects; a later run continues. */
+int ltp_ingest_run(ltp_ingest *g, uint64_t n_txns, const uint64_t *arrival_ns, ltp_serve_stats *st);
+/* Per request of the last run (any pointer may be NULL): committed flag,
+ * the batch that executed its last try and its position (TID) there, tries.
+ * vals (int64, one per op of requests 0..n_txns-1 in log order) needs
+ * LTP_SERVE_KEEP_RESULTS and n_txns <= n_pool. */
+int ltp_ingest_results(ltp_ingest *g, uint8_t *committed, uint64_t *batch_seq, uint32_t *pos, uint32_t *attempts,
+                       int64_t *vals);
+int ltp_ingest_close(ltp_ingest *g);
+
 /* ---- pinned host memory ------------------------------------------------ */
 void *ltp_host_alloc(size_t bytes);
 void ltp_host_free(void *p);

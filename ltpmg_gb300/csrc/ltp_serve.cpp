@@ -37,6 +37,7 @@
 #include <vector>
 
 #include "../../include/ltpmg_gb300.h"
+#include "ltp_histo.h"
 
 namespace {
 
@@ -140,41 +141,6 @@ struct Slot {
     std::atomic<bool> busy{false};  // set by the dispatcher, cleared by the completer
 };
 
-// Latency histogram without floating point: 64 linear sub-buckets per
-// power of two of nanoseconds (~1.6% wide).
-struct Histo {
-    static constexpr int kSub = 64;
-    std::vector<uint64_t> h = std::vector<uint64_t>(64 * kSub, 0);
-    uint64_t n = 0, mx = 0;
-    double sum = 0;
-    static int bucket(uint64_t ns) {
-        if (ns < kSub) return (int)ns;
-        const int e = 63 - __builtin_clzll(ns);  // >= 6
-        return e * kSub + (int)((ns >> (e - 6)) & (kSub - 1));
-    }
-    static double lower(int b) {
-        const int e = b / kSub, m = b % kSub;
-        if (e < 6) return (double)b;
-        return std::ldexp(1.0 + m / (double)kSub, e);
-    }
-    void add(uint64_t ns) {
-        h[bucket(ns)]++;
-        n++;
-        sum += (double)ns;
-        mx = std::max(mx, ns);
-    }
-    double pct(double p) const {
-        if (!n) return 0;
-        const uint64_t want = (uint64_t)std::ceil(p * (double)n);
-        uint64_t acc = 0;
-        for (size_t b = 0; b < h.size(); b++) {
-            acc += h[b];
-            if (acc >= want) return std::min(lower((int)b + 1), (double)mx);
-        }
-        return (double)mx;
-    }
-};
-
 }  // namespace
 
 struct ltp_server {
@@ -203,7 +169,7 @@ struct ltp_server {
     std::atomic<int> status{0};
     std::mutex res_mu;
     std::vector<ltp_serve_result> results;
-    Histo histo;
+    ltp::Histo histo;
     std::atomic<bool> started{false};
     std::atomic<uint64_t> completed{0}, committed{0};
     std::atomic<uint64_t> dispatch_ns{0}, complete_ns{0}, lg_total{0}, lg_late{0};

@@ -168,6 +168,10 @@ def load():
         "ltp_serve_stats_now": (ci, [vp, ctypes.POINTER(ServeStats)]),
         "ltp_serve_close": (ci, [vp, ctypes.POINTER(ServeStats)]),
         "ltp_now_ns": (u64, []),
+        "ltp_ingest_open": (ci, [vp, ctypes.POINTER(ServeConfig), u64, vp, vp, vp, vp, vp, pp]),
+        "ltp_ingest_run": (ci, [vp, u64, vp, ctypes.POINTER(ServeStats)]),
+        "ltp_ingest_results": (ci, [vp, vp, vp, vp, vp, vp]),
+        "ltp_ingest_close": (ci, [vp]),
         "ltp_execute_noalloc": (ci, [i32, i32, vp, u64, u64, u32, u64, vp, u32, u64, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
@@ -641,3 +645,55 @@ class Server:
             self.h = None
             self.ctx.check(rc)
         return st.as_dict()
+
+
+class Ingest:
+    """Serving from a device-resident request log (the C-ABI ltp_ingest):
+    the pool goes to the device once; run() serves requests 0..n-1 (request i
+    = pool transaction i mod pool size) at their arrival times."""
+
+    def __init__(self, ctx, txn_first, keys, opw, pay_first=None, payload=None, deadline_us=250, depth=3,
+                 budget_bytes=4 << 30, max_txns=1 << 20, max_ops=1 << 24, max_attempts=64, eager=True,
+                 keep_results=False):
+        self.ctx = ctx
+        flags = (1 if eager else 0) | (2 if keep_results else 0)
+        cfg = ServeConfig(deadline_us, depth, budget_bytes, max_txns, max_ops, max_attempts, flags)
+        self._pool = (np.ascontiguousarray(txn_first, np.uint32), np.ascontiguousarray(keys, np.uint64),
+                      np.ascontiguousarray(opw, np.uint32),
+                      None if pay_first is None else np.ascontiguousarray(pay_first, np.uint64),
+                      None if payload is None else np.ascontiguousarray(payload, np.int32))
+        tf, k, w, pf, pl = self._pool
+        self.n_pool = len(tf) - 1
+        h = ctypes.c_void_p()
+        ctx.check(ctx.L.ltp_ingest_open(ctx.h, ctypes.byref(cfg), self.n_pool, _p(tf), _p(k), _p(w), _p(pf), _p(pl),
+                                        ctypes.byref(h)))
+        self.h = h
+        self.n = 0
+
+    def run(self, arrival_ns):
+        """arrival_ns[i]: request i's arrival in ns after the run's start."""
+        arr = np.ascontiguousarray(arrival_ns, np.uint64)
+        st = ServeStats()
+        self.ctx.check(self.ctx.L.ltp_ingest_run(self.h, len(arr), _p(arr), ctypes.byref(st)))
+        self.n = len(arr)
+        return st.as_dict()
+
+    def results(self, values=False):
+        """(committed, batch_seq, pos, attempts[, values in log op order])."""
+        n = self.n
+        c = np.zeros(n, np.uint8)
+        seq = np.zeros(n, np.uint64)
+        pos = np.zeros(n, np.uint32)
+        att = np.zeros(n, np.uint32)
+        vals = None
+        if values:
+            tf = self._pool[0]
+            vals = np.zeros(int(tf[n]) if n else 0, np.int64)
+        self.ctx.check(self.ctx.L.ltp_ingest_results(self.h, _p(c), _p(seq), _p(pos), _p(att), _p(vals)))
+        return (c, seq, pos, att, vals) if values else (c, seq, pos, att)
+
+    def close(self):
+        if getattr(self, "h", None):
+            rc = self.ctx.L.ltp_ingest_close(self.h)
+            self.h = None
+            self.ctx.check(rc)
