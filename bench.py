@@ -787,6 +787,36 @@ def run_serve(args):
             st["committed_per_s_offered_window"] = st["committed"] / max(st["elapsed_s"], 1e-9)
             ingest_sweep.append({k: (round(v, 3) if isinstance(v, float) else v) for k, v in st.items()})
         ing.close()
+    # the same request-log loop on the Zipf 0.99 YCSB transactions alone,
+    # beside the plain batch path on the same 2^20-transaction pool
+    ycsb_sweep, plain_ycsb = [], None
+    if args.ycsb_loads:
+        ny = 1 << 20
+        ytf, yk, yw = tf[:ny + 1], keys[:int(tf[ny])], opw[:int(tf[ny])]
+        by = ctx.batch(ny, len(yk))
+        by.load(ytf, yk, yw)
+        for _ in range(3):
+            by.execute()
+        ctx.sync()
+        t0 = time.perf_counter()
+        for _ in range(10):
+            by.execute()
+        ctx.sync()
+        plain_ycsb = 10 * ny / (time.perf_counter() - t0)
+        by.finish()
+        del by
+        ing = G.Ingest(ctx, ytf, yk, yw, deadline_us=250, depth=2, budget_bytes=4 << 30, max_txns=1 << 20,
+                       max_ops=1 << 24, eager=True)
+        rng = np.random.default_rng(sh["seed"] + 29 + rank)
+        ing.run(np.cumsum(rng.exponential(1e9 / 50e6, 1 << 20)).astype(np.uint64))  # untimed warm-up
+        for rate in [float(x) * 1e6 for x in args.ycsb_loads.split(",")]:
+            n = int(rate * max(0.1, min(1.0, 40e6 / rate)))
+            st = ing.run(np.cumsum(rng.exponential(1e9 / rate, n)).astype(np.uint64))
+            st["offered_txn_per_s"] = rate
+            st["requests"] = n
+            st["committed_per_s_offered_window"] = st["committed"] / max(st["elapsed_s"], 1e-9)
+            ycsb_sweep.append({k: (round(v, 3) if isinstance(v, float) else v) for k, v in st.items()})
+        ing.close()
     ok_host = [p for p in sweep if p["p99_us"] <= 2000.0]
     ok_ing = [p for p in ingest_sweep if p["p99_us"] <= 2000.0]
     ok = ok_ing or ok_host
@@ -800,6 +830,7 @@ def run_serve(args):
                        "pool_txns": n_pool, "batch_execution": args.serve_mode,
                        "value_from": "device-resident request log" if ok_ing else "host submission API"},
             "serving": {"sweep": sweep, "ingest_sweep": ingest_sweep, "plain_batch_txn_per_s": plain,
+                        "ycsb_ingest_sweep": ycsb_sweep, "plain_ycsb_batch_txn_per_s": plain_ycsb,
                         "best_host_submit_txn_per_s": best_host["committed_per_s_offered_window"] if best_host else 0.0,
                         "best_p50_us": best["p50_us"] if best else None,
                         "best_p99_us": best["p99_us"] if best else None,
@@ -854,6 +885,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     ap.add_argument("--loadgen-threads", type=int, default=8, help="serving sweep: load-generator threads")
+    ap.add_argument("--ycsb-loads", default="200,400,600,800",
+                    help="request-log serving of the Zipf YCSB transactions alone: offered loads in M txn/s")
     ap.add_argument("--ingest-loads", default="50,100,200,250,300",
                     help="serving from a device-resident request log: offered loads in M txn/s ('' = skip)")
     ap.add_argument("--serve-mode", default="persistent", choices=["persistent", "stream"],

@@ -525,6 +525,7 @@ int host_fail(ltp_ctx *ctx, int status, const char *msg) { return fail(ctx, stat
 int host_cuda_fail(ltp_ctx *ctx, cudaError_t e, const char *where) { return cuda_fail(ctx, e, where); }
 int host_prepare(ltp_ctx *ctx, ltp_batch *const *bs, uint32_t n, cudaStream_t st) { return prepare(ctx, bs, n, st); }
 int host_execute(ltp_ctx *ctx, ltp_batch *b, cudaStream_t st) { return execute_one(ctx, b, st, false); }
+TablesDev host_tables(const ltp_ctx *ctx) { return tables_dev(ctx); }
 }  // namespace ltp
 
 extern "C" {
@@ -681,7 +682,10 @@ int ltp_batch_fetch64(ltp_ctx *ctx, ltp_batch *b, int64_t *vals, void *stream) {
     if (!b->out64) return fail(ctx, LTP_E_STATE, "the context has no int64 column");
     CK(cudaSetDevice(ctx->device));
     cudaStream_t st = pick_stream(ctx, stream);
-    if (vals && b->n_ops) CK(cudaMemcpyAsync(vals, b->out64, b->n_ops * 8, cudaMemcpyDeviceToHost, st));
+    if (vals && b->n_ops) {
+        CK(launch_widen_out(st, batch_dev(b), tables_dev(ctx)));
+        CK(cudaMemcpyAsync(vals, b->out64, b->n_ops * 8, cudaMemcpyDeviceToHost, st));
+    }
     return LTP_OK;
 }
 

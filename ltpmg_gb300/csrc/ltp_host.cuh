@@ -15,6 +15,7 @@ using ltp::Scratch;
 using ltp::Counters;
 using ltp::Tuning;
 using ltp::BatchDev;
+using ltp::TablesDev;
 using ltp::u64;
 using ltp::u32;
 
@@ -86,5 +87,7 @@ int host_prepare(ltp_ctx *ctx, ltp_batch *const *bs, uint32_t n, cudaStream_t st
 // Stream-ordered launches of one loaded batch (counters, commit init,
 // kernels, counter snapshot).
 int host_execute(ltp_ctx *ctx, ltp_batch *b, cudaStream_t st);
+// Device view of the context's tables.
+TablesDev host_tables(const ltp_ctx *ctx);
 
 }  // namespace ltp

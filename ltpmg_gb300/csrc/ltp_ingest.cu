@@ -110,12 +110,15 @@ __global__ void k_log_payload(const LogRun *runs, u32 n_runs, u64 n_slots, const
     }
 }
 
-// Op values of the batch into the log's value array (log index < pool size).
+// Op values of the batch into the log's value array (log index < pool size);
+// ops on int64 cells have theirs in out64, the others in out.
 __global__ void k_log_vals(u64 n_ops, const u32 *txn_first, const u32 *op_txn, const u64 *txn_log, const u32 *p_tf,
-                           const int32_t *out, const long long *out64, long long *vals) {
+                           const u32 *opw, const TablesDev T, const int32_t *out, const long long *out64,
+                           long long *vals) {
     for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < n_ops; j += (u64)gridDim.x * blockDim.x) {
-        const u32 t = op_txn[j];
-        vals[p_tf[txn_log[t]] + (j - txn_first[t])] = out64 ? out64[j] : (long long)out[j];
+        const u32 t = op_txn[j], w = opw[j], tb = opw_table(w);
+        const bool wide = out64 && opw_kind(w) <= LTP_OP_ADD && tb < T.n && col_wide(T.t[tb], opw_col(w));
+        vals[p_tf[txn_log[t]] + (j - txn_first[t])] = wide ? out64[j] : (long long)out[j];
     }
 }
 
@@ -243,8 +246,9 @@ int submit(ltp_ingest *g, IngestSlot &sl, uint32_t t, uint64_t o, uint64_t p, bo
     b->payload = sl.own_pay;
     if (rc) return rc;
     if (g->keep) {
-        k_log_vals<<<grid_for(o, ctx->num_sms), 256, 0, st>>>(o, b->txn_first, b->op_txn, sl.d_txn_log, g->p_tf,
-                                                             b->out, b->out64, g->d_vals);
+        const u32 *opw = view ? g->p_opw + g->tf[sl.runs[0].pool0] : sl.own_opw;
+        k_log_vals<<<grid_for(o, ctx->num_sms), 256, 0, st>>>(o, b->txn_first, b->op_txn, sl.d_txn_log, g->p_tf, opw,
+                                                             host_tables(ctx), b->out, b->out64, g->d_vals);
         IK(cudaGetLastError());
     }
     IK(cudaMemcpyAsync(sl.host_ctr, b->snap, sizeof(Counters), cudaMemcpyDeviceToHost, st));

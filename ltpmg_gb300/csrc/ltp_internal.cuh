@@ -59,7 +59,8 @@ struct BatchDev {
     const u32 *txn_first;  // [n_txns + 1]
     const u32 *op_txn;     // [n_ops] transaction of each op (variable-length batches)
     int32_t *out;          // [n_ops] value after each op (low 32 bits for int64 cells)
-    long long *out64;      // [n_ops] full value, when the context has int64 columns (else null)
+    long long *out64;      // [n_ops] full value, when the context has int64 columns (else null); the
+                           // kernels fill it for ops on int64 cells, launch_widen_out for the rest
     uint8_t *commit;       // [n_txns]
     const int32_t *payload;  // insert row images (LTP_OP_INSERT keys index it)
     u64 payload_len;
@@ -155,6 +156,8 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &
 cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s);
 cudaError_t launch_fill_seeded(cudaStream_t st, const TableDev &t, u64 seed);
 cudaError_t launch_expand_op_txn(cudaStream_t st, const u32 *txn_first, u64 n_txns, u32 *op_txn);
+// Completes out64 after execution (ops on int32 cells write only out).
+cudaError_t launch_widen_out(cudaStream_t st, const BatchDev &b, const TablesDev &T);
 cudaError_t launch_set_u64(cudaStream_t st, u64 *dst, u64 value);
 // One cooperative launch over n_batches device-resident batch descriptors.
 cudaError_t launch_persistent(cudaStream_t st, int num_sms, int rule, const BatchDev *d_batches,

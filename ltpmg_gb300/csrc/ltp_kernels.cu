@@ -238,6 +238,14 @@ __device__ __forceinline__ void store_out(const BatchDev &b, u64 i, long long v)
     if (b.out64) b.out64[i] = v;
 }
 
+// Output of op i (a valid read or RMW) at full width: ops on int64 cells
+// keep it in out64, ops on int32 cells only in out.
+__device__ __forceinline__ long long op_value(const BatchDev &b, const TablesDev &T, u64 i) {
+    const u32 w = b.opw[i], tb = opw_table(w);
+    const bool wide = b.out64 && tb < T.n && col_wide(T.t[tb], opw_col(w));
+    return wide ? b.out64[i] : (long long)b.out[i];
+}
+
 __device__ __forceinline__ char *cell_ptr(const TablesDev &T, u64 cell, bool *wide) {
     u32 k = 0;
     for (u32 i = 1; i < T.n; i++)
@@ -664,7 +672,7 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
                 }
                 const u64 i = wbase + (u64)k * 32 + lane;
                 __stcs(&b.out[i], (int32_t)v);
-                if (b.out64) b.out64[i] = v;
+                if (b.out64 && r[k].wide) b.out64[i] = v;  // int32 cells: widened from out on fetch
             }
         }
         if (threadIdx.x == 0) s_pbase = lookback_wait(s.st_cls, tile, s_run, ctr);
@@ -1031,7 +1039,8 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
                     const u64 dc = __ldg(&s.dcell[m]);
                     long long val = (long long)((u64)__ldg(&s.dbase[m]) + (u64)tot);
                     if (!(dc >> 63)) val = (int32_t)val;
-                    store_out(b, op, val);
+                    b.out[op] = (int32_t)val;
+                    if ((dc >> 63) && b.out64) b.out64[op] = val;  // int32 cells: widened from out on fetch
                     if (tail[k]) {
                         bool wd;
                         char *p = cell_ptr(T, dc & ~(1ull << 63), &wd);
@@ -1257,7 +1266,7 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
                 const u32 d = insert_link(w);
                 s_off[e] = (u32)b.keys[i];
                 s_lc[e] = d ? (unsigned char)opw_col(w) : (unsigned char)0xFF;
-                s_lv[e] = d ? (b.out64 ? b.out64[i - d] : (long long)b.out[i - d]) : 0ll;
+                s_lv[e] = d ? op_value(b, T, i - d) : 0ll;
                 store_out(b, i, (long long)(s_base[tb[k]] + r));
             }
         }
@@ -1360,6 +1369,16 @@ __global__ void k_fill_seeded(TableDev t, u64 seed) {
         const bool wc = col_wide(t, (u32)col);
         store_cell(t.data + col_off(t, (u32)col) + row * (wc ? 8ull : 4ull), wc,
                    (long long)(int32_t)(u32)mix64(base + row * t.n_cols + col));
+    }
+}
+
+// out64 of the ops on int32 cells, which the execution kernels leave to
+// this step: their value, sign-extended from out.
+__global__ void k_widen_out(BatchDev b, TablesDev T) {
+    for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < b.n_ops; i += (u64)gridDim.x * blockDim.x) {
+        const u32 w = b.opw[i], tb = opw_table(w);
+        if (opw_kind(w) > LTP_OP_ADD || tb >= T.n || col_wide(T.t[tb], opw_col(w))) continue;
+        b.out64[i] = (long long)b.out[i];
     }
 }
 
@@ -1672,6 +1691,14 @@ __global__ void k_set_u64(u64 *dst, u64 value) { *dst = value; }
 
 cudaError_t launch_set_u64(cudaStream_t st, u64 *dst, u64 value) {
     k_set_u64<<<1, 1, 0, st>>>(dst, value);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_widen_out(cudaStream_t st, const BatchDev &b, const TablesDev &T) {
+    if (b.n_ops == 0 || !b.out64) return cudaSuccess;
+    u64 blocks = (b.n_ops + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    k_widen_out<<<(unsigned)blocks, 256, 0, st>>>(b, T);
     return cudaGetLastError();
 }
 
