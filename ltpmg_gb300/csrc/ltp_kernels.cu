@@ -1176,6 +1176,7 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
     __shared__ u32 s_wcnt[NW][LTP_MAX_TABLES];
     __shared__ u64 s_base[LTP_MAX_TABLES];
     __shared__ u32 s_tcnt[LTP_MAX_TABLES], s_toff[LTP_MAX_TABLES];
+    __shared__ u32 s_item0[LTP_MAX_TABLES + 1];  // first (table, column, row) item of each table
     // staging of the tile's inserts in the dynamic shared memory (kInsSmem bytes)
     u32 *s_off = ltp_dyn_smem;                                                  // [kInsTile] payload offsets
     long long *s_lv = reinterpret_cast<long long *>(ltp_dyn_smem + kInsTile);  // [kInsTile] link values
@@ -1248,11 +1249,14 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
         }
         __syncthreads();
         if (threadIdx.x == 0) {  // the tile's inserts, grouped by table, in rank order
-            u32 run = 0;
+            u32 run = 0, items = 0;
             for (int t = 0; t < LTP_MAX_TABLES; t++) {
                 s_toff[t] = run;
                 run += s_tcnt[t];
+                s_item0[t] = items;
+                items += (u32)t < T.n ? s_tcnt[t] * T.t[t].n_cols : 0u;
             }
+            s_item0[LTP_MAX_TABLES] = items;
         }
         __syncthreads();
         // every insert notes its payload row and link; its output is its row id
@@ -1271,25 +1275,36 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
             }
         }
         __syncthreads();
-        // column by column, consecutive threads store consecutive rows
-        for (u32 t = 0; t < T.n; t++) {
-            const u32 cnt = s_tcnt[t];
-            if (!cnt) continue;
-            const TableDev &tab = T.t[t];
-            const u64 row0 = s_base[t];
-            u32 slot = 0;
-            for (u32 c = 0; c < tab.n_cols; c++) {
-                const bool wc = col_wide(tab, c);
-                char *col = tab.data + col_off(tab, c);
-                for (u32 j = threadIdx.x; j < cnt; j += BLK) {
-                    const u32 e = s_toff[t] + j;
-                    const int32_t *src = b.payload + s_off[e] + slot;
-                    long long v = wc ? (long long)(((u64)(u32)src[1] << 32) | (u64)(u32)src[0]) : (long long)src[0];
-                    if (s_lc[e] == c) v = s_lv[e];
-                    store_cell(col + (row0 + j) * (wc ? 8ull : 4ull), wc, v);
-                }
-                slot += wc ? 2 : 1;
+        // every (table, column, row) cell of the tile's new rows is one item,
+        // column-major within a table: consecutive threads store consecutive
+        // rows of a column, and a thread's items issue their loads together
+        const u32 n_items = s_item0[LTP_MAX_TABLES];
+        constexpr int U = 4;  // items per thread in flight: their loads issue before their stores
+        u32 t = 0;            // items of a thread only move forward through the tables
+        for (u32 it0 = threadIdx.x; it0 < n_items; it0 += U * BLK) {
+            long long v[U];
+            char *dst[U];
+            bool wc[U];
+#pragma unroll
+            for (int q = 0; q < U; q++) {
+                const u32 it = it0 + q * BLK;
+                dst[q] = nullptr;
+                if (it >= n_items) continue;
+                while (s_item0[t + 1] <= it) t++;
+                const TableDev &tab = T.t[t];
+                const u32 cnt = s_tcnt[t], rem = it - s_item0[t];
+                const u32 c = rem / cnt, j = rem - c * cnt;
+                wc[q] = col_wide(tab, c);
+                const u32 slot = c + (u32)__popcll(c ? (tab.wide & ((1ull << c) - 1ull)) : 0ull);  // payload slot of column c
+                const u32 e = s_toff[t] + j;
+                const int32_t *src = b.payload + s_off[e] + slot;
+                v[q] = wc[q] ? (long long)(((u64)(u32)src[1] << 32) | (u64)(u32)src[0]) : (long long)src[0];
+                if (s_lc[e] == c) v[q] = s_lv[e];
+                dst[q] = tab.data + col_off(tab, c) + (s_base[t] + j) * (wc[q] ? 8ull : 4ull);
             }
+#pragma unroll
+            for (int q = 0; q < U; q++)
+                if (dst[q]) store_cell(dst[q], wc[q], v[q]);
         }
         __syncthreads();
     }
