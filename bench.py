@@ -142,9 +142,10 @@ def load_peaks():
 MEASURED_TRAFFIC = {
     ("zipf", "classify"): (45.2, "ops"),
     ("zipf", "mark"): (22.4, "ops"),
-    ("zipf", "apply"): (28.9, "contended_ops"),
-    ("tpcc", "insert"): (64.2, "ops"),
-    ("tpcc", "mark"): (20.1, "ops"),
+    ("zipf", "apply"): (31.3, "contended_ops"),
+    ("zipf", "ids"): (8.0, "ops"),  # k_ids + k_dbase
+    ("tpcc", "insert"): (62.7, "ops"),
+    ("tpcc", "mark"): (20.0, "ops"),
 }
 
 
