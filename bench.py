@@ -403,7 +403,7 @@ def run_ours(args, config):
             "config": {"workload": WORKLOAD_TEXT[config], "batches_per_step": nb, "txns_per_step": txns_per_step,
                        "rule": "ordered (ascending TID per cell, all commit)", "mode": mode_name,
                        "mode_ms": {str(k): v for k, v in mode_ms.items()},
-                       "tuning": {str(k): f"{v['block']}x{v['ipt']}" + ("+precheck" if v.get("flags") else "")
+                       "tuning": {str(k): f"{v['block']}x{v['ipt']}" + ("w64" if v.get("word_bits") == 64 else "") + ("+precheck" if v.get("flags") else "")
                                   for k, v in tiles.items()},
                        "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
             "gpu_launches": launches, "roofline": roof, "clocks": clk, "e2e": e2e,
@@ -419,14 +419,17 @@ def fixed_tiles(ctx, dev, spec):
 
     import ltpmg_gb300 as G
 
+    # BLOCKxIPT[w64][+precheck], e.g. 512x4, 256x2w64+precheck
     base, _, opt = spec.partition("+")
+    base, _, wb = base.partition("w")
     blk, ipt = (int(x) for x in base.split("x"))
+    word_bits = int(wb) if wb else 32
     flags = G.lib.TUNE_MARK_PRECHECK if opt == "precheck" else 0
     out = {}
     for b in dev:
         k = AT.bucket_of(b.n_ops)
-        ctx.set_tuning(k, blk, ipt, flags=flags)
-        out[k] = {"block": blk, "ipt": ipt, "flags": flags}
+        ctx.set_tuning(k, blk, ipt, word_bits=word_bits, flags=flags)
+        out[k] = {"block": blk, "ipt": ipt, "word_bits": word_bits, "flags": flags}
     return out
 
 
@@ -629,7 +632,7 @@ def run_tpcc(args):
             "config": {"workload": WORKLOAD_TEXT["tpcc"], "batches_per_step": nb, "txns_per_step": txns_per_step,
                        "ops_per_step": ops_per_step, "rule": "ordered (ascending TID per cell, all commit)",
                        "mode": mode_name, "mode_ms": {str(k): v for k, v in mode_ms.items()},
-                       "tuning": {str(k): f"{v['block']}x{v['ipt']}" + ("+precheck" if v.get("flags") else "")
+                       "tuning": {str(k): f"{v['block']}x{v['ipt']}" + ("w64" if v.get("word_bits") == 64 else "") + ("+precheck" if v.get("flags") else "")
                                   for k, v in tiles.items()},
                        "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
             "gpu_launches": launches, "roofline": roof, "clocks": clk, "e2e": e2e,
@@ -882,7 +885,7 @@ def main():
     ap.add_argument("--batches", type=int, default=0, help="resident batches (default: the config's)")
     ap.add_argument("--tuning-out", default="", help="write the autotuner's choices to this JSON file")
     ap.add_argument("--tiles", default="",
-                    help="fixed BLOCKxIPT[+precheck] tiling instead of the autotuner's (e.g. 512x4)")
+                    help="fixed BLOCKxIPT[w64][+precheck] tiling instead of the autotuner's (e.g. 512x4, 256x2w64)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     ap.add_argument("--loadgen-threads", type=int, default=8, help="serving sweep: load-generator threads")

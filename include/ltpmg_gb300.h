@@ -103,7 +103,7 @@ typedef struct {
     uint64_t txns, ops, committed, aborted;
     uint64_t contended_ops;   /* ops on cells touched >1 time with >=1 write */
     uint64_t contended_cells;
-    uint64_t touched_words;   /* 32-cell bitmap words touched by the batch */
+    uint64_t touched_words;   /* conflict words (32 or 64 cells, ltp_tuning.word_bits) touched by the batch */
     uint64_t bytes_algorithmic;
     /* with LTP_FLAG_STAGE_TIMING, milliseconds per kernel of the batch:
      * ordered rule:  0 mark, 1 ids, 2 classify, 3-6 radix passes, 7 apply,
@@ -451,7 +451,8 @@ int ltp_tpcc_gen(const ltp_tpcc *g, uint64_t batch, uint64_t n_txns, uint32_t *t
 typedef struct {
     uint32_t block;      /* threads per block of the streaming kernels: 128, 256, 512 */
     uint32_t ipt;        /* ops per thread per tile: 1, 2, 4, 8 */
-    uint32_t word_bits;  /* conflict-word granularity: 32 cells (the only one built) */
+    uint32_t word_bits;  /* conflict-word granularity: 32 or 64 cells per word (64 needs block x ipt <= 2048;
+                          * the persistent kernel always uses 32) */
     uint32_t flags;      /* LTP_TUNE_* */
 } ltp_tuning;
 /* The mark kernel reads a conflict word it touched more than once in a tile

@@ -2,8 +2,10 @@
 
 Per size bucket (floor(log2(ops in the batch))) it times every candidate
 tiling of the streaming kernels -- threads per block x ops per thread, the
-knobs that set how many ops a tile stages in shared memory -- on a
-representative batch with CUDA events, and keeps the fastest.  For a list of
+knobs that set how many ops a tile stages in shared memory -- then 64-cell
+conflict words (bitmap word granularity) for the fastest tilings, then the
+mark kernel's hot-word pre-check, on a representative batch with CUDA
+events, and keeps the fastest.  For a list of
 batches it also times the multi-batch execution modes (CUDA graph vs the
 persistent cooperative kernel) and keeps the faster one.  Choices persist as
 JSON and are applied with Context.set_tuning.
@@ -54,16 +56,25 @@ def tune_tiles(ctx, batch, reps=3, blocks=BLOCKS, ipts=IPTS):
         for ipt in ipts:
             ctx.set_tuning(bucket, blk, ipt)
             results[f"{blk}x{ipt}"] = _time_batch(ctx, batch, reps)
+    # conflict-word granularity: 64-cell words for the three fastest tilings
+    # that have them (tiles of at most 2048 ops)
+    for name in sorted(results, key=results.get)[:6]:
+        blk, ipt = (int(x) for x in name.split("x"))
+        if blk * ipt <= 2048 and len([k for k in results if k.endswith("w64")]) < 3:
+            ctx.set_tuning(bucket, blk, ipt, word_bits=64)
+            results[f"{name}w64"] = _time_batch(ctx, batch, reps)
     best = min(results, key=results.get)
-    blk, ipt = (int(x) for x in best.split("x"))
+    base, _, wb = best.partition("w")
+    blk, ipt = (int(x) for x in base.split("x"))
+    word_bits = int(wb) if wb else 32
     # then, for the best tiling, the mark kernel's hot-word pre-check
-    ctx.set_tuning(bucket, blk, ipt, flags=L.TUNE_MARK_PRECHECK)
+    ctx.set_tuning(bucket, blk, ipt, word_bits=word_bits, flags=L.TUNE_MARK_PRECHECK)
     pre_ms = _time_batch(ctx, batch, reps)
-    results[f"{blk}x{ipt}+precheck"] = pre_ms
+    results[f"{best}+precheck"] = pre_ms
     flags = L.TUNE_MARK_PRECHECK if pre_ms < results[best] else 0
-    ctx.set_tuning(bucket, blk, ipt, flags=flags)
-    return {"bucket": bucket, "block": blk, "ipt": ipt, "flags": flags, "ms": min(results[best], pre_ms),
-            "candidates": results}
+    ctx.set_tuning(bucket, blk, ipt, word_bits=word_bits, flags=flags)
+    return {"bucket": bucket, "block": blk, "ipt": ipt, "word_bits": word_bits, "flags": flags,
+            "ms": min(results[best], pre_ms), "candidates": results}
 
 
 def tune_mode(ctx, batches, reps=2, modes=(L.MODE_GRAPH, L.MODE_PERSISTENT)):
@@ -100,7 +111,8 @@ def tune_buckets(ctx, batches, reps=3):
 
 
 def save(path, choices, mode=None):
-    doc = {"buckets": {str(k): {"block": v["block"], "ipt": v["ipt"], "flags": v.get("flags", 0), "ms": v["ms"]}
+    doc = {"buckets": {str(k): {"block": v["block"], "ipt": v["ipt"], "word_bits": v.get("word_bits", 32),
+                                "flags": v.get("flags", 0), "ms": v["ms"]}
                        for k, v in choices.items()},
            "mode": mode, "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
     with open(path, "w") as f:
@@ -111,5 +123,6 @@ def load(ctx, path):
     """Applies a saved tuning file to a context; returns its multi-batch mode."""
     doc = json.load(open(path))
     for k, v in doc["buckets"].items():
-        ctx.set_tuning(int(k), int(v["block"]), int(v["ipt"]), flags=int(v.get("flags", 0)))
+        ctx.set_tuning(int(k), int(v["block"]), int(v["ipt"]), word_bits=int(v.get("word_bits", 32)),
+                       flags=int(v.get("flags", 0)))
     return doc.get("mode")

@@ -89,8 +89,9 @@ int ensure_scratch(ltp_ctx *ctx, uint64_t n_ops) {
     if (words > ctx->alloc_words) {
         CK(cudaStreamSynchronize(ctx->stream));
         free_scratch_words(s);
-        CK(dalloc(&s.words, words));
-        CK(cudaMemset(s.words, 0, words * sizeof(WordState)));
+        // one spare entry: the 64-cell layout of the same buffer rounds up
+        CK(dalloc(&s.words, words + 1));
+        CK(cudaMemset(s.words, 0, (words + 1) * sizeof(WordState)));
         ctx->alloc_words = words;
     }
     s.n_words = words;
@@ -771,7 +772,9 @@ int ltp_set_tuning(ltp_ctx *ctx, uint32_t bucket, const ltp_tuning *t) {
     if (!ctx || !t || bucket >= 64) return LTP_E_BADARG;
     if (t->block != 128 && t->block != 256 && t->block != 512) return fail(ctx, LTP_E_BADARG, "block must be 128/256/512");
     if (t->ipt != 1 && t->ipt != 2 && t->ipt != 4 && t->ipt != 8) return fail(ctx, LTP_E_BADARG, "ipt must be 1/2/4/8");
-    if (t->word_bits != 32) return fail(ctx, LTP_E_BADARG, "word_bits must be 32 (32-cell conflict words)");
+    if (t->word_bits != 32 && t->word_bits != 64) return fail(ctx, LTP_E_BADARG, "word_bits must be 32 or 64");
+    if (!tiling_supported((int)t->block, (int)t->ipt, (int)t->word_bits))
+        return fail(ctx, LTP_E_BADARG, "64-cell conflict words need block x ipt <= 2048");
     if (t->flags & ~LTP_TUNE_MARK_PRECHECK) return fail(ctx, LTP_E_BADARG, "unknown tuning flag");
     ctx->tuning[bucket] = Tuning{t->block, t->ipt, t->word_bits, t->flags};
     return LTP_OK;

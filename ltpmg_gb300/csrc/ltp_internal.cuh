@@ -153,6 +153,8 @@ struct Launch {
 // Kernel launch wrappers (ltp_kernels.cu).  Each returns the CUDA status of
 // its launches.
 cudaError_t launch_execute(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr);
+// Is (threads per block, ops per thread, conflict-word bits) a built tiling?
+bool tiling_supported(int block, int ipt, int word_bits);
 cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s);
 cudaError_t launch_fill_seeded(cudaStream_t st, const TableDev &t, u64 seed);
 cudaError_t launch_expand_op_txn(cudaStream_t st, const u32 *txn_first, u64 n_txns, u32 *op_txn);

@@ -211,6 +211,101 @@ __device__ __forceinline__ uint4 ld_word_hint(const void *ptr, u64 pol) {
                  : "l"(ptr), "l"(pol));
     return v;
 }
+// ---- conflict words ----------------------------------------------------------
+// A conflict word covers 32 cells (WordState, 16 B: touched, written and
+// touched-twice masks, the word's first contended id) or 64 cells
+// (WordState64, 32 B: written and touched-twice masks in its first 16 bytes,
+// then the touched mask and the first id).  Both take 16 bytes per 32 cells,
+// so one scratch buffer serves either width; the width is a tuning knob of
+// the stream and graph launches (the persistent kernel uses 32).
+struct WordState64 {
+    u64 wbits, multi, touch;
+    u32 prefix, pad;
+};
+
+template <int WB>
+struct Wd;
+template <>
+struct Wd<32> {
+    typedef u32 T;
+    static constexpr int kShift = 5;
+    struct V {
+        u32 wbits, multi, prefix;
+    };
+    static __device__ __forceinline__ V load_hint(const Scratch &s, u64 w, u64 pol) {
+        const uint4 v = ld_word_hint(&s.words[w], pol);
+        return V{v.y, v.z, v.w};
+    }
+    static __device__ __forceinline__ V load_ro(const Scratch &s, u64 w) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(&s.words[w]));
+        return V{v.y, v.z, v.w};
+    }
+    static __device__ __forceinline__ V load(const Scratch &s, u64 w) {
+        const uint4 v = *reinterpret_cast<const uint4 *>(&s.words[w]);
+        return V{v.y, v.z, v.w};
+    }
+    // written and touched-twice masks, as the mark kernel's pre-check reads them
+    static __device__ __forceinline__ void load_relaxed(const Scratch &s, u64 w, T *wbits, T *multi) {
+        const uint4 v = ld_word_relaxed(&s.words[w]);
+        *wbits = v.y;
+        *multi = v.z;
+    }
+    static __device__ __forceinline__ T *touch(const Scratch &s, u64 w) { return &s.words[w].touch; }
+    static __device__ __forceinline__ T *wbits(const Scratch &s, u64 w) { return &s.words[w].wbits; }
+    static __device__ __forceinline__ T *multi(const Scratch &s, u64 w) { return &s.words[w].multi; }
+    static __device__ __forceinline__ u32 *prefix(const Scratch &s, u64 w) { return &s.words[w].prefix; }
+    static __device__ __forceinline__ void clear(const Scratch &s, u64 w) {
+        *reinterpret_cast<uint4 *>(&s.words[w]) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    static __device__ __forceinline__ u64 n_words(const Scratch &s) { return s.n_words; }
+    static __device__ __forceinline__ int popc(T x) { return __popc(x); }
+    static __device__ __forceinline__ int ffs(T x) { return __ffs(x); }
+};
+template <>
+struct Wd<64> {
+    typedef u64 T;
+    static constexpr int kShift = 6;
+    struct V {
+        u64 wbits, multi;
+        u32 prefix;
+    };
+    static __device__ __forceinline__ WordState64 *at(const Scratch &s, u64 w) {
+        return reinterpret_cast<WordState64 *>(s.words) + w;
+    }
+    static __device__ __forceinline__ V load_hint(const Scratch &s, u64 w, u64 pol) {
+        const uint4 a = ld_word_hint(at(s, w), pol);
+        const uint4 b = ld_word_hint(reinterpret_cast<const char *>(at(s, w)) + 16, pol);
+        return V{((u64)a.y << 32) | a.x, ((u64)a.w << 32) | a.z, b.z};
+    }
+    static __device__ __forceinline__ V load_ro(const Scratch &s, u64 w) {
+        const uint4 a = __ldg(reinterpret_cast<const uint4 *>(at(s, w)));
+        const u32 pre = __ldg(&at(s, w)->prefix);
+        return V{((u64)a.y << 32) | a.x, ((u64)a.w << 32) | a.z, pre};
+    }
+    static __device__ __forceinline__ V load(const Scratch &s, u64 w) {
+        const WordState64 *p = at(s, w);
+        return V{p->wbits, p->multi, p->prefix};
+    }
+    static __device__ __forceinline__ void load_relaxed(const Scratch &s, u64 w, T *wbits, T *multi) {
+        const uint4 a = ld_word_relaxed(at(s, w));
+        *wbits = ((u64)a.y << 32) | a.x;
+        *multi = ((u64)a.w << 32) | a.z;
+    }
+    static __device__ __forceinline__ T *touch(const Scratch &s, u64 w) { return &at(s, w)->touch; }
+    static __device__ __forceinline__ T *wbits(const Scratch &s, u64 w) { return &at(s, w)->wbits; }
+    static __device__ __forceinline__ T *multi(const Scratch &s, u64 w) { return &at(s, w)->multi; }
+    static __device__ __forceinline__ u32 *prefix(const Scratch &s, u64 w) { return &at(s, w)->prefix; }
+    static __device__ __forceinline__ void clear(const Scratch &s, u64 w) {
+        uint4 *p = reinterpret_cast<uint4 *>(at(s, w));
+        p[0] = make_uint4(0u, 0u, 0u, 0u);
+        p[1] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    // 64-cell words over the same buffer: half as many, rounded up
+    static __device__ __forceinline__ u64 n_words(const Scratch &s) { return (s.n_words + 1) / 2; }
+    static __device__ __forceinline__ int popc(T x) { return __popcll(x); }
+    static __device__ __forceinline__ int ffs(T x) { return __ffsll((long long)x); }
+};
+
 __device__ __forceinline__ long long load_cell_hint(const char *p, bool wide, u64 pol) {
     if (wide) {
         long long v;
@@ -280,10 +375,12 @@ __device__ __forceinline__ bool insert_link_ok(const BatchDev &b, const TableDev
 }
 
 // Is the cell contended (touched twice and written)?  If so, *m is its dense id.
+template <int WB>
 __device__ __forceinline__ bool contended_id(const Scratch &s, u64 cell, u32 *m) {
-    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(&s.words[cell >> 5]));
-    const u32 cw = v.y & v.z, bit = 1u << (cell & 31);
-    *m = v.w + __popc(cw & (bit - 1u));
+    typedef typename Wd<WB>::T WT;
+    const typename Wd<WB>::V v = Wd<WB>::load_ro(s, cell >> Wd<WB>::kShift);
+    const WT cw = v.wbits & v.multi, bit = (WT)1 << (cell & (WB - 1));
+    *m = v.prefix + Wd<WB>::popc(cw & (bit - 1));
     return (cw & bit) != 0;
 }
 
@@ -306,14 +403,20 @@ constexpr u32 kEmptyKey = 0xFFFFFFFFu;
 
 __device__ __forceinline__ u32 hash_word(u32 w) { return (w * 0x9E3779B1u) ^ (w >> 15); }
 
-template <int BLOCK, int IPT>
+// dynamic shared memory of the mark hash: key + touched, touched-twice and
+// written masks per slot, 2 slots per op of the tile
+template <int BLOCK, int IPT, int WB>
+constexpr size_t mark_smem_bytes() { return 2ull * BLOCK * IPT * (4 + 3 * (WB / 8)); }
+
+template <int BLOCK, int IPT, int WB>
 __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+    typedef typename Wd<WB>::T WT;
     if (block_err(ctr)) return;
     const bool precheck = (b.flags & LTP_TUNE_MARK_PRECHECK) != 0u;
     constexpr u32 TILE = (u32)BLOCK * IPT;
     constexpr u32 H = 2 * TILE;  // at most TILE distinct words: load factor <= 1/2
-    u32 *mark_smem = ltp_dyn_smem;  // 4 * H words (dynamic: up to 128 KB)
-    u32 *hk = mark_smem, *ht = hk + H, *hd = ht + H, *hw = hd + H;
+    u32 *hk = ltp_dyn_smem;  // H keys, then 3 * H masks (dynamic)
+    WT *ht = reinterpret_cast<WT *>(hk + H), *hd = ht + H, *hw = hd + H;
     __shared__ u32 s_ins[LTP_MAX_TABLES];  // insert ops of the tile per table
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const u64 n = b.n_ops;
@@ -355,7 +458,8 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
                 set_err(ctr, LTP_E_BADARG);
                 continue;
             }
-            const u32 word = (u32)(r.cell >> 5), bit = 1u << (r.cell & 31);
+            const u32 word = (u32)(r.cell >> Wd<WB>::kShift);
+            const WT bit = (WT)1 << (r.cell & (WB - 1));
             u32 slot = hash_word(word) & (H - 1);
             for (u32 probe = 0; probe < H; probe++) {
                 u32 cur = hk[slot];
@@ -371,7 +475,8 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
         // flush: every thread issues the touch atomics of all its slots before
         // consuming any result, so the returning atomics overlap
         constexpr int SPT = H / BLOCK;
-        u32 fw[SPT], ft[SPT], old[SPT];
+        u32 fw[SPT];
+        WT ft[SPT], old[SPT];
 #pragma unroll
         for (int q = 0; q < SPT; q++) {
             const u32 j = threadIdx.x + q * BLOCK;
@@ -384,20 +489,20 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
         // atomic that was not needed.  Only words this tile touched more than
         // once are checked first: a word touched once per tile is usually
         // cold, and the read would only add a round trip before its atomic.
-        uint4 cur[SPT];
+        WT cur_w[SPT], cur_m[SPT];  // the word's written and touched-twice bits as read
 #pragma unroll
         for (int q = 0; q < SPT; q++) {
             const u32 j = threadIdx.x + q * BLOCK;
-            const bool hot = precheck && fw[q] != kEmptyKey && (hd[j] != 0u || (ft[q] & (ft[q] - 1u)) != 0u);
-            cur[q] = hot ? ld_word_relaxed(&s.words[fw[q]]) : make_uint4(0u, 0u, 0u, 0u);
+            const bool hot = precheck && fw[q] != kEmptyKey && (hd[j] != 0 || (ft[q] & (ft[q] - 1)) != 0);
+            cur_w[q] = cur_m[q] = 0;
+            if (hot) Wd<WB>::load_relaxed(s, fw[q], &cur_w[q], &cur_m[q]);
         }
         u32 dmask = 0;  // slots that issued their atomics
 #pragma unroll
         for (int q = 0; q < SPT; q++) {
             const u32 j = threadIdx.x + q * BLOCK;
-            // cur: x touch, y wbits, z multi
-            const bool need = fw[q] != kEmptyKey && ((ft[q] & ~cur[q].z) || (hw[j] & ~cur[q].y));
-            old[q] = need ? atomicOr(&s.words[fw[q]].touch, ft[q]) : 0u;
+            const bool need = fw[q] != kEmptyKey && ((ft[q] & ~cur_m[q]) || (hw[j] & ~cur_w[q]));
+            old[q] = need ? atomicOr(Wd<WB>::touch(s, fw[q]), ft[q]) : 0;
             if (need) dmask |= 1u << q;
         }
         u32 fmask = 0, nfirst = 0;
@@ -405,10 +510,10 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
         for (int q = 0; q < SPT; q++) {
             const u32 j = threadIdx.x + q * BLOCK;
             if (dmask & (1u << q)) {
-                const u32 m = (old[q] & ft[q]) | hd[j];
-                if (m & ~cur[q].z) atomicOr(&s.words[fw[q]].multi, m);
-                if (hw[j] & ~cur[q].y) atomicOr(&s.words[fw[q]].wbits, hw[j]);
-                if (old[q] == 0u) {
+                const WT m = (old[q] & ft[q]) | hd[j];
+                if (m & ~cur_m[q]) atomicOr(Wd<WB>::multi(s, fw[q]), m);
+                if (hw[j] & ~cur_w[q]) atomicOr(Wd<WB>::wbits(s, fw[q]), hw[j]);
+                if (old[q] == 0) {
                     fmask |= 1u << q;
                     nfirst++;
                 }
@@ -444,9 +549,9 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
     }
 }
 
-template <int BLOCK, int IPT>
+template <int BLOCK, int IPT, int WB>
 __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
-    phase_mark<BLOCK, IPT>(b, T, s, ctr);
+    phase_mark<BLOCK, IPT, WB>(b, T, s, ctr);
 }
 
 // ============================================================================
@@ -455,8 +560,9 @@ __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch
 // When a batch touches more than a quarter of the conflict words, the ids
 // scan and the clean-up stream over every word in address order instead of
 // visiting the touched-word list in first-touch (random) order.
+template <int WB>
 __device__ __forceinline__ bool ids_dense(const Scratch &s, const Counters *ctr) {
-    return ctr->n_tw * 4 > s.n_words;
+    return ctr->n_tw * 4 > Wd<WB>::n_words(s);
 }
 
 // Per contended cell: its address width (bit 63 of dcell marks an int64
@@ -478,12 +584,13 @@ __global__ void __launch_bounds__(256) k_dbase(TablesDev T, Scratch s, Counters 
     phase_dbase(T, s, ctr, priority != 0);
 }
 
-template <int BLK>
+template <int BLK, int WB>
 __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, Counters *ctr) {
+    typedef typename Wd<WB>::T WT;
     constexpr u32 IPT = kIdsTile / BLK;
     if (block_err(ctr)) return;
-    const bool dense = ids_dense(s, ctr);
-    const u64 n = dense ? s.n_words : ctr->n_tw;
+    const bool dense = ids_dense<WB>(s, ctr);
+    const u64 n = dense ? Wd<WB>::n_words(s) : ctr->n_tw;
     const u32 tiles = (u32)((n + kIdsTile - 1) / kIdsTile);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ u32 s_warp[BLK / 32];
@@ -495,7 +602,8 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_IDS);
         if (tile >= tiles) break;
-        u32 wd[IPT], cw[IPT];
+        u32 wd[IPT];
+        WT cw[IPT];
         u32 cnt = 0;
         // striped arrangement (coalesced loads); a thread's entries get
         // consecutive ids -- any bijection onto 0..M-1 serves as ids
@@ -505,12 +613,12 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
             u64 j = t0 + (u64)k * BLK;
             wd[k] = j < n ? (dense ? (u32)j : s.tw_list[j]) : 0u;
             if (j < n) {
-                const uint4 v = *reinterpret_cast<const uint4 *>(&s.words[wd[k]]);
-                cw[k] = v.y & v.z;
+                const typename Wd<WB>::V v = Wd<WB>::load(s, wd[k]);
+                cw[k] = v.wbits & v.multi;
             } else {
-                cw[k] = 0u;
+                cw[k] = 0;
             }
-            cnt += __popc(cw[k]);
+            cnt += Wd<WB>::popc(cw[k]);
         }
         // block exclusive scan of cnt
         u32 incl = cnt;
@@ -538,12 +646,12 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
         for (int k = 0; k < IPT; k++) {
             u64 j = t0 + (u64)k * BLK;
             if (j < n) {
-                s.words[wd[k]].prefix = (u32)pre;
-                u32 bits = cw[k];
+                *Wd<WB>::prefix(s, wd[k]) = (u32)pre;
+                WT bits = cw[k];
                 while (bits) {  // the cells' values are read by k_dbase, fully parallel
-                    int bpos = __ffs(bits) - 1;
+                    const int bpos = Wd<WB>::ffs(bits) - 1;
                     bits &= bits - 1;
-                    s.dcell[pre++] = ((u64)wd[k] << 5) | (u64)bpos;
+                    s.dcell[pre++] = ((u64)wd[k] << Wd<WB>::kShift) | (u64)bpos;
                 }
             }
         }
@@ -551,8 +659,9 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
     }
 }
 
+template <int WB>
 __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Counters *ctr) {
-    phase_ids<kIdsBlock>(T, s, ctr);
+    phase_ids<kIdsBlock, WB>(T, s, ctr);
 }
 
 // ============================================================================
@@ -578,8 +687,9 @@ __device__ __forceinline__ int sort_passes_dev(u32 M) {
     return (bits + 7) / 8;
 }
 
-template <int BLOCK, int IPT>
+template <int BLOCK, int IPT, int WB>
 __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+    typedef typename Wd<WB>::T WT;
     if (block_err(ctr)) return;
     constexpr int NW = BLOCK / 32;
     constexpr u64 TILE = (u64)BLOCK * IPT;
@@ -608,24 +718,25 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
             w[k] = i < n ? __ldcs(&b.opw[i]) : 0xFFFFFFFFu;
         }
         OpRef r[IPT];
-        uint4 ws[IPT];
+        typename Wd<WB>::V ws[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             u64 i = wbase + (u64)k * 32 + lane;
             r[k] = decode_op(T, key[k], w[k]);
             r[k].valid = r[k].valid && i < n;
-            ws[k] = r[k].valid ? ld_word_hint(&s.words[r[k].cell >> 5], pol_keep) : make_uint4(0, 0, 0, 0);
+            if (r[k].valid) ws[k] = Wd<WB>::load_hint(s, r[k].cell >> Wd<WB>::kShift, pol_keep);
+            else ws[k].wbits = ws[k].multi = 0, ws[k].prefix = 0;
         }
         u64 rec[IPT];
         u32 wcnt = 0, lpos[IPT];
         bool con[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
-            const u32 bit = 1u << (r[k].cell & 31);
-            const u32 cw = ws[k].y & ws[k].z;
+            const WT bit = (WT)1 << (r[k].cell & (WB - 1));
+            const WT cw = ws[k].wbits & ws[k].multi;
             const u64 i = wbase + (u64)k * 32 + lane;
             con[k] = r[k].valid && (cw & bit);
-            const u32 m = ws[k].w + __popc(cw & (bit - 1u));
+            const u32 m = ws[k].prefix + Wd<WB>::popc(cw & (bit - 1));
             rec[k] = packed ? ((u64)m << 44) |
                                   ((u64)(opw_kind(w[k]) == LTP_OP_ADD ? ((u32)opw_imm(w[k]) & 0xFFFFFu) : 0u) << 24) |
                                   (u64)(u32)i
@@ -689,12 +800,12 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
     }
 }
 
-template <int BLOCK, int IPT>
+template <int BLOCK, int IPT, int WB>
 // register budget per thread: 40 up to 2 ops per thread, 48 up to 4, 96
 // above, so that 64-bit cell values do not cut the resident blocks
 __global__ void __launch_bounds__(BLOCK, 65536 / (BLOCK * (IPT <= 2 ? 40 : IPT <= 4 ? 48 : 96))) k_classify(BatchDev b, TablesDev T,
                                                                                           Scratch s, Counters *ctr) {
-    phase_classify<BLOCK, IPT>(b, T, s, ctr);
+    phase_classify<BLOCK, IPT, WB>(b, T, s, ctr);
 }
 
 // ============================================================================
@@ -1061,6 +1172,7 @@ __global__ void __launch_bounds__(kApplyBlock, 4) k_apply(BatchDev b, TablesDev 
 // ============================================================================
 // priority rule (R1): min writer TID per contended cell, aborts, execute
 // ============================================================================
+template <int WB>
 __device__ __forceinline__ void phase_r1_minw(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
     if (block_err(ctr)) return;
     const u64 n = b.n_ops;
@@ -1070,7 +1182,7 @@ __device__ __forceinline__ void phase_r1_minw(const BatchDev &b, const TablesDev
         if (i < n) {
             const u32 w = b.opw[i];
             OpRef r = decode_op(T, b.keys[i], w);
-            con = r.valid && contended_id(s, r.cell, &m);
+            con = r.valid && contended_id<WB>(s, r.cell, &m);
             if (con && opw_kind(w) == LTP_OP_ADD) {
                 act = true;
                 tid = op_tid(b, i);
@@ -1084,10 +1196,12 @@ __device__ __forceinline__ void phase_r1_minw(const BatchDev &b, const TablesDev
     }
 }
 
+template <int WB>
 __global__ void __launch_bounds__(256) k_r1_minw(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
-    phase_r1_minw(b, T, s, ctr);
+    phase_r1_minw<WB>(b, T, s, ctr);
 }
 
+template <int WB>
 __device__ __forceinline__ void phase_r1_abort(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
     if (block_err(ctr)) return;
     const u64 n = b.n_ops;
@@ -1095,17 +1209,19 @@ __device__ __forceinline__ void phase_r1_abort(const BatchDev &b, const TablesDe
         const u32 w = b.opw[i];
         OpRef r = decode_op(T, b.keys[i], w);
         u32 m;
-        if (r.valid && contended_id(s, r.cell, &m)) {
+        if (r.valid && contended_id<WB>(s, r.cell, &m)) {
             const u32 tid = op_tid(b, i);
             if (s.dminw[m] < tid) b.commit[tid] = 0;
         }
     }
 }
 
+template <int WB>
 __global__ void __launch_bounds__(256) k_r1_abort(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
-    phase_r1_abort(b, T, s, ctr);
+    phase_r1_abort<WB>(b, T, s, ctr);
 }
 
+template <int WB>
 __device__ __forceinline__ void phase_r1_exec(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
     if (block_err(ctr)) return;
     const u64 n = b.n_ops;
@@ -1122,7 +1238,7 @@ __device__ __forceinline__ void phase_r1_exec(const BatchDev &b, const TablesDev
         const bool add = opw_kind(w) == LTP_OP_ADD;
         long long v;
         bool store = add;
-        if (contended_id(s, r.cell, &m)) {
+        if (contended_id<WB>(s, r.cell, &m)) {
             // A committed op on a contended cell sees the pre-batch value,
             // plus -- when its transaction is the cell's only committed
             // writer (the smallest writing TID) -- the RMWs its own
@@ -1153,8 +1269,9 @@ __device__ __forceinline__ void phase_r1_exec(const BatchDev &b, const TablesDev
     }
 }
 
+template <int WB>
 __global__ void __launch_bounds__(256) k_r1_exec(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
-    phase_r1_exec(b, T, s, ctr);
+    phase_r1_exec<WB>(b, T, s, ctr);
 }
 
 // ============================================================================
@@ -1317,6 +1434,7 @@ __global__ void __launch_bounds__(kInsBlock) k_insert(BatchDev b, TablesDev T, S
 // ============================================================================
 // finish: return the scratch to its clean state, count commits
 // ============================================================================
+template <int WB>
 __device__ __forceinline__ void phase_finish(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr,
                                              int rule) {
     const u64 gsz = (u64)gridDim.x * blockDim.x, g0 = (u64)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1328,14 +1446,14 @@ __device__ __forceinline__ void phase_finish(const BatchDev &b, const TablesDev 
         for (u64 j = g0; j < t_ins * LTP_MAX_TABLES; j += gsz) s.st_ins[j] = 0;
     }
     const u64 ntw = ctr->n_tw;
-    const bool dense = ids_dense(s, ctr);
+    const bool dense = ids_dense<WB>(s, ctr);
+    const u64 nw = Wd<WB>::n_words(s);
     if (dense) {
-        for (u64 j = g0; j < s.n_words; j += gsz) *reinterpret_cast<uint4 *>(&s.words[j]) = make_uint4(0, 0, 0, 0);
+        for (u64 j = g0; j < nw; j += gsz) Wd<WB>::clear(s, j);
     } else {
-        for (u64 j = g0; j < ntw; j += gsz)
-            *reinterpret_cast<uint4 *>(&s.words[s.tw_list[j]]) = make_uint4(0, 0, 0, 0);
+        for (u64 j = g0; j < ntw; j += gsz) Wd<WB>::clear(s, s.tw_list[j]);
     }
-    const u64 t_ids = ((dense ? s.n_words : ntw) + kIdsTile - 1) / kIdsTile;
+    const u64 t_ids = ((dense ? nw : ntw) + kIdsTile - 1) / kIdsTile;
     for (u64 j = g0; j < t_ids; j += gsz) s.st_ids[j] = 0;
     const u64 nc = ctr->n_c;
     const u64 t_apply = (nc + kApplyTile - 1) / kApplyTile;
@@ -1358,8 +1476,9 @@ __device__ __forceinline__ void phase_finish(const BatchDev &b, const TablesDev 
     }
 }
 
+template <int WB>
 __global__ void __launch_bounds__(256) k_finish(BatchDev b, TablesDev T, Scratch s, Counters *ctr, int rule) {
-    phase_finish(b, T, s, ctr, rule);
+    phase_finish<WB>(b, T, s, ctr, rule);
 }
 
 __global__ void k_stall(Counters *ctr, u32 ms) {
@@ -1416,17 +1535,17 @@ static int occ_grid(K kernel, int block, int num_sms, size_t dyn_smem = 0) {
     return per_sm * num_sms;
 }
 
-template <int BLOCK, int IPT>
+template <int BLOCK, int IPT, int WB>
 struct Front {
     static int g_mark, g_cls, sms;
-    static constexpr size_t kMarkSmem = 4ull * 2 * BLOCK * IPT * sizeof(u32);
+    static constexpr size_t kMarkSmem = mark_smem_bytes<BLOCK, IPT, WB>();
     static void grids(int num_sms) {
         if (sms != num_sms) {
-            if (cudaFuncSetAttribute(k_mark<BLOCK, IPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            if (cudaFuncSetAttribute(k_mark<BLOCK, IPT, WB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kMarkSmem) != cudaSuccess)
                 return;  // the launch below then reports the error
-            g_mark = occ_grid(k_mark<BLOCK, IPT>, BLOCK, num_sms, kMarkSmem);
-            g_cls = occ_grid(k_classify<BLOCK, IPT>, BLOCK, num_sms);
+            g_mark = occ_grid(k_mark<BLOCK, IPT, WB>, BLOCK, num_sms, kMarkSmem);
+            g_cls = occ_grid(k_classify<BLOCK, IPT, WB>, BLOCK, num_sms);
             sms = num_sms;
         }
     }
@@ -1434,34 +1553,44 @@ struct Front {
         grids(L.num_sms);
         const u64 tiles = (b.n_ops + (u64)BLOCK * IPT - 1) / ((u64)BLOCK * IPT);
         const int g = (int)(tiles < (u64)g_mark ? (tiles ? tiles : 1) : (u64)g_mark);
-        k_mark<BLOCK, IPT><<<g, BLOCK, kMarkSmem, L.stream>>>(b, T, s, ctr);
+        k_mark<BLOCK, IPT, WB><<<g, BLOCK, kMarkSmem, L.stream>>>(b, T, s, ctr);
     }
     static void classify(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
         grids(L.num_sms);
         const u64 tiles = (b.n_ops + (u64)BLOCK * IPT - 1) / ((u64)BLOCK * IPT);
         const int g = (int)(tiles < (u64)g_cls ? (tiles ? tiles : 1) : (u64)g_cls);
-        k_classify<BLOCK, IPT><<<g, BLOCK, 0, L.stream>>>(b, T, s, ctr);
+        k_classify<BLOCK, IPT, WB><<<g, BLOCK, 0, L.stream>>>(b, T, s, ctr);
     }
 };
-template <int BLOCK, int IPT> int Front<BLOCK, IPT>::g_mark = 0;
-template <int BLOCK, int IPT> int Front<BLOCK, IPT>::g_cls = 0;
-template <int BLOCK, int IPT> int Front<BLOCK, IPT>::sms = 0;
+template <int BLOCK, int IPT, int WB> int Front<BLOCK, IPT, WB>::g_mark = 0;
+template <int BLOCK, int IPT, int WB> int Front<BLOCK, IPT, WB>::g_cls = 0;
+template <int BLOCK, int IPT, int WB> int Front<BLOCK, IPT, WB>::sms = 0;
 
 typedef void (*front_fn)(const Launch &, const BatchDev &, const TablesDev &, const Scratch &, Counters *);
 
+// 64-cell words exist for the tilings whose mark hash (28 B per slot) fits a
+// block's shared memory: up to 2,048 ops per tile
+bool tiling_supported(int block, int ipt, int word_bits) {
+    const bool known = (block == 128 || block == 256 || block == 512) && (ipt == 1 || ipt == 2 || ipt == 4 || ipt == 8);
+    return known && (word_bits == 32 || (word_bits == 64 && block * ipt <= 2048));
+}
+
 static void pick_front(const Tuning &t, front_fn *mark, front_fn *classify) {
-#define LTP_FRONT(B, I)                        \
-    if (t.block == B && t.ipt == I) {          \
-        *mark = Front<B, I>::mark;             \
-        *classify = Front<B, I>::classify;     \
-        return;                                \
+#define LTP_FRONT(B, I, W)                                     \
+    if (t.block == B && t.ipt == I && t.word_bits == W) {      \
+        *mark = Front<B, I, W>::mark;                          \
+        *classify = Front<B, I, W>::classify;                  \
+        return;                                                \
     }
-    LTP_FRONT(128, 1) LTP_FRONT(128, 2) LTP_FRONT(128, 4) LTP_FRONT(128, 8)
-    LTP_FRONT(256, 1) LTP_FRONT(256, 2) LTP_FRONT(256, 4) LTP_FRONT(256, 8)
-    LTP_FRONT(512, 1) LTP_FRONT(512, 2) LTP_FRONT(512, 4) LTP_FRONT(512, 8)
+    LTP_FRONT(128, 1, 32) LTP_FRONT(128, 2, 32) LTP_FRONT(128, 4, 32) LTP_FRONT(128, 8, 32)
+    LTP_FRONT(256, 1, 32) LTP_FRONT(256, 2, 32) LTP_FRONT(256, 4, 32) LTP_FRONT(256, 8, 32)
+    LTP_FRONT(512, 1, 32) LTP_FRONT(512, 2, 32) LTP_FRONT(512, 4, 32) LTP_FRONT(512, 8, 32)
+    LTP_FRONT(128, 1, 64) LTP_FRONT(128, 2, 64) LTP_FRONT(128, 4, 64) LTP_FRONT(128, 8, 64)
+    LTP_FRONT(256, 1, 64) LTP_FRONT(256, 2, 64) LTP_FRONT(256, 4, 64) LTP_FRONT(256, 8, 64)
+    LTP_FRONT(512, 1, 64) LTP_FRONT(512, 2, 64) LTP_FRONT(512, 4, 64)
 #undef LTP_FRONT
-    *mark = Front<256, 4>::mark;
-    *classify = Front<256, 4>::classify;
+    *mark = Front<256, 4, 32>::mark;
+    *classify = Front<256, 4, 32>::classify;
 }
 
 static int capped(int grid, u64 upper) { return (int)((u64)grid < upper ? (u64)grid : (upper ? upper : 1)); }
@@ -1484,16 +1613,20 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDe
     if (L.stall) k_stall<<<1, 1, 0, L.stream>>>(ctr, L.stall_ms);
     front_fn f_mark, f_cls;
     pick_front(L.tune, &f_mark, &f_cls);
+    // conflict-word width of every kernel of the batch (an unsupported tiling
+    // falls back to 256 x 4 with 32-cell words in pick_front)
+    const bool wide_words = L.tune.word_bits == 64 && tiling_supported(L.tune.block, L.tune.ipt, 64);
     f_mark(L, b, T, s, ctr);
     mark_ev(1);
     {
         static int gi = 0, sms = 0;
         if (sms != L.num_sms) {
-            gi = occ_grid(k_ids, kIdsBlock, L.num_sms);
+            gi = occ_grid(k_ids<32>, kIdsBlock, L.num_sms);
             sms = L.num_sms;
         }
         const int g = capped(gi, (b.n_ops + kIdsTile - 1) / kIdsTile);
-        k_ids<<<g, kIdsBlock, 0, L.stream>>>(T, s, ctr);
+        if (wide_words) k_ids<64><<<g, kIdsBlock, 0, L.stream>>>(T, s, ctr);
+        else k_ids<32><<<g, kIdsBlock, 0, L.stream>>>(T, s, ctr);
         k_dbase<<<L.num_sms * 8, 256, 0, L.stream>>>(T, s, ctr, L.rule == LTP_RULE_PRIORITY);
     }
     mark_ev(2);
@@ -1524,11 +1657,14 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDe
         else k_apply<u32><<<gapp, kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
         mark_ev(8);
     } else {
-        k_r1_minw<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        if (wide_words) k_r1_minw<64><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        else k_r1_minw<32><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
         mark_ev(3);
-        k_r1_abort<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        if (wide_words) k_r1_abort<64><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        else k_r1_abort<32><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
         mark_ev(4);
-        k_r1_exec<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        if (wide_words) k_r1_exec<64><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        else k_r1_exec<32><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
         for (int i = 5; i <= 8; i++) mark_ev(i);
     }
     {
@@ -1541,7 +1677,8 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDe
             k_insert<<<capped(gins, (b.n_ops + kInsTile - 1) / kInsTile), kInsBlock, kInsSmem, L.stream>>>(b, T, s, ctr);
     }
     mark_ev(9);
-    k_finish<<<gstream, 256, 0, L.stream>>>(b, T, s, ctr, L.rule);
+    if (wide_words) k_finish<64><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr, L.rule);
+    else k_finish<32><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr, L.rule);
     mark_ev(10);
     return cudaGetLastError();
 }
@@ -1611,14 +1748,14 @@ __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
         for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < b.n_txns; t += (u64)nb * blockDim.x) b.commit[t] = 1;
         grid_sync(a.bar, nb, a.ctr);
         if (block_err(a.ctr)) break;
-        phase_mark<kPBlock, kPIpt>(b, a.T, a.s, a.ctr);
+        phase_mark<kPBlock, kPIpt, 32>(b, a.T, a.s, a.ctr);
         grid_sync(a.bar, nb, a.ctr);
-        phase_ids<kPBlock>(a.T, a.s, a.ctr);
+        phase_ids<kPBlock, 32>(a.T, a.s, a.ctr);
         grid_sync(a.bar, nb, a.ctr);
         phase_dbase(a.T, a.s, a.ctr, a.rule == LTP_RULE_PRIORITY);
         grid_sync(a.bar, nb, a.ctr);
         if (a.rule != LTP_RULE_PRIORITY) {
-            phase_classify<kPBlock, kPIpt>(b, a.T, a.s, a.ctr);
+            phase_classify<kPBlock, kPIpt, 32>(b, a.T, a.s, a.ctr);
             grid_sync(a.bar, nb, a.ctr);
             // only the passes the contended ids need (M is the same for every
             // block after the barrier, so every block skips the same ones)
@@ -1630,18 +1767,18 @@ __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
             if (a.T.any_wide) phase_apply<kPBlock, u64>(b, a.T, a.s, a.ctr);
             else phase_apply<kPBlock, u32>(b, a.T, a.s, a.ctr);
         } else {
-            phase_r1_minw(b, a.T, a.s, a.ctr);
+            phase_r1_minw<32>(b, a.T, a.s, a.ctr);
             grid_sync(a.bar, nb, a.ctr);
-            phase_r1_abort(b, a.T, a.s, a.ctr);
+            phase_r1_abort<32>(b, a.T, a.s, a.ctr);
             grid_sync(a.bar, nb, a.ctr);
-            phase_r1_exec(b, a.T, a.s, a.ctr);
+            phase_r1_exec<32>(b, a.T, a.s, a.ctr);
         }
         grid_sync(a.bar, nb, a.ctr);
         if (b.payload_len) {  // a batch without payload has no valid insert
             phase_insert<kPBlock>(b, a.T, a.s, a.ctr);
             grid_sync(a.bar, nb, a.ctr);
         }
-        phase_finish(b, a.T, a.s, a.ctr, a.rule);
+        phase_finish<32>(b, a.T, a.s, a.ctr, a.rule);
         grid_sync(a.bar, nb, a.ctr);
         if (blockIdx.x == 0) {
             const u32 *src = reinterpret_cast<const u32 *>(a.ctr);
@@ -1687,7 +1824,7 @@ int persistent_grid(int num_sms) {
 }
 
 cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s) {
-    cudaMemsetAsync(s.words, 0, s.n_words * sizeof(WordState), st);
+    cudaMemsetAsync(s.words, 0, (s.n_words + 1) * sizeof(WordState), st);  // + the 64-cell layout's spare entry
     cudaMemsetAsync(s.st_sort[0], 0, s.cap_sort_tiles * 256 * 4, st);
     cudaMemsetAsync(s.st_sort[1], 0, s.cap_sort_tiles * 256 * 4, st);
     cudaMemsetAsync(s.st_ids, 0, s.cap_tiles * 8, st);

@@ -155,16 +155,19 @@ def test_empty_batch(lib_loaded):
         assert np.array_equal(before, ctx.download(t))
 
 
-@pytest.mark.parametrize("block,ipt,flags", [(b, i, 0) for b in (128, 256, 512) for i in (1, 2, 4, 8)] +
-                         [(512, 4, G.lib.TUNE_MARK_PRECHECK), (128, 1, G.lib.TUNE_MARK_PRECHECK)])
-def test_tuning_variants(lib_loaded, block, ipt, flags):
+@pytest.mark.parametrize("block,ipt,flags,word_bits",
+                         [(b, i, 0, 32) for b in (128, 256, 512) for i in (1, 2, 4, 8)] +
+                         [(b, i, 0, 64) for b in (128, 256, 512) for i in (1, 2, 4, 8) if b * i <= 2048] +
+                         [(512, 4, G.lib.TUNE_MARK_PRECHECK, 32), (128, 1, G.lib.TUNE_MARK_PRECHECK, 32),
+                          (256, 4, G.lib.TUNE_MARK_PRECHECK, 64)])
+def test_tuning_variants(lib_loaded, block, ipt, flags, word_bits):
     rows, cols = 1 << 12, 10
     with G.Context(device=0) as ctx:
         t = ctx.create_table(rows, cols)
         ctx.fill_seeded(t, 21)
         for bucket in range(64):
-            ctx.set_tuning(bucket, block, ipt, flags=flags)
-        assert ctx.get_tuning(5) == (block, ipt, 32, flags)
+            ctx.set_tuning(bucket, block, ipt, word_bits=word_bits, flags=flags)
+        assert ctx.get_tuning(5) == (block, ipt, word_bits, flags)
         b = ctx.batch(3000, 3000 * 32)
         ref_tab = O.table_init(21, rows, cols)
         for batch in range(2):  # the second batch sees hot words already marked by the first's tiles
@@ -177,10 +180,43 @@ def test_tuning_variants(lib_loaded, block, ipt, flags):
         assert np.array_equal(ctx.download(t), ref_tab)
 
 
-def test_tuning_rejects_unbuilt_word_size(lib_loaded):
+@pytest.mark.parametrize("rule", [0, 1])
+def test_word_widths_alternate_on_one_context(lib_loaded, rule):
+    """Batches of two size buckets, one tuned to 32-cell and one to 64-cell
+    conflict words, alternate on one context (both widths share the conflict
+    state buffer, each batch leaves it clean), under both rules; a table of
+    2^16 + 5 rows x 7 columns puts cells of one 64-cell word in two rows'
+    tails and the last word partly past the table."""
+    rows, cols = (1 << 16) + 5, 7
+    with G.Context(device=0, rule=rule) as ctx:
+        t = ctx.create_table(rows, cols)
+        ctx.fill_seeded(t, 23)
+        small, large = 2000, 20000
+        ctx.set_tuning(int(np.log2(small * 8)), 256, 2, word_bits=64)
+        ctx.set_tuning(int(np.log2(large * 8)), 512, 4, word_bits=32)
+        ref_tab = O.table_init(23, rows, cols)
+        for batch in range(6):
+            n = small if batch % 2 == 0 else large
+            tf, keys, opw = gen(23, rows, cols, 8, 8, 0.6, 1.1, batch, n)
+            ref_tab, rc, ro = O.replay(rule, ref_tab, tf, keys, opw)
+            b = ctx.batch(n, len(keys))
+            b.load(tf, keys, opw)
+            b.execute()
+            commit, vals, st = b.results()
+            assert np.array_equal(commit, rc[:n]) and np.array_equal(vals, ro), batch
+            if rule == 1:
+                assert st.aborted > 0
+        assert np.array_equal(ctx.download(t), ref_tab)
+
+
+def test_tuning_rejects_unbuilt_tilings(lib_loaded):
     with G.Context(device=0) as ctx:
+        with pytest.raises(G.LtpError):  # 64-cell words fit tiles of at most 2048 ops
+            ctx.set_tuning(3, 512, 8, word_bits=64)
         with pytest.raises(G.LtpError):
-            ctx.set_tuning(3, 512, 4, word_bits=64)
+            ctx.set_tuning(3, 256, 4, word_bits=16)
+        ctx.set_tuning(3, 512, 4, word_bits=64)
+        assert ctx.get_tuning(3) == (512, 4, 64, 0)
 
 
 def test_malformed_op_rejected_and_context_survives(lib_loaded):

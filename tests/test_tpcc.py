@@ -120,10 +120,13 @@ def _tables_for(g, extra):
     return ref
 
 
-def _run_tpcc(g, rule, n_batches, n_txns, mode="single"):
+def _run_tpcc(g, rule, n_batches, n_txns, mode="single", tuning=None):
     batches = [g.gen(b, n_txns) for b in range(n_batches)]
     extra = np.sum([x[5] for x in batches], axis=0)
     with G.Context(device=0, rule=rule) as ctx:
+        if tuning:
+            for bucket in range(64):
+                ctx.set_tuning(bucket, *tuning)
         ids = g.create_tables(ctx, extra)
         bs = []
         for tf, keys, opw, pay, _, _ in batches:
@@ -156,6 +159,12 @@ def test_tpcc_sequence_matches_oracle(small, rule):
     stats = _run_tpcc(small, rule, 3, 5000)
     if rule == 1:
         assert all(s.aborted > 0 for s in stats)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rule", [0, 1])
+def test_tpcc_sequence_with_64_cell_words(small, rule):
+    _run_tpcc(small, rule, 2, 4000, tuning=(256, 2, 64))
 
 
 @pytest.mark.gpu
