@@ -149,6 +149,35 @@ MEASURED_TRAFFIC = {
 }
 
 
+# mark's L2 atomic and reduction sectors per op (lts__t_sectors_srcunit_tex_op_atom / _red
+# over the batch's ops, from the same capture as MEASURED_TRAFFIC)
+MEASURED_ATOMICS = {"zipf": (0.760, 0.581)}
+
+
+def random_access_roof(G, device, sh, st, avg, config):
+    """The random-access roofline of mark and classify: their random accesses
+    at this GPU's measured rates (ltp_probe_random_access over arrays of the
+    workload's table and conflict-word sizes) give a floor time; frac = floor
+    over the measured kernel time."""
+    table_b = sh["rows"] * sh["cols"] * 4
+    words_b = max(4096, (sh["rows"] * sh["cols"] + 31) // 32 * 16)
+    pr = G.lib.probe_random_access
+    c = {"load_table": pr(device, table_b, G.lib.PROBE_LOAD), "load_words": pr(device, words_b, G.lib.PROBE_LOAD),
+         "atomic_words": pr(device, words_b, G.lib.PROBE_ATOMIC),
+         "reduce_words": pr(device, words_b, G.lib.PROBE_REDUCE)}
+    out = {"ceilings_per_s": c, "array_bytes": {"table": table_b, "words": words_b}}
+    ops, unc = st["ops"], st["ops"] - st["contended_ops"]
+    floor = ops / c["load_words"] + unc / c["load_table"]
+    out["classify"] = {"random_reads": {"words": ops, "cells": unc}, "floor_ms": floor * 1e3,
+                       "ms": avg["classify"], "frac": floor * 1e3 / avg["classify"]}
+    if config in MEASURED_ATOMICS:
+        a, r = MEASURED_ATOMICS[config]
+        floor = a * ops / c["atomic_words"] + r * ops / c["reduce_words"]
+        out["mark"] = {"atomics": a * ops, "reductions": r * ops, "floor_ms": floor * 1e3, "ms": avg["mark"],
+                       "frac": floor * 1e3 / avg["mark"]}
+    return out
+
+
 def measured_traffic(config, kernel, stats):
     t = MEASURED_TRAFFIC.get((config, kernel))
     return None if t is None else t[0] * stats[t[1]]
@@ -391,7 +420,8 @@ def run_ours(args, config):
         achieved = dom_bytes / (avg[dom] / 1e3) / 1e9
         traffic_b = measured_traffic(config, dom, mean_stats)
         roof.update({"kernel": dom, "achieved": achieved, "frac": achieved / peak, "traffic": traffic_b,
-                     "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": avg[dom], "kernel_ms": avg})
+                     "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": avg[dom], "kernel_ms": avg,
+                     "random_access": random_access_roof(G, local, sh, mean_stats, avg, config)})
     else:
         roof.update({"kernel": "k_persist (whole pipeline, one launch per step)", "achieved":
                      roof["pipeline"]["achieved"], "frac": roof["pipeline"]["frac"], "traffic": None,
@@ -870,7 +900,14 @@ def run_gather(args):
         s_per = e0.elapsed_time(e1) / 1e3 / reps
         out[name] = {"gathers_per_s": n_idx / s_per, "sector_GBps": n_idx * 32 / s_per / 1e9}
         del src, idx
-    print(json.dumps({"metric": "random 4-byte gathers/s", "gather": out}), flush=True)
+    # the library's own probe: random loads, atomicOr with result, reductions
+    import ltpmg_gb300 as G
+
+    probe = {}
+    for name, nbytes in (("table_640MB", 10 << 26), ("words_84MB", 84 << 20)):
+        probe[name] = {m: G.lib.probe_random_access(0, nbytes, k) for m, k in
+                       (("load", G.lib.PROBE_LOAD), ("atomic", G.lib.PROBE_ATOMIC), ("reduce", G.lib.PROBE_REDUCE))}
+    print(json.dumps({"metric": "random 4-byte accesses/s", "gather": out, "probe": probe}), flush=True)
 
 
 def main():

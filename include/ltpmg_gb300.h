@@ -359,6 +359,16 @@ int ltp_ingest_results(ltp_ingest *g, uint8_t *committed, uint64_t *batch_seq, u
                        int64_t *vals);
 int ltp_ingest_close(ltp_ingest *g);
 
+/* ---- random-access ceilings ---------------------------------------------
+ * The batch kernels touch random cells and conflict words, so random 4-byte
+ * accesses -- not copy bandwidth -- bound them.  Measures independent random
+ * accesses over a fresh array of `bytes` (4 KB .. 16 GB) on `device`:
+ * loads, atomicOr with its result used, or atomicOr as a reduction. */
+#define LTP_PROBE_LOAD 0
+#define LTP_PROBE_ATOMIC 1
+#define LTP_PROBE_REDUCE 2
+int ltp_probe_random_access(int32_t device, uint64_t bytes, int32_t mode, double *accesses_per_s);
+
 /* ---- pinned host memory ------------------------------------------------ */
 void *ltp_host_alloc(size_t bytes);
 void ltp_host_free(void *p);

@@ -19,7 +19,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "-I", os.path.join(ROOT, "include")]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I", os.path.join(ROOT, "include")]
 
-CU_SOURCES = ["ltp_kernels.cu", "ltp_api.cu", "ltp_noalloc.cu", "ltp_ingest.cu"]
+CU_SOURCES = ["ltp_kernels.cu", "ltp_api.cu", "ltp_noalloc.cu", "ltp_ingest.cu", "ltp_probe.cu"]
 CXX_SOURCES = ["ltp_gen.cpp", "ltp_compat.cpp", "ltp_serve.cpp", "ltp_tpcc.cpp"]
 
 

@@ -168,6 +168,7 @@ def load():
         "ltp_serve_stats_now": (ci, [vp, ctypes.POINTER(ServeStats)]),
         "ltp_serve_close": (ci, [vp, ctypes.POINTER(ServeStats)]),
         "ltp_now_ns": (u64, []),
+        "ltp_probe_random_access": (ci, [i32, u64, i32, ctypes.POINTER(ctypes.c_double)]),
         "ltp_ingest_open": (ci, [vp, ctypes.POINTER(ServeConfig), u64, vp, vp, vp, vp, vp, pp]),
         "ltp_ingest_run": (ci, [vp, u64, vp, ctypes.POINTER(ServeStats)]),
         "ltp_ingest_results": (ci, [vp, vp, vp, vp, vp, vp]),
@@ -697,3 +698,17 @@ class Ingest:
             rc = self.ctx.L.ltp_ingest_close(self.h)
             self.h = None
             self.ctx.check(rc)
+
+
+PROBE_LOAD, PROBE_ATOMIC, PROBE_REDUCE = 0, 1, 2
+
+
+def probe_random_access(device, nbytes, mode):
+    """Random 4-byte accesses per second over an array of nbytes (mode:
+    PROBE_LOAD, PROBE_ATOMIC with result, PROBE_REDUCE)."""
+    L = load()
+    out = ctypes.c_double()
+    rc = L.ltp_probe_random_access(device, nbytes, mode, ctypes.byref(out))
+    if rc:
+        raise LtpError(rc, "ltp_probe_random_access")
+    return out.value
