@@ -148,6 +148,7 @@ struct Launch {
     u32 stall_ms;
     cudaEvent_t *ev;  // LTP_N_STAGES events of the batch when timing
     bool timing;
+    bool pdl = false;  // programmatic dependent launch (set by launch_execute for uncaptured streams)
 };
 
 // Kernel launch wrappers (ltp_kernels.cu).  Each returns the CUDA status of

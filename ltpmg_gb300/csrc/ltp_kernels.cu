@@ -211,6 +211,18 @@ __device__ __forceinline__ uint4 ld_word_hint(const void *ptr, u64 pol) {
                  : "l"(ptr), "l"(pol));
     return v;
 }
+// ---- programmatic dependent launch -------------------------------------------
+// The batch kernels are launched with programmatic stream serialization, so a
+// kernel may be launched while its predecessor drains.  Each one first waits
+// for the predecessor grid's completion and memory (griddepcontrol.wait; a
+// no-op for a launch without the attribute), then lets its own successor be
+// launched: the successor's launch and block placement overlap this kernel's
+// run, and its blocks wait in turn before their first access.
+__device__ __forceinline__ void pdl_begin() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ---- conflict words ----------------------------------------------------------
 // A conflict word covers 32 cells (WordState, 16 B: touched, written and
 // touched-twice masks, the word's first contended id) or 64 cells
@@ -551,6 +563,7 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
 
 template <int BLOCK, int IPT, int WB>
 __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    pdl_begin();
     phase_mark<BLOCK, IPT, WB>(b, T, s, ctr);
 }
 
@@ -581,6 +594,7 @@ __device__ __forceinline__ void phase_dbase(const TablesDev &T, const Scratch &s
 }
 
 __global__ void __launch_bounds__(256) k_dbase(TablesDev T, Scratch s, Counters *ctr, int priority) {
+    pdl_begin();
     phase_dbase(T, s, ctr, priority != 0);
 }
 
@@ -661,6 +675,7 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
 
 template <int WB>
 __global__ void __launch_bounds__(kIdsBlock) k_ids(TablesDev T, Scratch s, Counters *ctr) {
+    pdl_begin();
     phase_ids<kIdsBlock, WB>(T, s, ctr);
 }
 
@@ -805,6 +820,7 @@ template <int BLOCK, int IPT, int WB>
 // above, so that 64-bit cell values do not cut the resident blocks
 __global__ void __launch_bounds__(BLOCK, 65536 / (BLOCK * (IPT <= 2 ? 40 : IPT <= 4 ? 48 : 96))) k_classify(BatchDev b, TablesDev T,
                                                                                           Scratch s, Counters *ctr) {
+    pdl_begin();
     phase_classify<BLOCK, IPT, WB>(b, T, s, ctr);
 }
 
@@ -974,6 +990,7 @@ __device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, C
 
 template <int P>
 __global__ void __launch_bounds__(kSortBlock, 3) k_sort_pass(Scratch s, Counters *ctr, u64 n_ops) {
+    pdl_begin();
     phase_sort_pass<kSortBlock>(P, s, ctr, n_ops);
 }
 
@@ -1166,6 +1183,7 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
 
 template <typename S>
 __global__ void __launch_bounds__(kApplyBlock, 4) k_apply(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    pdl_begin();
     phase_apply<kApplyBlock, S>(b, T, s, ctr);
 }
 
@@ -1198,6 +1216,7 @@ __device__ __forceinline__ void phase_r1_minw(const BatchDev &b, const TablesDev
 
 template <int WB>
 __global__ void __launch_bounds__(256) k_r1_minw(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    pdl_begin();
     phase_r1_minw<WB>(b, T, s, ctr);
 }
 
@@ -1218,6 +1237,7 @@ __device__ __forceinline__ void phase_r1_abort(const BatchDev &b, const TablesDe
 
 template <int WB>
 __global__ void __launch_bounds__(256) k_r1_abort(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    pdl_begin();
     phase_r1_abort<WB>(b, T, s, ctr);
 }
 
@@ -1271,6 +1291,7 @@ __device__ __forceinline__ void phase_r1_exec(const BatchDev &b, const TablesDev
 
 template <int WB>
 __global__ void __launch_bounds__(256) k_r1_exec(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    pdl_begin();
     phase_r1_exec<WB>(b, T, s, ctr);
 }
 
@@ -1428,6 +1449,7 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
 }
 
 __global__ void __launch_bounds__(kInsBlock) k_insert(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    pdl_begin();
     phase_insert<kInsBlock>(b, T, s, ctr);
 }
 
@@ -1478,6 +1500,7 @@ __device__ __forceinline__ void phase_finish(const BatchDev &b, const TablesDev 
 
 template <int WB>
 __global__ void __launch_bounds__(256) k_finish(BatchDev b, TablesDev T, Scratch s, Counters *ctr, int rule) {
+    pdl_begin();
     phase_finish<WB>(b, T, s, ctr, rule);
 }
 
@@ -1535,6 +1558,26 @@ static int occ_grid(K kernel, int block, int num_sms, size_t dyn_smem = 0) {
     return per_sm * num_sms;
 }
 
+// Launches a batch kernel, with programmatic stream serialization when `pdl`
+// (see pdl_begin): it may start while its predecessor on the stream drains.
+// Stream launches use it; captured graphs do not (their launches already
+// follow each other closely, and measured no faster with it).
+template <typename... KP, typename... A>
+static cudaError_t launch_k(bool pdl, void (*kernel)(KP...), unsigned grid, unsigned block, size_t smem,
+                            cudaStream_t st, A... args) {
+    cudaLaunchConfig_t c = {};
+    c.gridDim = dim3(grid);
+    c.blockDim = dim3(block);
+    c.dynamicSmemBytes = smem;
+    c.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    c.attrs = at;
+    c.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&c, kernel, static_cast<KP>(args)...);
+}
+
 template <int BLOCK, int IPT, int WB>
 struct Front {
     static int g_mark, g_cls, sms;
@@ -1549,24 +1592,25 @@ struct Front {
             sms = num_sms;
         }
     }
-    static void mark(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+    static cudaError_t mark(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
         grids(L.num_sms);
         const u64 tiles = (b.n_ops + (u64)BLOCK * IPT - 1) / ((u64)BLOCK * IPT);
         const int g = (int)(tiles < (u64)g_mark ? (tiles ? tiles : 1) : (u64)g_mark);
-        k_mark<BLOCK, IPT, WB><<<g, BLOCK, kMarkSmem, L.stream>>>(b, T, s, ctr);
+        return launch_k(L.pdl, k_mark<BLOCK, IPT, WB>, g, BLOCK, kMarkSmem, L.stream, b, T, s, ctr);
     }
-    static void classify(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+    static cudaError_t classify(const Launch &L, const BatchDev &b, const TablesDev &T, const Scratch &s,
+                                Counters *ctr) {
         grids(L.num_sms);
         const u64 tiles = (b.n_ops + (u64)BLOCK * IPT - 1) / ((u64)BLOCK * IPT);
         const int g = (int)(tiles < (u64)g_cls ? (tiles ? tiles : 1) : (u64)g_cls);
-        k_classify<BLOCK, IPT, WB><<<g, BLOCK, 0, L.stream>>>(b, T, s, ctr);
+        return launch_k(L.pdl, k_classify<BLOCK, IPT, WB>, g, BLOCK, 0, L.stream, b, T, s, ctr);
     }
 };
 template <int BLOCK, int IPT, int WB> int Front<BLOCK, IPT, WB>::g_mark = 0;
 template <int BLOCK, int IPT, int WB> int Front<BLOCK, IPT, WB>::g_cls = 0;
 template <int BLOCK, int IPT, int WB> int Front<BLOCK, IPT, WB>::sms = 0;
 
-typedef void (*front_fn)(const Launch &, const BatchDev &, const TablesDev &, const Scratch &, Counters *);
+typedef cudaError_t (*front_fn)(const Launch &, const BatchDev &, const TablesDev &, const Scratch &, Counters *);
 
 // 64-cell words exist for the tilings whose mark hash (28 B per slot) fits a
 // block's shared memory: up to 2,048 ops per tile
@@ -1595,8 +1639,9 @@ static void pick_front(const Tuning &t, front_fn *mark, front_fn *classify) {
 
 static int capped(int grid, u64 upper) { return (int)((u64)grid < upper ? (u64)grid : (upper ? upper : 1)); }
 
-cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDev &T, const Scratch &s,
+cudaError_t launch_execute(const Launch &L_in, const BatchDev &b_in, const TablesDev &T, const Scratch &s,
                            Counters *ctr) {
+    Launch L = L_in;
     BatchDev b = b_in;
     b.flags = L.tune.flags;
     (void)cudaGetLastError();  // report only the launches below
@@ -1604,7 +1649,8 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDe
     // under stream capture the stage events become external event nodes, so
     // they still carry timestamps when the graph replays
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    if (L.timing) cudaStreamIsCapturing(L.stream, &cap);
+    cudaStreamIsCapturing(L.stream, &cap);
+    L.pdl = cap != cudaStreamCaptureStatusActive;
     const unsigned ev_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
     auto mark_ev = [&](int i) {
         if (L.timing) cudaEventRecordWithFlags(L.ev[i], L.stream, ev_flags);
@@ -1616,7 +1662,11 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDe
     // conflict-word width of every kernel of the batch (an unsupported tiling
     // falls back to 256 x 4 with 32-cell words in pick_front)
     const bool wide_words = L.tune.word_bits == 64 && tiling_supported(L.tune.block, L.tune.ipt, 64);
-    f_mark(L, b, T, s, ctr);
+    cudaError_t le = cudaSuccess;  // the first failed launch
+    auto chk = [&](cudaError_t e) {
+        if (le == cudaSuccess) le = e;
+    };
+    chk(f_mark(L, b, T, s, ctr));
     mark_ev(1);
     {
         static int gi = 0, sms = 0;
@@ -1625,14 +1675,13 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDe
             sms = L.num_sms;
         }
         const int g = capped(gi, (b.n_ops + kIdsTile - 1) / kIdsTile);
-        if (wide_words) k_ids<64><<<g, kIdsBlock, 0, L.stream>>>(T, s, ctr);
-        else k_ids<32><<<g, kIdsBlock, 0, L.stream>>>(T, s, ctr);
-        k_dbase<<<L.num_sms * 8, 256, 0, L.stream>>>(T, s, ctr, L.rule == LTP_RULE_PRIORITY);
+        chk(launch_k(L.pdl, wide_words ? k_ids<64> : k_ids<32>, g, kIdsBlock, 0, L.stream, T, s, ctr));
+        chk(launch_k(L.pdl, k_dbase, L.num_sms * 8, 256, 0, L.stream, T, s, ctr, (int)(L.rule == LTP_RULE_PRIORITY)));
     }
     mark_ev(2);
     const int gstream = L.num_sms * 8;
     if (L.rule != LTP_RULE_PRIORITY) {
-        f_cls(L, b, T, s, ctr);
+        chk(f_cls(L, b, T, s, ctr));
         mark_ev(3);
         static int gs = 0, ga = 0, sms = 0;
         if (sms != L.num_sms) {
@@ -1644,27 +1693,23 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDe
         // at most n_ops contended ids: passes beyond their width are not launched
         int max_passes = 1;
         while (max_passes < 4 && ((b.n_ops - 1) >> (8 * max_passes)) != 0) max_passes++;
-        k_sort_pass<0><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
+        chk(launch_k(L.pdl, k_sort_pass<0>, gsort, kSortBlock, 0, L.stream, s, ctr, b.n_ops));
         mark_ev(4);
-        if (max_passes > 1) k_sort_pass<1><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
+        if (max_passes > 1) chk(launch_k(L.pdl, k_sort_pass<1>, gsort, kSortBlock, 0, L.stream, s, ctr, b.n_ops));
         mark_ev(5);
-        if (max_passes > 2) k_sort_pass<2><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
+        if (max_passes > 2) chk(launch_k(L.pdl, k_sort_pass<2>, gsort, kSortBlock, 0, L.stream, s, ctr, b.n_ops));
         mark_ev(6);
-        if (max_passes > 3) k_sort_pass<3><<<gsort, kSortBlock, 0, L.stream>>>(s, ctr, b.n_ops);
+        if (max_passes > 3) chk(launch_k(L.pdl, k_sort_pass<3>, gsort, kSortBlock, 0, L.stream, s, ctr, b.n_ops));
         mark_ev(7);
         const int gapp = capped(ga, (b.n_ops + kApplyTile - 1) / kApplyTile);
-        if (T.any_wide) k_apply<u64><<<gapp, kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
-        else k_apply<u32><<<gapp, kApplyBlock, 0, L.stream>>>(b, T, s, ctr);
+        chk(launch_k(L.pdl, T.any_wide ? k_apply<u64> : k_apply<u32>, gapp, kApplyBlock, 0, L.stream, b, T, s, ctr));
         mark_ev(8);
     } else {
-        if (wide_words) k_r1_minw<64><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
-        else k_r1_minw<32><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        chk(launch_k(L.pdl, wide_words ? k_r1_minw<64> : k_r1_minw<32>, gstream, 256, 0, L.stream, b, T, s, ctr));
         mark_ev(3);
-        if (wide_words) k_r1_abort<64><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
-        else k_r1_abort<32><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        chk(launch_k(L.pdl, wide_words ? k_r1_abort<64> : k_r1_abort<32>, gstream, 256, 0, L.stream, b, T, s, ctr));
         mark_ev(4);
-        if (wide_words) k_r1_exec<64><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
-        else k_r1_exec<32><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr);
+        chk(launch_k(L.pdl, wide_words ? k_r1_exec<64> : k_r1_exec<32>, gstream, 256, 0, L.stream, b, T, s, ctr));
         for (int i = 5; i <= 8; i++) mark_ev(i);
     }
     {
@@ -1674,13 +1719,14 @@ cudaError_t launch_execute(const Launch &L, const BatchDev &b_in, const TablesDe
             sms = L.num_sms;
         }
         if (b.payload_len)  // a batch without payload has no valid insert
-            k_insert<<<capped(gins, (b.n_ops + kInsTile - 1) / kInsTile), kInsBlock, kInsSmem, L.stream>>>(b, T, s, ctr);
+            chk(launch_k(L.pdl, k_insert, capped(gins, (b.n_ops + kInsTile - 1) / kInsTile), kInsBlock, kInsSmem, L.stream, b,
+                         T, s, ctr));
     }
     mark_ev(9);
-    if (wide_words) k_finish<64><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr, L.rule);
-    else k_finish<32><<<gstream, 256, 0, L.stream>>>(b, T, s, ctr, L.rule);
+    chk(launch_k(L.pdl, wide_words ? k_finish<64> : k_finish<32>, gstream, 256, 0, L.stream, b, T, s, ctr, L.rule));
     mark_ev(10);
-    return cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
+    return le != cudaSuccess ? le : e;
 }
 
 // ============================================================================
