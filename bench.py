@@ -45,10 +45,10 @@ WORKLOAD_TEXT = {
              "1M-50M txn/s, 250 us batch deadline, 4 GB read/write-set budget, aborts re-queued",
 }
 # algorithmic bytes per kernel launch, from the batch's counters
-KERNEL_BYTES = {
-    "mark": lambda st: 16 * st["ops"],
+KERNEL_BYTES = {  # st["key_bytes"]: 8, or 4 for batches loaded with 32-bit keys
+    "mark": lambda st: (8 + st["key_bytes"]) * st["ops"],
     "ids": lambda st: 20 * st["touched_words"] + 32 * st["contended_cells"],  # id scan + pre-batch values
-    "classify": lambda st: 28 * st["ops"],
+    "classify": lambda st: (20 + st["key_bytes"]) * st["ops"],
     "sort_pass0": lambda st: 16 * st["contended_ops"],
     "sort_pass1": lambda st: 16 * st["contended_ops"],
     "sort_pass2": lambda st: 16 * st["contended_ops"],
@@ -57,7 +57,14 @@ KERNEL_BYTES = {
     "insert": lambda st: st.get("insert_bytes", 0),
     "finish": lambda st: 12 * st["touched_words"],
 }
-KERNELS_PER_BATCH = 11  # mark, ids, dbase, classify, 4 radix passes, apply, insert, finish
+def kernels_per_batch(n_ops, has_payload):
+    """Kernels one batch launches under the ordered rule: mark, ids, dbase,
+    classify, one radix pass per 8 bits of the largest possible contended id
+    (n_ops - 1), apply, insert (only with a payload), finish."""
+    passes = 1
+    while passes < 4 and ((max(n_ops, 1) - 1) >> (8 * passes)) != 0:
+        passes += 1
+    return 4 + passes + 1 + (1 if has_payload else 0) + 1
 
 
 def dist_env():
@@ -140,8 +147,8 @@ def load_peaks():
 # workload (profiles/batch_kernels_zipf.md, profiles/k_mark_insert_tpcc.md);
 # a launch's traffic is this figure times the units it processed
 MEASURED_TRAFFIC = {
-    ("zipf", "classify"): (45.2, "ops"),
-    ("zipf", "mark"): (22.4, "ops"),
+    ("zipf", "classify"): (41.2, "ops"),  # 32-bit keys
+    ("zipf", "mark"): (17.7, "ops"),  # 32-bit keys
     ("zipf", "apply"): (31.3, "contended_ops"),
     ("zipf", "ids"): (8.0, "ops"),  # k_ids + k_dbase
     ("tpcc", "insert"): (62.7, "ops"),
@@ -297,7 +304,8 @@ def run_ours(args, config):
     dev = []
     for tf, keys, opw, n, opt in host:
         b = ctx.batch(n, len(keys))
-        b.load(None if opt else tf, keys, opw, ops_per_txn=opt)
+        # row ids below 2^32 load as 32-bit keys (the reference's row ids are 32-bit)
+        b.load(None if opt else tf, keys.astype(np.uint32) if sh["rows"] <= (1 << 32) else keys, opw, ops_per_txn=opt)
         dev.append(b)
     ctx.sync()
 
@@ -358,10 +366,12 @@ def run_ours(args, config):
         n_e2e = min(64, max(8, args.steps))
         hb = [max(range(nb), key=lambda i: host[i][3])]
         hb.append((hb[0] + 1) % nb)
+        # row ids below 2^32 travel as 32-bit keys (ltp_pipe_submit32)
+        key_t, key_b = (np.uint32, 4) if sh["rows"] <= (1 << 32) else (np.uint64, 8)
         pins = []
         for i in hb:
             tf, keys, opw, n, opt = host[i]
-            pk, pw = G.PinnedArray((len(keys),), np.uint64), G.PinnedArray((len(opw),), np.uint32)
+            pk, pw = G.PinnedArray((len(keys),), key_t), G.PinnedArray((len(opw),), np.uint32)
             pk.array[:] = keys
             pw.array[:] = opw
             ptf = G.PinnedArray((len(tf),), np.uint32)
@@ -392,7 +402,7 @@ def run_ours(args, config):
             if len(inflight) >= depth:
                 pipe.wait(inflight.pop(0))
             e2e_txns += n
-            h2d += 12 * nops + (0 if opt else 4 * (n + 1))
+            h2d += (key_b + 4) * nops + (0 if opt else 4 * (n + 1))
             d2h += 4 * nops + n
         for tk in inflight:
             pipe.wait(tk)
@@ -400,12 +410,14 @@ def run_ours(args, config):
         pipe.close()
         e2e = {"value": e2e_txns * world / e2e_s, "unit": "txn/s", "h2d_bytes_per_step": h2d // n_e2e,
                "d2h_bytes_per_step": d2h // n_e2e, "steps": n_e2e,
-               "note": "one batch per step through ltp_pipe (3 slots): H2D, execute, D2H overlapped across steps"}
+               "note": "one batch per step through ltp_pipe (3 slots): H2D, execute, D2H overlapped across steps; "
+                       f"{8 * key_b}-bit keys"}
 
     if rank != 0:
         return
     peak, peak_kind = load_peaks()
-    alg = W.algorithmic_bytes(ops_per_step, txns_per_step)
+    key_bytes = 4 if sh["rows"] <= (1 << 32) else 8  # the batches were loaded with 32-bit keys
+    alg = W.algorithmic_bytes(ops_per_step, txns_per_step, key_bytes)
     step_ms = ms / args.steps
     roof = {"bound": "hbm", "peak": peak, "unit": "GB/s", "peak_kind": peak_kind,
             "kernel_timing_pass_ms_per_step": ms_timed / max(1, min(args.steps, 5)),
@@ -413,6 +425,7 @@ def run_ours(args, config):
                          "achieved": alg / (step_ms / 1e3) / 1e9, "frac": alg / (step_ms / 1e3) / 1e9 / peak}}
     mean_stats = {k: sum(s[k] for s in stats) / len(stats) for k in ("ops", "touched_words", "contended_cells",
                                                                      "contended_ops")}
+    mean_stats["key_bytes"] = key_bytes
     if mode != G.MODE_PERSISTENT:
         avg = {name: sum(s["ms_stage"][name] for s in stats) / len(stats) for name in KERNEL_BYTES}
         dom = max(avg, key=avg.get)
@@ -426,7 +439,8 @@ def run_ours(args, config):
         roof.update({"kernel": "k_persist (whole pipeline, one launch per step)", "achieved":
                      roof["pipeline"]["achieved"], "frac": roof["pipeline"]["frac"], "traffic": None,
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": step_ms})
-    launches = args.steps * (1 if mode == G.MODE_PERSISTENT else KERNELS_PER_BATCH * nb)
+    launches = args.steps * (1 if mode == G.MODE_PERSISTENT else
+                             sum(kernels_per_batch(len(h[1]), False) for h in host))
     line = {"metric": METRIC, "value": value, "unit": "txn/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
@@ -541,7 +555,7 @@ def run_tpcc(args):
     dev = []
     for tf, keys, opw, pay, n, _ in host:
         b = ctx.batch(n, len(keys))
-        b.load(tf, keys, opw)
+        b.load(tf, keys.astype(np.uint32), opw)  # row ids and payload offsets are below 2^32
         b.load_payload(pay)
         dev.append(b)
     ctx.sync()
@@ -592,7 +606,7 @@ def run_tpcc(args):
         pins = []
         for tf, keys, opw, pay, n, _ in host[:2]:
             arrs = []
-            for a, dt in ((tf, np.uint32), (keys, np.uint64), (opw, np.uint32), (pay, np.int32)):
+            for a, dt in ((tf, np.uint32), (keys, np.uint32), (opw, np.uint32), (pay, np.int32)):
                 p = G.PinnedArray((len(a),), dt)
                 p.array[:] = a
                 arrs.append(p)
@@ -621,7 +635,7 @@ def run_tpcc(args):
             if len(inflight) >= depth:
                 pipe.wait(inflight.pop(0))
             e2e_txns += n
-            h2d += 12 * nops + 4 * (n + 1) + 4 * npay
+            h2d += 8 * nops + 4 * (n + 1) + 4 * npay  # 32-bit keys
             d2h += 4 * nops + n
         for tk in inflight:
             pipe.wait(tk)
@@ -633,7 +647,7 @@ def run_tpcc(args):
     if rank != 0:
         return
     peak, peak_kind = load_peaks()
-    alg = sum(W.tpcc_algorithmic_bytes(g, h[1], h[2], h[4]) for h in host)
+    alg = sum(W.tpcc_algorithmic_bytes(g, h[1], h[2], h[4], key_bytes=4) for h in host)  # 32-bit keys
     step_ms = ms / args.steps
     roof = {"bound": "hbm", "peak": peak, "unit": "GB/s", "peak_kind": peak_kind,
             "kernel_timing_pass_ms_per_step": ms_timed / timing_steps,
@@ -641,7 +655,8 @@ def run_tpcc(args):
                          "achieved": alg / (step_ms / 1e3) / 1e9, "frac": alg / (step_ms / 1e3) / 1e9 / peak}}
     mean_stats = {k: sum(s[k] for s in stats) / len(stats) for k in ("ops", "touched_words", "contended_cells",
                                                                      "contended_ops")}
-    mean_stats["insert_bytes"] = sum(W.tpcc_insert_bytes(g, h[1], h[2]) for h in host) / len(host)
+    mean_stats["insert_bytes"] = sum(W.tpcc_insert_bytes(g, h[1], h[2], key_bytes=4) for h in host) / len(host)
+    mean_stats["key_bytes"] = 4
     if mode != G.MODE_PERSISTENT:
         avg = {nm: sum(s["ms_stage"][nm] for s in stats) / len(stats) for nm in KERNEL_BYTES}
         dom = max(avg, key=avg.get)
@@ -654,7 +669,8 @@ def run_tpcc(args):
         roof.update({"kernel": "k_persist (whole pipeline, one launch per step)",
                      "achieved": roof["pipeline"]["achieved"], "frac": roof["pipeline"]["frac"], "traffic": None,
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": step_ms})
-    launches = args.steps * (1 if mode == G.MODE_PERSISTENT else KERNELS_PER_BATCH * nb)
+    launches = args.steps * (1 if mode == G.MODE_PERSISTENT else
+                             sum(kernels_per_batch(len(h[1]), True) for h in host))
     rows = {G.TPCC_TABLES[t]: ctx.table_rows(tid) for t, tid in enumerate(ctx_tables)}
     line = {"metric": METRIC, "value": value, "unit": "txn/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,

@@ -163,6 +163,11 @@ int ltp_batch_free(ltp_ctx *ctx, ltp_batch *b);
  * entries; when it is NULL every transaction has ops_per_txn ops. */
 int ltp_batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
                    uint64_t n_ops, const uint64_t *keys, const uint32_t *opw, void *stream);
+/* The same with 32-bit keys (row ids below 2^32, as the reference's YCSB
+ * ROW_ID): a third less to copy per op.  Insert keys (payload offsets) must
+ * fit too. */
+int ltp_batch_load32(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
+                     uint64_t n_ops, const uint32_t *keys, const uint32_t *opw, void *stream);
 /* Asynchronous host->device copy of the batch's insert payload (n int32
  * values, read by LTP_OP_INSERT ops through their key).  Call after
  * ltp_batch_load; a batch loaded without a payload has none. */
@@ -233,6 +238,10 @@ int ltp_pipe_free(ltp_pipe *p);
 int ltp_pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
                     const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
                     uint8_t *commit_out, int32_t *vals_out, uint64_t *ticket);
+/* The same with 32-bit keys (ltp_batch_load32). */
+int ltp_pipe_submit32(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
+                      const uint32_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
+                      uint8_t *commit_out, int32_t *vals_out, uint64_t *ticket);
 /* The same with the full 64-bit op values (the context must have an int64 column). */
 int ltp_pipe_submit64(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
                       const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,

@@ -388,6 +388,7 @@ int ltp_batch_free(ltp_ctx *ctx, ltp_batch *b) {
     if (!b) return LTP_E_BADARG;
     if (ctx) cudaSetDevice(ctx->device);
     cudaFree(b->keys);
+    cudaFree(b->keys32);
     cudaFree(b->opw);
     cudaFree(b->op_txn);
     cudaFree(b->out);
@@ -402,8 +403,8 @@ int ltp_batch_free(ltp_ctx *ctx, ltp_batch *b) {
     return LTP_OK;
 }
 
-int ltp_batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
-                   uint64_t n_ops, const uint64_t *keys, const uint32_t *opw, void *stream) {
+static int batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
+                      uint64_t n_ops, const void *keys, bool k32, const uint32_t *opw, void *stream) {
     if (!ctx || !b) return LTP_E_BADARG;
     if (n_txns > b->cap_txns || n_ops > b->cap_ops) return fail(ctx, LTP_E_CAPACITY, "batch larger than its capacity");
     if (n_ops && (!keys || !opw)) return fail(ctx, LTP_E_BADARG, "null op arrays");
@@ -421,8 +422,14 @@ int ltp_batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *
         CK(cudaStreamSynchronize(st));
         CK(dalloc(&b->out64, b->cap_ops));
     }
+    if (k32 && !b->keys32) {
+        CK(cudaStreamSynchronize(st));
+        CK(dalloc(&b->keys32, b->cap_ops));
+    }
+    b->key32 = k32;
     if (n_ops) {
-        CK(cudaMemcpyAsync(b->keys, keys, n_ops * 8, cudaMemcpyHostToDevice, st));
+        if (k32) CK(cudaMemcpyAsync(b->keys32, keys, n_ops * 4, cudaMemcpyHostToDevice, st));
+        else CK(cudaMemcpyAsync(b->keys, keys, n_ops * 8, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(b->opw, opw, n_ops * 4, cudaMemcpyHostToDevice, st));
     }
     b->n_txns = n_txns;
@@ -436,6 +443,16 @@ int ltp_batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *
     b->loaded = true;
     b->executed = false;
     return LTP_OK;
+}
+
+int ltp_batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
+                   uint64_t n_ops, const uint64_t *keys, const uint32_t *opw, void *stream) {
+    return batch_load(ctx, b, n_txns, txn_first, ops_per_txn, n_ops, keys, false, opw, stream);
+}
+
+int ltp_batch_load32(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
+                     uint64_t n_ops, const uint32_t *keys, const uint32_t *opw, void *stream) {
+    return batch_load(ctx, b, n_txns, txn_first, ops_per_txn, n_ops, keys, true, opw, stream);
 }
 
 int ltp_batch_load_payload(ltp_ctx *ctx, ltp_batch *b, const int32_t *payload, uint64_t n, void *stream) {
@@ -463,7 +480,8 @@ namespace {
 
 BatchDev batch_dev(const ltp_batch *b) {
     BatchDev bd;
-    bd.keys = (const u64 *)b->keys;
+    bd.keys = b->key32 ? nullptr : (const u64 *)b->keys;
+    bd.keys32 = b->key32 ? b->keys32 : nullptr;
     bd.opw = b->opw;
     bd.txn_first = b->txn_first;
     bd.op_txn = b->op_txn;
@@ -564,8 +582,9 @@ int ltp_batches_execute(ltp_ctx *ctx, ltp_batch *const *batches, uint32_t n, int
             const Tuning &t = ctx->tuning[bucket_of(b->n_ops)];
             key.insert(key.end(), {(uint64_t)(uintptr_t)b, b->n_ops, b->n_txns, b->ops_per_txn,
                                    (uint64_t)(uintptr_t)b->payload, b->payload_len,
-                                   ((uint64_t)t.block << 32) | t.ipt, (uint64_t)t.flags,
-                                   (uint64_t)(b->have_events && (ctx->flags & LTP_FLAG_STAGE_TIMING))});
+                                   ((uint64_t)t.block << 32) | t.ipt, ((uint64_t)t.word_bits << 32) | t.flags,
+                                   (uint64_t)(b->have_events && (ctx->flags & LTP_FLAG_STAGE_TIMING)),
+                                   (uint64_t)b->key32});
         }
         key.push_back(ctx->tables.size());
         key.push_back(ctx->any_wide ? 1u : 0u);
@@ -604,7 +623,7 @@ int ltp_batches_execute(ltp_ctx *ctx, ltp_batch *const *batches, uint32_t n, int
         const ltp_batch *b = batches[i];
         key.insert(key.end(), {(uint64_t)(uintptr_t)b, b->n_ops, b->n_txns, b->ops_per_txn,
                                (uint64_t)(uintptr_t)b->payload, b->payload_len,
-                               (uint64_t)ctx->tuning[bucket_of(b->n_ops)].flags});
+                               (uint64_t)ctx->tuning[bucket_of(b->n_ops)].flags, (uint64_t)b->key32});
     }
     if (key != ctx->p_key) {
         CK(cudaStreamSynchronize(st));
@@ -860,7 +879,8 @@ static int pipe_execute(ltp_ctx *ctx, PipeSlot &sl, cudaStream_t sx) {
     const ltp_batch *b = sl.b;
     const Tuning &t = ctx->tuning[bucket_of(b->n_ops)];
     const std::vector<uint64_t> key = {b->n_ops, b->n_txns, b->ops_per_txn, (uint64_t)(uintptr_t)b->payload,
-                                       b->payload_len, ((uint64_t)t.block << 32) | t.ipt, (uint64_t)t.flags,
+                                       b->payload_len, ((uint64_t)t.block << 32) | t.ipt,
+                                       ((uint64_t)t.word_bits << 32) | t.flags, (uint64_t)b->key32,
                                        (uint64_t)ctx->rule,
                                        (uint64_t)(b->have_events && (ctx->flags & LTP_FLAG_STAGE_TIMING)),
                                        ctx->tables.size(), ctx->any_wide ? 1u : 0u};
@@ -974,7 +994,7 @@ int ltp_pipe_free(ltp_pipe *p) {
 }  // extern "C"
 
 static int pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
-                       const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
+                       const void *keys, bool k32, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
                        uint8_t *commit_out, int32_t *vals_out, int64_t *vals64_out, uint64_t *ticket) {
     if (!p) return LTP_E_BADARG;
     ltp_ctx *ctx = p->ctx;
@@ -993,7 +1013,7 @@ static int pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, 
         }
     }
     if (ctx->dirty) return fail(ctx, LTP_E_STATE, "an earlier batch of this pipeline failed");
-    int rc = ltp_batch_load(ctx, sl.b, n_txns, txn_first, ops_per_txn, n_ops, keys, opw, p->s_in);
+    int rc = batch_load(ctx, sl.b, n_txns, txn_first, ops_per_txn, n_ops, keys, k32, opw, p->s_in);
     if (rc) return rc;
     if (payload && payload_len) {
         if (payload_len > sl.b->payload_cap) CK(cudaStreamSynchronize(p->s_in));
@@ -1035,15 +1055,22 @@ extern "C" {
 int ltp_pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
                     const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
                     uint8_t *commit_out, int32_t *vals_out, uint64_t *ticket) {
-    return pipe_submit(p, n_txns, txn_first, ops_per_txn, n_ops, keys, opw, payload, payload_len, commit_out, vals_out,
-                       nullptr, ticket);
+    return pipe_submit(p, n_txns, txn_first, ops_per_txn, n_ops, keys, false, opw, payload, payload_len, commit_out,
+                       vals_out, nullptr, ticket);
+}
+
+int ltp_pipe_submit32(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
+                      const uint32_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
+                      uint8_t *commit_out, int32_t *vals_out, uint64_t *ticket) {
+    return pipe_submit(p, n_txns, txn_first, ops_per_txn, n_ops, keys, true, opw, payload, payload_len, commit_out,
+                       vals_out, nullptr, ticket);
 }
 
 int ltp_pipe_submit64(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn, uint64_t n_ops,
                       const uint64_t *keys, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
                       uint8_t *commit_out, int64_t *vals_out, uint64_t *ticket) {
-    return pipe_submit(p, n_txns, txn_first, ops_per_txn, n_ops, keys, opw, payload, payload_len, commit_out, nullptr,
-                       vals_out, ticket);
+    return pipe_submit(p, n_txns, txn_first, ops_per_txn, n_ops, keys, false, opw, payload, payload_len, commit_out,
+                       nullptr, vals_out, ticket);
 }
 
 int ltp_pipe_wait(ltp_pipe *p, uint64_t ticket, ltp_stats *stats) {

@@ -62,6 +62,8 @@ struct ltp_ctx {
 struct ltp_batch {
     uint64_t cap_txns = 0, cap_ops = 0;
     uint64_t *keys = nullptr;
+    uint32_t *keys32 = nullptr;  // 32-bit keys (allocated at the first ltp_batch_load32)
+    bool key32 = false;          // the loaded batch carries 32-bit keys
     uint32_t *opw = nullptr, *txn_first = nullptr, *op_txn = nullptr;
     int32_t *out = nullptr;
     long long *out64 = nullptr;  // full outputs, allocated once the context has int64 columns

@@ -54,7 +54,8 @@ struct TablesDev {
 
 // Device view of one loaded batch.
 struct BatchDev {
-    const u64 *keys;       // [n_ops]
+    const u64 *keys;       // [n_ops] (null when the batch carries 32-bit keys)
+    const u32 *keys32;     // [n_ops] 32-bit keys (null when the batch carries 64-bit keys)
     const u32 *opw;        // [n_ops]
     const u32 *txn_first;  // [n_txns + 1]
     const u32 *op_txn;     // [n_ops] transaction of each op (variable-length batches)

@@ -396,6 +396,13 @@ __device__ __forceinline__ bool contended_id(const Scratch &s, u64 cell, u32 *m)
     return (cw & bit) != 0;
 }
 
+// Key of op i (the batch carries 64-bit or 32-bit keys; the choice is
+// uniform over the batch).
+__device__ __forceinline__ u64 op_key(const BatchDev &b, u64 i) { return b.keys32 ? (u64)b.keys32[i] : b.keys[i]; }
+__device__ __forceinline__ u64 op_key_stream(const BatchDev &b, u64 i) {  // read once: evict first
+    return b.keys32 ? (u64)__ldcs(&b.keys32[i]) : __ldcs(&b.keys[i]);
+}
+
 __device__ __forceinline__ u32 op_tid(const BatchDev &b, u64 i) {
     return b.ops_per_txn ? (u32)(i / b.ops_per_txn) : b.op_txn[i];
 }
@@ -446,7 +453,7 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             u64 i = wbase + (u64)k * 32 + lane;
-            key[k] = i < n ? b.keys[i] : 0;
+            key[k] = i < n ? op_key(b, i) : 0;
             w[k] = i < n ? b.opw[i] : 0xFFFFFFFFu;
         }
         __syncthreads();
@@ -729,7 +736,7 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             u64 i = wbase + (u64)k * 32 + lane;
-            key[k] = i < n ? __ldcs(&b.keys[i]) : 0;
+            key[k] = i < n ? op_key_stream(b, i) : 0;
             w[k] = i < n ? __ldcs(&b.opw[i]) : 0xFFFFFFFFu;
         }
         OpRef r[IPT];
@@ -1199,7 +1206,7 @@ __device__ __forceinline__ void phase_r1_minw(const BatchDev &b, const TablesDev
         u32 m = 0, tid = 0;
         if (i < n) {
             const u32 w = b.opw[i];
-            OpRef r = decode_op(T, b.keys[i], w);
+            OpRef r = decode_op(T, op_key(b, i), w);
             con = r.valid && contended_id<WB>(s, r.cell, &m);
             if (con && opw_kind(w) == LTP_OP_ADD) {
                 act = true;
@@ -1226,7 +1233,7 @@ __device__ __forceinline__ void phase_r1_abort(const BatchDev &b, const TablesDe
     const u64 n = b.n_ops;
     for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
         const u32 w = b.opw[i];
-        OpRef r = decode_op(T, b.keys[i], w);
+        OpRef r = decode_op(T, op_key(b, i), w);
         u32 m;
         if (r.valid && contended_id<WB>(s, r.cell, &m)) {
             const u32 tid = op_tid(b, i);
@@ -1247,7 +1254,7 @@ __device__ __forceinline__ void phase_r1_exec(const BatchDev &b, const TablesDev
     const u64 n = b.n_ops;
     for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
         const u32 w = b.opw[i];
-        OpRef r = decode_op(T, b.keys[i], w);
+        OpRef r = decode_op(T, op_key(b, i), w);
         if (!r.valid) continue;
         const u32 tid = op_tid(b, i);
         if (!b.commit[tid]) {
@@ -1266,7 +1273,7 @@ __device__ __forceinline__ void phase_r1_exec(const BatchDev &b, const TablesDev
             // transaction's last RMW on the cell stores.
             v = s.dbase[m];
             if (s.dminw[m] == tid) {
-                const u64 key = b.keys[i];
+                const u64 key = op_key(b, i);
                 const u32 same = w & 0xFFCu;  // column and table fields
                 // fixed-length batches carry ops_per_txn (their txn_first buffer is not loaded)
                 const u64 first = b.ops_per_txn ? (u64)tid * b.ops_per_txn : (u64)b.txn_first[tid];
@@ -1274,7 +1281,7 @@ __device__ __forceinline__ void phase_r1_exec(const BatchDev &b, const TablesDev
                 for (u64 j = first; j < end; j++) {
                     if (j == i) continue;
                     const u32 wj = b.opw[j];
-                    if (opw_kind(wj) != LTP_OP_ADD || (wj & 0xFFCu) != same || b.keys[j] != key) continue;
+                    if (opw_kind(wj) != LTP_OP_ADD || (wj & 0xFFCu) != same || op_key(b, j) != key) continue;
                     if (j < i) v = (long long)((u64)v + (u64)(long long)opw_imm(wj));
                     else store = false;
                 }
@@ -1406,7 +1413,7 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
                 const u32 e = s_toff[tb[k]] + r;
                 const u32 w = b.opw[i];
                 const u32 d = insert_link(w);
-                s_off[e] = (u32)b.keys[i];
+                s_off[e] = (u32)op_key(b, i);
                 s_lc[e] = d ? (unsigned char)opw_col(w) : (unsigned char)0xFF;
                 s_lv[e] = d ? op_value(b, T, i - d) : 0ll;
                 store_out(b, i, (long long)(s_base[tb[k]] + r));

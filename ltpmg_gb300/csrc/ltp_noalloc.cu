@@ -152,6 +152,7 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     T.t[0].n_cols = n_cols;
     BatchDev b;
     b.keys = (const u64 *)keys;
+    b.keys32 = nullptr;
     b.opw = opw;
     b.txn_first = txn_first;
     b.op_txn = op_txn;

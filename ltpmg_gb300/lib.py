@@ -124,6 +124,8 @@ def load():
         "ltp_batch_create": (ci, [vp, u64, u64, pp]),
         "ltp_batch_free": (ci, [vp, vp]),
         "ltp_batch_load": (ci, [vp, vp, u64, vp, u32, u64, vp, vp, vp]),
+        "ltp_batch_load32": (ci, [vp, vp, u64, vp, u32, u64, vp, vp, vp]),
+        "ltp_pipe_submit32": (ci, [vp, u64, vp, u32, u64, vp, vp, vp, u64, vp, vp, ctypes.POINTER(u64)]),
         "ltp_batch_execute": (ci, [vp, vp, vp]),
         "ltp_batch_fetch": (ci, [vp, vp, vp, vp, vp]),
         "ltp_batch_fetch64": (ci, [vp, vp, vp, vp]),
@@ -496,8 +498,10 @@ class Batch:
             pass
 
     def load(self, txn_first, keys, opw, ops_per_txn=0, stream=None):
-        """txn_first may be None when every transaction has ops_per_txn ops."""
-        keys = np.ascontiguousarray(keys, np.uint64)
+        """txn_first may be None when every transaction has ops_per_txn ops;
+        uint32 keys load as 32-bit keys (ltp_batch_load32), others as 64-bit."""
+        k32 = isinstance(keys, np.ndarray) and keys.dtype == np.uint32
+        keys = np.ascontiguousarray(keys, np.uint32 if k32 else np.uint64)
         opw = np.ascontiguousarray(opw, np.uint32)
         if txn_first is not None:
             txn_first = np.ascontiguousarray(txn_first, np.uint32)
@@ -505,8 +509,9 @@ class Batch:
         else:
             n_txns = len(keys) // ops_per_txn if ops_per_txn else 0
         self._keep = (txn_first, keys, opw)  # asynchronous copy: keep the sources alive
-        self.ctx.check(self.ctx.L.ltp_batch_load(self.ctx.h, self.h, n_txns, _p(txn_first), ops_per_txn, len(keys),
-                                                 _p(keys), _p(opw), _stream(stream)))
+        fn = self.ctx.L.ltp_batch_load32 if k32 else self.ctx.L.ltp_batch_load
+        self.ctx.check(fn(self.ctx.h, self.h, n_txns, _p(txn_first), ops_per_txn, len(keys), _p(keys), _p(opw),
+                          _stream(stream)))
         self.n_txns, self.n_ops = n_txns, len(keys)
 
     def load_payload(self, payload, stream=None):
@@ -557,13 +562,15 @@ class Pipe:
         self._keep = {}
 
     def submit(self, txn_first, keys, opw, commit_out=None, vals_out=None, ops_per_txn=0, payload=None):
-        """Arrays must stay alive (and unchanged) until wait(ticket)."""
+        """Arrays must stay alive (and unchanged) until wait(ticket); uint32 keys
+        go through ltp_pipe_submit32."""
         if txn_first is not None:
             n_txns = len(txn_first) - 1
         else:
             n_txns = len(keys) // ops_per_txn if ops_per_txn else 0
         t = ctypes.c_uint64()
-        self.ctx.check(self.ctx.L.ltp_pipe_submit(
+        fn = self.ctx.L.ltp_pipe_submit32 if keys.dtype == np.uint32 else self.ctx.L.ltp_pipe_submit
+        self.ctx.check(fn(
             self.h, n_txns, _p(txn_first), ops_per_txn, len(keys), _p(keys), _p(opw), _p(payload),
             0 if payload is None else len(payload), _p(commit_out), _p(vals_out), ctypes.byref(t)))
         self._keep[t.value] = (txn_first, keys, opw, commit_out, vals_out, payload)

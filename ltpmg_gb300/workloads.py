@@ -61,15 +61,16 @@ def generate(name, b, seed=None, rank=0):
     return tf, keys, opw, n, (omin if omin == omax else 0)
 
 
-def algorithmic_bytes(n_ops, n_txns):
-    """28 B per op (key 8, opword 4, value read 4, value written 4, conflict
-    state 8) + 4 B per transaction (commit word / descriptor)."""
-    return 28 * n_ops + 4 * n_txns
+def algorithmic_bytes(n_ops, n_txns, key_bytes=8):
+    """Per op its key (8 B, or 4 with 32-bit keys), opword 4, value read 4,
+    value written 4, conflict state 8 (28 B with 64-bit keys) + 4 B per
+    transaction (commit word / descriptor)."""
+    return (20 + key_bytes) * n_ops + 4 * n_txns
 
 
-def tpcc_algorithmic_bytes(g, keys, opw, n_txns):
+def tpcc_algorithmic_bytes(g, keys, opw, n_txns, key_bytes=8):
     """Bytes a batch of the TPC-C workload must move at least: per op its key
-    (8), opword (4), output (4) and conflict state (8); a read or RMW reads
+    (8, or 4 with 32-bit keys), opword (4), output (4) and conflict state (8); a read or RMW reads
     its cell (4 or 8 B, the column's width) and an RMW writes it back; an
     insert reads its payload row and writes the new row; 4 B per transaction.
     """
@@ -87,13 +88,13 @@ def tpcc_algorithmic_bytes(g, keys, opw, n_txns):
         rowb[t] = width[t, :n_cols].sum()
     w = width[tb, col]
     cell = np.where(kind == 0, w, np.where(kind == 1, 2 * w, 2 * rowb[tb]))
-    return int(24 * len(keys) + cell.sum() + 4 * n_txns)
+    return int((16 + key_bytes) * len(keys) + cell.sum() + 4 * n_txns)
 
 
-def tpcc_insert_bytes(g, keys, opw):
+def tpcc_insert_bytes(g, keys, opw, key_bytes=8):
     """Bytes the insert kernel of one batch moves at least: every opword
-    (4 B/op), and per insert its key (8), payload row (read), new row
-    (written) and output (4)."""
+    (4 B/op), and per insert its key (8, or 4 with 32-bit keys), payload row
+    (read), new row (written) and output (4)."""
     import numpy as np
 
     rowb = np.zeros(16, np.int64)
@@ -101,7 +102,7 @@ def tpcc_insert_bytes(g, keys, opw):
         n_cols, mask, _ = g.table(t)
         rowb[t] = 4 * n_cols + 4 * bin(mask).count("1")
     ins = (opw & 3) == 2
-    return int(4 * len(opw) + (12 * ins.sum()) + 2 * rowb[((opw >> 8) & 15)[ins]].sum())
+    return int(4 * len(opw) + ((4 + key_bytes) * ins.sum()) + 2 * rowb[((opw >> 8) & 15)[ins]].sum())
 
 
 def mixed_pool(ycsb, tpcc, seed, tpcc_table_base=1):

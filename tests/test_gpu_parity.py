@@ -559,3 +559,54 @@ def test_pipeline_replays_captured_graphs(lib_loaded, rule):
             assert np.array_equal(commit, rc) and np.array_equal(vals, ro)
         pipe.close()
         assert np.array_equal(ctx.download(t), ref)
+
+
+@pytest.mark.parametrize("rule", [0, 1])
+@pytest.mark.parametrize("mode", [G.lib.MODE_STREAM, G.lib.MODE_GRAPH, G.lib.MODE_PERSISTENT])
+def test_32_bit_keys(lib_loaded, rule, mode):
+    """Batches loaded with 32-bit keys (ltp_batch_load32), fixed- and
+    variable-length, in every multi-batch mode, alternating with 64-bit
+    loads of the same batch objects (the cached graph and persistent
+    descriptors must follow the key width), equal the oracle."""
+    rows, cols, seed = 1 << 14, 10, 77
+    with G.Context(device=0, rule=rule) as ctx:
+        t = ctx.create_table(rows, cols)
+        ctx.fill_seeded(t, seed)
+        ref = O.table_init(seed, rows, cols)
+        bs = [ctx.batch(3000, 3000 * 16), ctx.batch(2000, 2000 * 8)]
+        for rep in range(4):
+            data = []
+            for k, b in enumerate(bs):
+                fixed = k == 1
+                tf, keys, opw = gen(seed + rep, rows, cols, 8 if fixed else 1, 8 if fixed else 16, 0.7, 0.95, k,
+                                    2000 if fixed else 3000)
+                kk = keys.astype(np.uint32) if (rep + k) % 2 == 0 else keys
+                b.load(None if fixed else tf, kk, opw, ops_per_txn=8 if fixed else 0)
+                data.append((tf, keys, opw))
+            ctx.execute_many(bs, mode=mode)
+            for (tf, keys, opw), b in zip(data, bs):
+                commit, vals, st = b.results()
+                ref, rc, ro = O.replay(rule, ref, tf, keys, opw)
+                assert np.array_equal(commit, rc) and np.array_equal(vals, ro), rep
+        assert np.array_equal(ctx.download(t), ref)
+
+
+def test_pipeline_with_32_bit_keys(lib_loaded):
+    rows, cols, seed = 1 << 13, 10, 19
+    with G.Context(device=0) as ctx:
+        t = ctx.create_table(rows, cols)
+        ctx.fill_seeded(t, seed)
+        ref = O.table_init(seed, rows, cols)
+        pipe = G.Pipe(ctx, 3, 2048, 2048 * 16)
+        subs = []
+        for k in range(8):
+            tf, keys, opw = gen(seed, rows, cols, 16, 16, 0.7, 0.9, k, 2048)
+            commit, vals = np.zeros(2048, np.uint8), np.zeros(len(keys), np.int32)
+            kk = keys.astype(np.uint32) if k % 3 else keys
+            subs.append((pipe.submit(None, kk, opw, commit, vals, ops_per_txn=16), tf, keys, opw, commit, vals))
+        for tk, tf, keys, opw, commit, vals in subs:
+            pipe.wait(tk)
+            ref, rc, ro = O.replay(0, ref, tf, keys, opw)
+            assert np.array_equal(vals, ro)
+        pipe.close()
+        assert np.array_equal(ctx.download(t), ref)
