@@ -210,7 +210,9 @@ int ltp_batch_fetch64(ltp_ctx *ctx, ltp_batch *b, int64_t *vals, void *stream);
 int ltp_batch_finish(ltp_ctx *ctx, ltp_batch *b, ltp_stats *stats, void *stream);
 /* Convenience: fetch + finish. */
 int ltp_batch_results(ltp_ctx *ctx, ltp_batch *b, uint8_t *commit, int32_t *vals, ltp_stats *stats);
-/* Device pointers of a loaded batch's arrays (for zero-copy callers). */
+/* Device pointers of a loaded batch's arrays (for zero-copy callers); *keys
+ * is the 64-bit key array, or NULL while the batch carries 32-bit keys
+ * (ltp_batch_load32). */
 int ltp_batch_device_ptrs(ltp_batch *b, uint64_t **keys, uint32_t **opw, uint32_t **txn_first, int32_t **vals,
                           uint8_t **commit);
 

@@ -769,7 +769,7 @@ int ltp_batch_results(ltp_ctx *ctx, ltp_batch *b, uint8_t *commit, int32_t *vals
 int ltp_batch_device_ptrs(ltp_batch *b, uint64_t **keys, uint32_t **opw, uint32_t **txn_first, int32_t **vals,
                           uint8_t **commit) {
     if (!b) return LTP_E_BADARG;
-    if (keys) *keys = b->keys;
+    if (keys) *keys = b->key32 ? nullptr : b->keys;
     if (opw) *opw = b->opw;
     if (txn_first) *txn_first = b->txn_first;
     if (vals) *vals = b->out;
