@@ -46,10 +46,11 @@ def build(verbose=False, extra_nvcc=()):
         obj = os.path.join(BUILD, src + ".o")
         objs.append(obj)
         jobs.append([nvcc] + ARCH + NVCC_FLAGS + list(extra_nvcc) + ["-c", os.path.join(CSRC, src), "-o", obj])
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")  # NVTX headers
     for src in CXX_SOURCES:
         obj = os.path.join(BUILD, src + ".o")
         objs.append(obj)
-        jobs.append(["g++"] + CXX_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj])
+        jobs.append(["g++"] + CXX_FLAGS + ["-I", cuda_inc, "-c", os.path.join(CSRC, src), "-o", obj])
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         outs = list(ex.map(_run, jobs))
     if verbose:

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "ltp_host.cuh"
+#include "ltp_trace.h"
 
 using namespace ltp;
 
@@ -405,6 +406,7 @@ int ltp_batch_free(ltp_ctx *ctx, ltp_batch *b) {
 
 static int batch_load(ltp_ctx *ctx, ltp_batch *b, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
                       uint64_t n_ops, const void *keys, bool k32, const uint32_t *opw, void *stream) {
+    TraceRange tr("ltp_batch_load");
     if (!ctx || !b) return LTP_E_BADARG;
     if (n_txns > b->cap_txns || n_ops > b->cap_ops) return fail(ctx, LTP_E_CAPACITY, "batch larger than its capacity");
     if (n_ops && (!keys || !opw)) return fail(ctx, LTP_E_BADARG, "null op arrays");
@@ -551,6 +553,7 @@ extern "C" {
 
 int ltp_batch_execute(ltp_ctx *ctx, ltp_batch *b, void *stream) {
     if (!ctx || !b) return LTP_E_BADARG;
+    TraceRange tr("ltp_batch_execute");
     CK(cudaSetDevice(ctx->device));
     cudaStream_t st = pick_stream(ctx, stream);
     int rc = prepare(ctx, &b, 1, st);
@@ -560,6 +563,7 @@ int ltp_batch_execute(ltp_ctx *ctx, ltp_batch *b, void *stream) {
 
 int ltp_batches_execute(ltp_ctx *ctx, ltp_batch *const *batches, uint32_t n, int32_t mode, void *stream) {
     if (!ctx || (n && !batches)) return LTP_E_BADARG;
+    TraceRange tr("ltp_batches_execute");
     if (mode != LTP_MODE_STREAM && mode != LTP_MODE_GRAPH && mode != LTP_MODE_PERSISTENT)
         return fail(ctx, LTP_E_BADARG, "unknown execution mode");
     if (n == 0) return LTP_OK;
@@ -997,6 +1001,7 @@ static int pipe_submit(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, 
                        const void *keys, bool k32, const uint32_t *opw, const int32_t *payload, uint64_t payload_len,
                        uint8_t *commit_out, int32_t *vals_out, int64_t *vals64_out, uint64_t *ticket) {
     if (!p) return LTP_E_BADARG;
+    TraceRange tr("ltp_pipe_submit");
     ltp_ctx *ctx = p->ctx;
     CK(cudaSetDevice(ctx->device));
     const uint64_t t = p->next;
@@ -1075,6 +1080,7 @@ int ltp_pipe_submit64(ltp_pipe *p, uint64_t n_txns, const uint32_t *txn_first, u
 
 int ltp_pipe_wait(ltp_pipe *p, uint64_t ticket, ltp_stats *stats) {
     if (!p) return LTP_E_BADARG;
+    TraceRange tr("ltp_pipe_wait");
     auto it = p->done.find(ticket);
     if (it != p->done.end()) {
         const PipeDone d = it->second;

@@ -31,6 +31,7 @@
 
 #include "ltp_histo.h"
 #include "ltp_host.cuh"
+#include "ltp_trace.h"
 
 using namespace ltp;
 
@@ -272,6 +273,7 @@ struct RunState {
 
 // Folds a finished batch into the run: latencies, commits, re-queued aborts.
 int complete(ltp_ingest *g, RunState &R, IngestSlot &sl, uint64_t done) {
+    TraceRange tr("ingest: complete batch");
     if (sl.host_ctr->err) {
         g->ctx->dirty = true;
         return host_fail(g->ctx, sl.host_ctr->err, "a served batch failed on the device");
@@ -325,6 +327,7 @@ int maybe_close(ltp_ingest *g, RunState &R, uint64_t now) {
     const bool full = p_ops >= g->cap_ops || rq + fresh >= g->cfg.max_txns || p_pay >= g->max_payload;
     const bool idle = (g->cfg.flags & LTP_SERVE_EAGER) && R.inflight.empty();
     if (!deadline && !full && !idle) return LTP_OK;
+    TraceRange tr("ingest: close batch");
     const uint64_t t0 = mono_ns();
     const uint32_t si = (uint32_t)(g->seq % g->slots.size());
     IngestSlot &sl = g->slots[si];

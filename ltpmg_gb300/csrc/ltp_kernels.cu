@@ -31,6 +31,7 @@
 #include <stdint.h>
 
 #include "ltp_internal.cuh"
+#include "ltp_trace.h"
 
 namespace ltp {
 
@@ -1648,6 +1649,7 @@ static int capped(int grid, u64 upper) { return (int)((u64)grid < upper ? (u64)g
 
 cudaError_t launch_execute(const Launch &L_in, const BatchDev &b_in, const TablesDev &T, const Scratch &s,
                            Counters *ctr) {
+    TraceRange tr("launch batch kernels");
     Launch L = L_in;
     BatchDev b = b_in;
     b.flags = L.tune.flags;

@@ -38,6 +38,7 @@
 
 #include "../../include/ltpmg_gb300.h"
 #include "ltp_histo.h"
+#include "ltp_trace.h"
 
 namespace {
 
@@ -237,6 +238,7 @@ void drain_lanes(ltp_server *s) {
 }
 
 void complete_batch(ltp_server *s, Slot &sl) {
+    ltp::TraceRange tr("serve: complete batch");
     ltp_stats st;
     const int rc = ltp_pipe_wait(s->pipe, sl.ticket, &st);
     if (rc) {
@@ -390,6 +392,7 @@ bool close_batch(ltp_server *s, uint64_t now) {
     uint32_t si = 0;
     while (si < s->n_slots && s->slots[si].busy.load(std::memory_order_acquire)) si++;
     if (si == s->n_slots) return false;
+    ltp::TraceRange tr("serve: close batch");
     drain_lanes(s);
     if (s->pending_txns == 0) return false;
     if (deadline) s->closed_deadline++;

@@ -178,3 +178,47 @@ def test_tpcc_w8_batch_2_16():
     g = G.Tpcc(8, seed=23)
     stats = _run_tpcc(g, 0, 2, 1 << 16)
     assert stats[0].contended_cells > 0
+
+
+@pytest.mark.gpu
+def test_checkpoint_and_resume_replays_to_the_same_state(small):
+    """Checkpoint = every table's rows (ltp_table_download) after batch k;
+    resume = a fresh context with those rows uploaded, then the batches after
+    k.  Execution is deterministic, so the resumed run's op values, commit
+    vectors and final tables equal the uninterrupted run's (both rules)."""
+    for rule in (0, 1):
+        batches = [small.gen(b, 3000) for b in range(4)]
+        extra = np.sum([x[5] for x in batches], axis=0)
+        outs, snap = [], None
+        with G.Context(device=0, rule=rule) as ctx:
+            ids = small.create_tables(ctx, extra)
+            for k, (tf, keys, opw, pay, _, _) in enumerate(batches):
+                b = ctx.batch(len(tf) - 1, len(keys))
+                b.load(tf, keys, opw)
+                b.load_payload(pay)
+                b.execute()
+                outs.append(b.results64()[:2])
+                if k == 1:
+                    snap = [ctx.download(t) for t in ids]
+            final = [ctx.download(t) for t in ids]
+        with G.Context(device=0, rule=rule) as ctx:
+            ids2 = []
+            for t in range(9):
+                n_cols, mask, rows0 = small.table(t)
+                rows = snap[t].shape[1]
+                tid = ctx.create_table(rows, n_cols, rows_cap=max(1, rows0 + int(extra[t])),
+                                       wide=[c for c in range(n_cols) if (mask >> c) & 1])
+                if rows:
+                    for c in range(n_cols):
+                        ctx.upload_column(tid, c, snap[t][c])
+                ids2.append(tid)
+            for k in (2, 3):
+                tf, keys, opw, pay, _, _ = batches[k]
+                b = ctx.batch(len(tf) - 1, len(keys))
+                b.load(tf, keys, opw)
+                b.load_payload(pay)
+                b.execute()
+                commit, vals = b.results64()[:2]
+                assert np.array_equal(commit, outs[k][0]) and np.array_equal(vals, outs[k][1]), (rule, k)
+            for t, tid in enumerate(ids2):
+                assert np.array_equal(ctx.download(tid), final[t]), (rule, G.TPCC_TABLES[t])
