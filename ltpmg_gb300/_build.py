@@ -13,6 +13,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libltpmg_gb300.so")
+DEBUG_LIB = os.path.join(PKG, "libltpmg_gb300_debug.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
@@ -37,18 +38,24 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
-def build(verbose=False, extra_nvcc=()):
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose=False, extra_nvcc=(), debug_bounds=False):
+    """debug_bounds: build libltpmg_gb300_debug.so with every scatter index
+    checked against its capacity (-DLTP_DEBUG_BOUNDS) instead of the
+    release library."""
+    build_dir, lib = (BUILD + "_debug", DEBUG_LIB) if debug_bounds else (BUILD, LIB)
+    if debug_bounds:
+        extra_nvcc = tuple(extra_nvcc) + ("-DLTP_DEBUG_BOUNDS",)
+    os.makedirs(build_dir, exist_ok=True)
     nvcc = _nvcc()
     jobs = []
     objs = []
     for src in CU_SOURCES:
-        obj = os.path.join(BUILD, src + ".o")
+        obj = os.path.join(build_dir, src + ".o")
         objs.append(obj)
         jobs.append([nvcc] + ARCH + NVCC_FLAGS + list(extra_nvcc) + ["-c", os.path.join(CSRC, src), "-o", obj])
     cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")  # NVTX headers
     for src in CXX_SOURCES:
-        obj = os.path.join(BUILD, src + ".o")
+        obj = os.path.join(build_dir, src + ".o")
         objs.append(obj)
         jobs.append(["g++"] + CXX_FLAGS + ["-I", cuda_inc, "-c", os.path.join(CSRC, src), "-o", obj])
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
@@ -57,10 +64,10 @@ def build(verbose=False, extra_nvcc=()):
         for o in outs:
             if o.strip():
                 print(o)
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"])
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

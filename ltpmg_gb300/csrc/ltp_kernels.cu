@@ -89,6 +89,21 @@ __device__ __forceinline__ u32 lanemask_lt() {
     return m;
 }
 __device__ __forceinline__ void set_err(Counters *c, int e) { atomicCAS(&c->err, 0, e); }
+
+// Debug builds (-DLTP_DEBUG_BOUNDS) check the index of every scatter into a
+// scratch or table array, and of the conflict words, against the array's
+// capacity: a violation records LTP_E_DEVICE_ASSERT and skips the access
+// instead of trapping.  Release builds compile the checks away.
+#ifdef LTP_DEBUG_BOUNDS
+__device__ __forceinline__ bool in_bounds(Counters *ctr, u64 idx, u64 cap) {
+    if (idx < cap) return true;
+    set_err(ctr, LTP_E_DEVICE_ASSERT);
+    return false;
+}
+#define LTP_IN_BOUNDS(ctr, idx, cap) in_bounds((ctr), (u64)(idx), (u64)(cap))
+#else
+#define LTP_IN_BOUNDS(ctr, idx, cap) true
+#endif
 __device__ __forceinline__ u64 mix64(u64 z) {
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
@@ -521,7 +536,8 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
 #pragma unroll
         for (int q = 0; q < SPT; q++) {
             const u32 j = threadIdx.x + q * BLOCK;
-            const bool need = fw[q] != kEmptyKey && ((ft[q] & ~cur_m[q]) || (hw[j] & ~cur_w[q]));
+            const bool need = fw[q] != kEmptyKey && ((ft[q] & ~cur_m[q]) || (hw[j] & ~cur_w[q])) &&
+                              LTP_IN_BOUNDS(ctr, fw[q], Wd<WB>::n_words(s));
             old[q] = need ? atomicOr(Wd<WB>::touch(s, fw[q]), ft[q]) : 0;
             if (need) dmask |= 1u << q;
         }
@@ -564,7 +580,10 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
         u64 pos = s_base + s_wtot[warp] + (incl - nfirst);
 #pragma unroll
         for (int q = 0; q < SPT; q++)
-            if (fmask & (1u << q)) s.tw_list[pos++] = fw[q];
+            if (fmask & (1u << q)) {
+                if (LTP_IN_BOUNDS(ctr, pos, s.cap_ops)) s.tw_list[pos] = fw[q];
+                pos++;
+            }
         __syncthreads();
     }
 }
@@ -592,6 +611,7 @@ __device__ __forceinline__ void phase_dbase(const TablesDev &T, const Scratch &s
     if (block_err(ctr)) return;
     const u64 M = ctr->M;
     for (u64 m = (u64)blockIdx.x * blockDim.x + threadIdx.x; m < M; m += (u64)gridDim.x * blockDim.x) {
+        if (!LTP_IN_BOUNDS(ctr, m, s.cap_ops)) continue;
         const u64 cell = s.dcell[m];
         bool wide_c;
         const char *cp = cell_ptr(T, cell, &wide_c);
@@ -673,7 +693,8 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
                 while (bits) {  // the cells' values are read by k_dbase, fully parallel
                     const int bpos = Wd<WB>::ffs(bits) - 1;
                     bits &= bits - 1;
-                    s.dcell[pre++] = ((u64)wd[k] << Wd<WB>::kShift) | (u64)bpos;
+                    if (LTP_IN_BOUNDS(ctr, pre, s.cap_ops)) s.dcell[pre] = ((u64)wd[k] << Wd<WB>::kShift) | (u64)bpos;
+                    pre++;
                 }
             }
         }
@@ -814,7 +835,7 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
         const u64 pbase = s_pbase + s_wcnt[warp];
 #pragma unroll
         for (int k = 0; k < IPT; k++)
-            if (con[k]) s.list[0][pbase + lpos[k]] = rec[k];
+            if (con[k] && LTP_IN_BOUNDS(ctr, pbase + lpos[k], s.cap_ops)) s.list[0][pbase + lpos[k]] = rec[k];
         __syncthreads();
     }
     for (int i = threadIdx.x; i < passes * 256; i += BLOCK) {
@@ -990,7 +1011,7 @@ __device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, C
         for (u32 p = tid; p < tcnt; p += BLK) {
             const u64 x = s_stage[p];
             const u32 d = (u32)(x >> shift) & 255u;
-            dst[s_base[d] + (p - s_loc[d])] = x;
+            if (LTP_IN_BOUNDS(ctr, s_base[d] + (p - s_loc[d]), s.cap_ops)) dst[s_base[d] + (p - s_loc[d])] = x;
         }
         __syncthreads();
     }
@@ -1161,6 +1182,7 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
                 const u32 m = rec_id(e[k], packed);
                 const S tot = sf[k] ? sv[k] : sv[k] + carry;
                 const u32 op = rec_op(e[k], packed);
+                if (!LTP_IN_BOUNDS(ctr, op, b.n_ops) || !LTP_IN_BOUNDS(ctr, m, s.cap_ops)) continue;
                 if (!WIDE) {
                     const int32_t val = (int32_t)((u32)__ldg(&s.dbase[m]) + (u32)tot);
                     b.out[op] = val;
@@ -1218,7 +1240,8 @@ __device__ __forceinline__ void phase_r1_minw(const BatchDev &b, const TablesDev
         if ((threadIdx.x & 31) == 0 && nc) atomicAdd(&ctr->n_c, (u64)nc);
         const u32 peers = __match_any_sync(FULL_MASK, act ? m : 0xFFFFFFFFu);
         const u32 mn = __reduce_min_sync(peers, act ? tid : 0xFFFFFFFFu);
-        if (act && (threadIdx.x & 31) == (u32)(__ffs(peers) - 1)) atomicMin(&s.dminw[m], mn);
+        if (act && (threadIdx.x & 31) == (u32)(__ffs(peers) - 1) && LTP_IN_BOUNDS(ctr, m, s.cap_ops))
+            atomicMin(&s.dminw[m], mn);
     }
 }
 
@@ -1446,7 +1469,8 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
                 const int32_t *src = b.payload + s_off[e] + slot;
                 v[q] = wc[q] ? (long long)(((u64)(u32)src[1] << 32) | (u64)(u32)src[0]) : (long long)src[0];
                 if (s_lc[e] == c) v[q] = s_lv[e];
-                dst[q] = tab.data + col_off(tab, c) + (s_base[t] + j) * (wc[q] ? 8ull : 4ull);
+                if (LTP_IN_BOUNDS(ctr, s_base[t] + j, tab.rows_cap))
+                    dst[q] = tab.data + col_off(tab, c) + (s_base[t] + j) * (wc[q] ? 8ull : 4ull);
             }
 #pragma unroll
             for (int q = 0; q < U; q++)
@@ -1481,7 +1505,8 @@ __device__ __forceinline__ void phase_finish(const BatchDev &b, const TablesDev 
     if (dense) {
         for (u64 j = g0; j < nw; j += gsz) Wd<WB>::clear(s, j);
     } else {
-        for (u64 j = g0; j < ntw; j += gsz) Wd<WB>::clear(s, s.tw_list[j]);
+        for (u64 j = g0; j < ntw; j += gsz)
+            if (LTP_IN_BOUNDS(ctr, s.tw_list[j], nw)) Wd<WB>::clear(s, s.tw_list[j]);
     }
     const u64 t_ids = ((dense ? nw : ntw) + kIdsTile - 1) / kIdsTile;
     for (u64 j = g0; j < t_ids; j += gsz) s.st_ids[j] = 0;

@@ -11,7 +11,8 @@ import re
 import numpy as np
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "libltpmg_gb300.so")
+# LTPMG_LIB selects another build of the library (e.g. the bounds-checked one)
+LIB_PATH = os.environ.get("LTPMG_LIB") or os.path.join(PKG, "libltpmg_gb300.so")
 HEADER = os.path.join(os.path.dirname(PKG), "include", "ltpmg_gb300.h")
 
 LTP_OK = 0
