@@ -610,3 +610,50 @@ def test_pipeline_with_32_bit_keys(lib_loaded):
             assert np.array_equal(vals, ro)
         pipe.close()
         assert np.array_equal(ctx.download(t), ref)
+
+
+def _pattern_batch(pattern, n_ops, rows, cols, rng):
+    """n_ops single- and multi-op transactions over a key pattern."""
+    if pattern == "same_cell":
+        keys = np.full(n_ops, 7, np.uint64)
+        cols_ = np.zeros(n_ops, np.uint32)
+    elif pattern == "distinct":
+        cells = rng.permutation(rows * cols)[:n_ops]
+        keys, cols_ = (cells // cols).astype(np.uint64), (cells % cols).astype(np.uint32)
+    elif pattern == "skewed":
+        keys = np.minimum(rng.zipf(1.3, n_ops) - 1, rows - 1).astype(np.uint64)
+        cols_ = rng.integers(0, 2, n_ops).astype(np.uint32)
+    else:  # two hot cells in one conflict word, the rest distinct rows
+        keys = np.where(rng.random(n_ops) < 0.5, rng.integers(0, 2, n_ops), rng.integers(2, rows, n_ops))
+        keys, cols_ = keys.astype(np.uint64), np.zeros(n_ops, np.uint32)
+    kind = (rng.random(n_ops) < 0.5).astype(np.uint32)
+    imm = rng.integers(-3, 4, n_ops).astype(np.int64)
+    opw = np.array([O.opword(int(k), int(c), 0, int(i) if k else 0) for k, c, i in zip(kind, cols_, imm)], np.uint32)
+    cuts = np.unique(np.concatenate([[0, n_ops], rng.integers(0, n_ops + 1, max(1, n_ops // 3))]))
+    return cuts.astype(np.uint32), keys, opw
+
+
+@pytest.mark.parametrize("n_ops", [1, 63, 64, 65, 2047, 2048, 2049, 3071, 3072, 3073, 4097, 12289])
+@pytest.mark.parametrize("pattern", ["same_cell", "distinct", "skewed", "hot_pair"])
+def test_tile_boundaries_and_adversarial_keys(lib_loaded, n_ops, pattern):
+    """Batch sizes around every tile edge of the kernels (warps of 32, the
+    2048-op mark/classify/apply/insert/id tiles, the 3072-record sort tile)
+    with adversarial key patterns -- every op on one cell, every op on its
+    own cell, Zipf 1.3 skew, two hot cells sharing a conflict word -- under
+    both rules, loaded with 64- and then 32-bit keys."""
+    rows, cols = 1 << 12, 4
+    rng = np.random.default_rng(n_ops * 31 + len(pattern))
+    tf, keys, opw = _pattern_batch(pattern, n_ops, rows, cols, rng)
+    for rule in (0, 1):
+        with G.Context(device=0, rule=rule) as ctx:
+            t = ctx.create_table(rows, cols)
+            ctx.fill_seeded(t, 5)
+            ref = O.table_init(5, rows, cols)
+            b = ctx.batch(len(tf) - 1, n_ops)
+            for kk in (keys, keys.astype(np.uint32)):
+                b.load(tf, kk, opw)
+                b.execute()
+                commit, vals, st = b.results()
+                ref, rc, ro = O.replay(rule, ref, tf, keys, opw)
+                assert np.array_equal(commit, rc[:len(tf) - 1]) and np.array_equal(vals, ro), (rule, kk.dtype)
+            assert np.array_equal(ctx.download(t), ref)
