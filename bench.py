@@ -819,8 +819,30 @@ def run_serve(args):
     # serving from a device-resident request log: the same pool, requests
     # already in HBM (as a NIC writing by GPUDirect RDMA places them), the 256
     # streams' merged Poisson arrivals admitted by the clock
-    ingest_sweep = []
+    def tune_for(tf_, k_, w_, pf_, pay_):
+        """Autotunes the size buckets serving batches fall into, on leading
+        slices of the pool (untimed; the tables are truncated after)."""
+        from ltpmg_gb300 import autotune as AT
+
+        chosen = {}
+        for n in (1 << 12, 1 << 14, 1 << 16, 1 << 18):
+            n = min(n, len(tf_) - 1)
+            a, e = int(tf_[0]), int(tf_[n])
+            bt = ctx.batch(n, e - a)
+            bt.load((tf_[:n + 1] - tf_[0]).astype(np.uint32), k_[a:e], w_[a:e])
+            if pf_ is not None:
+                bt.load_payload(pay_[int(pf_[0]):int(pf_[n])])
+            ch = AT.tune_tiles(ctx, bt, reps=2)
+            chosen[ch["bucket"]] = f"{ch['block']}x{ch['ipt']}" + ("w64" if ch["word_bits"] == 64 else "") + \
+                ("+precheck" if ch["flags"] else "")
+            bt.finish()
+            del bt
+            truncate()
+        return chosen
+
+    ingest_sweep, tuned = [], {}
     if ingest_loads:
+        tuned["blend"] = tune_for(ptf, pk, pw, ppf, ppay)
         # two batches in flight: one executing, one queued behind it (a third
         # only queues a deadline-closed batch longer)
         ing = G.Ingest(ctx, ptf, pk, pw, ppf, ppay, deadline_us=250, depth=2, budget_bytes=4 << 30,
@@ -855,6 +877,7 @@ def run_serve(args):
         plain_ycsb = 10 * ny / (time.perf_counter() - t0)
         by.finish()
         del by
+        tuned["ycsb"] = tune_for(ytf, yk, yw, None, None)
         ing = G.Ingest(ctx, ytf, yk, yw, deadline_us=250, depth=2, budget_bytes=4 << 30, max_txns=1 << 20,
                        max_ops=1 << 24, eager=True)
         rng = np.random.default_rng(sh["seed"] + 29 + rank)
@@ -878,7 +901,8 @@ def run_serve(args):
             "dtype": "int32/int64", "data": "synthetic (seeded generator)",
             "config": {"workload": WORKLOAD_TEXT["serve"], "selection": "highest committed txn/s with p99 <= 2 ms",
                        "pool_txns": n_pool, "batch_execution": args.serve_mode,
-                       "value_from": "device-resident request log" if ok_ing else "host submission API"},
+                       "value_from": "device-resident request log" if ok_ing else "host submission API",
+                       "tuning": tuned},
             "serving": {"sweep": sweep, "ingest_sweep": ingest_sweep, "plain_batch_txn_per_s": plain,
                         "ycsb_ingest_sweep": ycsb_sweep, "plain_ycsb_batch_txn_per_s": plain_ycsb,
                         "best_host_submit_txn_per_s": best_host["committed_per_s_offered_window"] if best_host else 0.0,
