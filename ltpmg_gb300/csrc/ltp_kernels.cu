@@ -26,8 +26,16 @@
 // The priority rule (R1) replaces sort+apply by min-writer-TID / abort /
 // execute kernels.
 //
-// Every spin-wait (decoupled look-back, the debug stall) is bounded by the
-// global timer; on expiry the kernel records LTP_E_TIMEOUT and returns.
+// Tuning knobs per batch-size bucket (picked by the autotuner): threads per
+// block and ops per thread of mark and classify, the conflict-word width
+// (32 or 64 cells per bitmap word), and mark's hot-word pre-check.  Batches
+// carry 64- or 32-bit keys.  Stream-launched batch kernels use programmatic
+// dependent launch; one persistent cooperative kernel can run a whole list
+// of batches instead.
+//
+// Every spin-wait (decoupled look-back, grid barrier, the debug stall) is
+// bounded by the global timer; on expiry the kernel records LTP_E_TIMEOUT
+// and returns.  Debug builds (-DLTP_DEBUG_BOUNDS) check scatter indices.
 #include <stdint.h>
 
 #include "ltp_internal.cuh"
