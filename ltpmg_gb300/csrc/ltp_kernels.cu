@@ -868,8 +868,8 @@ __global__ void __launch_bounds__(BLOCK, 65536 / (BLOCK * (IPT <= 2 ? 40 : IPT <
 // and writes every digit's run with coalesced stores
 // ============================================================================
 // Stable LSD radix pass (8-bit digit P) over the dense contended records.
-// Per tile of kSortTile records: warp ranking by ballots (8 ballots give the
-// lanes that share a digit; the group's lowest lane adds the group size to
+// Per tile of kSortTile records: warp ranking by peer masks (8 ballots or
+// one match.any give the lanes that share a digit; the group's lowest lane adds the group size to
 // the warp's shared counter, whose old value is the group's offset -- a
 // warp's shared-memory atomics take effect in program order, which keeps
 // the ranks stable), per-digit decoupled look-back over a window of eight
@@ -936,11 +936,20 @@ __device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, C
         for (int k = 0; k < SIPT; k++) {
             const bool v = lbase + (u32)k * 32 + lane < tcnt;
             const u32 d = (u32)(e[k] >> shift) & 255u;
-            u32 peers = __ballot_sync(FULL_MASK, v);
+            // lanes holding the same digit (an empty lane matches only
+            // itself): eight ballots on the first pass, whose records are
+            // still in op order; match.any on the later ones (measured
+            // faster there, slower on the first)
+            u32 peers;
+            if (P == 0) {
+                peers = __ballot_sync(FULL_MASK, v);
 #pragma unroll
-            for (int bit = 0; bit < 8; bit++) {
-                const u32 m = __ballot_sync(FULL_MASK, (d >> bit) & 1u);
-                peers &= ((d >> bit) & 1u) ? m : ~m;
+                for (int bit = 0; bit < 8; bit++) {
+                    const u32 m = __ballot_sync(FULL_MASK, (d >> bit) & 1u);
+                    peers &= ((d >> bit) & 1u) ? m : ~m;
+                }
+            } else {
+                peers = __match_any_sync(FULL_MASK, v ? d : 256u + (u32)lane);
             }
             const u32 ld = (u32)__ffs(peers) - 1u;
             u32 o = 0;
