@@ -1701,7 +1701,10 @@ cudaError_t launch_execute(const Launch &L_in, const BatchDev &b_in, const Table
     // they still carry timestamps when the graph replays
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(L.stream, &cap);
-    L.pdl = cap != cudaStreamCaptureStatusActive;
+    // dependent launch for stream launches, and inside captured graphs for
+    // small batches only (measured: a gain for batches of a few thousand
+    // transactions, a loss at 2^16 x 10 ops and above)
+    L.pdl = cap != cudaStreamCaptureStatusActive || b_in.n_ops < (1ull << 18);
     const unsigned ev_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
     auto mark_ev = [&](int i) {
         if (L.timing) cudaEventRecordWithFlags(L.ev[i], L.stream, ev_flags);
