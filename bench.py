@@ -151,8 +151,8 @@ MEASURED_TRAFFIC = {
     ("zipf", "mark"): (17.7, "ops"),  # 32-bit keys
     ("zipf", "apply"): (31.3, "contended_ops"),
     ("zipf", "ids"): (8.0, "ops"),  # k_ids + k_dbase
-    ("tpcc", "insert"): (62.7, "ops"),
-    ("tpcc", "mark"): (20.0, "ops"),
+    ("tpcc", "insert"): (59.3, "ops"),  # 32-bit keys
+    ("tpcc", "mark"): (15.7, "ops"),  # 32-bit keys
 }
 
 
@@ -966,9 +966,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     ap.add_argument("--loadgen-threads", type=int, default=8, help="serving sweep: load-generator threads")
-    ap.add_argument("--ycsb-loads", default="200,400,600,800",
+    ap.add_argument("--ycsb-loads", default="200,400,600,650,700",
                     help="request-log serving of the Zipf YCSB transactions alone: offered loads in M txn/s")
-    ap.add_argument("--ingest-loads", default="50,100,200,250,300",
+    ap.add_argument("--ingest-loads", default="50,100,200,250,275,300",
                     help="serving from a device-resident request log: offered loads in M txn/s ('' = skip)")
     ap.add_argument("--serve-mode", default="persistent", choices=["persistent", "stream"],
                     help="serving: each batch as one persistent-kernel launch, or as a kernel sequence")
