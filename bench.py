@@ -31,7 +31,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "committed txn/s"
-DEFAULT_STEPS = {"zipf": 20, "plain": 50, "uneven": 30, "serve": 1, "tpcc": 10, "gather": 1}
+DEFAULT_STEPS = {"zipf": 20, "plain": 50, "uneven": 30, "serve": 1, "tpcc": 10, "ycsbe": 10, "gather": 1}
 WORKLOAD_TEXT = {
     "zipf": "ycsb-zipf0.99: 2^24 rows x 10 int32, 32 batches x 2^20 txns x 16 ops, 80% read / 20% +1 RMW",
     "plain": "ycsb-uniform: 2^20 rows x 10 int32, 16 batches x 2^16 txns x 10 ops, 50% read / 50% +1 RMW",
@@ -40,6 +40,8 @@ WORKLOAD_TEXT = {
     "tpcc": "tpcc-shaped order entry: 64 warehouses (10 districts, 30,000 customers, 100,000 stock rows each; "
             "100,000 items), 4 batches x 2^18 txns, 50% new-order (5-15 lines, NURand items, 1% remote) / 50% payment "
             "(NURand customers, 15% remote, 60% by last name, int64 cents), 9 tables, int32/int64 columns",
+    "ycsbe": "ycsb-e: 2^20 rows x 3 int32 (the reference YCSB schema's int attributes), 16 batches x 2^16 txns, "
+             "each 9 scans of rows [r, r+2) (every int column read) + 1 insert, zipf0.99 rows",
     "serve": "serving: 256 Poisson client streams, seeded 50/50 blend of zipf0.99 YCSB txns (2^24 rows x 10 int32, "
              "16 ops, 80/20) and tpcc-shaped new-order/payment txns (W=64, 9 tables, inserts), offered load swept "
              "1M-50M txn/s, 250 us batch deadline, 4 GB read/write-set budget, aborts re-queued",
@@ -496,7 +498,97 @@ def tpcc_cpu_tables(g, sample_inserts):
     return O.TablesDB(tabs)
 
 
-def tpcc_cpu_baseline(g, host, budget_s=12.0, threads=0, slice_txns=1 << 16):
+class TpccLoad:
+    """The order-entry workload for the payload runner: 9 tables, batches of
+    new-order / payment transactions with inserts."""
+    config = "tpcc"
+    dtype = "int32/int64"
+
+    def __init__(self, rank):
+        self.g, self.sh = tpcc_setup(rank)
+        self.n_batches = self.sh["batches"]
+
+    def batch(self, b):
+        tf, keys, opw, pay, n_no, ins = self.g.gen(b, self.sh["batch"])
+        return tf, keys, opw, pay, len(tf) - 1, ins
+
+    def create_tables(self, ctx, extra):
+        return self.g.create_tables(ctx, extra)
+
+    def table_names(self):
+        import ltpmg_gb300 as G
+
+        return G.TPCC_TABLES
+
+    def alg_bytes(self, h):
+        from ltpmg_gb300 import workloads as W
+
+        return W.tpcc_algorithmic_bytes(self.g, h[1], h[2], h[4], key_bytes=4)
+
+    def insert_bytes(self, h):
+        from ltpmg_gb300 import workloads as W
+
+        return W.tpcc_insert_bytes(self.g, h[1], h[2], key_bytes=4)
+
+    def cpu_tables(self, sample_inserts):
+        return tpcc_cpu_tables(self.g, sample_inserts)
+
+
+class YcsbeLoad:
+    """The YCSB-E workload (9 scans of two rows + one insert per
+    transaction, as the compatibility layer expands the reference's YCSB_E
+    query) for the payload runner: one 3-column int32 table."""
+    config = "ycsbe"
+    dtype = "int32"
+
+    def __init__(self, rank):
+        from ltpmg_gb300 import workloads as W
+
+        self.rank = rank
+        self.sh = W.SHAPES["ycsbe"]
+        self.n_batches = self.sh["batches"]
+
+    def batch(self, b):
+        from ltpmg_gb300 import workloads as W
+
+        return W.ycsbe_batch(b, rank=self.rank)
+
+    def create_tables(self, ctx, extra):
+        sh = self.sh
+        t = ctx.create_table(sh["rows"], sh["cols"], rows_cap=sh["rows"] + int(extra[0]))
+        ctx.fill_seeded(t, sh["seed"] + self.rank)
+        return [t]
+
+    def table_names(self):
+        return ["ycsb"]
+
+    def alg_bytes(self, h):
+        from ltpmg_gb300 import workloads as W
+
+        return W.ycsbe_algorithmic_bytes(len(h[1]), h[4], int(h[5][0]), self.sh["cols"])
+
+    def insert_bytes(self, h):
+        from ltpmg_gb300 import workloads as W
+
+        return W.ycsbe_insert_bytes(len(h[1]), int(h[5][0]), self.sh["cols"])
+
+    def cpu_tables(self, sample_inserts):
+        import numpy as np
+
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        sh = self.sh
+        data = np.zeros((sh["cols"], sh["rows"] + int(sample_inserts[0])), np.int32)
+        data[:, :sh["rows"]] = O.table_init(sh["seed"] + self.rank, sh["rows"], sh["cols"])
+        return O.TablesDB([(data, sh["rows"])])
+
+
+def payload_load(config, rank):
+    return TpccLoad(rank) if config == "tpcc" else YcsbeLoad(rank)
+
+
+def tpcc_cpu_baseline(wl, host, budget_s=12.0, threads=0, slice_txns=1 << 16):
     """Replay of whole-batch slices of the workload by the oracle port; only
     the replay call is timed."""
     import numpy as np
@@ -511,7 +603,7 @@ def tpcc_cpu_baseline(g, host, budget_s=12.0, threads=0, slice_txns=1 << 16):
     per = np.zeros(9, np.int64)
     for tf, keys, opw, pay, n in sample:
         per += np.bincount(((opw >> 8) & 15)[(opw & 3) == 2], minlength=16)[:9]
-    db = tpcc_cpu_tables(g, per)
+    db = wl.cpu_tables(per)
     for tf, keys, opw, pay, n in sample:
         t0 = time.perf_counter()
         db.replay(0, tf, keys, opw, pay, threads=threads)
@@ -522,7 +614,10 @@ def tpcc_cpu_baseline(g, host, budget_s=12.0, threads=0, slice_txns=1 << 16):
     return done / t_used, done, t_used
 
 
-def run_tpcc(args):
+def run_payload(args, config):
+    """Resident batches with inserts (the order-entry or the YCSB-E
+    workload): device throughput, end to end with payload, roofline, CPU
+    baseline."""
     import numpy as np
     import torch
 
@@ -536,12 +631,9 @@ def run_tpcc(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    g, sh = tpcc_setup(rank)
-    nb = args.batches or sh["batches"]
-    host = []
-    for b in range(nb):
-        tf, keys, opw, pay, n_no, ins = g.gen(b, sh["batch"])
-        host.append((tf, keys, opw, pay, len(tf) - 1, ins))
+    wl = payload_load(config, rank)
+    nb = args.batches or wl.n_batches
+    host = [wl.batch(b) for b in range(nb)]
     # every execution appends its inserts: size the insert tables for all
     # executions this run makes (tuning, warm-up, timed steps, the kernel
     # timing pass and the end-to-end pass)
@@ -551,7 +643,7 @@ def run_tpcc(args):
     per_batch = np.max([h[5] for h in host], axis=0)
     extra = per_batch * (execs_all * nb + (0 if args.tiles else 40) + (0 if args.no_e2e else n_e2e + 3))
     ctx = G.Context(device=local, stage_timing=True)
-    ctx_tables = g.create_tables(ctx, extra)
+    ctx_tables = wl.create_tables(ctx, extra)
     dev = []
     for tf, keys, opw, pay, n, _ in host:
         b = ctx.batch(n, len(keys))
@@ -647,7 +739,7 @@ def run_tpcc(args):
     if rank != 0:
         return
     peak, peak_kind = load_peaks()
-    alg = sum(W.tpcc_algorithmic_bytes(g, h[1], h[2], h[4], key_bytes=4) for h in host)  # 32-bit keys
+    alg = sum(wl.alg_bytes(h) for h in host)  # 32-bit keys
     step_ms = ms / args.steps
     roof = {"bound": "hbm", "peak": peak, "unit": "GB/s", "peak_kind": peak_kind,
             "kernel_timing_pass_ms_per_step": ms_timed / timing_steps,
@@ -655,7 +747,7 @@ def run_tpcc(args):
                          "achieved": alg / (step_ms / 1e3) / 1e9, "frac": alg / (step_ms / 1e3) / 1e9 / peak}}
     mean_stats = {k: sum(s[k] for s in stats) / len(stats) for k in ("ops", "touched_words", "contended_cells",
                                                                      "contended_ops")}
-    mean_stats["insert_bytes"] = sum(W.tpcc_insert_bytes(g, h[1], h[2], key_bytes=4) for h in host) / len(host)
+    mean_stats["insert_bytes"] = sum(wl.insert_bytes(h) for h in host) / len(host)
     mean_stats["key_bytes"] = 4
     if mode != G.MODE_PERSISTENT:
         avg = {nm: sum(s["ms_stage"][nm] for s in stats) / len(stats) for nm in KERNEL_BYTES}
@@ -663,7 +755,7 @@ def run_tpcc(args):
         dom_bytes = KERNEL_BYTES[dom](mean_stats)
         achieved = dom_bytes / (avg[dom] / 1e3) / 1e9
         roof.update({"kernel": dom, "achieved": achieved, "frac": achieved / peak,
-                     "traffic": measured_traffic("tpcc", dom, mean_stats),
+                     "traffic": measured_traffic(config, dom, mean_stats),
                      "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": avg[dom], "kernel_ms": avg})
     else:
         roof.update({"kernel": "k_persist (whole pipeline, one launch per step)",
@@ -671,11 +763,11 @@ def run_tpcc(args):
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": step_ms})
     launches = args.steps * (1 if mode == G.MODE_PERSISTENT else
                              sum(kernels_per_batch(len(h[1]), True) for h in host))
-    rows = {G.TPCC_TABLES[t]: ctx.table_rows(tid) for t, tid in enumerate(ctx_tables)}
+    rows = {wl.table_names()[t]: ctx.table_rows(tid) for t, tid in enumerate(ctx_tables)}
     line = {"metric": METRIC, "value": value, "unit": "txn/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64", "data": "synthetic (seeded generator)",
-            "config": {"workload": WORKLOAD_TEXT["tpcc"], "batches_per_step": nb, "txns_per_step": txns_per_step,
+            "scaling": "weak", "vs_baseline": None, "dtype": wl.dtype, "data": "synthetic (seeded generator)",
+            "config": {"workload": WORKLOAD_TEXT[config], "batches_per_step": nb, "txns_per_step": txns_per_step,
                        "ops_per_step": ops_per_step, "rule": "ordered (ascending TID per cell, all commit)",
                        "mode": mode_name, "mode_ms": {str(k): v for k, v in mode_ms.items()},
                        "tuning": {str(k): f"{v['block']}x{v['ipt']}" + ("w64" if v.get("word_bits") == 64 else "") + ("+precheck" if v.get("flags") else "")
@@ -686,22 +778,22 @@ def run_tpcc(args):
                            "contended_cells_per_batch": mean_stats["contended_cells"]},
             "table_rows_after": rows}
     if world == 1 and not args.no_cpu_baseline:
-        v, done, t_used = tpcc_cpu_baseline(g, host[:1])
+        v, done, t_used = tpcc_cpu_baseline(wl, host[:1])
         line["cpu_baseline"] = {"value": v, "unit": "txn/s", "cores": 1, "kind": "port",
-                                "sample": f"{done} txns of batch 0 in slices of 2^16, serial replay of the 9 tables "
-                                          f"(ordered rule), {t_used:.1f} s"}
+                                "sample": f"{done} txns of batch 0 in slices of 2^16, serial replay of the "
+                                          f"{len(ctx_tables)} table(s) (ordered rule), {t_used:.1f} s"}
     print(json.dumps(line), flush=True)
 
 
-def run_reference_tpcc(args):
+def run_reference_payload(args, config):
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import numpy as np
 
-    g, sh = tpcc_setup(0)
+    wl = payload_load(config, 0)
     threads = os.cpu_count() or 1
-    tf, keys, opw, pay, n_no, ins = g.gen(0, sh["batch"])
+    tf, keys, opw, pay, n, ins = wl.batch(0)
     slice_txns = 1 << 16
     slices = []
     for lo in range(0, len(tf) - 1, slice_txns):
@@ -713,7 +805,7 @@ def run_reference_tpcc(args):
     for i in range(n_steps):
         w = slices[i % len(slices)][2]
         per += np.bincount(((w >> 8) & 15)[(w & 3) == 2], minlength=16)[:9]
-    db = tpcc_cpu_tables(g, per)
+    db = wl.cpu_tables(per)
 
     def step(i):
         tfs, k, w, n = slices[i % len(slices)]
@@ -728,13 +820,14 @@ def run_reference_tpcc(args):
     value = txns / dt
     line = {"metric": METRIC, "value": value, "unit": "txn/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64", "data": "synthetic (seeded generator)",
-            "config": {"workload": WORKLOAD_TEXT["tpcc"], "step": f"up to {slice_txns} txns of the workload",
+            "scaling": "weak", "vs_baseline": None, "dtype": wl.dtype, "data": "synthetic (seeded generator)",
+            "config": {"workload": WORKLOAD_TEXT[config], "step": f"up to {slice_txns} txns of the workload",
                        "l2": "inputs larger than L2"},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "txn/s", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} slices of up to {slice_txns} txns of batch 0, 9 tables, "
-                                       f"cell-partitioned replay on {threads} threads (inserts split by table)"},
+                             "sample": f"{args.steps} slices of up to {slice_txns} txns of batch 0, "
+                                       f"{len(wl.table_names())} table(s), cell-partitioned replay on {threads} "
+                                       "threads (inserts split by table)"},
             "e2e": {"value": value, "unit": "txn/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -977,14 +1070,14 @@ def main():
     if not args.steps:
         args.steps = DEFAULT_STEPS[args.config]
     if args.impl == "reference":
-        if args.config == "tpcc":
-            run_reference_tpcc(args)
+        if args.config in ("tpcc", "ycsbe"):
+            run_reference_payload(args, args.config)
         else:
             run_reference(args, "zipf" if args.config in ("serve", "gather") else args.config)
     elif args.config == "serve":
         run_serve(args)
-    elif args.config == "tpcc":
-        run_tpcc(args)
+    elif args.config in ("tpcc", "ycsbe"):
+        run_payload(args, args.config)
     elif args.config == "gather":
         run_gather(args)
     else:

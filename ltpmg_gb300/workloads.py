@@ -27,6 +27,10 @@ SHAPES = {
     "zipf": dict(rows=1 << 24, cols=10, batches=32, seed=SEED + 2),
     "uneven": dict(rows=1 << 24, cols=10, batches=64, seed=SEED + 4),
     "tpcc": dict(warehouses=64, batch=1 << 18, batches=4, seed=SEED + 6),
+    # the reference's YCSB_E query (cuda/src/gpuquery.cu:3234-3303): 9 scans
+    # of rows [r, r+2) and one insert, over the int attributes of its YCSB
+    # schema (a, d, g: 3 int32 columns), rows drawn Zipf 0.99
+    "ycsbe": dict(rows=1 << 20, cols=3, batch=1 << 16, batches=16, theta=0.99, seed=SEED + 8),
 }
 
 
@@ -155,3 +159,46 @@ def expected_txns(name):
 
 
 _ = math
+
+
+def ycsbe_batch(b, rank=0, n_txns=None):
+    """Batch b of the YCSB-E workload, expanded as the compatibility layer
+    expands the reference's YCSB_E query: 9 scans of rows [r, r+2) -- each
+    row's every int column read, a row past the table's end skipped -- then
+    one insert whose int columns hold the query's tenth row id.  Returns
+    (txn_first, keys, opw, payload, n_txns, inserts per table)."""
+    import numpy as np
+
+    sh = SHAPES["ycsbe"]
+    n = sh["batch"] if n_txns is None else n_txns
+    rows, cols = sh["rows"], sh["cols"]
+    # ten distinct Zipf row ids per transaction from the library's generator
+    _, k10, _ = L.gen_ycsb(sh["seed"] + rank, rows, cols, 10, 10, 1.0, sh["theta"], batch=b, n_txns=n)
+    k = k10[:10 * n].reshape(n, 10).astype(np.int64)
+    scan = k[:, :9, None] + np.arange(2)[None, None, :]                # [n, 9, 2] rows
+    rk = np.broadcast_to(scan[..., None], (n, 9, 2, cols))             # [n, 9, 2, cols]
+    rc = np.broadcast_to(np.arange(cols), (n, 9, 2, cols))
+    keys = np.concatenate([rk.reshape(n, -1), np.arange(n)[:, None] * cols], axis=1)  # insert key: payload offset
+    opw = np.concatenate([(rc.reshape(n, -1) << 2).astype(np.uint32), np.full((n, 1), L.OP_INSERT, np.uint32)],
+                         axis=1)
+    keep = np.concatenate([np.broadcast_to(scan[..., None] < rows, (n, 9, 2, cols)).reshape(n, -1),
+                           np.ones((n, 1), bool)], axis=1)
+    tf = np.zeros(n + 1, np.uint32)
+    tf[1:] = np.cumsum(keep.sum(axis=1))
+    payload = np.repeat(k[:, 9], cols).astype(np.int32)
+    ins = np.zeros(9, np.int64)
+    ins[0] = n
+    return tf, keys[keep].astype(np.uint64), opw[keep], payload, n, ins
+
+
+def ycsbe_algorithmic_bytes(n_ops, n_txns, n_inserts, cols, key_bytes=4):
+    """Per op its key, opword (4), value read (4), output (4) and conflict
+    state (8); per insert its payload row read and new row written; 4 B per
+    transaction."""
+    return (20 + key_bytes) * n_ops + 2 * 4 * cols * n_inserts + 4 * n_txns
+
+
+def ycsbe_insert_bytes(n_ops, n_inserts, cols, key_bytes=4):
+    """Bytes the insert kernel moves at least: every opword, and per insert
+    its key, payload row, new row and output."""
+    return 4 * n_ops + (4 + key_bytes) * n_inserts + 2 * 4 * cols * n_inserts
