@@ -853,6 +853,11 @@ def run_serve(args):
     t_tf, t_k, t_w, t_pay, _, t_ins, t_pf = g.gen(0, n_each, with_pay_first=True)
     ptf, pk, pw, ppf, ppay, src = W.mixed_pool(ycsb, (t_tf, t_k, t_w, t_pay, t_pf), seed=sh["seed"] + rank)
     n_pool = len(ptf) - 1
+
+    def k32(k):
+        """Keys as 32-bit keys when they fit: the request log stores them so."""
+        return k.astype(np.uint32) if len(k) and int(k.max()) < (1 << 32) else k
+
     loads = [float(x) * 1e6 for x in args.loads.split(",")]
     t_loads = [max(0.3, min(2.0, 20e6 / r)) for r in loads]
     ingest_loads = [float(x) * 1e6 for x in args.ingest_loads.split(",")] if args.ingest_loads else []
@@ -874,7 +879,7 @@ def run_serve(args):
     # the plain batch path on the same GPU and the same blend: the whole pool
     # as one batch, executed back to back
     b = ctx.batch(n_pool, len(pk))
-    b.load(ptf, pk, pw)
+    b.load(ptf, k32(pk), pw)
     b.load_payload(ppay)
     for _ in range(3):
         b.execute()
@@ -922,7 +927,7 @@ def run_serve(args):
             n = min(n, len(tf_) - 1)
             a, e = int(tf_[0]), int(tf_[n])
             bt = ctx.batch(n, e - a)
-            bt.load((tf_[:n + 1] - tf_[0]).astype(np.uint32), k_[a:e], w_[a:e])
+            bt.load((tf_[:n + 1] - tf_[0]).astype(np.uint32), k32(k_[a:e]), w_[a:e])
             if pf_ is not None:
                 bt.load_payload(pay_[int(pf_[0]):int(pf_[n])])
             ch = AT.tune_tiles(ctx, bt, reps=2)
@@ -959,7 +964,7 @@ def run_serve(args):
         ny = 1 << 20
         ytf, yk, yw = tf[:ny + 1], keys[:int(tf[ny])], opw[:int(tf[ny])]
         by = ctx.batch(ny, len(yk))
-        by.load(ytf, yk, yw)
+        by.load(ytf, k32(yk), yw)
         for _ in range(3):
             by.execute()
         ctx.sync()
@@ -1059,9 +1064,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     ap.add_argument("--loadgen-threads", type=int, default=8, help="serving sweep: load-generator threads")
-    ap.add_argument("--ycsb-loads", default="200,400,600,650,700",
+    ap.add_argument("--ycsb-loads", default="400,600,650,700,750,800",
                     help="request-log serving of the Zipf YCSB transactions alone: offered loads in M txn/s")
-    ap.add_argument("--ingest-loads", default="50,100,200,250,275,300",
+    ap.add_argument("--ingest-loads", default="100,200,250,300,325,350",
                     help="serving from a device-resident request log: offered loads in M txn/s ('' = skip)")
     ap.add_argument("--serve-mode", default="persistent", choices=["persistent", "stream"],
                     help="serving: each batch as one persistent-kernel launch, or as a kernel sequence")

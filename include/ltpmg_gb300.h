@@ -278,6 +278,7 @@ typedef struct {
 #define LTP_SERVE_EAGER 1u        /* close a batch as soon as the device has none queued */
 #define LTP_SERVE_KEEP_RESULTS 2u /* keep per-transaction results for ltp_serve_poll */
 #define LTP_SERVE_PERSISTENT 4u   /* execute each batch as one persistent-kernel launch */
+#define LTP_SERVE_KEYS64 8u       /* request log: keep 64-bit keys even when every key fits 32 bits */
 
 typedef struct {
     uint64_t tag;           /* caller's tag */
@@ -345,11 +346,15 @@ uint64_t ltp_now_ns(void);
  * (deadline, max_txns / max_ops / 6 x max_ops payload slots, read/write-set
  * budget, LTP_SERVE_EAGER), keeps `depth` batches in flight, and re-queues
  * transactions the priority rule aborted at the head of the next batch it
- * closes (up to max_attempts tries).  Batches are gathered on the device:
- * re-queued transactions first, then the newly arrived requests in arrival
- * order; a batch of new requests only (no wrap of the pool) is executed in
- * place from the log.  Latency = the host time the batch was seen complete -
- * arrival time.
+ * closes (up to max_attempts tries).  A batch of new requests only, at most
+ * n_pool of them, executes in place from the log: the log's keys and
+ * opwords are stored twice back to back, so a window that wraps the pool is
+ * contiguous.  Other batches (re-queued transactions first, then the newly
+ * arrived requests in arrival order) are gathered on the device.  Keys travel
+ * as 32-bit keys when every key of the pool fits (unless LTP_SERVE_KEYS64);
+ * a pool whose transactions all have the same op count runs fixed-length
+ * batches.  Latency = the host time the batch was seen complete - arrival
+ * time.
  *
  * The log is a pool of n_pool transactions (txn_first[n_pool + 1] op
  * offsets; optional payload as in ltp_serve_loadgen_rows); request i of a run

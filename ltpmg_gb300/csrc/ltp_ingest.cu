@@ -11,10 +11,13 @@
 //     with LTP_SERVE_EAGER -- when the device has nothing in flight);
 //   * a batch is a list of log runs: re-queued aborts first (the priority
 //     rule's losers, oldest batch first, in their batch order), then the
-//     newly arrived requests in arrival order.  Gather kernels build the
-//     batch's op arrays from the log; a batch of new requests only that does
-//     not wrap the pool executes in place from the log (only its transaction
-//     offsets are rebased);
+//     newly arrived requests in arrival order.  The log's keys and opwords
+//     are stored twice back to back, so any window of at most n_pool
+//     consecutive requests is contiguous: a batch of new requests only
+//     executes in place from the log (its transaction offsets are rebased;
+//     a pool of equal-length transactions needs not even that).  Other
+//     batches are gathered from the log by kernels.  Keys are stored as
+//     32-bit keys when every key of the pool fits;
 //   * completion: the batch's counters (and, under the priority rule, its
 //     commit vector) come back; latencies of a run of requests are added to
 //     the histogram with one binary search per bucket, because arrivals
@@ -87,17 +90,20 @@ __global__ void k_log_txns(const LogRun *runs, u32 n_runs, u32 n_txns, u64 n_ops
     if (blockIdx.x == 0 && threadIdx.x == 0) txn_first[n_txns] = (u32)n_ops;
 }
 
-// Keys and opwords of the batch; an insert's key (a payload offset in the
-// pool) is moved onto the batch payload.
-__global__ void k_log_ops(const LogRun *runs, u32 n_runs, u64 n_ops, const u32 *txn_first, const u32 *op_txn,
-                          const u32 *p_tf, const u64 *p_keys, const u32 *p_opw, const u64 *p_pf, u64 *keys, u32 *opw) {
+// Keys (u64 or u32) and opwords of the batch; an insert's key (a payload
+// offset in the pool) is moved onto the batch payload.  opt > 0: every
+// transaction has opt ops (txn_first and op_txn are not built).
+template <typename K>
+__global__ void k_log_ops(const LogRun *runs, u32 n_runs, u64 n_ops, u32 opt, const u32 *txn_first,
+                          const u32 *op_txn, const u32 *p_tf, const K *p_keys, const u32 *p_opw, const u64 *p_pf,
+                          K *keys, u32 *opw) {
     for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < n_ops; j += (u64)gridDim.x * blockDim.x) {
-        const u32 t = op_txn[j];
+        const u32 t = opt ? (u32)(j / opt) : op_txn[j];
         const LogRun R = runs[run_of_txn(runs, n_runs, t)];
-        const u64 src = p_tf[R.pool0 + (t - R.t0)] + (j - txn_first[t]);
-        u64 k = p_keys[src];
+        const u64 src = p_tf[R.pool0 + (t - R.t0)] + (j - (opt ? (u64)t * opt : (u64)txn_first[t]));
+        K k = p_keys[src];
         const u32 w = p_opw[src];
-        if (p_pf && opw_kind(w) == LTP_OP_INSERT) k = k - p_pf[R.pool0] + R.p0;
+        if (p_pf && opw_kind(w) == LTP_OP_INSERT) k = (K)(k - p_pf[R.pool0] + R.p0);
         keys[j] = k;
         opw[j] = w;
     }
@@ -113,13 +119,13 @@ __global__ void k_log_payload(const LogRun *runs, u32 n_runs, u64 n_slots, const
 
 // Op values of the batch into the log's value array (log index < pool size);
 // ops on int64 cells have theirs in out64, the others in out.
-__global__ void k_log_vals(u64 n_ops, const u32 *txn_first, const u32 *op_txn, const u64 *txn_log, const u32 *p_tf,
-                           const u32 *opw, const TablesDev T, const int32_t *out, const long long *out64,
-                           long long *vals) {
+__global__ void k_log_vals(u64 n_ops, u32 opt, const u32 *txn_first, const u32 *op_txn, const u64 *txn_log,
+                           const u32 *p_tf, const u32 *opw, const TablesDev T, const int32_t *out,
+                           const long long *out64, long long *vals) {
     for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < n_ops; j += (u64)gridDim.x * blockDim.x) {
-        const u32 t = op_txn[j], w = opw[j], tb = opw_table(w);
+        const u32 t = opt ? (u32)(j / opt) : op_txn[j], w = opw[j], tb = opw_table(w);
         const bool wide = out64 && opw_kind(w) <= LTP_OP_ADD && tb < T.n && col_wide(T.t[tb], opw_col(w));
-        vals[p_tf[txn_log[t]] + (j - txn_first[t])] = wide ? out64[j] : (long long)out[j];
+        vals[p_tf[txn_log[t]] + (j - (opt ? (u64)t * opt : (u64)txn_first[t]))] = wide ? out64[j] : (long long)out[j];
     }
 }
 
@@ -130,7 +136,8 @@ unsigned grid_for(u64 n, int num_sms) {
 
 struct IngestSlot {
     ltp_batch *b = nullptr;
-    uint64_t *own_keys = nullptr;  // the batch's own arrays (gathered batches)
+    uint64_t *own_keys = nullptr;  // the batch's own arrays (gathered batches; 32-bit keys use own_keys' storage)
+    uint32_t *own_keys32 = nullptr;
     uint32_t *own_opw = nullptr;
     int32_t *own_pay = nullptr;
     LogRun *h_runs = nullptr, *d_runs = nullptr;  // pinned staging, device copy
@@ -154,10 +161,13 @@ struct ltp_ingest {
     ltp_serve_config cfg;
     uint64_t cap_ops = 0, max_payload = 0;
     bool keep = false;
-    // the pool, on the device and its offsets on the host
+    // the pool, on the device and its offsets on the host; keys and opwords
+    // are stored twice back to back ([2 * pool_ops]), keys as u32 when k32
     uint64_t n_pool = 0, pool_ops = 0, pool_pay = 0;
+    bool k32 = false;
+    uint32_t fixed_ops = 0;  // > 0: every pool transaction has this many ops
     u32 *p_tf = nullptr;
-    uint64_t *p_keys = nullptr;
+    void *p_keys = nullptr;
     u64 *p_pf = nullptr;
     u32 *p_opw = nullptr;
     int32_t *p_pay = nullptr;
@@ -190,6 +200,7 @@ void free_slot(IngestSlot &sl, ltp_ctx *ctx) {
     if (sl.done) cudaEventSynchronize(sl.done);
     if (sl.b) {
         sl.b->keys = sl.own_keys;
+        sl.b->keys32 = sl.own_keys32;
         sl.b->opw = sl.own_opw;
         sl.b->payload = sl.own_pay;
         ltp_batch_free(ctx, sl.b);
@@ -204,30 +215,44 @@ void free_slot(IngestSlot &sl, ltp_ctx *ctx) {
 }
 
 // Launches one batch of the given runs (t txns, o ops, p payload slots) in
-// slot sl.  `view`: one run of new requests, executed in place from the log.
+// slot sl.  `view`: new requests only (at most n_pool, so at most two runs,
+// contiguous in the doubled log), executed in place from the log.
 int submit(ltp_ingest *g, IngestSlot &sl, uint32_t t, uint64_t o, uint64_t p, bool view) {
     ltp_ctx *ctx = g->ctx;
     cudaStream_t st = ctx->stream;
     ltp_batch *b = sl.b;
     const uint32_t nr = (uint32_t)sl.runs.size();
+    const uint32_t opt = g->fixed_ops;
     memcpy(sl.h_runs, sl.runs.data(), nr * sizeof(LogRun));
     IK(cudaMemcpyAsync(sl.d_runs, sl.h_runs, nr * sizeof(LogRun), cudaMemcpyHostToDevice, st));
-    k_log_txns<<<grid_for(t, ctx->num_sms), 256, 0, st>>>(sl.d_runs, nr, t, o, g->p_tf, b->txn_first, sl.d_txn_log);
-    IK(cudaGetLastError());
-    IK(launch_expand_op_txn(st, b->txn_first, t, b->op_txn));
+    if (!opt || g->keep) {  // fixed-length batches need neither offsets nor op -> transaction map
+        k_log_txns<<<grid_for(t, ctx->num_sms), 256, 0, st>>>(sl.d_runs, nr, t, o, g->p_tf, b->txn_first,
+                                                             sl.d_txn_log);
+        IK(cudaGetLastError());
+    }
+    if (!opt) IK(launch_expand_op_txn(st, b->txn_first, t, b->op_txn));
+    b->key32 = g->k32;
     if (view) {
-        b->keys = g->p_keys + g->tf[sl.runs[0].pool0];
-        b->opw = g->p_opw + g->tf[sl.runs[0].pool0];
+        const uint64_t first = g->tf[sl.runs[0].pool0];
+        if (g->k32) b->keys32 = (uint32_t *)g->p_keys + first;
+        else b->keys = (uint64_t *)g->p_keys + first;
+        b->opw = g->p_opw + first;
         b->payload = g->p_pay;  // insert keys index the whole pool payload
         b->payload_len = g->pool_pay;
     } else {
         b->keys = sl.own_keys;
+        b->keys32 = (uint32_t *)sl.own_keys;
         b->opw = sl.own_opw;
         b->payload = sl.own_pay;
         b->payload_len = p;
-        k_log_ops<<<grid_for(o, ctx->num_sms), 256, 0, st>>>(sl.d_runs, nr, o, b->txn_first, b->op_txn, g->p_tf,
-                                                            (const u64 *)g->p_keys, g->p_opw, g->p_pf, (u64 *)b->keys,
-                                                            b->opw);
+        if (g->k32)
+            k_log_ops<u32><<<grid_for(o, ctx->num_sms), 256, 0, st>>>(sl.d_runs, nr, o, opt, b->txn_first, b->op_txn,
+                                                                     g->p_tf, (const u32 *)g->p_keys, g->p_opw,
+                                                                     g->p_pf, b->keys32, b->opw);
+        else
+            k_log_ops<u64><<<grid_for(o, ctx->num_sms), 256, 0, st>>>(sl.d_runs, nr, o, opt, b->txn_first, b->op_txn,
+                                                                     g->p_tf, (const u64 *)g->p_keys, g->p_opw,
+                                                                     g->p_pf, (u64 *)b->keys, b->opw);
         IK(cudaGetLastError());
         if (p) {
             k_log_payload<<<grid_for(p, ctx->num_sms), 256, 0, st>>>(sl.d_runs, nr, p, g->p_pf, g->p_pay, b->payload);
@@ -236,20 +261,22 @@ int submit(ltp_ingest *g, IngestSlot &sl, uint32_t t, uint64_t o, uint64_t p, bo
     }
     b->n_txns = t;
     b->n_ops = o;
-    b->ops_per_txn = 0;
+    b->ops_per_txn = opt;
     b->loaded = true;
     b->executed = false;
     int rc = host_prepare(ctx, &b, 1, st);
     if (!rc) rc = host_execute(ctx, b, st);
     // the launches hold the pointers they were given: the batch owns its arrays again
     b->keys = sl.own_keys;
+    b->keys32 = sl.own_keys32;
+    b->key32 = false;
     b->opw = sl.own_opw;
     b->payload = sl.own_pay;
     if (rc) return rc;
     if (g->keep) {
         const u32 *opw = view ? g->p_opw + g->tf[sl.runs[0].pool0] : sl.own_opw;
-        k_log_vals<<<grid_for(o, ctx->num_sms), 256, 0, st>>>(o, b->txn_first, b->op_txn, sl.d_txn_log, g->p_tf, opw,
-                                                             host_tables(ctx), b->out, b->out64, g->d_vals);
+        k_log_vals<<<grid_for(o, ctx->num_sms), 256, 0, st>>>(o, opt, b->txn_first, b->op_txn, sl.d_txn_log, g->p_tf,
+                                                             opw, host_tables(ctx), b->out, b->out64, g->d_vals);
         IK(cudaGetLastError());
     }
     IK(cudaMemcpyAsync(sl.host_ctr, b->snap, sizeof(Counters), cudaMemcpyDeviceToHost, st));
@@ -375,7 +402,7 @@ int maybe_close(ltp_ingest *g, RunState &R, uint64_t now) {
     if (deadline) R.closed_deadline++;
     else if (full) R.closed_budget++;
     else R.closed_idle++;
-    const bool view = !had_requeue && sl.runs.size() == 1;
+    const bool view = !had_requeue && t <= g->n_pool;
     sl.seq = g->seq++;
     const int rc = submit(g, sl, t, o, p, view);
     if (rc) return rc;
@@ -412,6 +439,11 @@ int ltp_ingest_open(ltp_ctx *ctx, const ltp_serve_config *cfg, uint64_t n_pool, 
     }
     const uint64_t pool_ops = txn_first[n_pool], pool_pay = pay_first ? pay_first[n_pool] : 0;
     if (pool_pay >= (1ull << 32)) return host_fail(ctx, LTP_E_CAPACITY, "pool payload must be below 2^32 slots");
+    bool k32 = !(cfg->flags & LTP_SERVE_KEYS64);
+    for (uint64_t j = 0; j < pool_ops && k32; j++) k32 = keys[j] < (1ull << 32);
+    uint32_t fixed_ops = txn_first[1];
+    for (uint64_t k = 1; k < n_pool && fixed_ops; k++)
+        if (txn_first[k + 1] - txn_first[k] != fixed_ops) fixed_ops = 0;
     if (cudaSetDevice(ctx->device) != cudaSuccess) return LTP_E_CUDA;
     ltp_ingest *g = new ltp_ingest();
     g->ctx = ctx;
@@ -423,6 +455,8 @@ int ltp_ingest_open(ltp_ctx *ctx, const ltp_serve_config *cfg, uint64_t n_pool, 
     g->n_pool = n_pool;
     g->pool_ops = pool_ops;
     g->pool_pay = pool_pay;
+    g->k32 = k32;
+    g->fixed_ops = fixed_ops;
     g->tf.assign(txn_first, txn_first + n_pool + 1);
     if (pay_first) g->pf.assign(pay_first, pay_first + n_pool + 1);
     auto up = [&](void **dst, const void *src, size_t bytes) -> cudaError_t {
@@ -430,9 +464,23 @@ int ltp_ingest_open(ltp_ctx *ctx, const ltp_serve_config *cfg, uint64_t n_pool, 
         if (e == cudaSuccess && bytes) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
         return e;
     };
+    // the log's keys and opwords twice, back to back
+    auto up2 = [&](void **dst, const void *src, size_t bytes) -> cudaError_t {
+        cudaError_t e = cudaMalloc(dst, bytes ? 2 * bytes : 4);
+        if (e == cudaSuccess && bytes) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && bytes) e = cudaMemcpy((char *)*dst + bytes, src, bytes, cudaMemcpyHostToDevice);
+        return e;
+    };
     cudaError_t e = up((void **)&g->p_tf, txn_first, (n_pool + 1) * 4);
-    if (e == cudaSuccess) e = up((void **)&g->p_keys, keys, pool_ops * 8);
-    if (e == cudaSuccess) e = up((void **)&g->p_opw, opw, pool_ops * 4);
+    if (e == cudaSuccess) {
+        if (k32) {
+            std::vector<uint32_t> k4(keys, keys + pool_ops);
+            e = up2(&g->p_keys, k4.data(), pool_ops * 4);
+        } else {
+            e = up2(&g->p_keys, keys, pool_ops * 8);
+        }
+    }
+    if (e == cudaSuccess) e = up2((void **)&g->p_opw, opw, pool_ops * 4);
     if (e == cudaSuccess && pay_first) e = up((void **)&g->p_pf, pay_first, (n_pool + 1) * 8);
     if (e == cudaSuccess && pay_first) e = up((void **)&g->p_pay, payload, pool_pay * 4);
     if (e == cudaSuccess && g->keep) e = cudaMalloc((void **)&g->d_vals, std::max<uint64_t>(pool_ops, 1) * 8);
@@ -442,6 +490,7 @@ int ltp_ingest_open(ltp_ctx *ctx, const ltp_serve_config *cfg, uint64_t n_pool, 
         if (e != cudaSuccess || rc) break;
         if ((rc = ltp_batch_create(ctx, cfg->max_txns, cap_ops, &sl.b))) break;
         sl.own_keys = sl.b->keys;
+        sl.own_keys32 = sl.b->keys32;
         sl.own_opw = sl.b->opw;
         e = cudaMalloc((void **)&sl.own_pay, std::max<uint64_t>(max_payload, 1) * 4);
         sl.b->payload = sl.own_pay;

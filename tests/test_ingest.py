@@ -92,9 +92,10 @@ def test_ingest_ordered_blend_equals_log_order_replay(eager):
     assert st["p99_us"] > 0 and st["p50_us"] <= st["p99_us"] <= st["max_us"] + 1
 
 
-def test_ingest_priority_rule_requeues_aborts():
+@pytest.mark.parametrize("ops", [(1, 8), (8, 8)])
+def test_ingest_priority_rule_requeues_aborts(ops):
     rows, cols, seed = 256, 4, 52
-    tf, keys, opw = G.gen_ycsb(seed, rows, cols, 1, 8, 0.7, 1.3, batch=0, n_txns=4000)
+    tf, keys, opw = G.gen_ycsb(seed, rows, cols, ops[0], ops[1], 0.7, 1.3, batch=0, n_txns=4000)
     n = len(tf) - 1
     arr = _arrivals(n, 1e6, seed)
     with G.Context(device=0, rule=G.RULE_PRIORITY) as ctx:
@@ -154,6 +155,54 @@ def test_ingest_log_wraps_its_pool():
                                      *_history(order, tf, keys, opw, pf, pay))
     for t, fin in enumerate(finals):
         assert np.array_equal(fin, after[t][0][:, :after[t][1]]), t
+
+
+@pytest.mark.parametrize("keys64", [False, True])
+def test_ingest_fixed_length_pool_wraps_in_place(keys64):
+    """A pool of equal-length transactions runs fixed-length batches; windows
+    that wrap the pool execute in place from the doubled log; 32- and 64-bit
+    log keys give the same tables and values."""
+    rows, cols, seed = 1 << 14, 10, 56
+    tf, keys, opw = G.gen_ycsb(seed, rows, cols, 16, 16, 0.8, 0.99, batch=0, n_txns=3000)
+    n_pool = len(tf) - 1
+    n = n_pool * 7 // 2  # requests wrap the pool three and a half times
+    arr = _arrivals(n, 4e6, seed)
+    with G.Context(device=0) as ctx:
+        t = ctx.create_table(rows, cols)
+        ctx.fill_seeded(t, seed)
+        # first the kept values of one pool's worth of requests
+        ing = G.Ingest(ctx, tf, keys, opw, deadline_us=120, depth=2, max_txns=1024, max_ops=1024 * 16,
+                       keep_results=True, keys64=keys64)
+        st = ing.run(arr[:n_pool])
+        committed, seq, pos, att, vals = ing.results(values=True)
+        ing.close()
+        mid = ctx.download(t)
+        # then a log that wraps the pool, with batches of up to the whole pool
+        ing = G.Ingest(ctx, tf, keys, opw, deadline_us=300, depth=2, max_txns=n_pool, max_ops=n_pool * 16,
+                       keys64=keys64)
+        st2 = ing.run(arr[n_pool:] - arr[n_pool])
+        ing.close()
+        mid2 = ctx.download(t)
+        # a burst larger than the pool: batches of more than n_pool requests are gathered
+        n3 = n_pool * 5 // 2
+        ing = G.Ingest(ctx, tf, keys, opw, deadline_us=300, depth=2, max_txns=2 * n_pool, max_ops=2 * n_pool * 16,
+                       keys64=keys64)
+        st3 = ing.run(np.zeros(n3, np.uint64))
+        ing.close()
+        final = ctx.download(t)
+    assert st["committed"] == n_pool and committed.all() and st["batches"] > 2
+    tab, rc, out = O.replay(0, O.table_init(seed, rows, cols), tf, keys, opw)
+    assert np.array_equal(vals, out) and np.array_equal(mid, tab)
+    assert st2["committed"] == n - n_pool and st2["batches"] > 3
+    order = [i % n_pool for i in range(n_pool, n)]
+    htf, hk, hw, _ = _history(order, tf, keys, opw, np.zeros(n_pool + 1, np.uint64), np.zeros(1, np.int32))
+    tab2, rc2, _ = O.replay(0, tab, htf, hk, hw)
+    assert np.array_equal(mid2, tab2)
+    assert st3["committed"] == n3 and st3["batches"] >= 2
+    htf, hk, hw, _ = _history([i % n_pool for i in range(n3)], tf, keys, opw, np.zeros(n_pool + 1, np.uint64),
+                              np.zeros(1, np.int32))
+    tab3, rc3, _ = O.replay(0, tab2, htf, hk, hw)
+    assert np.array_equal(final, tab3)
 
 
 def test_ingest_rejects_bad_pools_and_arrivals():
