@@ -944,7 +944,7 @@ def run_serve(args):
         # two batches in flight: one executing, one queued behind it (a third
         # only queues a deadline-closed batch longer)
         ing = G.Ingest(ctx, ptf, pk, pw, ppf, ppay, deadline_us=250, depth=2, budget_bytes=4 << 30,
-                       max_txns=1 << 20, max_ops=1 << 24, eager=True)
+                       max_txns=1 << 20, max_ops=1 << 24, eager=True, jit=bool(args.ingest_jit))
         rng = np.random.default_rng(sh["seed"] + 17 + rank)
         ing.run(np.cumsum(rng.exponential(1e9 / 20e6, 1 << 20)).astype(np.uint64))  # untimed warm-up
         truncate()
@@ -977,7 +977,7 @@ def run_serve(args):
         del by
         tuned["ycsb"] = tune_for(ytf, yk, yw, None, None)
         ing = G.Ingest(ctx, ytf, yk, yw, deadline_us=250, depth=2, budget_bytes=4 << 30, max_txns=1 << 20,
-                       max_ops=1 << 24, eager=True)
+                       max_ops=1 << 24, eager=True, jit=bool(args.ingest_jit))
         rng = np.random.default_rng(sh["seed"] + 29 + rank)
         ing.run(np.cumsum(rng.exponential(1e9 / 50e6, 1 << 20)).astype(np.uint64))  # untimed warm-up
         for rate in [float(x) * 1e6 for x in args.ycsb_loads.split(",")]:
@@ -999,6 +999,8 @@ def run_serve(args):
             "dtype": "int32/int64", "data": "synthetic (seeded generator)",
             "config": {"workload": WORKLOAD_TEXT["serve"], "selection": "highest committed txn/s with p99 <= 2 ms",
                        "pool_txns": n_pool, "batch_execution": args.serve_mode,
+                       "request_log": {"keys": "32-bit", "just_in_time_queueing": bool(args.ingest_jit),
+                                       "batches_in_flight": 2},
                        "value_from": "device-resident request log" if ok_ing else "host submission API",
                        "tuning": tuned},
             "serving": {"sweep": sweep, "ingest_sweep": ingest_sweep, "plain_batch_txn_per_s": plain,
@@ -1064,9 +1066,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     ap.add_argument("--loadgen-threads", type=int, default=8, help="serving sweep: load-generator threads")
-    ap.add_argument("--ycsb-loads", default="400,600,650,700,750,800",
+    ap.add_argument("--ycsb-loads", default="600,700,750,800,825,850",
                     help="request-log serving of the Zipf YCSB transactions alone: offered loads in M txn/s")
-    ap.add_argument("--ingest-loads", default="100,200,250,300,325,350",
+    ap.add_argument("--ingest-jit", type=int, default=1,
+                    help="serve: request log queues a batch only once the one ahead is past its sort (1) or at once (0)")
+    ap.add_argument("--ingest-loads", default="200,250,300,325,350,375",
                     help="serving from a device-resident request log: offered loads in M txn/s ('' = skip)")
     ap.add_argument("--serve-mode", default="persistent", choices=["persistent", "stream"],
                     help="serving: each batch as one persistent-kernel launch, or as a kernel sequence")

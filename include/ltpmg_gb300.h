@@ -279,6 +279,7 @@ typedef struct {
 #define LTP_SERVE_KEEP_RESULTS 2u /* keep per-transaction results for ltp_serve_poll */
 #define LTP_SERVE_PERSISTENT 4u   /* execute each batch as one persistent-kernel launch */
 #define LTP_SERVE_KEYS64 8u       /* request log: keep 64-bit keys even when every key fits 32 bits */
+#define LTP_SERVE_JIT 16u         /* request log: queue the next batch only once the batch ahead is past its sort */
 
 typedef struct {
     uint64_t tag;           /* caller's tag */

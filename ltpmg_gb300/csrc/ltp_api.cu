@@ -513,6 +513,8 @@ int execute_one(ltp_ctx *ctx, ltp_batch *b, cudaStream_t st, bool allow_stall) {
     if (allow_stall) ctx->stall_ms_next = 0;
     L.timing = b->have_events && (ctx->flags & LTP_FLAG_STAGE_TIMING);
     L.ev = b->ev;
+    L.progress = b->progress;
+    L.progress_stage = b->progress_stage;
     if (b->n_ops) CK(launch_execute(L, batch_dev(b), tables_dev(ctx), ctx->s, ctx->ctr));
     CK(cudaMemcpyAsync(b->snap, ctx->ctr, sizeof(Counters), cudaMemcpyDeviceToDevice, st));
     b->rule = ctx->rule;

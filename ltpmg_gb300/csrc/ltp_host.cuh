@@ -77,6 +77,8 @@ struct ltp_batch {
     uint64_t payload_cap = 0, payload_len = 0;
     cudaEvent_t ev[LTP_N_STAGES];
     bool have_events = false;
+    cudaEvent_t progress = nullptr;  // recorded after stage progress_stage of the next execution
+    int progress_stage = 0;
 };
 
 namespace ltp {

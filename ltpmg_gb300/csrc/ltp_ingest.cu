@@ -18,6 +18,11 @@
 //     a pool of equal-length transactions needs not even that).  Other
 //     batches are gathered from the log by kernels.  Keys are stored as
 //     32-bit keys when every key of the pool fits;
+//   * just-in-time queueing (LTP_SERVE_JIT): with a batch executing, the
+//     next one is closed only once the executing batch has passed a late
+//     stage (its radix sort, or classify for small batches), so requests
+//     arriving meanwhile still join it instead of waiting a whole batch
+//     behind a queued one;
 //   * completion: the batch's counters (and, under the priority rule, its
 //     commit vector) come back; latencies of a run of requests are added to
 //     the histogram with one binary search per bucket, because arrivals
@@ -145,6 +150,7 @@ struct IngestSlot {
     Counters *host_ctr = nullptr;
     uint8_t *h_commit = nullptr;
     cudaEvent_t done = nullptr;
+    cudaEvent_t progress = nullptr;  // the batch is past its sort (LTP_SERVE_JIT)
     std::vector<LogRun> runs;
     uint64_t seq = 0;
 };
@@ -211,6 +217,7 @@ void free_slot(IngestSlot &sl, ltp_ctx *ctx) {
     if (sl.host_ctr) cudaFreeHost(sl.host_ctr);
     if (sl.h_commit) cudaFreeHost(sl.h_commit);
     if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.progress) cudaEventDestroy(sl.progress);
     sl = IngestSlot();
 }
 
@@ -262,6 +269,10 @@ int submit(ltp_ingest *g, IngestSlot &sl, uint32_t t, uint64_t o, uint64_t p, bo
     b->n_txns = t;
     b->n_ops = o;
     b->ops_per_txn = opt;
+    // the "nearly done" mark: after the last radix pass of a large batch,
+    // after the first passes of a mid-sized one, after classify of a small one
+    b->progress = (g->cfg.flags & LTP_SERVE_JIT) ? sl.progress : nullptr;
+    b->progress_stage = o >= (1ull << 22) ? 7 : o >= (1ull << 20) ? 5 : 3;
     b->loaded = true;
     b->executed = false;
     int rc = host_prepare(ctx, &b, 1, st);
@@ -272,6 +283,7 @@ int submit(ltp_ingest *g, IngestSlot &sl, uint32_t t, uint64_t o, uint64_t p, bo
     b->key32 = false;
     b->opw = sl.own_opw;
     b->payload = sl.own_pay;
+    b->progress = nullptr;
     if (rc) return rc;
     if (g->keep) {
         const u32 *opw = view ? g->p_opw + g->tf[sl.runs[0].pool0] : sl.own_opw;
@@ -352,7 +364,12 @@ int maybe_close(ltp_ingest *g, RunState &R, uint64_t now) {
     const uint64_t p_pay = R.rq_pay + g->log_pay(R.arrived) - g->log_pay(R.head);
     const bool deadline = now >= oldest + (uint64_t)g->cfg.deadline_us * 1000ull;
     const bool full = p_ops >= g->cap_ops || rq + fresh >= g->cfg.max_txns || p_pay >= g->max_payload;
-    const bool idle = (g->cfg.flags & LTP_SERVE_EAGER) && R.inflight.empty();
+    // just in time: the batch ahead (the last one launched) is past its sort
+    const bool jit = (g->cfg.flags & LTP_SERVE_JIT) != 0;
+    const bool ahead_ending =
+        R.inflight.empty() || (jit && cudaEventQuery(g->slots[R.inflight.back()].progress) != cudaErrorNotReady);
+    if (jit && !ahead_ending && !full) return LTP_OK;
+    const bool idle = (g->cfg.flags & LTP_SERVE_EAGER) && ahead_ending;
     if (!deadline && !full && !idle) return LTP_OK;
     TraceRange tr("ingest: close batch");
     const uint64_t t0 = mono_ns();
@@ -501,6 +518,7 @@ int ltp_ingest_open(ltp_ctx *ctx, const ltp_serve_config *cfg, uint64_t n_pool, 
         if (e == cudaSuccess) e = cudaMallocHost((void **)&sl.host_ctr, sizeof(Counters));
         if (e == cudaSuccess) e = cudaMallocHost((void **)&sl.h_commit, cfg->max_txns);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.progress, cudaEventDisableTiming);
     }
     if (rc || e != cudaSuccess) {
         if (!rc) rc = host_cuda_fail(ctx, e, "ltp_ingest_open");

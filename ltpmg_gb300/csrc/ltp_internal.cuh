@@ -149,6 +149,8 @@ struct Launch {
     u32 stall_ms;
     cudaEvent_t *ev;  // LTP_N_STAGES events of the batch when timing
     bool timing;
+    cudaEvent_t progress = nullptr;  // recorded after stage progress_stage (the serving loop's "nearly done")
+    int progress_stage = 0;
     bool pdl = false;  // programmatic dependent launch (set by launch_execute for uncaptured streams)
 };
 

@@ -1708,6 +1708,7 @@ cudaError_t launch_execute(const Launch &L_in, const BatchDev &b_in, const Table
     const unsigned ev_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
     auto mark_ev = [&](int i) {
         if (L.timing) cudaEventRecordWithFlags(L.ev[i], L.stream, ev_flags);
+        if (L.progress && i == L.progress_stage) cudaEventRecordWithFlags(L.progress, L.stream, ev_flags);
     };
     mark_ev(0);
     if (L.stall) k_stall<<<1, 1, 0, L.stream>>>(ctr, L.stall_ms);

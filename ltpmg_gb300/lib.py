@@ -660,13 +660,14 @@ class Ingest:
     """Serving from a device-resident request log (the C-ABI ltp_ingest):
     the pool goes to the device once; run() serves requests 0..n-1 (request i
     = pool transaction i mod pool size) at their arrival times.  keys64 keeps
-    64-bit keys on the device even when every key fits 32 bits."""
+    64-bit keys on the device even when every key fits 32 bits; jit queues
+    the next batch only once the batch ahead is past its sort."""
 
     def __init__(self, ctx, txn_first, keys, opw, pay_first=None, payload=None, deadline_us=250, depth=3,
                  budget_bytes=4 << 30, max_txns=1 << 20, max_ops=1 << 24, max_attempts=64, eager=True,
-                 keep_results=False, keys64=False):
+                 keep_results=False, keys64=False, jit=False):
         self.ctx = ctx
-        flags = (1 if eager else 0) | (2 if keep_results else 0) | (8 if keys64 else 0)
+        flags = (1 if eager else 0) | (2 if keep_results else 0) | (8 if keys64 else 0) | (16 if jit else 0)
         cfg = ServeConfig(deadline_us, depth, budget_bytes, max_txns, max_ops, max_attempts, flags)
         self._pool = (np.ascontiguousarray(txn_first, np.uint32), np.ascontiguousarray(keys, np.uint64),
                       np.ascontiguousarray(opw, np.uint32),

@@ -65,8 +65,8 @@ def _history(order, tf, keys, opw, pf, pay):
             np.array(hp or [0], np.int32))
 
 
-@pytest.mark.parametrize("eager", [True, False])
-def test_ingest_ordered_blend_equals_log_order_replay(eager):
+@pytest.mark.parametrize("eager,jit", [(True, False), (False, False), (True, True), (False, True)])
+def test_ingest_ordered_blend_equals_log_order_replay(eager, jit):
     rows, cols, seed = 1 << 12, 10, 51
     g, tf, keys, opw, pf, pay, ins = _blend(seed, rows, cols, 6000)
     n = len(tf) - 1
@@ -74,7 +74,7 @@ def test_ingest_ordered_blend_equals_log_order_replay(eager):
     with G.Context(device=0) as ctx:
         tabs = _tables(ctx, g, seed, rows, cols, ins)
         ing = G.Ingest(ctx, tf, keys, opw, pf, pay, deadline_us=250, depth=3, max_txns=2048, max_ops=2048 * 48,
-                       eager=eager, keep_results=True)
+                       eager=eager, keep_results=True, jit=jit)
         st = ing.run(arr)
         committed, seq, pos, att, vals = ing.results(values=True)
         ing.close()
@@ -179,7 +179,7 @@ def test_ingest_fixed_length_pool_wraps_in_place(keys64):
         mid = ctx.download(t)
         # then a log that wraps the pool, with batches of up to the whole pool
         ing = G.Ingest(ctx, tf, keys, opw, deadline_us=300, depth=2, max_txns=n_pool, max_ops=n_pool * 16,
-                       keys64=keys64)
+                       keys64=keys64, jit=True)
         st2 = ing.run(arr[n_pool:] - arr[n_pool])
         ing.close()
         mid2 = ctx.download(t)
