@@ -269,10 +269,12 @@ int submit(ltp_ingest *g, IngestSlot &sl, uint32_t t, uint64_t o, uint64_t p, bo
     b->n_txns = t;
     b->n_ops = o;
     b->ops_per_txn = opt;
-    // the "nearly done" mark: after the last radix pass of a large batch,
-    // after the first passes of a mid-sized one, after classify of a small one
+    // the "nearly done" mark: after apply in a large batch (inserts and
+    // clean-up left), after the radix sort in a mid-sized one, after
+    // classify in a small one -- what is left must cover the host's close
+    // and first launches of the next batch (~40 us)
     b->progress = (g->cfg.flags & LTP_SERVE_JIT) ? sl.progress : nullptr;
-    b->progress_stage = o >= (1ull << 22) ? 7 : o >= (1ull << 20) ? 5 : 3;
+    b->progress_stage = o >= (1ull << 22) ? 8 : o >= (1ull << 20) ? 7 : 3;
     b->loaded = true;
     b->executed = false;
     int rc = host_prepare(ctx, &b, 1, st);
