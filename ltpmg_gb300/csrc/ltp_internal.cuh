@@ -130,7 +130,7 @@ constexpr u32 kApplyBlock = 256;
 constexpr u32 kApplyIpt = 8;
 constexpr u32 kApplyTile = kApplyBlock * kApplyIpt;
 constexpr u32 kMinTile = 128;  // smallest classify tile (block 128 x 1 op)
-constexpr u32 kInsBlock = 256;
+constexpr u32 kInsBlock = 512;
 constexpr u32 kInsIpt = 8;
 constexpr u32 kInsTile = kInsBlock * kInsIpt;
 constexpr u32 kInsSmem = kInsTile * (4 + 8 + 1);  // insert staging: payload offset, link value, link column

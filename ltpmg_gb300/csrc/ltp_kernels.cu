@@ -1770,6 +1770,7 @@ cudaError_t launch_execute(const Launch &L_in, const BatchDev &b_in, const Table
     {
         static int gins = 0, sms = 0;
         if (sms != L.num_sms) {
+            chk(cudaFuncSetAttribute(k_insert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInsSmem));
             gins = occ_grid(k_insert, kInsBlock, L.num_sms, kInsSmem);
             sms = L.num_sms;
         }

@@ -381,6 +381,52 @@ def test_inserts_two_tables_sequence(lib_loaded, rule):
                 assert np.array_equal(ctx.download(tid), ref[k][0][:, :ref[k][1]])
 
 
+@pytest.mark.parametrize("layout", ["reversed", "gaps", "half_shuffled"])
+def test_inserts_scattered_payload_rows(lib_loaded, layout):
+    """Insert rows placed anywhere in the payload (reversed, separated by
+    unused words, shuffled in half the batch): tiles whose rows span more
+    than the kernel's payload stage read them from global memory, the others
+    through the stage; both must give the serial replay's tables."""
+    rng = np.random.default_rng(77)
+    shapes = [(500, 3), (64, 5)]
+    with G.Context(device=0) as ctx:
+        ids, ref = [], []
+        for k, (rows, cols) in enumerate(shapes):
+            tid = ctx.create_table(rows, cols, rows_cap=rows + 20000)
+            ctx.fill_seeded(tid, 7 + k)
+            data = np.zeros((cols, rows + 20000), np.int32)
+            data[:, :rows] = O.table_init(7 + k, rows, cols)
+            ids.append(tid)
+            ref.append((data, rows))
+        tf, keys, opw, payload = _insert_batch(rng, list(shapes), 6000, p_ins=0.4)
+        ins = np.nonzero((opw & 3) == 2)[0]
+        width = [shapes[(int(opw[i]) >> 8) & 15][1] for i in ins]
+        rows_ = [payload[int(keys[i]):int(keys[i]) + w] for i, w in zip(ins, width)]
+        order = np.arange(len(ins))
+        if layout == "reversed":
+            order = order[::-1]
+        elif layout == "half_shuffled":
+            h = len(order) // 2
+            order[:h] = rng.permutation(order[:h])
+        new_pay, new_keys = [], keys.copy()
+        for j in order:
+            if layout == "gaps" and rng.random() < 0.05:
+                new_pay.extend(rng.integers(-9, 9, int(rng.integers(1000, 6000))).tolist())
+            new_keys[ins[j]] = len(new_pay)
+            new_pay.extend(rows_[j].tolist())
+        payload = np.array(new_pay, np.int32)
+        b = ctx.batch(6000, len(keys))
+        b.load(tf, new_keys, opw)
+        b.load_payload(payload)
+        b.execute()
+        commit, vals, st = b.results()
+        ref, rc, ro = O.replay_tables(0, ref, tf, new_keys, opw, payload)
+        assert np.array_equal(commit, rc) and np.array_equal(vals, ro)
+        for k, tid in enumerate(ids):
+            assert ctx.table_rows(tid) == ref[k][1]
+            assert np.array_equal(ctx.download(tid), ref[k][0][:, :ref[k][1]])
+
+
 def test_insert_capacity_and_payload_errors(lib_loaded):
     with G.Context(device=0) as ctx:
         t = ctx.create_table(10, 2, rows_cap=12)
