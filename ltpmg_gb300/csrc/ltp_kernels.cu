@@ -1131,61 +1131,70 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
             s_ws[warp] = cs;
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            // exclusive prefix over warps, then tile look-back
+        if (warp == 0) {
+            // lane 0: exclusive prefix over warps and the tile's aggregate;
+            // then the whole warp looks back, 32 predecessors per round trip
             u32 af = 0;
             S as = 0;
-            for (int w = 0; w < NW; w++) {
-                u32 f = s_wf[w];
-                S sm = s_ws[w];
-                s_wf[w] = af;
-                s_ws[w] = as;
-                if (f) {
-                    af = 1;
-                    as = sm;
-                } else {
-                    as += sm;
+            if (lane == 0) {
+                for (int w = 0; w < NW; w++) {
+                    u32 f = s_wf[w];
+                    S sm = s_ws[w];
+                    s_wf[w] = af;
+                    s_ws[w] = as;
+                    if (f) {
+                        af = 1;
+                        as = sm;
+                    } else {
+                        as += sm;
+                    }
                 }
+                const u64 agg = ((u64)af << 61) | ((u64)as & kSum61);
+                st_status(&s.st_apply[tile], (tile == 0 ? kInc : kAgg) | agg);
             }
-            u64 agg = ((u64)af << 61) | ((u64)as & kSum61);
+            af = __shfl_sync(FULL_MASK, af, 0);
+            as = __shfl_sync(FULL_MASK, as, 0);
             u64 *st = s.st_apply;
             u32 ef = 0;
             S es = 0;
-            if (tile == 0) {
-                st_status(&st[0], kInc | agg);
-            } else {
-                st_status(&st[tile], kAgg | agg);
-                long long t = (long long)tile - 1;
+            if (tile > 0) {
+                long long t = (long long)tile - 1;  // lane j reads predecessor t - j
                 const u64 t0 = gtimer();
-                for (;;) {  // four predecessors per round trip
-                    u64 x[4];
+                for (;;) {
+                    const long long q = t - lane;
+                    const u64 x = q >= 0 ? ld_status(&st[q]) : kInc;
+                    const u32 fl = (u32)(x >> 62);
+                    const u32 hb = (u32)((x >> 61) & 1ull);
+                    const u32 nr = __ballot_sync(FULL_MASK, fl == 0);               // not yet published
+                    const u32 sp = __ballot_sync(FULL_MASK, fl == 2 || (fl != 0 && hb));  // ends the walk
+                    const int first_nr = nr ? __ffs(nr) - 1 : 32;
+                    const int first_sp = sp ? __ffs(sp) - 1 : 32;
+                    const bool stop = first_sp < first_nr;
+                    const int upto = stop ? first_sp + 1 : first_nr;  // lanes [0, upto) are summed
+                    S v = lane < upto ? unpack_sum<S>(x) : (S)0;
 #pragma unroll
-                    for (int j = 0; j < 4; j++) x[j] = t - j >= 0 ? ld_status(&st[t - j]) : kInc;
-                    bool stop = false;
-                    int j = 0;
-                    for (; j < 4; j++) {
-                        const u64 fl = x[j] >> 62;
-                        if (fl == 0) break;
-                        es += unpack_sum<S>(x[j]);
-                        ef = (u32)((x[j] >> 61) & 1ull);
-                        if (fl == 2 || ef) {
-                            stop = true;
-                            break;
-                        }
+                    for (int d = 16; d >= 1; d >>= 1) v += __shfl_xor_sync(FULL_MASK, v, d);
+                    es += v;
+                    if (stop) {
+                        ef = __shfl_sync(FULL_MASK, hb, first_sp);
+                        break;
                     }
-                    if (stop) break;
-                    t -= j;
-                    if (gtimer() - t0 > kSpinLimitNs) {
-                        set_err(ctr, LTP_E_TIMEOUT);
+                    t -= first_nr;
+                    if (__shfl_sync(FULL_MASK, (u32)(gtimer() - t0 > kSpinLimitNs), 0)) {
+                        if (lane == 0) set_err(ctr, LTP_E_TIMEOUT);
                         break;
                     }
                 }
-                u32 incf = af ? 1u : ef;
-                S incs = af ? as : es + as;
-                st_status(&st[tile], kInc | ((u64)incf << 61) | ((u64)incs & kSum61));
+                if (lane == 0) {
+                    const u32 incf = af ? 1u : ef;
+                    const S incs = af ? as : es + as;
+                    st_status(&st[tile], kInc | ((u64)incf << 61) | ((u64)incs & kSum61));
+                }
             }
-            s_tf = ef;
-            s_ts = es;
+            if (lane == 0) {
+                s_tf = ef;
+                s_ts = es;
+            }
         }
         __syncthreads();
         // carry into this warp = combine(tile exclusive, warp exclusive)
