@@ -63,7 +63,6 @@ void free_scratch_ops(Scratch &s) {
     cudaFree(s.dminw);
     cudaFree(s.st_sort[0]);
     cudaFree(s.st_sort[1]);
-    cudaFree(s.st_ids);
     cudaFree(s.st_cls);
     cudaFree(s.st_apply);
     cudaFree(s.st_ins);
@@ -74,7 +73,7 @@ void free_scratch_ops(Scratch &s) {
     s.dbase = nullptr;
     s.dminw = nullptr;
     s.st_sort[0] = s.st_sort[1] = nullptr;
-    s.st_ids = s.st_cls = s.st_apply = nullptr;
+    s.st_cls = s.st_apply = nullptr;
     s.cap_ops = 0;
 }
 
@@ -111,7 +110,6 @@ int ensure_scratch(ltp_ctx *ctx, uint64_t n_ops) {
         CK(dalloc(&s.dminw, cap));
         CK(dalloc(&s.st_sort[0], stiles * 256));
         CK(dalloc(&s.st_sort[1], stiles * 256));
-        CK(dalloc(&s.st_ids, tiles));
         CK(dalloc(&s.st_cls, tiles));
         CK(dalloc(&s.st_apply, tiles));
         CK(dalloc(&s.st_ins, tiles * LTP_MAX_TABLES));

@@ -74,7 +74,7 @@ struct BatchDev {
 constexpr int kMaxPasses = 4;
 
 // Look-back status slots of the kernels that use decoupled look-back.
-enum TileSlot { SLOT_IDS = 0, SLOT_CLASSIFY = 1, SLOT_SORT0 = 2, SLOT_APPLY = 6, SLOT_INSERT = 7, N_SLOTS = 8 };
+enum TileSlot { SLOT_CLASSIFY = 0, SLOT_SORT0 = 1, SLOT_APPLY = 5, SLOT_INSERT = 6, N_SLOTS = 7 };
 
 // Per-batch device counters; zeroed by the host before every batch.
 struct Counters {
@@ -110,7 +110,6 @@ struct Scratch {
     long long *dbase; // [cap_ops] value of each contended cell before the batch
     u32 *dminw;     // [cap_ops] smallest writer TID of each contended cell (priority rule)
     u32 *st_sort[2];// [tiles * 256] radix look-back status
-    u64 *st_ids;    // [tiles] id-scan look-back status
     u64 *st_cls;    // [tiles] classify look-back status (dense record offsets)
     u64 *st_apply;  // [tiles] segmented-apply look-back status
     u32 *st_ins;    // [tiles * LTP_MAX_TABLES] insert-slot look-back status

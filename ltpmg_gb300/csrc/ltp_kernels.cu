@@ -4,8 +4,9 @@
 //   mark      read/write-set bitmaps per cell (touched, touched twice,
 //             written) built with warp-aggregated atomicOr; records every
 //             bitmap word the batch touches
-//   ids       contended cell = touched twice and written; scan over the
-//             touched words gives every contended cell a dense id
+//   ids       contended cell = touched twice and written; a block scan over
+//             a tile of touched words numbers its contended cells, and one
+//             atomic per tile takes the next free range of dense ids
 //   dbase     per contended id: the cell's address, width and value before
 //             the batch
 //   classify  uncontended ops execute in place (one toucher, or no writer);
@@ -649,9 +650,7 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
         const u32 tb = threadIdx.x;
         if (T.rows_now[tb] + ctr->ins_total[tb] > T.t[tb].row_limit) set_err(ctr, LTP_E_CAPACITY);
     }
-    for (;;) {
-        const u32 tile = claim_tile(ctr, SLOT_IDS);
-        if (tile >= tiles) break;
+    for (u32 tile = blockIdx.x; tile < tiles; tile += gridDim.x) {  // tiles wait for no other tile
         u32 wd[IPT];
         WT cw[IPT];
         u32 cnt = 0;
@@ -686,9 +685,10 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
                 s_warp[i] = run;
                 run += c;
             }
-            u64 excl = lookback_sum(s.st_ids, tile, run, ctr);
-            s_prefix = excl;
-            if (tile == tiles - 1) ctr->M = (u32)(excl + run);
+            // ids need only be a bijection onto 0..M-1 with each word's ids
+            // consecutive: a tile takes the next free range with one atomic
+            // and waits for no other tile (M ends as the total)
+            s_prefix = run ? atomicAdd(&ctr->M, run) : 0u;
         }
         __syncthreads();
         u64 pre = s_prefix + s_warp[warp] + (incl - cnt);
@@ -1534,8 +1534,6 @@ __device__ __forceinline__ void phase_finish(const BatchDev &b, const TablesDev 
         for (u64 j = g0; j < ntw; j += gsz)
             if (LTP_IN_BOUNDS(ctr, s.tw_list[j], nw)) Wd<WB>::clear(s, s.tw_list[j]);
     }
-    const u64 t_ids = ((dense ? nw : ntw) + kIdsTile - 1) / kIdsTile;
-    for (u64 j = g0; j < t_ids; j += gsz) s.st_ids[j] = 0;
     const u64 nc = ctr->n_c;
     const u64 t_apply = (nc + kApplyTile - 1) / kApplyTile;
     for (u64 j = g0; j < t_apply; j += gsz) s.st_apply[j] = 0;
@@ -1938,7 +1936,6 @@ cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s) {
     cudaMemsetAsync(s.words, 0, (s.n_words + 1) * sizeof(WordState), st);  // + the 64-cell layout's spare entry
     cudaMemsetAsync(s.st_sort[0], 0, s.cap_sort_tiles * 256 * 4, st);
     cudaMemsetAsync(s.st_sort[1], 0, s.cap_sort_tiles * 256 * 4, st);
-    cudaMemsetAsync(s.st_ids, 0, s.cap_tiles * 8, st);
     cudaMemsetAsync(s.st_cls, 0, s.cap_tiles * 8, st);
     cudaMemsetAsync(s.st_apply, 0, s.cap_tiles * 8, st);
     cudaMemsetAsync(s.st_ins, 0, s.cap_tiles * LTP_MAX_TABLES * 4, st);

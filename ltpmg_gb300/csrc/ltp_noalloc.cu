@@ -47,8 +47,7 @@ constexpr u64 kOffDminw = kOffDbase + align256(kNaMaxOps * 8);
 constexpr u64 kOffOpTxn = kOffDminw + align256(kNaMaxOps * 4);
 constexpr u64 kOffSort0 = kOffOpTxn + align256(kNaMaxOps * 4);
 constexpr u64 kOffSort1 = kOffSort0 + align256(kNaSortTiles * 256 * 4);
-constexpr u64 kOffIds = kOffSort1 + align256(kNaSortTiles * 256 * 4);
-constexpr u64 kOffCls = kOffIds + align256(kNaTiles * 8);
+constexpr u64 kOffCls = kOffSort1 + align256(kNaSortTiles * 256 * 4);
 constexpr u64 kOffApply = kOffCls + align256(kNaTiles * 8);
 constexpr u64 kOffIns = kOffApply + align256(kNaTiles * 8);
 constexpr u64 kOffRows = kOffIns + align256(kNaTiles * LTP_MAX_TABLES * 4);
@@ -119,7 +118,6 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     s.dminw = (u32 *)(base + kOffDminw);
     s.st_sort[0] = (u32 *)(base + kOffSort0);
     s.st_sort[1] = (u32 *)(base + kOffSort1);
-    s.st_ids = (u64 *)(base + kOffIds);
     s.st_cls = (u64 *)(base + kOffCls);
     s.st_apply = (u64 *)(base + kOffApply);
     s.st_ins = (u32 *)(base + kOffIns);
