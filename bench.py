@@ -365,7 +365,7 @@ def run_ours(args, config):
         # op values back into pinned host memory; copies of neighbouring steps
         # overlap execution (3-deep pipeline, three streams)
         depth = 3
-        n_e2e = min(64, max(8, args.steps))
+        n_e2e = min(64, max(32, args.steps))
         hb = [max(range(nb), key=lambda i: host[i][3])]
         hb.append((hb[0] + 1) % nb)
         # row ids below 2^32 travel as 32-bit keys (ltp_pipe_submit32)
@@ -638,7 +638,7 @@ def run_payload(args, config):
     # executions this run makes (tuning, warm-up, timed steps, the kernel
     # timing pass and the end-to-end pass)
     timing_steps = max(1, min(args.steps, 5))
-    n_e2e = min(32, max(8, args.steps))
+    n_e2e = max(32, min(64, args.steps))
     execs_all = (6 if args.mode == "auto" else 0) + args.warmup * 2 + args.steps + timing_steps
     per_batch = np.max([h[5] for h in host], axis=0)
     extra = per_batch * (execs_all * nb + (0 if args.tiles else 40) + (0 if args.no_e2e else n_e2e + 3))
