@@ -313,7 +313,8 @@ def run_ours(args, config):
 
     # autotuning (untimed): tilings per size bucket, then the multi-batch mode
     ctx.set_stage_timing(False)  # tune what the timed region runs: no event nodes
-    tiles = fixed_tiles(ctx, dev, args.tiles) if args.tiles else AT.tune_buckets(ctx, dev, reps=3)
+    # resident batches run from captured graphs: candidates are timed that way
+    tiles = fixed_tiles(ctx, dev, args.tiles) if args.tiles else AT.tune_buckets(ctx, dev, reps=3, copies=4)
     if args.mode == "auto":
         mode, mode_ms = AT.tune_mode(ctx, dev)
     else:

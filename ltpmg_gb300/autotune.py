@@ -28,48 +28,61 @@ def bucket_of(n_ops):
     return max(0, int(math.floor(math.log2(n_ops)))) if n_ops > 0 else 0
 
 
-def _time_batch(ctx, batch, reps):
+def _time_batch(ctx, batch, reps, copies=1):
+    """Median over reps of one execution's time.  copies > 1: the batch runs
+    that many times back to back in one captured graph per rep (the way
+    resident batches run), so host launch gaps do not blur small batches."""
     import torch
 
     stream = torch.cuda.ExternalStream(ctx.stream)
+    if copies > 1:
+        ctx.execute_many([batch] * copies, mode=L.MODE_GRAPH)  # captures this tuning's graph
     ms = []
     for _ in range(reps):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        batch.execute()
+        if copies > 1:
+            ctx.execute_many([batch] * copies, mode=L.MODE_GRAPH)
+        else:
+            batch.execute()
         e1.record(stream)
         e1.synchronize()
-        ms.append(e0.elapsed_time(e1))
+        ms.append(e0.elapsed_time(e1) / copies)
     batch.finish()
     ms.sort()
     return ms[len(ms) // 2]
 
 
-def tune_tiles(ctx, batch, reps=3, blocks=BLOCKS, ipts=IPTS):
+def tune_tiles(ctx, batch, reps=3, blocks=BLOCKS, ipts=IPTS, copies=1):
     """Times every (block, ipt) on one loaded batch; sets and returns the best
-    for the batch's size bucket as {"block", "ipt", "ms", "candidates"}."""
+    for the batch's size bucket as {"block", "ipt", "ms", "candidates"}.
+    copies > 1 times graph-captured back-to-back executions (see _time_batch);
+    a batch with insert payload is always timed one execution at a time, so
+    that tuning appends as few rows as possible."""
     bucket = bucket_of(batch.n_ops)
+    if getattr(batch, "_keep_payload", None) is not None or batch.n_ops >= (1 << 22):
+        copies = 1  # (a batch of 2^22 ops runs long enough to time alone)
     results = {}
     batch.execute()  # warm-up
     batch.finish()
     for blk in blocks:
         for ipt in ipts:
             ctx.set_tuning(bucket, blk, ipt)
-            results[f"{blk}x{ipt}"] = _time_batch(ctx, batch, reps)
+            results[f"{blk}x{ipt}"] = _time_batch(ctx, batch, reps, copies)
     # conflict-word granularity: 64-cell words for the three fastest tilings
     # that have them (tiles of at most 2048 ops)
     for name in sorted(results, key=results.get)[:6]:
         blk, ipt = (int(x) for x in name.split("x"))
         if blk * ipt <= 2048 and len([k for k in results if k.endswith("w64")]) < 3:
             ctx.set_tuning(bucket, blk, ipt, word_bits=64)
-            results[f"{name}w64"] = _time_batch(ctx, batch, reps)
+            results[f"{name}w64"] = _time_batch(ctx, batch, reps, copies)
     best = min(results, key=results.get)
     base, _, wb = best.partition("w")
     blk, ipt = (int(x) for x in base.split("x"))
     word_bits = int(wb) if wb else 32
     # then, for the best tiling, the mark kernel's hot-word pre-check
     ctx.set_tuning(bucket, blk, ipt, word_bits=word_bits, flags=L.TUNE_MARK_PRECHECK)
-    pre_ms = _time_batch(ctx, batch, reps)
+    pre_ms = _time_batch(ctx, batch, reps, copies)
     results[f"{best}+precheck"] = pre_ms
     flags = L.TUNE_MARK_PRECHECK if pre_ms < results[best] else 0
     ctx.set_tuning(bucket, blk, ipt, word_bits=word_bits, flags=flags)
@@ -100,14 +113,14 @@ def tune_mode(ctx, batches, reps=2, modes=(L.MODE_GRAPH, L.MODE_PERSISTENT)):
     return min(out, key=out.get), out
 
 
-def tune_buckets(ctx, batches, reps=3):
+def tune_buckets(ctx, batches, reps=3, copies=1):
     """One representative batch per size bucket; returns {bucket: choice}."""
     seen = {}
     for b in batches:
         k = bucket_of(b.n_ops)
         if k not in seen or b.n_ops > seen[k].n_ops:
             seen[k] = b
-    return {k: tune_tiles(ctx, b, reps) for k, b in sorted(seen.items())}
+    return {k: tune_tiles(ctx, b, reps, copies=copies) for k, b in sorted(seen.items())}
 
 
 def save(path, choices, mode=None):

@@ -510,6 +510,7 @@ class Batch:
         else:
             n_txns = len(keys) // ops_per_txn if ops_per_txn else 0
         self._keep = (txn_first, keys, opw)  # asynchronous copy: keep the sources alive
+        self._keep_payload = None  # a load drops the previous payload
         fn = self.ctx.L.ltp_batch_load32 if k32 else self.ctx.L.ltp_batch_load
         self.ctx.check(fn(self.ctx.h, self.h, n_txns, _p(txn_first), ops_per_txn, len(keys), _p(keys), _p(opw),
                           _stream(stream)))
