@@ -151,7 +151,7 @@ def load_peaks():
 MEASURED_TRAFFIC = {
     ("zipf", "classify"): (41.2, "ops"),  # 32-bit keys
     ("zipf", "mark"): (17.7, "ops"),  # 32-bit keys
-    ("zipf", "apply"): (31.3, "contended_ops"),
+    ("zipf", "apply"): (33.3, "contended_ops"),
     ("zipf", "ids"): (8.0, "ops"),  # k_ids + k_dbase
     ("tpcc", "insert"): (59.3, "ops"),  # 32-bit keys
     ("tpcc", "mark"): (15.7, "ops"),  # 32-bit keys
