@@ -148,9 +148,8 @@ __device__ __forceinline__ void lookback_publish(u64 *status, u32 tile, u64 agg)
     st_status(&status[tile], (tile == 0 ? kInc : kAgg) | agg);
 }
 // ... and later walks back for the exclusive prefix, then publishes the
-// inclusive one.  Bounded: gives up with LTP_E_TIMEOUT after 2 s.  One
-// thread per tile calls it; it stays out of line.
-__device__ __noinline__ u64 lookback_wait(u64 *status, u32 tile, u64 agg, Counters *ctr) {
+// inclusive one.  Bounded: gives up with LTP_E_TIMEOUT after 2 s.
+__device__ __forceinline__ u64 lookback_wait(u64 *status, u32 tile, u64 agg, Counters *ctr) {
     constexpr int WIN = 4;  // predecessors read per round trip
     if (tile == 0) return 0;
     u64 excl = 0;
