@@ -68,6 +68,8 @@ class ServeConfig(ctypes.Structure):
 
 
 SERVE_MAX_OPS = 64
+# ltp_serve_config.flags
+SERVE_EAGER, SERVE_KEEP_RESULTS, SERVE_PERSISTENT, SERVE_KEYS64, SERVE_JIT = 1, 2, 4, 8, 16
 
 
 class ServeResult(ctypes.Structure):
@@ -606,7 +608,8 @@ class Server:
     def __init__(self, ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 20, max_ops=1 << 24,
                  max_attempts=64, eager=True, keep_results=True, persistent=False):
         self.ctx = ctx
-        flags = (1 if eager else 0) | (2 if keep_results else 0) | (4 if persistent else 0)
+        flags = (SERVE_EAGER if eager else 0) | (SERVE_KEEP_RESULTS if keep_results else 0) | \
+            (SERVE_PERSISTENT if persistent else 0)
         cfg = ServeConfig(deadline_us, depth, budget_bytes, max_txns, max_ops, max_attempts, flags)
         h = ctypes.c_void_p()
         ctx.check(ctx.L.ltp_serve_open(ctx.h, ctypes.byref(cfg), ctypes.byref(h)))
@@ -668,7 +671,8 @@ class Ingest:
                  budget_bytes=4 << 30, max_txns=1 << 20, max_ops=1 << 24, max_attempts=64, eager=True,
                  keep_results=False, keys64=False, jit=False):
         self.ctx = ctx
-        flags = (1 if eager else 0) | (2 if keep_results else 0) | (8 if keys64 else 0) | (16 if jit else 0)
+        flags = (SERVE_EAGER if eager else 0) | (SERVE_KEEP_RESULTS if keep_results else 0) | \
+            (SERVE_KEYS64 if keys64 else 0) | (SERVE_JIT if jit else 0)
         cfg = ServeConfig(deadline_us, depth, budget_bytes, max_txns, max_ops, max_attempts, flags)
         self._pool = (np.ascontiguousarray(txn_first, np.uint32), np.ascontiguousarray(keys, np.uint64),
                       np.ascontiguousarray(opw, np.uint32),

@@ -48,3 +48,21 @@ def test_pinned_alloc_without_gpu_is_null_or_valid(lib):
 
 def test_build_artifacts_in_tree():
     assert os.path.dirname(G.lib.LIB_PATH).endswith("ltpmg_gb300")
+
+
+def test_binding_constants_match_the_header():
+    """The ctypes binding's flag, mode, rule, op and status constants equal
+    the header's #defines."""
+    import re
+
+    hdr = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                            "ltpmg_gb300.h")).read()
+    defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define LTP_(\w+)\s+\(?(-?\d+)u?\)?", hdr)}
+    for name in ("SERVE_EAGER", "SERVE_KEEP_RESULTS", "SERVE_PERSISTENT", "SERVE_KEYS64", "SERVE_JIT",
+                 "SERVE_MAX_OPS", "MODE_STREAM", "MODE_GRAPH", "MODE_PERSISTENT", "RULE_ORDERED", "RULE_PRIORITY",
+                 "OP_READ", "OP_ADD", "OP_INSERT", "FLAG_STAGE_TIMING", "TUNE_MARK_PRECHECK", "PROBE_LOAD",
+                 "PROBE_ATOMIC", "PROBE_REDUCE"):
+        assert name in defs, name
+        assert getattr(G.lib, name) == defs[name], name
+    for name in ("E_BADARG", "E_CUDA", "E_CAPACITY", "E_TIMEOUT", "E_DEVICE_ASSERT", "E_NOMEM", "E_STATE"):
+        assert getattr(G.lib, "LTP_" + name) == defs[name], name
