@@ -31,7 +31,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "committed txn/s"
-DEFAULT_STEPS = {"zipf": 20, "plain": 50, "uneven": 30, "serve": 1, "tpcc": 10, "ycsbe": 10, "gather": 1}
+DEFAULT_STEPS = {"zipf": 20, "plain": 50, "uneven": 30, "serve": 1, "tpcc": 10, "ycsbe": 10, "gather": 1,
+                 "refcuda": 5}
 WORKLOAD_TEXT = {
     "zipf": "ycsb-zipf0.99: 2^24 rows x 10 int32, 32 batches x 2^20 txns x 16 ops, 80% read / 20% +1 RMW",
     "plain": "ycsb-uniform: 2^20 rows x 10 int32, 16 batches x 2^16 txns x 10 ops, 50% read / 50% +1 RMW",
@@ -42,6 +43,8 @@ WORKLOAD_TEXT = {
             "(NURand customers, 15% remote, 60% by last name, int64 cents), 9 tables, int32/int64 columns",
     "ycsbe": "ycsb-e: 2^20 rows x 3 int32 (the reference YCSB schema's int attributes), 16 batches x 2^16 txns, "
              "each 9 scans of rows [r, r+2) (every int column read) + 1 insert, zipf0.99 rows",
+    "refcuda": "the reference's own CUDA path (cuda/src, unchanged, sm_103a) on YCSB_A batches: 2^20 rows "
+               "(3 int, 3 double, 4 string columns), 2^16 txns x 10 distinct uniform rows (5 selects, 5 updates)",
     "serve": "serving: 256 Poisson client streams, seeded 50/50 blend of zipf0.99 YCSB txns (2^24 rows x 10 int32, "
              "16 ops, 80/20) and tpcc-shaped new-order/payment txns (W=64, 9 tables, inserts), offered load swept "
              "1M-50M txn/s, 250 us batch deadline, 4 GB read/write-set budget, aborts re-queued",
@@ -228,7 +231,42 @@ def cpu_baseline(config, host, budget_s=12.0):
             "sample": f"{done} whole batch(es), {done_txns} txns, serial replay (ordered rule), {t_used:.1f} s"}
 
 
+def oracle_batches(config, nb, seed=None):
+    """Batches of the workload drawn by the oracle's own generator
+    (ltpo_gen_ycsb_batch), fingerprint-equal to the library's, so that the
+    reference arm never loads the product library."""
+    from ltpmg_gb300 import workloads as W  # shapes only: importing it loads no library
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    sh = W.SHAPES[config]
+    s = sh["seed"] if seed is None else seed
+    out = []
+    for b in range(nb):
+        n, omin, omax, rf, th = W.batch_params(config, b, s)
+        tf, keys, opw = O.gen_ycsb_batch(O.ycsb_params(s, sh["rows"], sh["cols"], omin, omax, rf, th), b, n)
+        out.append((tf, keys, opw, n))
+    return out
+
+
+def product_library_mapped():
+    """Is libltpmg_gb300.so mapped into this process?"""
+    try:
+        return "libltpmg_gb300" in open("/proc/self/maps").read()
+    except OSError:
+        return False
+
+
 def run_reference(args, config):
+    """The reference arm: the reference's execution rule on the host cores.
+    The reference has no executable CPU path for execution (execute_on_CPU is
+    never called, cuda/src/gpulauncher.cu:771), so the oracle's
+    cell-partitioned serial replay on every host thread stands in for it.
+    Each step replays one whole batch of the workload (the same batches the
+    GPU arm runs: for the default workload 2^20 transactions x 16 ops) on a
+    table that carries every earlier step's effects.  Inputs come from the
+    oracle's generator; the product library is never loaded."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -241,25 +279,16 @@ def run_reference(args, config):
 
     threads = os.cpu_count() or 1
     sh = W.SHAPES[config]
-    nb = min(sh["batches"], 4)
-    host = gen_batches(config, nb, 0)
+    nb = min(sh["batches"], 4 if config == "zipf" else 8)
+    host = oracle_batches(config, nb)
     tab = O.table_init(sh["seed"], sh["rows"], sh["cols"])
     L = O.lib()
-    slice_txns = 1 << 16
-
-    # each step replays a slice of up to 2^16 transactions of the workload
-    slices = []
-    for tf, keys, opw, n, _ in host:
-        for lo in range(0, n, slice_txns):
-            hi = min(n, lo + slice_txns)
-            a, b = int(tf[lo]), int(tf[hi])
-            slices.append(((tf[lo:hi + 1] - tf[lo]).astype(np.uint32), keys[a:b], opw[a:b], hi - lo))
 
     def step(i):
-        tfs, k, w, n = slices[i % len(slices)]
+        tf, k, w, n = host[i % len(host)]
         commit = np.zeros(n, np.uint8)
         out = np.zeros(len(k), np.int32)
-        rc = L.ltpo_replay_r0_mt(sh["rows"], sh["cols"], tab.ctypes.data, n, tfs.ctypes.data, k.ctypes.data,
+        rc = L.ltpo_replay_r0_mt(sh["rows"], sh["cols"], tab.ctypes.data, n, tf.ctypes.data, k.ctypes.data,
                                  w.ctypes.data, commit.ctypes.data, out.ctypes.data, threads)
         assert rc == 0
         return n
@@ -269,16 +298,20 @@ def run_reference(args, config):
     t0 = time.perf_counter()
     txns = sum(step(args.warmup + i) for i in range(args.steps))
     dt = time.perf_counter() - t0
+    assert not product_library_mapped(), "the reference arm must not load the product library"
     value = txns / dt
+    sizes = sorted({h[3] for h in host})
     line = {"metric": METRIC, "value": value, "unit": "txn/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
-            "config": {"workload": WORKLOAD_TEXT[config], "step": f"up to {slice_txns} txns of the workload",
-                       "l2": "inputs larger than L2"},
+            "config": {"workload": WORKLOAD_TEXT[config],
+                       "step": "one whole batch of the workload (" + "/".join(str(x) for x in sizes) + " txns), "
+                               f"cycling over its first {nb} batches",
+                       "l2": "inputs larger than L2", "same_config": True},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "txn/s", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} slices of up to {slice_txns} txns from {nb} batches, "
-                                       f"cell-partitioned serial replay on {threads} threads"},
+                             "sample": f"{args.steps} whole batches, cell-partitioned serial replay (ordered rule) "
+                                       f"on {threads} threads; inputs from the oracle's generator"},
             "e2e": {"value": value, "unit": "txn/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -1013,6 +1046,56 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def uniform_distinct_rows(rows, n, per, seed):
+    """n x per row ids, uniform over rows and distinct within each row of
+    the result (the reference's YCSB generator redraws repeats,
+    src/txn_generator.cpp:627-642)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    q = rng.integers(0, rows, size=(n, per), dtype=np.int64)
+    while True:
+        s = np.sort(q, axis=1)
+        bad = (s[:, 1:] == s[:, :-1]).any(axis=1)
+        if not bad.any():
+            return q.astype(np.uint32)
+        q[bad] = rng.integers(0, rows, size=(int(bad.sum()), per), dtype=np.int64)
+
+
+def run_refcuda(args):
+    """The reference's own CUDA path timed on this GPU (oracle/_ref/
+    ltpmg_ref_cuda): its host-timed cost_gpu per epoch (txn_executor through
+    txn_commit, cuda/src/gpulauncher.cu:1070-1099) on the same YCSB_A batch
+    re-sent every epoch, as its Scheduler does.  Its updates do not write and
+    it never aborts, so this is an ordering-only throughput: a reported
+    reference number, not this build's arm."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    if not os.path.exists(O.REF_CUDA):
+        print(json.dumps({"impl": "reference-cuda", "unavailable": "oracle/_ref/ltpmg_ref_cuda not built "
+                          "(the reference sources were never staged)"}), flush=True)
+        return
+    rows, n = 1 << 20, 1 << 16
+    q = uniform_distinct_rows(rows, n, 10, 0x4C54504D47)
+    tab = O.table_init(0x4C54504D47, rows, 3)
+    epochs = args.warmup + args.steps
+    out = O.ref_cuda_run(rows, q, tab.T, epochs=epochs, timeout=1200)
+    timed = out["cost_gpu"][args.warmup:]
+    sec = sum(timed) / len(timed)
+    line = {"metric": METRIC + " (reference CUDA path, ordering only)", "value": n / sec, "unit": "txn/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+            "higher_is_better": True, "impl": "reference-cuda", "data": "synthetic (seeded generator)",
+            "config": {"workload": WORKLOAD_TEXT["refcuda"], "timer": "the reference's own cost_gpu (host clock, "
+                       "stream synchronisations between its kernels)"},
+            "cost_gpu_s": out["cost_gpu"], "used_rows": out["used_rows"],
+            "ops_per_step": 10 * n}
+    print(json.dumps(line), flush=True)
+
+
 def run_gather(args):
     """Random-access ceiling of this GPU: uniformly random 4-byte gathers
     (torch indexing kernel, not this library) from a table of the Zipf
@@ -1083,13 +1166,15 @@ def main():
         if args.config in ("tpcc", "ycsbe"):
             run_reference_payload(args, args.config)
         else:
-            run_reference(args, "zipf" if args.config in ("serve", "gather") else args.config)
+            run_reference(args, "zipf" if args.config in ("serve", "gather", "refcuda") else args.config)
     elif args.config == "serve":
         run_serve(args)
     elif args.config in ("tpcc", "ycsbe"):
         run_payload(args, args.config)
     elif args.config == "gather":
         run_gather(args)
+    elif args.config == "refcuda":
+        run_refcuda(args)
     else:
         run_ours(args, args.config)
 

@@ -376,16 +376,6 @@ int ltp_ingest_results(ltp_ingest *g, uint8_t *committed, uint64_t *batch_seq, u
                        int64_t *vals);
 int ltp_ingest_close(ltp_ingest *g);
 
-/* ---- random-access ceilings ---------------------------------------------
- * The batch kernels touch random cells and conflict words, so random 4-byte
- * accesses -- not copy bandwidth -- bound them.  Measures independent random
- * accesses over a fresh array of `bytes` (4 KB .. 16 GB) on `device`:
- * loads, atomicOr with its result used, or atomicOr as a reduction. */
-#define LTP_PROBE_LOAD 0
-#define LTP_PROBE_ATOMIC 1
-#define LTP_PROBE_REDUCE 2
-int ltp_probe_random_access(int32_t device, uint64_t bytes, int32_t mode, double *accesses_per_s);
-
 /* ---- pinned host memory ------------------------------------------------ */
 void *ltp_host_alloc(size_t bytes);
 void ltp_host_free(void *p);
@@ -518,7 +508,13 @@ int ltp_debug_stall_next(ltp_ctx *ctx, uint32_t ms);
  * its start; calls that overlap on the GPU race, so serialise them.  The
  * call waits for its stream and returns the batch's status.  Semantics and
  * outputs equal ltp_batch_execute's for the same rule and inputs (reads and
- * read-modify-writes; the call takes no insert payload). */
+ * read-modify-writes; the call takes no insert payload).  txn_first (device
+ * memory, n_txns + 1 entries, or NULL for ops_per_txn ops per transaction)
+ * must start at 0, never decrease and end at n_ops: it is checked on the
+ * device, and a malformed one makes the call return LTP_E_BADARG with the
+ * table untouched.  rows_cap is at most 2^48.  The cached device address of
+ * the array goes stale after a cudaDeviceReset of its device: do not call
+ * this entry point on that device again in the same process. */
 #define LTP_NOALLOC_MAX_OPS (1ull << 18)
 #define LTP_NOALLOC_MAX_CELLS (1ull << 23)
 #define LTP_NOALLOC_SCRATCH_BYTES 16076288ull

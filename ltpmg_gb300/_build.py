@@ -20,7 +20,10 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "-I", os.path.join(ROOT, "include")]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I", os.path.join(ROOT, "include")]
 
-CU_SOURCES = ["ltp_kernels.cu", "ltp_api.cu", "ltp_noalloc.cu", "ltp_ingest.cu", "ltp_probe.cu"]
+CU_SOURCES = ["ltp_kernels.cu", "ltp_api.cu", "ltp_noalloc.cu", "ltp_ingest.cu"]
+# the benchmark's random-access probe: its own library, outside the product
+PROBE_SOURCE = "ltp_probe.cu"
+PROBE_LIB = os.path.join(PKG, "libltpmg_probe.so")
 CXX_SOURCES = ["ltp_gen.cpp", "ltp_compat.cpp", "ltp_serve.cpp", "ltp_tpcc.cpp"]
 
 
@@ -58,8 +61,14 @@ def build(verbose=False, extra_nvcc=(), debug_bounds=False):
         obj = os.path.join(build_dir, src + ".o")
         objs.append(obj)
         jobs.append(["g++"] + CXX_FLAGS + ["-I", cuda_inc, "-c", os.path.join(CSRC, src), "-o", obj])
+    probe_job = None
+    if not debug_bounds:
+        probe_job = [nvcc] + ARCH + NVCC_FLAGS + ["-shared", os.path.join(CSRC, PROBE_SOURCE), "-o", PROBE_LIB + ".tmp"]
+        jobs.append(probe_job)
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         outs = list(ex.map(_run, jobs))
+    if probe_job:
+        os.replace(PROBE_LIB + ".tmp", PROBE_LIB)
     if verbose:
         for o in outs:
             if o.strip():

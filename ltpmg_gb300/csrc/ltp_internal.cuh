@@ -161,6 +161,11 @@ bool tiling_supported(int block, int ipt, int word_bits);
 cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s);
 cudaError_t launch_fill_seeded(cudaStream_t st, const TableDev &t, u64 seed);
 cudaError_t launch_expand_op_txn(cudaStream_t st, const u32 *txn_first, u64 n_txns, u32 *op_txn);
+// The same for a txn_first the host has not checked: a malformed one sets
+// ctr->err = LTP_E_BADARG (the batch's kernels then do nothing) and no write
+// leaves op_txn[0, n_ops).
+cudaError_t launch_expand_op_txn_checked(cudaStream_t st, const u32 *txn_first, u64 n_txns, u64 n_ops, u32 *op_txn,
+                                         Counters *ctr);
 // Completes out64 after execution (ops on int32 cells write only out).
 cudaError_t launch_widen_out(cudaStream_t st, const BatchDev &b, const TablesDev &T);
 cudaError_t launch_set_u64(cudaStream_t st, u64 *dst, u64 value);

@@ -1596,6 +1596,19 @@ __global__ void k_expand_op_txn(const u32 *txn_first, u64 n_txns, u32 *op_txn) {
         for (u32 i = txn_first[t]; i < txn_first[t + 1]; i++) op_txn[i] = (u32)t;
 }
 
+// The same for a txn_first that only the device has seen (no host check):
+// it must start at 0, never decrease and end at n_ops.  A violation records
+// LTP_E_BADARG -- every later kernel of the batch then exits at its first
+// error check -- and no entry outside op_txn[0, n_ops) is written.
+__global__ void k_expand_op_txn_checked(const u32 *txn_first, u64 n_txns, u64 n_ops, u32 *op_txn, Counters *ctr) {
+    for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < n_txns; t += (u64)gridDim.x * blockDim.x) {
+        const u64 a = txn_first[t], e = txn_first[t + 1];
+        if ((t == 0 && a != 0) || e < a || (t + 1 == n_txns && e != n_ops)) set_err(ctr, LTP_E_BADARG);
+        const u64 hi = e < n_ops ? e : n_ops;
+        for (u64 i = a; i < hi; i++) op_txn[i] = (u32)t;
+    }
+}
+
 // ============================================================================
 // host-side launch plans
 // ============================================================================
@@ -1962,6 +1975,15 @@ cudaError_t launch_expand_op_txn(cudaStream_t st, const u32 *txn_first, u64 n_tx
     u64 blocks = (n_txns + 255) / 256;
     if (blocks > 4096) blocks = 4096;
     k_expand_op_txn<<<(unsigned)blocks, 256, 0, st>>>(txn_first, n_txns, op_txn);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_expand_op_txn_checked(cudaStream_t st, const u32 *txn_first, u64 n_txns, u64 n_ops, u32 *op_txn,
+                                         Counters *ctr) {
+    if (n_txns == 0) return cudaSuccess;
+    u64 blocks = (n_txns + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    k_expand_op_txn_checked<<<(unsigned)blocks, 256, 0, st>>>(txn_first, n_txns, n_ops, op_txn, ctr);
     return cudaGetLastError();
 }
 

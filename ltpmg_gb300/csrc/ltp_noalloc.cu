@@ -15,7 +15,10 @@
 // The array is shared by every call on a device and keeps the last call's
 // contents, so each call first clears what must start at zero.  Calls that
 // overlap on the GPU (two streams, or two host threads) race on it; callers
-// must serialise them.
+// must serialise them.  The array's device address is looked up once per
+// device and cached: after a cudaDeviceReset of that device the cached
+// address is stale, so the entry point must not be used on it again in the
+// same process.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -30,8 +33,11 @@ namespace {
 
 constexpr u64 kNaMaxOps = LTP_NOALLOC_MAX_OPS;
 constexpr u64 kNaMaxCells = LTP_NOALLOC_MAX_CELLS;
-constexpr u64 kNaWords = kNaMaxCells / 32 + 1;
+// n_words = cells / 32 + 1 at most, plus the spare entry the 64-cell layout
+// and the reset use (the allocating path allocates words + 1 as well)
+constexpr u64 kNaWords = kNaMaxCells / 32 + 2;
 constexpr u64 kNaTiles = kNaMaxOps / kMinTile + 2;
+constexpr u64 kNaMaxRowsCap = 1ull << 48;
 constexpr u64 kNaSortTiles = kNaMaxOps / kSortTile + 2;
 
 constexpr u64 align256(u64 x) { return (x + 255) & ~255ull; }
@@ -96,10 +102,14 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     if (rule != LTP_RULE_ORDERED && rule != LTP_RULE_PRIORITY) return LTP_E_BADARG;
     if (device < 0 || device >= kMaxDevices || !table || n_cols == 0 || n_cols > LTP_MAX_COLS || n_rows > rows_cap)
         return LTP_E_BADARG;
-    if (n_ops > kNaMaxOps || n_rows * n_cols > kNaMaxCells) return LTP_E_CAPACITY;
+    // column offsets are rows_cap * 4 * col bytes: keep them far from wrapping
+    if (rows_cap > kNaMaxRowsCap) return LTP_E_BADARG;
+    // n_rows * n_cols compared without forming a product that could wrap
+    if (n_ops > kNaMaxOps || n_rows > kNaMaxCells / n_cols) return LTP_E_CAPACITY;
     if (n_ops && (!keys || !opw || !out)) return LTP_E_BADARG;
     if (n_txns && !commit) return LTP_E_BADARG;
     if (!txn_first && (uint64_t)ops_per_txn * n_txns != n_ops) return LTP_E_BADARG;
+    if (txn_first && n_txns == 0 && n_ops != 0) return LTP_E_BADARG;  // ops that belong to no transaction
     if (cudaSetDevice(device) != cudaSuccess) return LTP_E_CUDA;
     unsigned char *base = nullptr;
     int sms = 0;
@@ -135,7 +145,9 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     u64 *rows_now = (u64 *)(base + kOffRows);
     if (e == cudaSuccess) e = launch_set_u64(st, rows_now, n_rows);
     if (e == cudaSuccess && n_txns) e = cudaMemsetAsync(commit, 1, n_txns, st);
-    if (e == cudaSuccess && txn_first && n_txns) e = launch_expand_op_txn(st, txn_first, n_txns, op_txn);
+    // txn_first lives in device memory the host never reads: checked there
+    if (e == cudaSuccess && txn_first && n_txns)
+        e = launch_expand_op_txn_checked(st, txn_first, n_txns, n_ops, op_txn, ctr);
     if (e != cudaSuccess) return LTP_E_CUDA;
 
     TablesDev T;

@@ -5,10 +5,27 @@
 // The probe runs one kernel of independent random accesses over an array of
 // the given size (a table-sized array lives in HBM, a conflict-word-sized
 // one in L2) and reports accesses per second.
+//
+// A measurement tool for the benchmark, not part of the product: it builds
+// into its own library (libltpmg_probe.so), outside libltpmg_gb300.so and
+// its C ABI.
+//
+//   int ltp_probe_random_access(int32_t device, uint64_t bytes, int32_t mode,
+//                               double *accesses_per_s);
+//
+// bytes: 4 KB .. 16 GB; mode 0 loads, 1 atomicOr with its result used,
+// 2 atomicOr as a reduction.  Returns 0, or a negative status as the
+// product's (-4 bad argument, -6 no memory, -1 CUDA error).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "../../include/ltpmg_gb300.h"
+#define LTP_PROBE_LOAD 0
+#define LTP_PROBE_ATOMIC 1
+#define LTP_PROBE_REDUCE 2
+#define LTP_OK 0
+#define LTP_E_CUDA (-1)
+#define LTP_E_BADARG (-4)
+#define LTP_E_NOMEM (-6)
 
 namespace {
 

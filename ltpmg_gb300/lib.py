@@ -173,7 +173,6 @@ def load():
         "ltp_serve_stats_now": (ci, [vp, ctypes.POINTER(ServeStats)]),
         "ltp_serve_close": (ci, [vp, ctypes.POINTER(ServeStats)]),
         "ltp_now_ns": (u64, []),
-        "ltp_probe_random_access": (ci, [i32, u64, i32, ctypes.POINTER(ctypes.c_double)]),
         "ltp_ingest_open": (ci, [vp, ctypes.POINTER(ServeConfig), u64, vp, vp, vp, vp, vp, pp]),
         "ltp_ingest_run": (ci, [vp, u64, vp, ctypes.POINTER(ServeStats)]),
         "ltp_ingest_results": (ci, [vp, vp, vp, vp, vp, vp]),
@@ -716,14 +715,24 @@ class Ingest:
 
 
 PROBE_LOAD, PROBE_ATOMIC, PROBE_REDUCE = 0, 1, 2
+PROBE_LIB_PATH = os.path.join(PKG, "libltpmg_probe.so")
+_probe = None
 
 
 def probe_random_access(device, nbytes, mode):
     """Random 4-byte accesses per second over an array of nbytes (mode:
-    PROBE_LOAD, PROBE_ATOMIC with result, PROBE_REDUCE)."""
-    L = load()
+    PROBE_LOAD, PROBE_ATOMIC with result, PROBE_REDUCE).  A benchmark tool in
+    its own library (libltpmg_probe.so), not part of the product's C ABI."""
+    global _probe
+    if _probe is None:
+        if not os.path.exists(PROBE_LIB_PATH):
+            raise LtpError(LTP_E_STATE, f"{PROBE_LIB_PATH} is not built")
+        _probe = ctypes.CDLL(PROBE_LIB_PATH)
+        _probe.ltp_probe_random_access.restype = ctypes.c_int
+        _probe.ltp_probe_random_access.argtypes = [ctypes.c_int32, ctypes.c_uint64, ctypes.c_int32,
+                                                   ctypes.POINTER(ctypes.c_double)]
     out = ctypes.c_double()
-    rc = L.ltp_probe_random_access(device, nbytes, mode, ctypes.byref(out))
+    rc = _probe.ltp_probe_random_access(device, nbytes, mode, ctypes.byref(out))
     if rc:
         raise LtpError(rc, "ltp_probe_random_access")
     return out.value

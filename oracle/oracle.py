@@ -28,11 +28,80 @@ def build(verbose=False):
     return LIB_PATH
 
 
+# where the reference tree is read from when LTPMG_REFERENCE is not set (the
+# recipe stages what it needs under oracle/_ref/src, which then travels with
+# the working tree to machines without the tree)
+REFERENCE_TREE = "/root/reference"
+REF_CUDA = os.path.join(HERE, "_ref", "ltpmg_ref_cuda")
+REF_GEN = os.path.join(HERE, "_ref", "ltpmg_ref_gen")
+
+
 def build_ref(verbose=False):
-    """Compile the reference's own generator code into oracle/_ref when the
-    reference tree is present (no-op elsewhere)."""
-    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True, capture_output=not verbose)
+    """Compile the reference's own code into oracle/_ref (build_ref.sh): from
+    the reference tree when it is present, else from a staged copy of it;
+    a no-op with neither."""
+    env = dict(os.environ)
+    if not env.get("LTPMG_REFERENCE") and os.path.isdir(REFERENCE_TREE):
+        env["LTPMG_REFERENCE"] = REFERENCE_TREE
+    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True, capture_output=not verbose, env=env)
     return REF_LIB_PATH if os.path.exists(REF_LIB_PATH) else None
+
+
+def ref_cuda_run(rows, row_ids, ints, epochs=1, workdir=None, timeout=600):
+    """Runs the reference's own CUDA path (oracle/_ref/ltpmg_ref_cuda, built
+    from its unchanged cuda/src) on one GPU: YCSB_A queries row_ids
+    uint32[n, 10] over a table whose int columns are ints int32[rows, 3].
+    Returns a dict: per-epoch cost_gpu, the op records (TID, type, table,
+    row) in the reference's record order, per-row op counts registered by
+    txn_executor (cnt) and scattered by txn_analyze_regular (tmp),
+    used-row count, type-list lengths and the int columns after the batch."""
+    import tempfile
+
+    row_ids = np.ascontiguousarray(row_ids, np.uint32)
+    ints = np.ascontiguousarray(ints, np.int32)
+    n = row_ids.shape[0]
+    assert row_ids.shape == (n, 10) and ints.shape == (rows, 3)
+    d = workdir or tempfile.mkdtemp(prefix="ltpref")
+    fin, fout = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
+    with open(fin, "wb") as f:
+        f.write(np.array([rows, n, epochs, 0], np.uint32).tobytes())
+        f.write(row_ids.tobytes())
+        f.write(ints.tobytes())
+    r = subprocess.run([REF_CUDA, fin, fout], capture_output=True, text=True, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference CUDA run failed ({r.returncode}): {r.stderr[-2000:]}")
+    raw = np.fromfile(fout, np.uint8)
+    off = 0
+
+    def take(dtype, count):
+        nonlocal off
+        a = raw[off:off + count * np.dtype(dtype).itemsize].view(dtype)
+        off += count * np.dtype(dtype).itemsize
+        return a
+
+    hdr = take(np.uint32, 6)
+    n_ops = int(hdr[1])
+    out = {"status": int(hdr[0]), "n_ops": n_ops, "used_rows": int(hdr[3]), "select_cur": int(hdr[4]),
+           "update_cur": int(hdr[5])}
+    out["cost_gpu"] = take(np.float32, epochs).astype(float).tolist()
+    out["rec"] = take(np.uint32, n_ops * 4).reshape(n_ops, 4)
+    out["cnt"] = take(np.uint32, rows)
+    out["tmp"] = take(np.uint32, rows)
+    out["ints_after"] = take(np.int32, rows * 3).reshape(rows, 3)
+    return out
+
+
+def ref_gen_time(benchmark, table_size, batch, dist, zipf, reps=1, timeout=900):
+    """Seconds per call of the reference's own host generator
+    (Query::generate_txn) on every hardware thread; parsed from
+    oracle/_ref/ltpmg_ref_gen's JSON line."""
+    import json
+
+    r = subprocess.run([REF_GEN, benchmark, str(table_size), str(batch), dist, str(zipf), str(reps)],
+                       capture_output=True, text=True, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference generator failed ({r.returncode}): {r.stderr[-2000:]}")
+    return json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
 
 
 class YcsbParams(ctypes.Structure):

@@ -60,9 +60,18 @@ def test_binding_constants_match_the_header():
     defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define LTP_(\w+)\s+\(?(-?\d+)u?\)?", hdr)}
     for name in ("SERVE_EAGER", "SERVE_KEEP_RESULTS", "SERVE_PERSISTENT", "SERVE_KEYS64", "SERVE_JIT",
                  "SERVE_MAX_OPS", "MODE_STREAM", "MODE_GRAPH", "MODE_PERSISTENT", "RULE_ORDERED", "RULE_PRIORITY",
-                 "OP_READ", "OP_ADD", "OP_INSERT", "FLAG_STAGE_TIMING", "TUNE_MARK_PRECHECK", "PROBE_LOAD",
-                 "PROBE_ATOMIC", "PROBE_REDUCE"):
+                 "OP_READ", "OP_ADD", "OP_INSERT", "FLAG_STAGE_TIMING", "TUNE_MARK_PRECHECK"):
         assert name in defs, name
         assert getattr(G.lib, name) == defs[name], name
     for name in ("E_BADARG", "E_CUDA", "E_CAPACITY", "E_TIMEOUT", "E_DEVICE_ASSERT", "E_NOMEM", "E_STATE"):
         assert getattr(G.lib, "LTP_" + name) == defs[name], name
+
+
+def test_probe_is_outside_the_product_library():
+    """The benchmark's random-access probe builds into its own library; the
+    product library exports no probe."""
+    out = subprocess.run(["nm", "-D", "--defined-only", G.lib.LIB_PATH], capture_output=True, text=True).stdout
+    assert "ltp_probe_random_access" not in out
+    assert os.path.exists(G.lib.PROBE_LIB_PATH)
+    out = subprocess.run(["nm", "-D", "--defined-only", G.lib.PROBE_LIB_PATH], capture_output=True, text=True).stdout
+    assert "ltp_probe_random_access" in out

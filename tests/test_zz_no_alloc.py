@@ -10,6 +10,8 @@ the first failure has already run every other test; it passes alone in a
 fresh process as well.
 """
 import ctypes
+import os
+import sys
 
 import numpy as np
 import pytest
@@ -20,6 +22,13 @@ from ltpmg_gb300 import lib as LB
 
 def _vp(t):
     return ctypes.c_void_p(t.data_ptr())
+
+
+def _oracle():
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+    import oracle
+
+    return oracle
 
 
 def _noalloc_call(L, torch, rule, table_t, rows, cols, tf, keys, opw, fixed):
@@ -64,10 +73,17 @@ def test_noalloc_matches_allocating_entry_point_twice(rule):
         ref_final = ctx.download(t)
 
     table_t = torch.from_numpy(tab0.copy()).to("cuda:0")  # [cols, rows] column-major, caller-owned
+    O = _oracle()
+    otab = tab0
     for ((tf, keys, opw), fixed), (rvals, rcommit) in zip(((b0, 16), (b1, 0)), ref):
         vals, commit = _noalloc_call(L, torch, rule, table_t, rows, cols, tf, keys, opw, fixed)
         assert np.array_equal(vals, rvals)
         assert np.array_equal(commit, rcommit)
+        # and directly against the oracle's serial replay of the same batch
+        otab, ocommit, oout = O.replay(rule, otab, tf, keys, opw)
+        assert np.array_equal(vals, oout)
+        assert np.array_equal(commit, ocommit)
+        assert np.array_equal(table_t.cpu().numpy(), otab)
     assert np.array_equal(table_t.cpu().numpy(), ref_final)
 
 
@@ -80,3 +96,61 @@ def test_noalloc_rejects_oversized_batches():
     rc = L.ltp_execute_noalloc(0, 0, ctypes.c_void_p(16), 1 << 22, 1 << 22, 4, 1, None, 4, 4,
                                ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_void_p(16), None)
     assert rc == LB.LTP_E_CAPACITY
+
+
+@pytest.mark.gpu
+def test_noalloc_rejects_malformed_txn_first_on_the_device():
+    """txn_first is device memory the host never reads, so the check runs on
+    the device: a start other than 0, a decreasing entry, or an end other
+    than n_ops makes the call return LTP_E_BADARG, leaves the table as it
+    was and writes nothing past the caller's buffers; a valid call after it
+    still runs correctly."""
+    torch = pytest.importorskip("torch")
+    L = G.load()
+    rows, cols, seed = 1 << 12, 4, 5
+    tf, keys, opw = G.gen_ycsb(seed, rows, cols, 1, 8, 0.5, 0.0, batch=0, n_txns=500)
+    n_txns, n_ops = len(tf) - 1, len(keys)
+    dev = torch.device("cuda:0")
+    with G.Context(device=0) as ctx:
+        t = ctx.create_table(rows, cols)
+        ctx.fill_seeded(t, seed)
+        tab0 = ctx.download(t)
+    table_t = torch.from_numpy(tab0.copy()).to(dev)
+    k_t = torch.from_numpy(keys.view(np.int64)).to(dev)
+    w_t = torch.from_numpy(opw.view(np.int32)).to(dev)
+    pad = 4096  # sentinel room after each output buffer
+    out_t = torch.full((n_ops + pad,), 0x5A5A5A5A, dtype=torch.int32, device=dev)
+    com_t = torch.full((n_txns + pad,), 0xA5, dtype=torch.uint8, device=dev)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def bad(mutate):
+        f = tf.copy()
+        mutate(f)
+        f_t = torch.from_numpy(f.view(np.int32)).to(dev)
+        return L.ltp_execute_noalloc(0, G.RULE_ORDERED, _vp(table_t), rows, rows, cols, n_txns, _vp(f_t), 0, n_ops,
+                                     _vp(k_t), _vp(w_t), _vp(out_t), _vp(com_t), stream)
+
+    def set_first(f):
+        f[0] = 1
+
+    def decrease(f):
+        f[n_txns // 2] = f[n_txns // 2 + 1] + 3
+
+    def short_end(f):
+        f[-1] = n_ops - 5
+
+    def long_end(f):
+        f[-1] = n_ops + 1000
+
+    for mutate in (set_first, decrease, short_end, long_end):
+        assert bad(mutate) == LB.LTP_E_BADARG, mutate.__name__
+        assert np.array_equal(table_t.cpu().numpy(), tab0), mutate.__name__
+        assert (out_t[n_ops:].cpu().numpy() == 0x5A5A5A5A).all(), mutate.__name__
+        assert (com_t[n_txns:].cpu().numpy() == 0xA5).all(), mutate.__name__
+    # the array recovers: a valid call equals the oracle's serial replay
+    O = _oracle()
+    vals, commit = _noalloc_call(L, torch, G.RULE_ORDERED, table_t, rows, cols, tf, keys, opw, 0)
+    ref_tab, ref_commit, ref_out = O.replay(0, tab0, tf, keys, opw)
+    assert np.array_equal(vals, ref_out)
+    assert np.array_equal(commit, ref_commit)
+    assert np.array_equal(table_t.cpu().numpy(), ref_tab)
