@@ -491,6 +491,13 @@ def run_ours(args, config):
                            "contended_cells_per_batch": mean_stats["contended_cells"]}}
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(config, host)
+    if config == "zipf" and world == 1 and not args.no_serving:
+        # the serving half of the metric (p50/p99/p99.9 and serving vs the
+        # plain path), after the headline measurement, on a fresh context
+        for b in dev:
+            b.free()
+        ctx.close()
+        line["serving"] = serving_measure(args, local, rank, point_s=0.5)
     print(json.dumps(line), flush=True)
 
 
@@ -866,19 +873,30 @@ def run_reference_payload(args, config):
     print(json.dumps(line), flush=True)
 
 
-def run_serve(args):
-    """Offered-load sweep of the serving loop over a seeded 50/50 blend of
-    Zipf 0.99 YCSB transactions and TPC-C-shaped order-entry transactions on
-    device-resident tables of both shapes; value = the highest committed
-    txn/s among the loads served at p99 <= 2 ms."""
+def serving_measure(args, local, rank, point_s):
+    """The serving half of the metric, on one GPU.  Two request pools over
+    device-resident tables: the Zipf 0.99 YCSB transactions of the headline
+    workload (batch 0, 2^20 transactions x 16 ops, 2^24 x 10 int32 table)
+    and the seeded 50/50 blend of 2^18 of those with 2^18 TPC-C-shaped
+    order-entry transactions (W=64, nine tables, inserts).  Per pool:
+      - the plain batch path on the same tables: the whole pool as one batch,
+        executed back to back;
+      - the device-resident request log (ltp_ingest: requests in HBM, merged
+        Poisson arrivals of the client streams admitted by the clock, 250 us
+        deadline, 4 GB read/write-set budget, aborts re-queued) swept over
+        offered loads, each point at least point_s seconds of arrivals;
+    and for the blend the host submission API (ltp_serve: 256 client
+    streams submitting from 8 load-generator threads) swept over
+    args.loads.  Per point: p50/p99/p99.9 latency (arrival -> result) and
+    committed txn/s; per pool: the best committed txn/s at p99 <= 2 ms and
+    its ratio to the plain path.  Before each sweep the serving size buckets
+    are autotuned (untimed)."""
     import numpy as np
-    import torch
 
     import ltpmg_gb300 as G
+    from ltpmg_gb300 import autotune as AT
     from ltpmg_gb300 import workloads as W
 
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
     sh = W.SHAPES["zipf"]
     n_each = 1 << 18
     tf, keys, opw, n, _ = W.generate("zipf", 0, rank=rank)
@@ -892,14 +910,15 @@ def run_serve(args):
         """Keys as 32-bit keys when they fit: the request log stores them so."""
         return k.astype(np.uint32) if len(k) and int(k.max()) < (1 << 32) else k
 
-    loads = [float(x) * 1e6 for x in args.loads.split(",")]
-    t_loads = [max(0.3, min(2.0, 20e6 / r)) for r in loads]
-    ingest_loads = [float(x) * 1e6 for x in args.ingest_loads.split(",")] if args.ingest_loads else []
-    ingest_n = [int(r * max(0.1, min(1.0, 40e6 / r))) for r in ingest_loads]
-    # insert-table room for the most transactions one sweep point (or the
-    # plain-path comparison) can run; the tables are truncated between points
+    host_loads = [float(x) * 1e6 for x in args.loads.split(",")] if args.loads else []
+    blend_loads = [float(x) * 1e6 for x in args.ingest_loads.split(",")] if args.ingest_loads else []
+    ycsb_loads = [float(x) * 1e6 for x in args.ycsb_loads.split(",")] if args.ycsb_loads else []
+    t_host = [max(point_s, min(2.0, 20e6 / r)) for r in host_loads]
+    # insert-table room for the most transactions one point can run; the
+    # insert tables are truncated between points
     per_txn = np.asarray(t_ins, np.float64) / (2 * n_each)
-    most = max(max(r * t for r, t in zip(loads, t_loads)), 13 * n_pool, max(ingest_n, default=0)) * 1.25 + n_pool
+    most = max([r * t for r, t in zip(host_loads, t_host)] + [r * point_s for r in blend_loads] +
+               [13 * n_pool]) * 1.25 + n_pool
     ctx = G.Context(device=local)
     t = ctx.create_table(sh["rows"], sh["cols"])
     ctx.fill_seeded(t, sh["seed"] + rank)
@@ -910,60 +929,36 @@ def run_serve(args):
         for tid, r in base_rows.items():
             ctx.truncate(tid, r)
 
-    # the plain batch path on the same GPU and the same blend: the whole pool
-    # as one batch, executed back to back
-    b = ctx.batch(n_pool, len(pk))
-    b.load(ptf, k32(pk), pw)
-    b.load_payload(ppay)
-    for _ in range(3):
-        b.execute()
-    ctx.sync()
-    t0 = time.perf_counter()
-    for _ in range(10):
-        b.execute()
-    ctx.sync()
-    plain = 10 * n_pool / (time.perf_counter() - t0)
-    b.finish()
-    del b
-    truncate()
-    # one short untimed load first: allocations and first-touch of the
-    # server's host buffers happen here, not in the first sweep point
-    srv = G.Server(ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 18, max_ops=1 << 22,
-                   keep_results=False, persistent=args.serve_mode == "persistent")
-    srv.loadgen(1e6, 0.1, 256, ptf, pk, pw, seed=1, threads=8, pay_first=ppf, payload=ppay)
-    srv.close()
-    truncate()
-    sweep = []
-    for rate, t_load in zip(loads, t_loads):
-        srv = G.Server(ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 18, max_ops=1 << 22,
-                       keep_results=False, persistent=args.serve_mode == "persistent")
-        # eight load-generator threads (half the host cores of the GPU
-        # machine): more of them busy-wait the dispatcher and completer off
-        # their cores
-        srv.loadgen(rate, t_load, 256, ptf, pk, pw, seed=int(rate), threads=args.loadgen_threads, pay_first=ppf,
-                    payload=ppay)
-        st = srv.close()
+    def plain_rate(tf_, k_, w_, pay_=None, reps=10):
+        """The plain batch path on the same tables: the pool as one batch."""
+        b = ctx.batch(len(tf_) - 1, len(k_))
+        b.load(tf_, k32(k_), w_)
+        if pay_ is not None:
+            b.load_payload(pay_)
+        for _ in range(3):
+            b.execute()
+        ctx.sync()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            b.execute()
+        ctx.sync()
+        r = reps * (len(tf_) - 1) / (time.perf_counter() - t0)
+        b.finish()
+        del b
         truncate()
-        st["offered_txn_per_s"] = rate
-        st["load_seconds"] = t_load
-        st["committed_per_s_offered_window"] = st["committed"] / max(st["elapsed_s"], 1e-9)
-        sweep.append({k: (round(v, 3) if isinstance(v, float) else v) for k, v in st.items()})
-    # serving from a device-resident request log: the same pool, requests
-    # already in HBM (as a NIC writing by GPUDirect RDMA places them), the 256
-    # streams' merged Poisson arrivals admitted by the clock
+        return r
+
     def tune_for(tf_, k_, w_, pf_, pay_):
         """Autotunes the size buckets serving batches fall into, on leading
         slices of the pool (untimed; the tables are truncated after)."""
-        from ltpmg_gb300 import autotune as AT
-
         chosen = {}
-        for n in (1 << 12, 1 << 14, 1 << 16, 1 << 18):
-            n = min(n, len(tf_) - 1)
-            a, e = int(tf_[0]), int(tf_[n])
-            bt = ctx.batch(n, e - a)
-            bt.load((tf_[:n + 1] - tf_[0]).astype(np.uint32), k32(k_[a:e]), w_[a:e])
+        for m in (1 << 12, 1 << 14, 1 << 16, 1 << 18):
+            m = min(m, len(tf_) - 1)
+            a, e = int(tf_[0]), int(tf_[m])
+            bt = ctx.batch(m, e - a)
+            bt.load((tf_[:m + 1] - tf_[0]).astype(np.uint32), k32(k_[a:e]), w_[a:e])
             if pf_ is not None:
-                bt.load_payload(pay_[int(pf_[0]):int(pf_[n])])
+                bt.load_payload(pay_[int(pf_[0]):int(pf_[m])])
             ch = AT.tune_tiles(ctx, bt, reps=2)
             chosen[ch["bucket"]] = f"{ch['block']}x{ch['ipt']}" + ("w64" if ch["word_bits"] == 64 else "") + \
                 ("+precheck" if ch["flags"] else "")
@@ -972,77 +967,105 @@ def run_serve(args):
             truncate()
         return chosen
 
-    ingest_sweep, tuned = [], {}
-    if ingest_loads:
-        tuned["blend"] = tune_for(ptf, pk, pw, ppf, ppay)
-        # two batches in flight: one executing, one queued behind it (a third
-        # only queues a deadline-closed batch longer)
-        ing = G.Ingest(ctx, ptf, pk, pw, ppf, ppay, deadline_us=250, depth=2, budget_bytes=4 << 30,
-                       max_txns=1 << 20, max_ops=1 << 24, eager=True, jit=bool(args.ingest_jit))
-        rng = np.random.default_rng(sh["seed"] + 17 + rank)
-        ing.run(np.cumsum(rng.exponential(1e9 / 20e6, 1 << 20)).astype(np.uint64))  # untimed warm-up
+    def point(st, rate, requests=None):
+        st["offered_txn_per_s"] = rate
+        if requests is not None:
+            st["requests"] = requests
+        st["committed_per_s"] = st["committed"] / max(st["elapsed_s"], 1e-9)
+        return {k: (round(v, 3) if isinstance(v, float) else v) for k, v in st.items()}
+
+    def ingest_sweep(ing, loads, seed):
+        out = []
+        ing.run(G.lib.poisson_arrivals(1 << 20, 20e6, seed))  # untimed warm-up
         truncate()
-        for rate, n in zip(ingest_loads, ingest_n):
-            arr = np.cumsum(rng.exponential(1e9 / rate, n)).astype(np.uint64)
-            st = ing.run(arr)
+        for i, rate in enumerate(loads):
+            m = int(rate * point_s)
+            st = ing.run(G.lib.poisson_arrivals(m, rate, seed + 1 + i))
             truncate()
-            st["offered_txn_per_s"] = rate
-            st["requests"] = n
-            st["committed_per_s_offered_window"] = st["committed"] / max(st["elapsed_s"], 1e-9)
-            ingest_sweep.append({k: (round(v, 3) if isinstance(v, float) else v) for k, v in st.items()})
-        ing.close()
-    # the same request-log loop on the Zipf 0.99 YCSB transactions alone,
-    # beside the plain batch path on the same 2^20-transaction pool
-    ycsb_sweep, plain_ycsb = [], None
-    if args.ycsb_loads:
+            out.append(point(st, rate, m))
+        return out
+
+    def best_of(sweep):
+        ok = [p for p in sweep if p["p99_us"] <= 2000.0]
+        return max(ok, key=lambda p: p["committed_per_s"]) if ok else None
+
+    def summary(sweep, plain):
+        b = best_of(sweep)
+        return {"committed_txn_per_s_at_p99_le_2ms": b["committed_per_s"] if b else 0.0,
+                "p50_us": b["p50_us"] if b else None, "p99_us": b["p99_us"] if b else None,
+                "p999_us": b["p999_us"] if b else None,
+                "offered_txn_per_s": b["offered_txn_per_s"] if b else None,
+                "plain_batch_txn_per_s": plain,
+                "serving_over_plain": (b["committed_per_s"] / plain) if (b and plain) else 0.0}
+
+    out = {"point_seconds": point_s, "p99_bound_us": 2000.0, "deadline_us": 250, "budget_bytes": 4 << 30,
+           "client_streams": 256}
+    t_start = time.perf_counter()
+    # 1. Zipf YCSB alone, request log
+    if ycsb_loads:
         ny = 1 << 20
         ytf, yk, yw = tf[:ny + 1], keys[:int(tf[ny])], opw[:int(tf[ny])]
-        by = ctx.batch(ny, len(yk))
-        by.load(ytf, k32(yk), yw)
-        for _ in range(3):
-            by.execute()
-        ctx.sync()
-        t0 = time.perf_counter()
-        for _ in range(10):
-            by.execute()
-        ctx.sync()
-        plain_ycsb = 10 * ny / (time.perf_counter() - t0)
-        by.finish()
-        del by
-        tuned["ycsb"] = tune_for(ytf, yk, yw, None, None)
+        plain_y = plain_rate(ytf, yk, yw)
+        tuning_y = tune_for(ytf, yk, yw, None, None)
         ing = G.Ingest(ctx, ytf, yk, yw, deadline_us=250, depth=2, budget_bytes=4 << 30, max_txns=1 << 20,
                        max_ops=1 << 24, eager=True, jit=bool(args.ingest_jit))
-        rng = np.random.default_rng(sh["seed"] + 29 + rank)
-        ing.run(np.cumsum(rng.exponential(1e9 / 50e6, 1 << 20)).astype(np.uint64))  # untimed warm-up
-        for rate in [float(x) * 1e6 for x in args.ycsb_loads.split(",")]:
-            n = int(rate * max(0.1, min(1.0, 40e6 / rate)))
-            st = ing.run(np.cumsum(rng.exponential(1e9 / rate, n)).astype(np.uint64))
-            st["offered_txn_per_s"] = rate
-            st["requests"] = n
-            st["committed_per_s_offered_window"] = st["committed"] / max(st["elapsed_s"], 1e-9)
-            ycsb_sweep.append({k: (round(v, 3) if isinstance(v, float) else v) for k, v in st.items()})
+        sw = ingest_sweep(ing, ycsb_loads, sh["seed"] + 29 + rank)
         ing.close()
-    ok_host = [p for p in sweep if p["p99_us"] <= 2000.0]
-    ok_ing = [p for p in ingest_sweep if p["p99_us"] <= 2000.0]
-    ok = ok_ing or ok_host
-    best = max(ok, key=lambda p: p["committed_per_s_offered_window"]) if ok else None
-    value = best["committed_per_s_offered_window"] if best else 0.0
-    best_host = max(ok_host, key=lambda p: p["committed_per_s_offered_window"]) if ok_host else None
-    line = {"metric": METRIC, "value": value, "unit": "txn/s", "n_gpus": world, "steps": len(loads),
-            "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "int32/int64", "data": "synthetic (seeded generator)",
+        out["ycsb_request_log"] = dict(summary(sw, plain_y), sweep=sw, tuning=tuning_y,
+                                       pool_txns=ny, workload="zipf0.99 YCSB, 16 ops, 80/20")
+    # 2. the 50/50 blend, request log
+    plain_b = plain_rate(ptf, pk, pw, ppay)
+    if blend_loads:
+        tuning_b = tune_for(ptf, pk, pw, ppf, ppay)
+        ing = G.Ingest(ctx, ptf, pk, pw, ppf, ppay, deadline_us=250, depth=2, budget_bytes=4 << 30,
+                       max_txns=1 << 20, max_ops=1 << 24, eager=True, jit=bool(args.ingest_jit))
+        sw = ingest_sweep(ing, blend_loads, sh["seed"] + 17 + rank)
+        ing.close()
+        out["blend_request_log"] = dict(summary(sw, plain_b), sweep=sw, tuning=tuning_b, pool_txns=n_pool,
+                                        workload="50/50 zipf0.99 YCSB + tpcc-shaped new-order/payment")
+    # 3. the blend through the host submission API
+    if host_loads:
+        srv = G.Server(ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 18, max_ops=1 << 22,
+                       keep_results=False, persistent=args.serve_mode == "persistent")
+        srv.loadgen(1e6, 0.1, 256, ptf, pk, pw, seed=1, threads=8, pay_first=ppf, payload=ppay)  # untimed
+        srv.close()
+        truncate()
+        sw = []
+        for rate, t_load in zip(host_loads, t_host):
+            srv = G.Server(ctx, deadline_us=250, depth=3, budget_bytes=4 << 30, max_txns=1 << 18,
+                           max_ops=1 << 22, keep_results=False, persistent=args.serve_mode == "persistent")
+            # eight load-generator threads (half the host cores of the GPU
+            # machine): more busy-wait the dispatcher and completer off their cores
+            srv.loadgen(rate, t_load, 256, ptf, pk, pw, seed=int(rate), threads=args.loadgen_threads,
+                        pay_first=ppf, payload=ppay)
+            st = srv.close()
+            truncate()
+            st["load_seconds"] = t_load
+            sw.append(point(st, rate))
+        out["blend_host_api"] = dict(summary(sw, plain_b), sweep=sw, pool_txns=n_pool,
+                                     loadgen_threads=args.loadgen_threads)
+    out["seconds"] = round(time.perf_counter() - t_start, 1)
+    ctx.close()
+    return out
+
+
+def run_serve(args):
+    """The serving sweeps alone (longer points than the default line's);
+    value = the highest committed txn/s at p99 <= 2 ms over the blend's
+    request-log and host-API sweeps."""
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    sv = serving_measure(args, local, rank, point_s=args.serve_point_s)
+    cands = [sv[k] for k in ("blend_request_log", "blend_host_api") if k in sv]
+    best = max(cands, key=lambda d: d["committed_txn_per_s_at_p99_le_2ms"]) if cands else None
+    line = {"metric": METRIC, "value": best["committed_txn_per_s_at_p99_le_2ms"] if best else 0.0, "unit": "txn/s",
+            "n_gpus": world, "steps": 1, "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64", "data": "synthetic (seeded generator)",
             "config": {"workload": WORKLOAD_TEXT["serve"], "selection": "highest committed txn/s with p99 <= 2 ms",
-                       "pool_txns": n_pool, "batch_execution": args.serve_mode,
-                       "request_log": {"keys": "32-bit", "just_in_time_queueing": bool(args.ingest_jit),
-                                       "batches_in_flight": 2},
-                       "value_from": "device-resident request log" if ok_ing else "host submission API",
-                       "tuning": tuned},
-            "serving": {"sweep": sweep, "ingest_sweep": ingest_sweep, "plain_batch_txn_per_s": plain,
-                        "ycsb_ingest_sweep": ycsb_sweep, "plain_ycsb_batch_txn_per_s": plain_ycsb,
-                        "best_host_submit_txn_per_s": best_host["committed_per_s_offered_window"] if best_host else 0.0,
-                        "best_p50_us": best["p50_us"] if best else None,
-                        "best_p99_us": best["p99_us"] if best else None,
-                        "best_p999_us": best["p999_us"] if best else None}}
+                       "batch_execution": args.serve_mode},
+            "serving": sv}
     print(json.dumps(line), flush=True)
 
 
@@ -1150,12 +1173,14 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     ap.add_argument("--loadgen-threads", type=int, default=8, help="serving sweep: load-generator threads")
-    ap.add_argument("--ycsb-loads", default="600,700,750,800,825,850",
+    ap.add_argument("--ycsb-loads", default="700,800,850,900",
                     help="request-log serving of the Zipf YCSB transactions alone: offered loads in M txn/s")
     ap.add_argument("--ingest-jit", type=int, default=1,
                     help="serve: request log queues a batch only once the one ahead is past its sort (1) or at once (0)")
-    ap.add_argument("--ingest-loads", default="200,250,300,325,350,375",
+    ap.add_argument("--ingest-loads", default="250,300,350,375",
                     help="serving from a device-resident request log: offered loads in M txn/s ('' = skip)")
+    ap.add_argument("--serve-point-s", type=float, default=1.0, help="serve: seconds of arrivals per sweep point")
+    ap.add_argument("--no-serving", action="store_true", help="default workload: skip the serving section")
     ap.add_argument("--serve-mode", default="persistent", choices=["persistent", "stream"],
                     help="serving: each batch as one persistent-kernel launch, or as a kernel sequence")
     args = ap.parse_args()

@@ -338,6 +338,12 @@ int ltp_serve_stats_now(ltp_server *s, ltp_serve_stats *st);
 int ltp_serve_close(ltp_server *s, ltp_serve_stats *st);
 /* Current CLOCK_MONOTONIC time in ns (the clock arrivals are stamped with). */
 uint64_t ltp_now_ns(void);
+/* Arrival times (ns after the start, non-decreasing) of n requests of an
+ * open-loop Poisson process at `rate` requests/s -- the merged arrivals of
+ * any number of independent Poisson client streams whose rates sum to
+ * `rate` -- drawn from `seed` on n_threads threads (<= 0: all hardware
+ * threads); for ltp_ingest_run. */
+int ltp_poisson_arrivals(uint64_t n, double rate, uint64_t seed, uint64_t *arrival_ns, int n_threads);
 
 /* ---- serving from a device-resident request log --------------------------
  * Requests are already in HBM when they arrive -- the way a NIC writing by

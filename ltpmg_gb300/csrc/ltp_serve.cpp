@@ -696,6 +696,42 @@ int ltp_serve_loadgen_rows(ltp_server *s, double rate, double seconds, uint32_t 
     return s->status;
 }
 
+int ltp_poisson_arrivals(uint64_t n, double rate, uint64_t seed, uint64_t *arrival_ns, int n_threads) {
+    if (!arrival_ns || !(rate > 0)) return n ? LTP_E_BADARG : LTP_OK;
+    if (n_threads <= 0) n_threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    const uint64_t chunks = std::min<uint64_t>((uint64_t)n_threads, std::max<uint64_t>(1, n / 65536));
+    const double mean_gap_ns = 1e9 / rate;
+    // each chunk draws its own gaps (its own seeded stream) and sums them;
+    // the chunks' totals then shift every later chunk
+    std::vector<double> total(chunks, 0.0);
+    auto body = [&](uint64_t c, bool shift, double base) {
+        const uint64_t lo = n * c / chunks, hi = n * (c + 1) / chunks;
+        if (shift) {
+            for (uint64_t i = lo; i < hi; i++) arrival_ns[i] += (uint64_t)base;
+            return;
+        }
+        std::mt19937_64 rng(seed * 0x9E3779B97F4A7C15ULL + c * 0xD1B54A32D192ED03ULL + 1);
+        std::exponential_distribution<double> gap(1.0 / mean_gap_ns);
+        double t = 0.0;
+        for (uint64_t i = lo; i < hi; i++) {
+            t += gap(rng);
+            arrival_ns[i] = (uint64_t)t;
+        }
+        total[c] = t;
+    };
+    std::vector<std::thread> th;
+    for (uint64_t c = 0; c < chunks; c++) th.emplace_back(body, c, false, 0.0);
+    for (auto &x : th) x.join();
+    th.clear();
+    double base = 0.0;
+    for (uint64_t c = 1; c < chunks; c++) {
+        base += total[c - 1];
+        th.emplace_back(body, c, true, base);
+    }
+    for (auto &x : th) x.join();
+    return LTP_OK;
+}
+
 int ltp_serve_stats_now(ltp_server *s, ltp_serve_stats *st) {
     if (!s || !st) return LTP_E_BADARG;
     memset(st, 0, sizeof(*st));

@@ -173,6 +173,7 @@ def load():
         "ltp_serve_stats_now": (ci, [vp, ctypes.POINTER(ServeStats)]),
         "ltp_serve_close": (ci, [vp, ctypes.POINTER(ServeStats)]),
         "ltp_now_ns": (u64, []),
+        "ltp_poisson_arrivals": (ci, [u64, ctypes.c_double, u64, vp, ctypes.c_int]),
         "ltp_ingest_open": (ci, [vp, ctypes.POINTER(ServeConfig), u64, vp, vp, vp, vp, vp, pp]),
         "ltp_ingest_run": (ci, [vp, u64, vp, ctypes.POINTER(ServeStats)]),
         "ltp_ingest_results": (ci, [vp, vp, vp, vp, vp, vp]),
@@ -712,6 +713,18 @@ class Ingest:
             rc = self.ctx.L.ltp_ingest_close(self.h)
             self.h = None
             self.ctx.check(rc)
+
+
+def poisson_arrivals(n, rate, seed, threads=0):
+    """uint64[n] arrival times (ns after the start) of an open-loop Poisson
+    process at `rate` requests/s (the merged arrivals of independent Poisson
+    client streams), for Ingest.run."""
+    L = load()
+    out = np.empty(max(int(n), 1), np.uint64)
+    rc = L.ltp_poisson_arrivals(int(n), float(rate), int(seed), _p(out), int(threads))
+    if rc:
+        raise LtpError(rc, "ltp_poisson_arrivals")
+    return out[:int(n)]
 
 
 PROBE_LOAD, PROBE_ATOMIC, PROBE_REDUCE = 0, 1, 2
