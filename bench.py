@@ -227,8 +227,44 @@ def cpu_baseline(config, host, budget_s=12.0):
         done_txns += n
         if t_used >= budget_s:
             break
-    return {"value": done_txns / t_used, "unit": "txn/s", "cores": 1, "kind": "port",
-            "sample": f"{done} whole batch(es), {done_txns} txns, serial replay (ordered rule), {t_used:.1f} s"}
+    out = {"value": done_txns / t_used, "unit": "txn/s", "cores": 1, "kind": "port",
+           "sample": f"{done} whole batch(es), {done_txns} txns, serial replay (ordered rule), {t_used:.1f} s"}
+    gen = reference_generator_rate(config)
+    if gen and "value" in gen:
+        # (i) the reference's own generator/scheduler path, then (i)+(ii):
+        # generating a transaction and replaying it, back to back
+        out["generator"] = gen
+        out["generator_plus_replay"] = {"value": 1.0 / (1.0 / gen["value"] + 1.0 / out["value"]), "unit": "txn/s",
+                                        "cores": f"{gen['cores']} (generator) + 1 (replay)"}
+    elif gen:
+        out["generator"] = gen
+    return out
+
+
+def reference_generator_rate(config):
+    """The reference's own host generator (Txn_Generator + Query::generate_txn,
+    src/txn_generator.cpp:601-673, src/query.cpp:270-311) timed on this
+    machine's host cores with hardware_concurrency() threads, as the reference
+    runs it, at its closest settings to the workload (YCSB_A; its "zipf" is a
+    100-rank truncated law, src/random.cpp:105-161); None when it was not
+    built here."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    if not os.path.exists(O.REF_GEN):
+        return None
+    settings = {"zipf": ("YCSB_A", 16, 1 << 18, "zipf", 0.99), "uneven": ("YCSB_A", 16, 1 << 18, "zipf", 0.75),
+                "plain": ("YCSB_A", 1, 1 << 16, "unif", 0.0)}.get(config)
+    if settings is None:
+        return None
+    try:
+        r = O.ref_gen_time(*settings, reps=2)
+    except Exception as e:  # reported, not fatal: the baseline is informational
+        return {"unavailable": str(e)[:200]}
+    sec = min(r["seconds"])
+    return {"value": r["txns"] / sec, "unit": "txn/s", "cores": r["threads"], "kind": "reference",
+            "sample": f"{r['benchmark']} {r['txns']} txns over {r['rows']} rows, {r['distribution']} "
+                      f"{r['zipf_config']}: Query::generate_txn, best of {len(r['seconds'])} calls ({sec:.3f} s)"}
 
 
 def oracle_batches(config, nb, seed=None):

@@ -22,6 +22,26 @@
  *  - YCSB_E's 9 scans of rows [r, r+2) read those rows; its insert appends a
  *    row whose int columns are the query's ROW_ID[9] (the reference's insert
  *    operator is also an identity on an existing row);
+ *  - TPC-C (TPCC_PART / TPCC_ALL; Neworder_Query and Payment_Query): the
+ *    row operations of parse<Neworder_Query> / parse<Payment_Query>
+ *    (cuda/src/gpuquery.cu:2474-2734), on the tables in data/TPCC.json order
+ *    (0 warehouse, 1 district, 2 customer, 3 new-order, 4 history, 5 order,
+ *    6 order-line, 7 stock, 8 item), each row taken modulo its table's rows
+ *    as the reference's register_cc does (cuda/src/gpulauncher.cu:400):
+ *    new-order reads warehouse W_ID, district W_ID*10+D_ID, customer
+ *    (W_ID*10+D_ID)*3000+C_ID, inserts a new-order and an order row, and per
+ *    line inserts an order-line row and updates stock
+ *    OL_SUPPLY_W_ID*1000000+OL_I_ID twice; payment reads warehouse,
+ *    district and the customer (by last name: the first of the district's
+ *    3000 customers whose index entry equals C_LAST, :2641-2650), updates the
+ *    customer, the warehouse and the district and inserts a history row.
+ *    Selects and updates act on every int column as for YCSB.  An insert
+ *    appends a row (the reference writes a preallocated row that its insert
+ *    operator leaves unchanged) whose int columns hold the ids the query
+ *    names, in the schema's int-column order: new-order (N_O_ID, D_ID, W_ID);
+ *    order (O_ID, D_ID, W_ID, C_ID, 0, O_OL_CNT, all lines local);
+ *    order-line (O_ID, D_ID, W_ID, line number, OL_I_ID, OL_SUPPLY_W_ID, 0,
+ *    OL_QUANTITY); history (C_ID, C_D_ID, C_W_ID, D_ID, W_ID);
  *  - double and string columns stay on the host: this library stores int32
  *    columns only, and no reference operation changes the others.
  */
@@ -71,6 +91,36 @@ struct YCSB_B_Query { uint32_t TID; uint32_t ROW_ID[10]; };
 struct YCSB_C_Query { uint32_t TID; uint32_t ROW_ID[10]; };
 struct YCSB_D_Query { uint32_t TID; uint32_t ROW_ID[10]; };
 struct YCSB_E_Query { uint32_t TID; uint32_t ROW_ID[10]; };
+
+struct Neworder_Query {
+    uint32_t TID;
+    uint32_t W_ID;
+    uint32_t D_ID;
+    uint32_t C_ID;
+    uint32_t O_ID;
+    uint32_t N_O_ID;
+    uint32_t O_OL_CNT;
+    uint32_t O_OL_ID;
+    struct Info {
+        uint32_t OL_I_ID;
+        uint32_t OL_SUPPLY_W_ID;
+        uint32_t OL_QUANTITY;
+    };
+    Info INFO[15];
+};
+
+struct Payment_Query {
+    uint32_t TID;
+    uint32_t W_ID;
+    uint32_t D_ID;
+    uint32_t C_ID;
+    uint32_t C_LAST;
+    uint32_t isName; /* 0: by C_ID, 1: by C_LAST through the customer index */
+    uint32_t C_D_ID;
+    uint32_t C_W_ID;
+    uint32_t H_AMOUNT;
+    uint32_t H_ID;
+};
 
 /* include/param.h: data members in the reference's order */
 struct Result {

@@ -119,3 +119,113 @@ def test_reference_host_program_links_against_the_library():
         assert sym in und, sym
     deps = subprocess.run(["ldd", REF_HOST], capture_output=True, text=True).stdout
     assert "libltpmg_gb300.so" in deps and "not found" not in deps
+
+
+TPCC_INT_COLS = [1, 3, 5, 3, 5, 7, 8, 5, 2]  # int attributes of data/TPCC.json's nine tables
+
+
+def expand_tpcc(flat, cidx, rows):
+    """The compat layer's expansion of TPC-C queries (the row operations of
+    parse<Neworder_Query> / parse<Payment_Query>, cuda/src/gpuquery.cu:2474-2734,
+    on every int column; rows modulo the table's rows; inserts append the ids
+    the query names)."""
+    tf, keys, opw, payload = [0], [], [], []
+
+    def row_op(kind, t, row, vals=()):
+        cols = TPCC_INT_COLS[t]
+        if kind == 1:
+            keys.append(len(payload))
+            opw.append(O.opword(2, 0, t, 0))
+            payload.extend([int(v) for v in vals] + [0] * (cols - len(vals)))
+            return
+        r = row % rows[t]
+        for c in range(cols):
+            keys.append(r)
+            opw.append(O.opword(1, c, t, 1) if kind == 2 else O.opword(0, c, t, 0))
+
+    i = 0
+    while i < len(flat):
+        kind = int(flat[i])
+        if kind == 0:
+            q = [int(x) for x in flat[i + 1:i + 54]]
+            i += 54
+            tid, w, d, c, o_id, n_o_id, ol_cnt, _ = q[:8]
+            info = [q[8 + 3 * k:11 + 3 * k] for k in range(15)]
+            wd = w * 10 + d
+            lines = min(ol_cnt, 15)
+            local = all(info[k][1] == w for k in range(lines))
+            row_op(0, 0, w)
+            row_op(0, 1, wd)
+            row_op(0, 2, wd * 3000 + c)
+            row_op(1, 3, 0, (n_o_id, d, w))
+            row_op(1, 5, 0, (o_id, d, w, c, 0, lines, 1 if local else 0))
+            for k in range(lines):
+                i_id, sw, qty = info[k]
+                row_op(1, 6, 0, (o_id, d, w, k + 1, i_id, sw, 0, qty))
+                row_op(2, 7, sw * 1000000 + i_id)
+                row_op(2, 7, sw * 1000000 + i_id)
+        else:
+            q = [int(x) for x in flat[i + 1:i + 11]]
+            i += 11
+            tid, w, d, c, c_last, is_name, c_d, c_w, _, _ = q
+            wd = w * 10 + d
+            if is_name == 1:
+                c = 0
+                for k in range(3000):
+                    at = wd * 3000 + k
+                    if at < len(cidx) and int(cidx[at]) == c_last:
+                        c = k
+                        break
+            cust = (c_w * 10 + c_d) * 3000 + c
+            row_op(0, 0, w)
+            row_op(0, 1, wd)
+            row_op(0, 2, cust)
+            row_op(2, 2, cust)
+            row_op(2, 0, w)
+            row_op(2, 1, wd)
+            row_op(1, 4, 0, (c, c_d, c_w, d, w))
+        tf.append(len(keys))
+    return (np.array(tf, np.uint32), np.array(keys, np.uint64), np.array(opw, np.uint32),
+            np.array(payload or [0], np.int32))
+
+
+@pytest.mark.gpu
+def test_tpcc_scheduler_sequence_matches_oracle(lib, tmp_path):
+    """TPCC_PART through the reference's eight entry points: new-order and
+    payment queries (the reference's own structs) re-sent every epoch; the
+    final int tables equal the oracle's serial replay of the expanded batch."""
+    W, txns, epochs, seed = 2, 2000, 2, 31
+    build_driver()
+    out = tmp_path / "tpcc.bin"
+    r = subprocess.run([DRIVER, str(out), "5", str(W), str(txns), str(epochs), str(seed)], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    raw = np.fromfile(out, np.int32)
+    st, w_, ntx, nep = raw[:4]
+    assert st == 0 and w_ == W and ntx == txns
+    nflat = int(raw[4])
+    flat = raw[5:5 + nflat].view(np.uint32)
+    d = W * 10
+    rows = [W, d, d * 3000, d * 3000, d * 3000, d * 3000, d * 45000, W * 100000, 100000]
+    cidx = raw[5 + nflat:5 + nflat + rows[2]].view(np.uint32)
+    off = 5 + nflat + rows[2]
+    finals = []
+    for t in range(9):
+        n = rows[t] * TPCC_INT_COLS[t]
+        finals.append(raw[off:off + n].reshape(rows[t], TPCC_INT_COLS[t]))
+        off += n
+    tf, keys, opw, payload = expand_tpcc(flat, cidx, rows)
+    assert len(tf) - 1 == txns
+    tables = []
+    for t in range(9):
+        cols = TPCC_INT_COLS[t]
+        cap = rows[t] + (txns * epochs * (15 if t == 6 else 1) if 3 <= t <= 6 else 0)
+        data = np.zeros((cols, cap), np.int32)
+        data[:, :rows[t]] = O.table_init(seed + t, rows[t], cols)  # ltp_table_value, column-major
+        tables.append((data, rows[t]))
+    for _ in range(epochs):
+        tables, commit, vals = O.replay_tables(0, tables, tf, keys, opw, payload)
+        assert commit.all()
+    for t in range(9):
+        assert np.array_equal(finals[t], tables[t][0][:, :rows[t]].T), t
+
