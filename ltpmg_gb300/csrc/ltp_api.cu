@@ -131,13 +131,12 @@ int ensure_scratch(ltp_ctx *ctx, uint64_t n_ops) {
         CK(dalloc(&s.smp_cnt, kSampleSlots));
         CK(dalloc(&s.hot_key, kHotMapSlots));
         CK(dalloc(&s.hot_id, kHotMapSlots));
-        const uint64_t gtiles = cap / kGenTile + 2;
-        CK(dalloc(&s.st_csort, 2 * gtiles * 256));
+        CK(dalloc(&s.st_csort, stiles * 256));
         CK(cudaMemsetAsync(s.smp_key, 0, kSampleSlots * sizeof(u64), ctx->stream));
         CK(cudaMemsetAsync(s.smp_cnt, 0, kSampleSlots * sizeof(u32), ctx->stream));
         CK(cudaMemsetAsync(s.hot_key, 0, kHotMapSlots * sizeof(u64), ctx->stream));
         CK(cudaMemsetAsync(s.hot_id, 0, kHotMapSlots * sizeof(u32), ctx->stream));
-        CK(cudaMemsetAsync(s.st_csort, 0, 2 * gtiles * 256 * sizeof(u32), ctx->stream));
+        CK(cudaMemsetAsync(s.st_csort, 0, stiles * 256 * sizeof(u32), ctx->stream));
         s.cap_ops = cap;
         s.cap_tiles = tiles;
         s.cap_sort_tiles = stiles;

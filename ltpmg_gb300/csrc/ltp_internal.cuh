@@ -124,7 +124,7 @@ struct Scratch {
     u32 *smp_cnt;   // [kSampleSlots] samples per cell
     u64 *hot_key;   // [kHotMapSlots] hot cell + 1 (0: empty slot)
     u32 *hot_id;    // [kHotMapSlots] its dense hot id
-    u32 *st_csort;  // [2 x (cap_ops / kGenTile + 2) * 256] look-back status of the bucket and hot radix passes
+    u32 *st_csort;  // [cap_sort_tiles * 256] look-back status of the bucket radix pass
     u64 n_words;
     u64 cap_ops;
     u64 cap_tiles;  // tiles of the smallest look-back tile size at cap_ops
@@ -159,9 +159,9 @@ struct Tuning {
 // sort by cell, segmented scan, table write-back).  No conflict words.
 constexpr u32 kHotMax = 256;        // hot cells: their ids sort in one 8-bit pass
 constexpr u32 kHotMapSlots = 1024;  // hot-cell lookup table (load <= 1/4)
-constexpr u32 kSampleStride = 64;   // one op in 64 is sampled
+constexpr u32 kSampleStride = 32;   // one op in 32 is sampled
 constexpr u32 kSampleSlots = 1u << 19;
-constexpr u32 kHotMinSamples = 32;  // hot: >= 32 samples (about 2048 ops)
+constexpr u32 kHotMinSamples = 64;  // hot: >= 64 samples (about 2048 ops)
 constexpr u32 kGenBlock = 256, kGenIpt = 8, kGenTile = kGenBlock * kGenIpt;
 constexpr u32 kBktBlock = 512, kBktIpt = 8, kBktChunk = kBktBlock * kBktIpt;
 constexpr u32 kBuckets = 256;

@@ -875,20 +875,13 @@ __global__ void __launch_bounds__(BLOCK, 65536 / (BLOCK * (IPT <= 2 ? 40 : IPT <
 // (zero on entry) and tile-claim slot `slot`; `recycle` (may be null) is the
 // previous pass's status array, cleared here for reuse.  A pass whose first
 // record sorts ahead by the first digit (first == true) ranks by ballots.
-// Sparse input (tile_counts non-null): tile t's records are
-// src[t * kGenTile, + count) with count = (tile_counts[t] >> count_shift) &
-// 0xFFFFFFFF, over n_tiles tiles; n is then unused.
 template <int BLK>
 __device__ __forceinline__ void sort_pass_core(const u64 *src, u64 *dst, u32 *status, u32 *recycle, const u32 *hist,
-                                               u64 n, int shift, int slot, bool first, u64 cap, Counters *ctr,
-                                               const u64 *tile_counts = nullptr, int count_shift = 0,
-                                               u32 n_tiles = 0) {
+                                               u64 n, int shift, int slot, bool first, u64 cap, Counters *ctr) {
     static_assert(BLK == 256, "one thread per radix digit");
-    static_assert(kGenTile <= kSortTile, "a sparse tile fits a sort tile");
     constexpr u32 SIPT = kSortTile / BLK;
     constexpr int WIN = 8;
-    const u32 tiles = tile_counts ? n_tiles : (u32)((n + kSortTile - 1) / kSortTile);
-    const u64 stride = tile_counts ? kGenTile : kSortTile;
+    const u32 tiles = (u32)((n + kSortTile - 1) / kSortTile);
     if (recycle) {  // the previous pass is complete: recycle its look-back slots
         for (u64 j = (u64)blockIdx.x * BLK + threadIdx.x; j < (u64)tiles * 256; j += (u64)gridDim.x * BLK)
             recycle[j] = 0;
@@ -921,14 +914,13 @@ __device__ __forceinline__ void sort_pass_core(const u64 *src, u64 *dst, u32 *st
         const u32 tile = claim_tile(ctr, slot);
         if (tile >= tiles) break;
         for (u32 i = tid; i < NW * 256; i += BLK) (&s_cnt[0][0])[i] = 0;
-        const u32 tcnt = tile_counts ? (u32)(tile_counts[tile] >> count_shift)
-                                     : (u32)min((u64)kSortTile, n - (u64)tile * kSortTile);
+        const u32 tcnt = (u32)min((u64)kSortTile, n - (u64)tile * kSortTile);
         const u32 lbase = (u32)warp * 32 * SIPT;
         u64 e[SIPT];
 #pragma unroll
         for (int k = 0; k < SIPT; k++) {
             const u32 li = lbase + (u32)k * 32 + lane;
-            e[k] = li < tcnt ? __ldcs(&src[(u64)tile * stride + li]) : ~0ull;
+            e[k] = li < tcnt ? __ldcs(&src[(u64)tile * kSortTile + li]) : ~0ull;
         }
         __syncthreads();
         u32 rank[SIPT], old[SIPT], lead[SIPT];
@@ -1633,32 +1625,10 @@ __global__ void k_expand_op_txn_checked(const u32 *txn_first, u64 n_txns, u64 n_
 __device__ __forceinline__ u32 hash_cell(u64 c) { return (u32)(mix64(c) >> 32); }
 
 // A sample of the ops (one in kSampleStride, at a hashed offset inside its
-// stride) counted per cell: first in a block-local shared-memory table (a
-// hot cell costs one global atomic per block, not one per sample), then
-// added into an open-addressing table in global memory.
-constexpr u32 kSampleBlockSlots = 4096;
+// stride) counted per cell in an open-addressing table.
 __global__ void __launch_bounds__(256) k_hsample(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
     pdl_begin();
     if (block_err(ctr)) return;
-    __shared__ u64 s_key[kSampleBlockSlots];
-    __shared__ u32 s_n[kSampleBlockSlots];
-    for (u32 i = threadIdx.x; i < kSampleBlockSlots; i += blockDim.x) {
-        s_key[i] = 0;
-        s_n[i] = 0;
-    }
-    __syncthreads();
-    auto to_global = [&](u64 key, u32 c) {
-        u32 slot = hash_cell(key - 1) & (kSampleSlots - 1);
-        for (u32 probe = 0; probe < 64; probe++) {  // a full neighbourhood only loses samples
-            u64 cur = s.smp_key[slot];
-            if (cur == 0) cur = atomicCAS(&s.smp_key[slot], 0ull, key);
-            if (cur == 0 || cur == key) {
-                atomicAdd(&s.smp_cnt[slot], c);
-                return;
-            }
-            slot = (slot + 1) & (kSampleSlots - 1);
-        }
-    };
     const u64 n = b.n_ops;
     const u64 ns = (n + kSampleStride - 1) / kSampleStride;
     for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < ns; j += (u64)gridDim.x * blockDim.x) {
@@ -1667,22 +1637,17 @@ __global__ void __launch_bounds__(256) k_hsample(BatchDev b, TablesDev T, Scratc
         const OpRef r = decode_op(T, op_key(b, i), b.opw[i]);
         if (!r.valid) continue;  // reported by the op-record kernel
         const u64 key = r.cell + 1;
-        u32 slot = hash_cell(r.cell) & (kSampleBlockSlots - 1);
-        bool done = false;
-        for (u32 probe = 0; probe < 32 && !done; probe++) {
-            u64 cur = s_key[slot];
-            if (cur == 0) cur = atomicCAS(&s_key[slot], 0ull, key);
+        u32 slot = hash_cell(r.cell) & (kSampleSlots - 1);
+        for (u32 probe = 0; probe < 64; probe++) {  // a full neighbourhood only loses a sample
+            u64 cur = s.smp_key[slot];
+            if (cur == 0) cur = atomicCAS(&s.smp_key[slot], 0ull, key);
             if (cur == 0 || cur == key) {
-                atomicAdd(&s_n[slot], 1u);
-                done = true;
+                atomicAdd(&s.smp_cnt[slot], 1u);
+                break;
             }
-            slot = (slot + 1) & (kSampleBlockSlots - 1);
+            slot = (slot + 1) & (kSampleSlots - 1);
         }
-        if (!done) to_global(key, 1u);  // a crowded block table: straight to the global one
     }
-    __syncthreads();
-    for (u32 i = threadIdx.x; i < kSampleBlockSlots; i += blockDim.x)
-        if (s_key[i]) to_global(s_key[i], s_n[i]);
 }
 
 // Hot cells: sampled at least kHotMinSamples times, at most kHotMax of them,
@@ -1741,10 +1706,9 @@ __device__ __forceinline__ long long cold_imm(u64 rec, const BucketPlan &p, cons
 }
 
 // Op records: every op becomes a hot record (packed contended-record form,
-// hot id in place of the dense id) or a cold record, each kept in op order
-// inside its tile's own slot range (tile t's records at t * kGenTile; the
-// two counts of tile t in st_cls[t], hot << 32 | cold); digit histograms of
-// the hot ids and of the cold records' buckets.  Malformed ops
+// hot id in place of the dense id) or a cold record, both compacted in op
+// order (one decoupled look-back of the two counts per tile); digit
+// histograms of the hot ids and of the cold records' buckets.  Malformed ops
 // and inserts (a batch on this path has no insert payload) are reported as
 // the mark kernel reports them.
 template <int BLOCK, int IPT>
@@ -1753,11 +1717,12 @@ __global__ void __launch_bounds__(BLOCK) k_gen(BatchDev b, TablesDev T, Scratch 
     if (block_err(ctr)) return;
     constexpr int NW = BLOCK / 32;
     constexpr u64 TILE = (u64)BLOCK * IPT;
-    static_assert(TILE == kGenTile, "sparse record tiles are kGenTile ops");
+    constexpr u64 kLow = (1ull << 31) - 1ull;
     __shared__ u64 s_hk[kHotMapSlots];
     __shared__ unsigned short s_hid[kHotMapSlots];
     __shared__ u32 s_hist[2][256];
     __shared__ u32 s_wh[NW], s_wc[NW];
+    __shared__ u64 s_run, s_base;
     const u32 H = *(volatile u32 *)&ctr->M;
     for (u32 i = threadIdx.x; i < kHotMapSlots; i += BLOCK) {
         const u64 k = H ? s.hot_key[i] : 0ull;
@@ -1824,7 +1789,7 @@ __global__ void __launch_bounds__(BLOCK) k_gen(BatchDev b, TablesDev T, Scratch 
             s_wc[warp] = nc;
         }
         __syncthreads();
-        if (threadIdx.x == 0) {  // the tile's records stay in its own slot range: no look-back
+        if (threadIdx.x == 0) {
             u32 rh = 0, rc = 0;
             for (int w = 0; w < NW; w++) {
                 const u32 a = s_wh[w], c = s_wc[w];
@@ -1833,12 +1798,14 @@ __global__ void __launch_bounds__(BLOCK) k_gen(BatchDev b, TablesDev T, Scratch 
                 rh += a;
                 rc += c;
             }
-            s.st_cls[tile] = ((u64)rh << 32) | (u64)rc;
+            s_run = ((u64)rh << 31) | (u64)rc;
+            lookback_publish(s.st_cls, tile, s_run);
             if (rh) atomicAdd(&ctr->n_c, (u64)rh);
             if (rc) atomicAdd(&ctr->n_cold, (u64)rc);
+            s_base = lookback_wait(s.st_cls, tile, s_run, ctr);
         }
         __syncthreads();
-        const u64 base = (u64)tile * TILE, hb = base + s_wh[warp], cb = base + s_wc[warp];
+        const u64 hb = (s_base >> 31) + s_wh[warp], cb = (s_base & kLow) + s_wc[warp];
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             if (hot[k] && LTP_IN_BOUNDS(ctr, hb + hpos[k], s.cap_ops)) s.list[0][hb + hpos[k]] = rec[k];
@@ -1854,23 +1821,11 @@ __global__ void __launch_bounds__(BLOCK) k_gen(BatchDev b, TablesDev T, Scratch 
 
 // The bucket radix pass: cold records in op order -> grouped by bucket (the
 // cell's top 8 bits), stably.
-__global__ void __launch_bounds__(kSortBlock, 3) k_csort(BatchDev b, Scratch s, Counters *ctr, BucketPlan p) {
+__global__ void __launch_bounds__(kSortBlock, 3) k_csort(Scratch s, Counters *ctr, BucketPlan p) {
     pdl_begin();
     if (block_err(ctr)) return;
-    const u32 tiles = (u32)((b.n_ops + kGenTile - 1) / kGenTile);
-    sort_pass_core<kSortBlock>(s.clist[0], s.clist[1], s.st_csort, nullptr, ctr->hist[2], 0, (int)(p.cs + p.cl),
-                               SLOT_CSORT, true, s.cap_ops, ctr, s.st_cls, 0, tiles);
-}
-
-// The hot records' radix pass: by hot id (one 8-bit digit), from the op
-// record tiles into one dense list for the segmented scan.
-__global__ void __launch_bounds__(kSortBlock, 3) k_hsort(BatchDev b, Scratch s, Counters *ctr) {
-    pdl_begin();
-    if (block_err(ctr)) return;
-    if (ctr->M == 0) return;
-    const u32 tiles = (u32)((b.n_ops + kGenTile - 1) / kGenTile);
-    sort_pass_core<kSortBlock>(s.list[0], s.list[1], s.st_csort + (s.cap_ops / kGenTile + 2) * 256, nullptr,
-                               ctr->hist[0], 0, 44, SLOT_SORT0, true, s.cap_ops, ctr, s.st_cls, 32, tiles);
+    sort_pass_core<kSortBlock>(s.clist[0], s.clist[1], s.st_csort, nullptr, ctr->hist[2], ctr->n_cold,
+                               (int)(p.cs + p.cl), SLOT_CSORT, true, s.cap_ops, ctr);
 }
 
 // One stable 8-bit radix pass of the block's BLOCK x IPT records in shared
@@ -2048,25 +2003,19 @@ __global__ void __launch_bounds__(BLOCK) k_bucket(BatchDev b, TablesDev T, Scrat
             const S carry = s_ws[warp];
             // every op's value from its cell's value before the chunk ...
             long long nv[IPT];
-            bool wr[IPT], wdk[IPT];
-            // all loads first, so that they are in flight together
-#pragma unroll
-            for (int k = 0; k < IPT; k++) {
-                const u32 e = wb + (u32)k * 32 + (u32)lane;
-                nv[k] = 0;
-                wdk[k] = false;
-                if (e < cnt) nv[k] = load_cell(cell_ptr(T, (cur[e] >> p.cs) & cell_mask, &wdk[k]), wdk[k]);
-            }
+            bool wr[IPT];
 #pragma unroll
             for (int k = 0; k < IPT; k++) {
                 const u32 e = wb + (u32)k * 32 + (u32)lane;
                 wr[k] = false;
+                nv[k] = 0;
                 if (e >= cnt) continue;
                 const u64 x = cur[e];
+                const u64 cell = (x >> p.cs) & cell_mask;
                 const S tot = sf[k] ? sv[k] : sv[k] + carry;
                 const u32 op = (u32)x & 0xFFFFFFu;
-                const bool wd = wdk[k];
-                const long long base = nv[k];
+                bool wd;
+                const long long base = load_cell(cell_ptr(T, cell, &wd), wd);
                 long long val = (long long)((u64)base + (u64)(long long)tot);
                 if (!wd) val = (int32_t)val;
                 nv[k] = val;
@@ -2093,15 +2042,11 @@ __global__ void __launch_bounds__(BLOCK) k_bucket(BatchDev b, TablesDev T, Scrat
 // Clean-up of the bucket path's own scratch: the bucket pass's look-back
 // slots and the hot-cell lookup table (the sample table was cleared by the
 // selection kernel; the shared slots by k_finish).
-__global__ void __launch_bounds__(256) k_bclear(BatchDev b, Scratch s, Counters *ctr) {
+__global__ void __launch_bounds__(256) k_bclear(Scratch s, Counters *ctr) {
     pdl_begin();
-    const u64 t_sort = (b.n_ops + kGenTile - 1) / kGenTile;
-    const u64 half = (s.cap_ops / kGenTile + 2) * 256;  // the hot pass's slots follow the cold pass's
+    const u64 t_sort = (ctr->n_cold + kSortTile - 1) / kSortTile;
     const u64 gsz = (u64)gridDim.x * blockDim.x, g0 = (u64)blockIdx.x * blockDim.x + threadIdx.x;
-    for (u64 j = g0; j < t_sort * 256; j += gsz) {
-        s.st_csort[j] = 0;
-        s.st_csort[half + j] = 0;
-    }
+    for (u64 j = g0; j < t_sort * 256; j += gsz) s.st_csort[j] = 0;
     for (u64 j = g0; j < kHotMapSlots; j += gsz) {
         s.hot_key[j] = 0;
         s.hot_id[j] = 0;
@@ -2270,14 +2215,14 @@ cudaError_t launch_execute(const Launch &L_in, const BatchDev &b_in, const Table
             sms = L.num_sms;
         }
         const u64 n = b.n_ops;
-        const int g_small = capped(L.num_sms * 2, (n / kSampleStride + 255) / 256 + 1);
+        const int g_small = capped(L.num_sms * 8, (n / kSampleStride + 255) / 256 + 1);
         chk(launch_k(L.pdl, k_hsample, g_small, 256, 0, L.stream, b, T, s, ctr));
         chk(launch_k(L.pdl, k_hselect, L.num_sms * 8, 256, 0, L.stream, s, ctr));
         mark_ev(1);
         chk(launch_k(L.pdl, k_gen<kGenBlock, kGenIpt>, capped(g_gen, (n + kGenTile - 1) / kGenTile), kGenBlock, 0,
                      L.stream, b, T, s, ctr, p));
         mark_ev(2);
-        chk(launch_k(L.pdl, k_csort, capped(g_srt, (n + kGenTile - 1) / kGenTile), kSortBlock, 0, L.stream, b, s, ctr,
+        chk(launch_k(L.pdl, k_csort, capped(g_srt, (n + kSortTile - 1) / kSortTile), kSortBlock, 0, L.stream, s, ctr,
                      p));
         mark_ev(3);
         if (T.any_wide)
@@ -2289,15 +2234,15 @@ cudaError_t launch_execute(const Launch &L_in, const BatchDev &b_in, const Table
         mark_ev(4);
         chk(launch_k(L.pdl, k_dbase, L.num_sms * 8, 256, 0, L.stream, T, s, ctr, 0));
         mark_ev(5);
-        chk(launch_k(L.pdl, k_hsort, capped(g_srt, (n + kGenTile - 1) / kGenTile), kSortBlock, 0, L.stream, b, s,
-                     ctr));
+        chk(launch_k(L.pdl, k_sort_pass<0>, capped(g_srt, (n + kSortTile - 1) / kSortTile), kSortBlock, 0, L.stream,
+                     s, ctr, n));
         mark_ev(6);
         mark_ev(7);
         chk(launch_k(L.pdl, T.any_wide ? k_apply<u64> : k_apply<u32>, capped(g_app, (n + kApplyTile - 1) / kApplyTile),
                      kApplyBlock, 0, L.stream, b, T, s, ctr));
         mark_ev(8);
         mark_ev(9);
-        chk(launch_k(L.pdl, k_bclear, L.num_sms * 8, 256, 0, L.stream, b, s, ctr));
+        chk(launch_k(L.pdl, k_bclear, L.num_sms * 8, 256, 0, L.stream, s, ctr));
         chk(launch_k(L.pdl, k_finish<32>, L.num_sms * 8, 256, 0, L.stream, b, T, s, ctr, L.rule));
         mark_ev(10);
         const cudaError_t e = cudaGetLastError();
