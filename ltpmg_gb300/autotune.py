@@ -4,8 +4,8 @@ Per size bucket (floor(log2(ops in the batch))) it times every candidate
 tiling of the streaming kernels -- threads per block x ops per thread, the
 knobs that set how many ops a tile stages in shared memory -- then 64-cell
 conflict words (bitmap word granularity) for the fastest tilings, then the
-mark kernel's hot-word pre-check, then the cell-bucket path, on a
-representative batch with CUDA events, and keeps the fastest.  For a list of
+mark kernel's hot-word pre-check, on a representative batch with CUDA
+events, and keeps the fastest.  For a list of
 batches it also times the multi-batch execution modes (CUDA graph vs the
 persistent cooperative kernel) and keeps the faster one.  Choices persist as
 JSON and are applied with Context.set_tuning.
@@ -85,19 +85,9 @@ def tune_tiles(ctx, batch, reps=3, blocks=BLOCKS, ipts=IPTS, copies=1):
     pre_ms = _time_batch(ctx, batch, reps, copies)
     results[f"{best}+precheck"] = pre_ms
     flags = L.TUNE_MARK_PRECHECK if pre_ms < results[best] else 0
-    best_ms = min(results[best], pre_ms)
-    # then the cell-bucket path (it applies to ordered-rule batches without
-    # inserts; for others the flag changes nothing, so it is kept only when
-    # it is faster on this batch)
-    ctx.set_tuning(bucket, blk, ipt, word_bits=word_bits, flags=flags | L.TUNE_BUCKET)
-    bkt_ms = _time_batch(ctx, batch, reps, copies)
-    results["bucket"] = bkt_ms
-    if bkt_ms < best_ms:
-        flags |= L.TUNE_BUCKET
-        best_ms = bkt_ms
     ctx.set_tuning(bucket, blk, ipt, word_bits=word_bits, flags=flags)
     return {"bucket": bucket, "block": blk, "ipt": ipt, "word_bits": word_bits, "flags": flags,
-            "ms": best_ms, "candidates": results}
+            "ms": min(results[best], pre_ms), "candidates": results}
 
 
 def tune_mode(ctx, batches, reps=2, modes=(L.MODE_GRAPH, L.MODE_PERSISTENT)):

@@ -60,7 +60,7 @@ def test_chunk_edges_and_adversarial_keys(lib_loaded, n_ops, pattern):
     the 4096-record bucket chunk; keys on one cell (a hot cell, or with few
     ops a cold one), all distinct, Zipf 1.3, two hot cells; random
     immediates in [-3, 3]."""
-    rows, cols = 1 << 14, 4  # room for 40,000 distinct cells
+    rows, cols = 1 << 12, 4
     rng = np.random.default_rng(n_ops * 17 + len(pattern))
     tf, keys, opw = _pattern_batch(pattern, n_ops, rows, cols, rng)
     stats = run_and_check(0, rows, cols, [(tf, keys, opw)], seed=5, tuning=BUCKET)
