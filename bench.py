@@ -62,48 +62,6 @@ KERNEL_BYTES = {  # st["key_bytes"]: 8, or 4 for batches loaded with 32-bit keys
     "insert": lambda st: st.get("insert_bytes", 0),
     "finish": lambda st: 12 * st["touched_words"],
 }
-# the same for the cell-bucket path (stats path == 1): records are 8 B
-BUCKET_KERNEL_BYTES = {
-    "hot_select": lambda st: (4 + st["key_bytes"]) * st["ops"] // 32,  # the sampled ops
-    "gen": lambda st: (12 + st["key_bytes"]) * st["ops"],  # key + opword in, one 8-byte record out
-    "bucket_sort": lambda st: 16 * st["bucket_ops"],
-    "bucket": lambda st: 16 * st["bucket_ops"],  # record in, cell read, value out
-    "hot_dbase": lambda st: 24 * st["contended_cells"],
-    "hot_sort": lambda st: 16 * st["contended_ops"],
-    "hot_apply": lambda st: 16 * st["contended_ops"] + 12 * st["contended_cells"],
-    "finish": lambda st: 0,
-}
-
-
-def kernel_roofline(stats, key_bytes, extra=None):
-    """Per kernel over the batches that ran it: mean launch time (ms) and
-    algorithmic bytes per launch from each batch's counters (the
-    conflict-word path's kernels, or the cell-bucket path's); the dominant
-    kernel is the one with the most total time.  Returns (avg ms per
-    kernel, dominant kernel, its bytes per launch, its GB/s)."""
-    ms, nbytes, cnt = {}, {}, {}
-    for st in stats:
-        table = BUCKET_KERNEL_BYTES if st.get("path") == 1 else KERNEL_BYTES
-        c = dict(st, key_bytes=key_bytes, **(extra or {}))
-        for name, fn in table.items():
-            t = st["ms_stage"].get(name, 0.0)
-            if t <= 0:
-                continue
-            ms[name] = ms.get(name, 0.0) + t
-            nbytes[name] = nbytes.get(name, 0.0) + fn(c)
-            cnt[name] = cnt.get(name, 0) + 1
-    avg = {k: ms[k] / cnt[k] for k in ms}
-    dom = max(ms, key=ms.get)
-    return avg, dom, nbytes[dom] / cnt[dom], nbytes[dom] / (ms[dom] / 1e3) / 1e9
-
-
-def tiling_label(v):
-    """512x4, 256x2w64+precheck, 512x4+bucket ..."""
-    f = v.get("flags", 0)
-    return (f"{v['block']}x{v['ipt']}" + ("w64" if v.get("word_bits") == 64 else "") +
-            ("+precheck" if f & 1 else "") + ("+bucket" if f & 2 else ""))
-
-
 def kernels_per_batch(n_ops, has_payload):
     """Kernels one batch launches under the ordered rule: mark, ids, dbase,
     classify, one radix pass per 8 bits of the largest possible contended id
@@ -538,30 +496,31 @@ def run_ours(args, config):
             "pipeline": {"algorithmic_bytes_per_step": alg, "avg_step_ms": step_ms,
                          "achieved": alg / (step_ms / 1e3) / 1e9, "frac": alg / (step_ms / 1e3) / 1e9 / peak}}
     mean_stats = {k: sum(s[k] for s in stats) / len(stats) for k in ("ops", "touched_words", "contended_cells",
-                                                                     "contended_ops", "bucket_ops")}
+                                                                     "contended_ops")}
     mean_stats["key_bytes"] = key_bytes
     if mode != G.MODE_PERSISTENT:
-        avg, dom, dom_bytes, achieved = kernel_roofline(stats, key_bytes)
+        avg = {name: sum(s["ms_stage"][name] for s in stats) / len(stats) for name in KERNEL_BYTES}
+        dom = max(avg, key=avg.get)
+        dom_bytes = KERNEL_BYTES[dom](mean_stats)
+        achieved = dom_bytes / (avg[dom] / 1e3) / 1e9
         traffic_b = measured_traffic(config, dom, mean_stats)
         roof.update({"kernel": dom, "achieved": achieved, "frac": achieved / peak, "traffic": traffic_b,
                      "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": avg[dom], "kernel_ms": avg,
-                     "batches_on_bucket_path": sum(1 for st in stats if st["path"] == 1)})
-        if "classify" in avg and "mark" in avg:
-            roof["random_access"] = random_access_roof(G, local, sh, mean_stats, avg, config)
+                     "random_access": random_access_roof(G, local, sh, mean_stats, avg, config)})
     else:
         roof.update({"kernel": "k_persist (whole pipeline, one launch per step)", "achieved":
                      roof["pipeline"]["achieved"], "frac": roof["pipeline"]["frac"], "traffic": None,
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": step_ms})
     launches = args.steps * (1 if mode == G.MODE_PERSISTENT else
-                             sum(10 if st["path"] == 1 else kernels_per_batch(len(h[1]), False)
-                                 for h, st in zip(host, stats)))
+                             sum(kernels_per_batch(len(h[1]), False) for h in host))
     line = {"metric": METRIC, "value": value, "unit": "txn/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
             "config": {"workload": WORKLOAD_TEXT[config], "batches_per_step": nb, "txns_per_step": txns_per_step,
                        "rule": "ordered (ascending TID per cell, all commit)", "mode": mode_name,
                        "mode_ms": {str(k): v for k, v in mode_ms.items()},
-                       "tuning": {str(k): tiling_label(v) for k, v in tiles.items()},
+                       "tuning": {str(k): f"{v['block']}x{v['ipt']}" + ("w64" if v.get("word_bits") == 64 else "") + ("+precheck" if v.get("flags") else "")
+                                  for k, v in tiles.items()},
                        "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
             "gpu_launches": launches, "roofline": roof, "clocks": clk, "e2e": e2e,
             "contention": {"contended_ops_per_batch": mean_stats["contended_ops"],
@@ -583,12 +542,12 @@ def fixed_tiles(ctx, dev, spec):
 
     import ltpmg_gb300 as G
 
-    # BLOCKxIPT[w64][+precheck][+bucket], e.g. 512x4, 256x2w64+precheck, 512x4+bucket
-    base, *opts = spec.split("+")
+    # BLOCKxIPT[w64][+precheck], e.g. 512x4, 256x2w64+precheck
+    base, _, opt = spec.partition("+")
     base, _, wb = base.partition("w")
     blk, ipt = (int(x) for x in base.split("x"))
     word_bits = int(wb) if wb else 32
-    flags = (G.lib.TUNE_MARK_PRECHECK if "precheck" in opts else 0) | (G.lib.TUNE_BUCKET if "bucket" in opts else 0)
+    flags = G.lib.TUNE_MARK_PRECHECK if opt == "precheck" else 0
     out = {}
     for b in dev:
         k = AT.bucket_of(b.n_ops)
@@ -888,7 +847,8 @@ def run_payload(args, config):
             "config": {"workload": WORKLOAD_TEXT[config], "batches_per_step": nb, "txns_per_step": txns_per_step,
                        "ops_per_step": ops_per_step, "rule": "ordered (ascending TID per cell, all commit)",
                        "mode": mode_name, "mode_ms": {str(k): v for k, v in mode_ms.items()},
-                       "tuning": {str(k): tiling_label(v) for k, v in tiles.items()},
+                       "tuning": {str(k): f"{v['block']}x{v['ipt']}" + ("w64" if v.get("word_bits") == 64 else "") + ("+precheck" if v.get("flags") else "")
+                                  for k, v in tiles.items()},
                        "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
             "gpu_launches": launches, "roofline": roof, "clocks": clk, "e2e": e2e,
             "contention": {"contended_ops_per_batch": mean_stats["contended_ops"],
@@ -1245,8 +1205,7 @@ def main():
     ap.add_argument("--batches", type=int, default=0, help="resident batches (default: the config's)")
     ap.add_argument("--tuning-out", default="", help="write the autotuner's choices to this JSON file")
     ap.add_argument("--tiles", default="",
-                    help="fixed BLOCKxIPT[w64][+precheck][+bucket] tiling instead of the autotuner's (e.g. 512x4, "
-                         "256x2w64, 512x4+bucket: the cell-bucket path)")
+                    help="fixed BLOCKxIPT[w64][+precheck] tiling instead of the autotuner's (e.g. 512x4, 256x2w64)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     ap.add_argument("--loadgen-threads", type=int, default=8, help="serving sweep: load-generator threads")
