@@ -110,18 +110,8 @@ typedef struct {
      *                8 insert, 9 finish
      * priority rule: 0 mark, 1 ids, 2 min-writer, 3 abort, 4 execute,
      *                8 insert, 9 finish
-     * cell-bucket path (LTP_TUNE_BUCKET): 0 hot-cell sampling and selection,
-     *                1 op records, 2 bucket radix pass, 3 bucket pass, 4 hot
-     *                cells' values, 5 hot radix pass, 7 hot segmented scan,
-     *                9 clean-up
      * and 11 the whole batch */
     float ms_stage[LTP_N_STAGES];
-    /* ops executed by the bucket pass of the cell-bucket path (0 on the
-     * conflict-word path); contended_ops / contended_cells then count the
-     * hot cells' ops and the hot cells */
-    uint64_t bucket_ops;
-    uint32_t path;  /* 0: conflict-word path, 1: cell-bucket path */
-    uint32_t reserved;
 } ltp_stats;
 
 typedef struct {
@@ -493,15 +483,6 @@ typedef struct {
  * a few words are hot in every tile (order-entry warehouse and district
  * rows), a loss when repeated words are still filling up (Zipf tails). */
 #define LTP_TUNE_MARK_PRECHECK 1u
-/* The cell-bucket path for batches of this size bucket: under the ordered
- * rule, for batches without inserts of at most 2^24 ops, the cells a sample
- * of the ops shows to be hottest are executed by a radix sort of their ops
- * and a segmented scan, and every other op by one radix pass into 256
- * buckets of consecutive cells, each executed by one block (local sort by
- * cell, segmented scan, write-back) -- no conflict words.  Other batches of
- * the bucket, and the persistent kernel, use the conflict-word path.  Same
- * results either way. */
-#define LTP_TUNE_BUCKET 2u
 /* Tuning used for batches whose op count falls in size bucket floor(log2(ops)). */
 int ltp_set_tuning(ltp_ctx *ctx, uint32_t bucket, const ltp_tuning *t);
 int ltp_get_tuning(ltp_ctx *ctx, uint32_t bucket, ltp_tuning *t);

@@ -66,16 +66,6 @@ void free_scratch_ops(Scratch &s) {
     cudaFree(s.st_cls);
     cudaFree(s.st_apply);
     cudaFree(s.st_ins);
-    cudaFree(s.clist[0]);
-    cudaFree(s.clist[1]);
-    cudaFree(s.smp_key);
-    cudaFree(s.smp_cnt);
-    cudaFree(s.hot_key);
-    cudaFree(s.hot_id);
-    cudaFree(s.st_csort);
-    s.clist[0] = s.clist[1] = nullptr;
-    s.smp_key = s.hot_key = nullptr;
-    s.smp_cnt = s.hot_id = s.st_csort = nullptr;
     s.st_ins = nullptr;
     s.tw_list = nullptr;
     s.list[0] = s.list[1] = nullptr;
@@ -123,20 +113,6 @@ int ensure_scratch(ltp_ctx *ctx, uint64_t n_ops) {
         CK(dalloc(&s.st_cls, tiles));
         CK(dalloc(&s.st_apply, tiles));
         CK(dalloc(&s.st_ins, tiles * LTP_MAX_TABLES));
-        // the cell-bucket path's records, sample and hot-cell tables (zeroed
-        // here; each batch on the path leaves them zeroed)
-        CK(dalloc(&s.clist[0], cap));
-        CK(dalloc(&s.clist[1], cap));
-        CK(dalloc(&s.smp_key, kSampleSlots));
-        CK(dalloc(&s.smp_cnt, kSampleSlots));
-        CK(dalloc(&s.hot_key, kHotMapSlots));
-        CK(dalloc(&s.hot_id, kHotMapSlots));
-        CK(dalloc(&s.st_csort, stiles * 256));
-        CK(cudaMemsetAsync(s.smp_key, 0, kSampleSlots * sizeof(u64), ctx->stream));
-        CK(cudaMemsetAsync(s.smp_cnt, 0, kSampleSlots * sizeof(u32), ctx->stream));
-        CK(cudaMemsetAsync(s.hot_key, 0, kHotMapSlots * sizeof(u64), ctx->stream));
-        CK(cudaMemsetAsync(s.hot_id, 0, kHotMapSlots * sizeof(u32), ctx->stream));
-        CK(cudaMemsetAsync(s.st_csort, 0, stiles * 256 * sizeof(u32), ctx->stream));
         s.cap_ops = cap;
         s.cap_tiles = tiles;
         s.cap_sort_tiles = stiles;
@@ -754,8 +730,6 @@ int ltp_batch_finish(ltp_ctx *ctx, ltp_batch *b, ltp_stats *stats, void *stream)
         stats->contended_ops = c.n_c;
         stats->contended_cells = c.M;
         stats->touched_words = c.n_tw;
-        stats->bucket_ops = c.n_cold;
-        stats->path = c.path;
         stats->bytes_algorithmic = 28ull * b->n_ops + 4ull * b->n_txns;
         if (b->have_events && (ctx->flags & LTP_FLAG_STAGE_TIMING) && b->n_ops) {
             // stage events are absent for batches run by the persistent kernel
@@ -824,7 +798,7 @@ int ltp_set_tuning(ltp_ctx *ctx, uint32_t bucket, const ltp_tuning *t) {
     if (t->word_bits != 32 && t->word_bits != 64) return fail(ctx, LTP_E_BADARG, "word_bits must be 32 or 64");
     if (!tiling_supported((int)t->block, (int)t->ipt, (int)t->word_bits))
         return fail(ctx, LTP_E_BADARG, "64-cell conflict words need block x ipt <= 2048");
-    if (t->flags & ~(LTP_TUNE_MARK_PRECHECK | LTP_TUNE_BUCKET)) return fail(ctx, LTP_E_BADARG, "unknown tuning flag");
+    if (t->flags & ~LTP_TUNE_MARK_PRECHECK) return fail(ctx, LTP_E_BADARG, "unknown tuning flag");
     ctx->tuning[bucket] = Tuning{t->block, t->ipt, t->word_bits, t->flags};
     return LTP_OK;
 }
@@ -899,8 +873,6 @@ static void pipe_stats(const PipeSlot &sl, ltp_stats *stats) {
     stats->contended_ops = c.n_c;
     stats->contended_cells = c.M;
     stats->touched_words = c.n_tw;
-    stats->bucket_ops = c.n_cold;
-    stats->path = c.path;
     stats->bytes_algorithmic = 28ull * sl.b->n_ops + 4ull * sl.b->n_txns;
 }
 

@@ -74,11 +74,7 @@ struct BatchDev {
 constexpr int kMaxPasses = 4;
 
 // Look-back status slots of the kernels that use decoupled look-back.
-enum TileSlot {
-    SLOT_CLASSIFY = 0, SLOT_SORT0 = 1, SLOT_APPLY = 5, SLOT_INSERT = 6,
-    SLOT_CSORT = 7, SLOT_BUCKET = 8,  // cell-bucket path: cold radix pass, bucket claims
-    N_SLOTS = 9
-};
+enum TileSlot { SLOT_CLASSIFY = 0, SLOT_SORT0 = 1, SLOT_APPLY = 5, SLOT_INSERT = 6, N_SLOTS = 7 };
 
 // Per-batch device counters; zeroed by the host before every batch.
 struct Counters {
@@ -91,10 +87,9 @@ struct Counters {
     u32 tile_ctr[N_SLOTS];
     u32 hist[kMaxPasses][256];  // radix digit histograms of the contended list
     u32 stall;         // polled by the debug stall kernel; never set
-    u32 path;          // 1: the batch ran on the cell-bucket path
+    u32 pad;
     u32 ins_total[LTP_MAX_TABLES];      // insert ops per table in the batch
     u32 ins_committed[LTP_MAX_TABLES];  // committed inserts per table
-    u64 n_cold;        // cell-bucket path: ops executed by the bucket pass
 };
 
 // Conflict state of 32 consecutive cells, kept together so that building,
@@ -118,13 +113,6 @@ struct Scratch {
     u64 *st_cls;    // [tiles] classify look-back status (dense record offsets)
     u64 *st_apply;  // [tiles] segmented-apply look-back status
     u32 *st_ins;    // [tiles * LTP_MAX_TABLES] insert-slot look-back status
-    // cell-bucket path (allocated when a size bucket is tuned to it; null otherwise)
-    u64 *clist[2];  // [cap_ops] cold-op records, before and after the bucket radix pass
-    u64 *smp_key;   // [kSampleSlots] sampled cell + 1 (0: empty slot)
-    u32 *smp_cnt;   // [kSampleSlots] samples per cell
-    u64 *hot_key;   // [kHotMapSlots] hot cell + 1 (0: empty slot)
-    u32 *hot_id;    // [kHotMapSlots] its dense hot id
-    u32 *st_csort;  // [cap_sort_tiles * 256] look-back status of the bucket radix pass
     u64 n_words;
     u64 cap_ops;
     u64 cap_tiles;  // tiles of the smallest look-back tile size at cap_ops
@@ -148,29 +136,6 @@ constexpr u32 kInsSmem = kInsTile * (4 + 8 + 1);  // insert staging: payload off
 
 struct Tuning {
     u32 block, ipt, word_bits, flags;
-};
-
-// ---- cell-bucket path ------------------------------------------------------
-// Ordered rule, batches without inserts, n_ops <= 2^24: the hottest cells
-// (found from a sample of the ops) are executed like contended cells (radix
-// sort by hot id + segmented scan); every other op goes, by one radix pass
-// on the top 8 bits of its cell, to one of 256 buckets of consecutive cells,
-// and one block per bucket executes the bucket's ops chunk by chunk (local
-// sort by cell, segmented scan, table write-back).  No conflict words.
-constexpr u32 kHotMax = 256;        // hot cells: their ids sort in one 8-bit pass
-constexpr u32 kHotMapSlots = 1024;  // hot-cell lookup table (load <= 1/4)
-constexpr u32 kSampleStride = 32;   // one op in 32 is sampled
-constexpr u32 kSampleSlots = 1u << 19;
-constexpr u32 kHotMinSamples = 64;  // hot: >= 64 samples (about 2048 ops)
-constexpr u32 kGenBlock = 256, kGenIpt = 8, kGenTile = kGenBlock * kGenIpt;
-constexpr u32 kBktBlock = 512, kBktIpt = 8, kBktChunk = kBktBlock * kBktIpt;
-constexpr u32 kBuckets = 256;
-// Cold-op record: cell << cs | immcode << 24 | op, cs = 64 - cell bits; the
-// immcode's top bit says "read the immediate from the opword", its other
-// cs - 25 bits hold a signed immediate that fits them (reads carry 0).
-struct BucketPlan {
-    u32 cs;  // cell shift in a cold record
-    u32 cl;  // cell-lo bits: bucket = cell >> cl (< 256)
 };
 
 // Host-side launch plan for one batch.

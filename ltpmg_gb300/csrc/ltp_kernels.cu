@@ -870,21 +870,23 @@ __global__ void __launch_bounds__(BLOCK, 65536 / (BLOCK * (IPT <= 2 ? 40 : IPT <
 // the ranks stable), per-digit decoupled look-back over a window of eight
 // predecessor tiles with relaxed loads, shared-memory staging so every
 // digit's run leaves as coalesced stores.
-// One stable radix pass: n records src -> dst by the 8-bit digit at `shift`,
-// with the digit histogram `hist` of all n records, look-back slots `status`
-// (zero on entry) and tile-claim slot `slot`; `recycle` (may be null) is the
-// previous pass's status array, cleared here for reuse.  A pass whose first
-// record sorts ahead by the first digit (first == true) ranks by ballots.
 template <int BLK>
-__device__ __forceinline__ void sort_pass_core(const u64 *src, u64 *dst, u32 *status, u32 *recycle, const u32 *hist,
-                                               u64 n, int shift, int slot, bool first, u64 cap, Counters *ctr) {
+__device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, Counters *ctr, u64 n_ops) {
     static_assert(BLK == 256, "one thread per radix digit");
     constexpr u32 SIPT = kSortTile / BLK;
     constexpr int WIN = 8;
+    if (block_err(ctr)) return;
+    const int passes = sort_passes_dev(ctr->M);
+    if (P >= passes) return;
+    const u64 n = ctr->n_c;
     const u32 tiles = (u32)((n + kSortTile - 1) / kSortTile);
-    if (recycle) {  // the previous pass is complete: recycle its look-back slots
+    const u64 *src = s.list[P & 1];
+    u64 *dst = s.list[(P + 1) & 1];
+    u32 *status = s.st_sort[P & 1];
+    if (P >= 1) {  // the previous pass is complete: recycle its look-back slots
+        u32 *other = s.st_sort[(P + 1) & 1];
         for (u64 j = (u64)blockIdx.x * BLK + threadIdx.x; j < (u64)tiles * 256; j += (u64)gridDim.x * BLK)
-            recycle[j] = 0;
+            other[j] = 0;
     }
     constexpr int NW = BLK / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -896,7 +898,7 @@ __device__ __forceinline__ void sort_pass_core(const u64 *src, u64 *dst, u32 *st
     __shared__ u32 s_wsum[NW];
     __shared__ u64 s_stage[kSortTile];
     {  // global start of every digit: exclusive scan of the histogram
-        const u32 h = hist[tid];
+        const u32 h = ctr->hist[P][tid];
         u32 incl = h;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -910,8 +912,9 @@ __device__ __forceinline__ void sort_pass_core(const u64 *src, u64 *dst, u32 *st
         s_start[tid] = off + incl - h;
         __syncthreads();
     }
+    const int shift = rec_shift(rec_packed(ctr->M, n_ops)) + 8 * P;
     for (;;) {
-        const u32 tile = claim_tile(ctr, slot);
+        const u32 tile = claim_tile(ctr, SLOT_SORT0 + P);
         if (tile >= tiles) break;
         for (u32 i = tid; i < NW * 256; i += BLK) (&s_cnt[0][0])[i] = 0;
         const u32 tcnt = (u32)min((u64)kSortTile, n - (u64)tile * kSortTile);
@@ -933,7 +936,7 @@ __device__ __forceinline__ void sort_pass_core(const u64 *src, u64 *dst, u32 *st
             // still in op order; match.any on the later ones (measured
             // faster there, slower on the first)
             u32 peers;
-            if (first) {
+            if (P == 0) {
                 peers = __ballot_sync(FULL_MASK, v);
 #pragma unroll
                 for (int bit = 0; bit < 8; bit++) {
@@ -1020,21 +1023,10 @@ __device__ __forceinline__ void sort_pass_core(const u64 *src, u64 *dst, u32 *st
         for (u32 p = tid; p < tcnt; p += BLK) {
             const u64 x = s_stage[p];
             const u32 d = (u32)(x >> shift) & 255u;
-            if (LTP_IN_BOUNDS(ctr, s_base[d] + (p - s_loc[d]), cap)) dst[s_base[d] + (p - s_loc[d])] = x;
+            if (LTP_IN_BOUNDS(ctr, s_base[d] + (p - s_loc[d]), s.cap_ops)) dst[s_base[d] + (p - s_loc[d])] = x;
         }
         __syncthreads();
     }
-}
-
-// Pass P of the contended-record sort (digit P of the dense ids).
-template <int BLK>
-__device__ __forceinline__ void phase_sort_pass(const int P, const Scratch &s, Counters *ctr, u64 n_ops) {
-    if (block_err(ctr)) return;
-    const int passes = sort_passes_dev(ctr->M);
-    if (P >= passes) return;
-    sort_pass_core<BLK>(s.list[P & 1], s.list[(P + 1) & 1], s.st_sort[P & 1], P >= 1 ? s.st_sort[(P + 1) & 1] : nullptr,
-                        ctr->hist[P], ctr->n_c, rec_shift(rec_packed(ctr->M, n_ops)) + 8 * P, SLOT_SORT0 + P, P == 0,
-                        s.cap_ops, ctr);
 }
 
 template <int P>
@@ -1618,442 +1610,6 @@ __global__ void k_expand_op_txn_checked(const u32 *txn_first, u64 n_txns, u64 n_
 }
 
 // ============================================================================
-// cell-bucket path (ordered rule, no inserts): hot cells by sort + segmented
-// scan, every other op by one radix pass into 256 buckets of consecutive
-// cells and one block per bucket
-// ============================================================================
-__device__ __forceinline__ u32 hash_cell(u64 c) { return (u32)(mix64(c) >> 32); }
-
-// A sample of the ops (one in kSampleStride, at a hashed offset inside its
-// stride) counted per cell in an open-addressing table.
-__global__ void __launch_bounds__(256) k_hsample(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
-    pdl_begin();
-    if (block_err(ctr)) return;
-    const u64 n = b.n_ops;
-    const u64 ns = (n + kSampleStride - 1) / kSampleStride;
-    for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < ns; j += (u64)gridDim.x * blockDim.x) {
-        const u64 i = j * kSampleStride + (mix64(j) & (kSampleStride - 1));
-        if (i >= n) continue;
-        const OpRef r = decode_op(T, op_key(b, i), b.opw[i]);
-        if (!r.valid) continue;  // reported by the op-record kernel
-        const u64 key = r.cell + 1;
-        u32 slot = hash_cell(r.cell) & (kSampleSlots - 1);
-        for (u32 probe = 0; probe < 64; probe++) {  // a full neighbourhood only loses a sample
-            u64 cur = s.smp_key[slot];
-            if (cur == 0) cur = atomicCAS(&s.smp_key[slot], 0ull, key);
-            if (cur == 0 || cur == key) {
-                atomicAdd(&s.smp_cnt[slot], 1u);
-                break;
-            }
-            slot = (slot + 1) & (kSampleSlots - 1);
-        }
-    }
-}
-
-// Hot cells: sampled at least kHotMinSamples times, at most kHotMax of them,
-// numbered densely (dcell) and entered into the hot-cell lookup table.  Every
-// sample slot is cleared for the next batch, whatever the batch's status.
-__global__ void __launch_bounds__(256) k_hselect(Scratch s, Counters *ctr) {
-    pdl_begin();
-    const bool ok = *(volatile int *)&ctr->err == 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) ctr->path = 1u;
-    for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < kSampleSlots; j += (u64)gridDim.x * blockDim.x) {
-        const u64 key = s.smp_key[j];
-        if (!key) continue;
-        const u32 c = s.smp_cnt[j];
-        s.smp_key[j] = 0;
-        s.smp_cnt[j] = 0;
-        if (!ok || c < kHotMinSamples) continue;
-        u32 old = *(volatile u32 *)&ctr->M, hid = kHotMax;
-        while (old < kHotMax) {  // the next id while fewer than kHotMax are taken
-            const u32 prev = atomicCAS(&ctr->M, old, old + 1);
-            if (prev == old) {
-                hid = old;
-                break;
-            }
-            old = prev;
-        }
-        if (hid >= kHotMax) continue;  // over the cap: the cell stays on the bucket path
-        s.dcell[hid] = key - 1;
-        u32 slot = hash_cell(key - 1) & (kHotMapSlots - 1);
-        for (u32 probe = 0; probe < kHotMapSlots; probe++) {
-            if (atomicCAS(&s.hot_key[slot], 0ull, key) == 0ull) {
-                s.hot_id[slot] = hid;
-                break;
-            }
-            slot = (slot + 1) & (kHotMapSlots - 1);
-        }
-    }
-}
-
-// Cold-op record of op i on `cell` (kind read or add, immediate `imm`).
-__device__ __forceinline__ u64 cold_record(u64 cell, u32 kind, int32_t imm, u64 i, const BucketPlan &p) {
-    const u32 ib = p.cs - 25;  // bits of an immediate kept in the record
-    u64 code = 0;
-    if (kind == LTP_OP_ADD && imm != 0) {
-        // opword immediates are 20-bit signed: 20 bits or more always hold one
-        const bool fits = ib >= 20 || (ib > 0 && imm >= -(1 << (ib - 1)) && imm < (1 << (ib - 1)));
-        code = fits ? ((u64)(u32)imm & ((1ull << ib) - 1ull)) : (1ull << ib);
-    }
-    return (cell << p.cs) | (code << 24) | i;
-}
-__device__ __forceinline__ long long cold_imm(u64 rec, const BucketPlan &p, const BatchDev &b) {
-    const u32 ib = p.cs - 25;
-    const u64 code = (rec >> 24) & ((1ull << (ib + 1)) - 1ull);
-    if ((code >> ib) & 1ull) return (long long)opw_imm(__ldg(&b.opw[(u32)rec & 0xFFFFFFu]));
-    if (ib == 0) return 0;
-    return (long long)(((long long)(code << (64 - ib))) >> (64 - ib));
-}
-
-// Op records: every op becomes a hot record (packed contended-record form,
-// hot id in place of the dense id) or a cold record, both compacted in op
-// order (one decoupled look-back of the two counts per tile); digit
-// histograms of the hot ids and of the cold records' buckets.  Malformed ops
-// and inserts (a batch on this path has no insert payload) are reported as
-// the mark kernel reports them.
-template <int BLOCK, int IPT>
-__global__ void __launch_bounds__(BLOCK) k_gen(BatchDev b, TablesDev T, Scratch s, Counters *ctr, BucketPlan p) {
-    pdl_begin();
-    if (block_err(ctr)) return;
-    constexpr int NW = BLOCK / 32;
-    constexpr u64 TILE = (u64)BLOCK * IPT;
-    constexpr u64 kLow = (1ull << 31) - 1ull;
-    __shared__ u64 s_hk[kHotMapSlots];
-    __shared__ unsigned short s_hid[kHotMapSlots];
-    __shared__ u32 s_hist[2][256];
-    __shared__ u32 s_wh[NW], s_wc[NW];
-    __shared__ u64 s_run, s_base;
-    const u32 H = *(volatile u32 *)&ctr->M;
-    for (u32 i = threadIdx.x; i < kHotMapSlots; i += BLOCK) {
-        const u64 k = H ? s.hot_key[i] : 0ull;
-        s_hk[i] = k;
-        s_hid[i] = k ? (unsigned short)s.hot_id[i] : (unsigned short)0;
-    }
-    for (u32 i = threadIdx.x; i < 2 * 256; i += BLOCK) (&s_hist[0][0])[i] = 0;
-    __syncthreads();
-    const u64 n = b.n_ops;
-    const u32 tiles = (u32)((n + TILE - 1) / TILE);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (;;) {
-        const u32 tile = claim_tile(ctr, SLOT_CLASSIFY);
-        if (tile >= tiles) break;
-        const u64 wbase = (u64)tile * TILE + (u64)warp * 32 * IPT;
-        u64 rec[IPT];
-        u32 hpos[IPT], cpos[IPT], nh = 0, nc = 0;
-        bool hot[IPT], cold[IPT];
-#pragma unroll
-        for (int k = 0; k < IPT; k++) {
-            const u64 i = wbase + (u64)k * 32 + lane;
-            const u64 key = i < n ? op_key_stream(b, i) : 0;
-            const u32 w = i < n ? __ldcs(&b.opw[i]) : 0xFFFFFFFFu;
-            const OpRef r = decode_op(T, key, w);
-            hot[k] = cold[k] = false;
-            rec[k] = 0;
-            if (i < n && !r.valid) {
-                atomicMax(&ctr->bad_op, ~i);
-                set_err(ctr, LTP_E_BADARG);
-            } else if (i < n) {
-                u32 hid = kHotMax;
-                if (H) {
-                    const u64 want = r.cell + 1;
-                    u32 slot = hash_cell(r.cell) & (kHotMapSlots - 1);
-                    for (u32 probe = 0; probe < kHotMapSlots; probe++) {
-                        const u64 cur = s_hk[slot];
-                        if (cur == want) {
-                            hid = s_hid[slot];
-                            break;
-                        }
-                        if (cur == 0) break;
-                        slot = (slot + 1) & (kHotMapSlots - 1);
-                    }
-                }
-                if (hid < kHotMax) {
-                    hot[k] = true;
-                    rec[k] = ((u64)hid << 44) |
-                             ((u64)(opw_kind(w) == LTP_OP_ADD ? ((u32)opw_imm(w) & 0xFFFFFu) : 0u) << 24) | i;
-                    atomicAdd(&s_hist[0][hid & 255u], 1u);
-                } else {
-                    cold[k] = true;
-                    rec[k] = cold_record(r.cell, opw_kind(w), opw_imm(w), i, p);
-                    atomicAdd(&s_hist[1][(u32)(r.cell >> p.cl) & 255u], 1u);
-                }
-            }
-            const u32 bh = __ballot_sync(FULL_MASK, hot[k]), bc = __ballot_sync(FULL_MASK, cold[k]);
-            hpos[k] = nh + __popc(bh & lanemask_lt());
-            cpos[k] = nc + __popc(bc & lanemask_lt());
-            nh += __popc(bh);
-            nc += __popc(bc);
-        }
-        if (lane == 0) {
-            s_wh[warp] = nh;
-            s_wc[warp] = nc;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            u32 rh = 0, rc = 0;
-            for (int w = 0; w < NW; w++) {
-                const u32 a = s_wh[w], c = s_wc[w];
-                s_wh[w] = rh;
-                s_wc[w] = rc;
-                rh += a;
-                rc += c;
-            }
-            s_run = ((u64)rh << 31) | (u64)rc;
-            lookback_publish(s.st_cls, tile, s_run);
-            if (rh) atomicAdd(&ctr->n_c, (u64)rh);
-            if (rc) atomicAdd(&ctr->n_cold, (u64)rc);
-            s_base = lookback_wait(s.st_cls, tile, s_run, ctr);
-        }
-        __syncthreads();
-        const u64 hb = (s_base >> 31) + s_wh[warp], cb = (s_base & kLow) + s_wc[warp];
-#pragma unroll
-        for (int k = 0; k < IPT; k++) {
-            if (hot[k] && LTP_IN_BOUNDS(ctr, hb + hpos[k], s.cap_ops)) s.list[0][hb + hpos[k]] = rec[k];
-            if (cold[k] && LTP_IN_BOUNDS(ctr, cb + cpos[k], s.cap_ops)) s.clist[0][cb + cpos[k]] = rec[k];
-        }
-        __syncthreads();
-    }
-    for (int i = threadIdx.x; i < 256; i += BLOCK) {
-        if (s_hist[0][i]) atomicAdd(&ctr->hist[0][i], s_hist[0][i]);
-        if (s_hist[1][i]) atomicAdd(&ctr->hist[2][i], s_hist[1][i]);
-    }
-}
-
-// The bucket radix pass: cold records in op order -> grouped by bucket (the
-// cell's top 8 bits), stably.
-__global__ void __launch_bounds__(kSortBlock, 3) k_csort(Scratch s, Counters *ctr, BucketPlan p) {
-    pdl_begin();
-    if (block_err(ctr)) return;
-    sort_pass_core<kSortBlock>(s.clist[0], s.clist[1], s.st_csort, nullptr, ctr->hist[2], ctr->n_cold,
-                               (int)(p.cs + p.cl), SLOT_CSORT, true, s.cap_ops, ctr);
-}
-
-// One stable 8-bit radix pass of the block's BLOCK x IPT records in shared
-// memory, src -> dst, by the digit at `shift`.  Warps own contiguous runs of
-// 32 x IPT records; equal digits are ranked with match.any and per-warp
-// counters (a warp's shared-memory atomics take effect in program order, so
-// equal digits keep their order).
-template <int BLOCK, int IPT>
-__device__ __forceinline__ void block_radix_pass(const u64 *src, u64 *dst, int shift, u32 *cnt, u32 *loc, u32 *wsum) {
-    constexpr int NW = BLOCK / 32;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (u32 i = threadIdx.x; i < NW * 256; i += BLOCK) cnt[i] = 0;
-    __syncthreads();
-    const u32 base = (u32)warp * 32 * IPT;
-    u64 e[IPT];
-    u32 rank[IPT], old[IPT], lead[IPT];
-#pragma unroll
-    for (int k = 0; k < IPT; k++) {
-        e[k] = src[base + k * 32 + lane];
-        const u32 d = (u32)(e[k] >> shift) & 255u;
-        const u32 peers = __match_any_sync(FULL_MASK, d);
-        const u32 ld = (u32)__ffs(peers) - 1u;
-        u32 o = 0;
-        if ((u32)lane == ld) o = atomicAdd(&cnt[warp * 256 + d], (u32)__popc(peers));
-        old[k] = o;
-        lead[k] = ld;
-        rank[k] = __popc(peers & lanemask_lt());
-    }
-#pragma unroll
-    for (int k = 0; k < IPT; k++) rank[k] += __shfl_sync(FULL_MASK, old[k], lead[k]);
-    __syncthreads();
-    if (threadIdx.x < 256) {  // per digit: offsets of the warps, then the digit's total
-        const u32 d = threadIdx.x;
-        u32 run = 0;
-        for (int w = 0; w < NW; w++) {
-            const u32 c = cnt[w * 256 + d];
-            cnt[w * 256 + d] = run;
-            run += c;
-        }
-        u32 incl = run;  // exclusive scan of the digit totals
-#pragma unroll
-        for (int dd = 1; dd < 32; dd <<= 1) {
-            const u32 v = __shfl_up_sync(FULL_MASK, incl, dd);
-            if (lane >= dd) incl += v;
-        }
-        if (lane == 31) wsum[warp] = incl;
-        loc[d] = incl - run;
-    }
-    __syncthreads();
-    if (threadIdx.x < 256) {
-        u32 off = 0;
-        for (int w = 0; w < warp; w++) off += wsum[w];
-        loc[threadIdx.x] += off;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < IPT; k++) {
-        const u32 d = (u32)(e[k] >> shift) & 255u;
-        dst[loc[d] + cnt[warp * 256 + d] + rank[k]] = e[k];
-    }
-    __syncthreads();
-}
-
-// The bucket pass: one block per bucket, the bucket's records in op order,
-// chunk by chunk: local stable sort by cell, segmented inclusive scan of the
-// immediates per cell, every op's value = the cell's value before the chunk
-// + its prefix, the cell's new value written back at its last op.  A bucket
-// holds the only ops of its cells, and its chunks run in order in one block,
-// so the table itself carries each cell's value from chunk to chunk.
-template <int BLOCK, int IPT, typename S>
-__global__ void __launch_bounds__(BLOCK) k_bucket(BatchDev b, TablesDev T, Scratch s, Counters *ctr, BucketPlan p) {
-    pdl_begin();
-    if (block_err(ctr)) return;
-    constexpr int NW = BLOCK / 32;
-    constexpr u32 CH = (u32)BLOCK * IPT;
-    constexpr bool WIDE = sizeof(S) == 8;
-    u64 *buf = reinterpret_cast<u64 *>(ltp_dyn_smem);  // 2 x CH records
-    __shared__ u32 s_cnt[NW * 256];
-    __shared__ u32 s_loc[256];
-    __shared__ u32 s_wsum[NW];
-    __shared__ u32 s_bstart[kBuckets + 1];
-    __shared__ u32 s_wf[NW];
-    __shared__ S s_ws[NW];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x < 256) {  // bucket starts: exclusive scan of the bucket histogram
-        const u32 h = ctr->hist[2][threadIdx.x];
-        u32 incl = h;
-#pragma unroll
-        for (int dd = 1; dd < 32; dd <<= 1) {
-            const u32 v = __shfl_up_sync(FULL_MASK, incl, dd);
-            if (lane >= dd) incl += v;
-        }
-        if (lane == 31) s_wsum[warp] = incl;
-        s_loc[threadIdx.x] = incl - h;
-    }
-    __syncthreads();
-    if (threadIdx.x < 256) {
-        u32 off = 0;
-        for (int w = 0; w < warp; w++) off += s_wsum[w];
-        s_bstart[threadIdx.x] = s_loc[threadIdx.x] + off;
-        if (threadIdx.x == 255) s_bstart[256] = s_loc[255] + off + ctr->hist[2][255];
-    }
-    __syncthreads();
-    const u64 *src = s.clist[1];
-    const int passes = (int)((p.cl + 7) / 8);
-    const u64 cell_mask = (1ull << (64 - p.cs)) - 1ull;
-    for (;;) {
-        const u32 bucket = claim_tile(ctr, SLOT_BUCKET);
-        if (bucket >= kBuckets) break;
-        const u32 lo = s_bstart[bucket], hi = s_bstart[bucket + 1];
-        for (u32 c0 = lo; c0 < hi; c0 += CH) {
-            const u32 cnt = min(CH, hi - c0);
-            for (u32 i = threadIdx.x; i < CH; i += BLOCK) buf[i] = i < cnt ? __ldcs(&src[(u64)c0 + i]) : ~0ull;
-            __syncthreads();
-            u64 *cur = buf, *oth = buf + CH;
-            for (int q = 0; q < passes; q++) {
-                block_radix_pass<BLOCK, IPT>(cur, oth, (int)p.cs + 8 * q, s_cnt, s_loc, s_wsum);
-                u64 *t = cur;
-                cur = oth;
-                oth = t;
-            }
-            // segmented inclusive scan by cell over the sorted chunk
-            const u32 wb = (u32)warp * 32 * IPT;
-            S sv[IPT];
-            bool sf[IPT];
-            S cs = 0;
-            u32 cf = 0;
-#pragma unroll
-            for (int k = 0; k < IPT; k++) {
-                const u32 e = wb + (u32)k * 32 + (u32)lane;
-                const bool v = e < cnt;
-                const u64 x = cur[e];
-                const u64 cell = x >> p.cs;
-                const bool head = v && (e == 0 || (cur[e - 1] >> p.cs) != cell);
-                S val = v ? (S)cold_imm(x, p, b) : (S)0;
-                u32 f = head ? 1u : 0u;
-#pragma unroll
-                for (int d = 1; d < 32; d <<= 1) {
-                    const S us = __shfl_up_sync(FULL_MASK, val, d);
-                    const u32 uf = __shfl_up_sync(FULL_MASK, f, d);
-                    if (lane >= d) {
-                        if (!f) val += us;
-                        f |= uf;
-                    }
-                }
-                if (!f) val += cs;
-                f |= cf;
-                sv[k] = val;
-                sf[k] = f != 0;
-                cs = __shfl_sync(FULL_MASK, val, 31);
-                cf = __shfl_sync(FULL_MASK, f, 31);
-            }
-            if (lane == 0) {
-                s_wf[warp] = cf;
-                s_ws[warp] = cs;
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {  // exclusive carries over the warps
-                u32 af = 0;
-                S as = 0;
-                for (int w = 0; w < NW; w++) {
-                    const u32 f = s_wf[w];
-                    const S sm = s_ws[w];
-                    s_wf[w] = af;
-                    s_ws[w] = as;
-                    if (f) {
-                        af = 1;
-                        as = sm;
-                    } else {
-                        as += sm;
-                    }
-                }
-            }
-            __syncthreads();
-            const S carry = s_ws[warp];
-            // every op's value from its cell's value before the chunk ...
-            long long nv[IPT];
-            bool wr[IPT];
-#pragma unroll
-            for (int k = 0; k < IPT; k++) {
-                const u32 e = wb + (u32)k * 32 + (u32)lane;
-                wr[k] = false;
-                nv[k] = 0;
-                if (e >= cnt) continue;
-                const u64 x = cur[e];
-                const u64 cell = (x >> p.cs) & cell_mask;
-                const S tot = sf[k] ? sv[k] : sv[k] + carry;
-                const u32 op = (u32)x & 0xFFFFFFu;
-                bool wd;
-                const long long base = load_cell(cell_ptr(T, cell, &wd), wd);
-                long long val = (long long)((u64)base + (u64)(long long)tot);
-                if (!wd) val = (int32_t)val;
-                nv[k] = val;
-                // the cell's last op in the chunk writes its new value back
-                wr[k] = tot != (S)0 && (e + 1 == cnt || (cur[e + 1] >> p.cs) != (x >> p.cs));
-                if (!LTP_IN_BOUNDS(ctr, op, b.n_ops)) continue;
-                b.out[op] = (int32_t)val;
-                if (WIDE && wd && b.out64) b.out64[op] = val;
-            }
-            __syncthreads();  // ... read by every thread before any write-back
-#pragma unroll
-            for (int k = 0; k < IPT; k++) {
-                if (!wr[k]) continue;
-                const u32 e = wb + (u32)k * 32 + (u32)lane;
-                bool wd;
-                char *cp = cell_ptr(T, (cur[e] >> p.cs) & cell_mask, &wd);
-                store_cell(cp, wd, nv[k]);
-            }
-            __syncthreads();  // this chunk's write-backs before the next chunk's reads
-        }
-    }
-}
-
-// Clean-up of the bucket path's own scratch: the bucket pass's look-back
-// slots and the hot-cell lookup table (the sample table was cleared by the
-// selection kernel; the shared slots by k_finish).
-__global__ void __launch_bounds__(256) k_bclear(Scratch s, Counters *ctr) {
-    pdl_begin();
-    const u64 t_sort = (ctr->n_cold + kSortTile - 1) / kSortTile;
-    const u64 gsz = (u64)gridDim.x * blockDim.x, g0 = (u64)blockIdx.x * blockDim.x + threadIdx.x;
-    for (u64 j = g0; j < t_sort * 256; j += gsz) s.st_csort[j] = 0;
-    for (u64 j = g0; j < kHotMapSlots; j += gsz) {
-        s.hot_key[j] = 0;
-        s.hot_id[j] = 0;
-    }
-}
-
-// ============================================================================
 // host-side launch plans
 // ============================================================================
 template <typename K>
@@ -2148,26 +1704,6 @@ static void pick_front(const Tuning &t, front_fn *mark, front_fn *classify) {
 
 static int capped(int grid, u64 upper) { return (int)((u64)grid < upper ? (u64)grid : (upper ? upper : 1)); }
 
-// Does the batch run on the cell-bucket path?  Its size bucket is tuned to
-// it, the rule is the ordered one, the batch has no insert payload and at
-// most 2^24 ops (op indices fit its records), and the context has the
-// path's scratch.
-static bool bucket_path_eligible(const Launch &L, const BatchDev &b, const Scratch &s) {
-    return (L.tune.flags & LTP_TUNE_BUCKET) && L.rule == LTP_RULE_ORDERED && b.payload_len == 0 && b.n_ops > 0 &&
-           b.n_ops <= (1ull << 24) && s.clist[0] && s.clist[1] && s.smp_key && s.hot_key && s.st_csort;
-}
-
-// Record layout of the cell-bucket path for the context's cell space.
-static BucketPlan bucket_plan(const Scratch &s) {
-    const u64 cells = s.n_words * 32ull;  // cell ids are below this
-    int cb = 1;
-    while (cb < 40 && (cells - 1) >> cb) cb++;
-    BucketPlan p;
-    p.cs = (u32)(64 - cb);
-    p.cl = cb > 8 ? (u32)(cb - 8) : 0u;
-    return p;
-}
-
 cudaError_t launch_execute(const Launch &L_in, const BatchDev &b_in, const TablesDev &T, const Scratch &s,
                            Counters *ctr) {
     TraceRange tr("launch batch kernels");
@@ -2191,68 +1727,15 @@ cudaError_t launch_execute(const Launch &L_in, const BatchDev &b_in, const Table
     };
     mark_ev(0);
     if (L.stall) k_stall<<<1, 1, 0, L.stream>>>(ctr, L.stall_ms);
-    cudaError_t le = cudaSuccess;  // the first failed launch
-    auto chk = [&](cudaError_t e) {
-        if (le == cudaSuccess) le = e;
-    };
-    if (bucket_path_eligible(L, b, s)) {
-        // cell-bucket path; stage events: 0 hot sampling and selection, 1 op
-        // records, 2 bucket radix pass, 3 bucket pass, 4 hot pre-batch values,
-        // 5 hot radix pass, 7 hot segmented scan, 9 clean-up
-        const BucketPlan p = bucket_plan(s);
-        static int g_gen = 0, g_srt = 0, g_bkt32 = 0, g_bkt64 = 0, g_app = 0, sms = 0;
-        constexpr size_t kBktSmem = 2ull * kBktChunk * sizeof(u64);
-        if (sms != L.num_sms) {
-            chk(cudaFuncSetAttribute(k_bucket<kBktBlock, kBktIpt, u32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)kBktSmem));
-            chk(cudaFuncSetAttribute(k_bucket<kBktBlock, kBktIpt, u64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)kBktSmem));
-            g_gen = occ_grid(k_gen<kGenBlock, kGenIpt>, kGenBlock, L.num_sms);
-            g_srt = occ_grid(k_csort, kSortBlock, L.num_sms);
-            g_bkt32 = occ_grid(k_bucket<kBktBlock, kBktIpt, u32>, kBktBlock, L.num_sms, kBktSmem);
-            g_bkt64 = occ_grid(k_bucket<kBktBlock, kBktIpt, u64>, kBktBlock, L.num_sms, kBktSmem);
-            g_app = occ_grid(k_apply<u64>, kApplyBlock, L.num_sms);
-            sms = L.num_sms;
-        }
-        const u64 n = b.n_ops;
-        const int g_small = capped(L.num_sms * 8, (n / kSampleStride + 255) / 256 + 1);
-        chk(launch_k(L.pdl, k_hsample, g_small, 256, 0, L.stream, b, T, s, ctr));
-        chk(launch_k(L.pdl, k_hselect, L.num_sms * 8, 256, 0, L.stream, s, ctr));
-        mark_ev(1);
-        chk(launch_k(L.pdl, k_gen<kGenBlock, kGenIpt>, capped(g_gen, (n + kGenTile - 1) / kGenTile), kGenBlock, 0,
-                     L.stream, b, T, s, ctr, p));
-        mark_ev(2);
-        chk(launch_k(L.pdl, k_csort, capped(g_srt, (n + kSortTile - 1) / kSortTile), kSortBlock, 0, L.stream, s, ctr,
-                     p));
-        mark_ev(3);
-        if (T.any_wide)
-            chk(launch_k(L.pdl, k_bucket<kBktBlock, kBktIpt, u64>, capped(g_bkt64, kBuckets), kBktBlock, kBktSmem,
-                         L.stream, b, T, s, ctr, p));
-        else
-            chk(launch_k(L.pdl, k_bucket<kBktBlock, kBktIpt, u32>, capped(g_bkt32, kBuckets), kBktBlock, kBktSmem,
-                         L.stream, b, T, s, ctr, p));
-        mark_ev(4);
-        chk(launch_k(L.pdl, k_dbase, L.num_sms * 8, 256, 0, L.stream, T, s, ctr, 0));
-        mark_ev(5);
-        chk(launch_k(L.pdl, k_sort_pass<0>, capped(g_srt, (n + kSortTile - 1) / kSortTile), kSortBlock, 0, L.stream,
-                     s, ctr, n));
-        mark_ev(6);
-        mark_ev(7);
-        chk(launch_k(L.pdl, T.any_wide ? k_apply<u64> : k_apply<u32>, capped(g_app, (n + kApplyTile - 1) / kApplyTile),
-                     kApplyBlock, 0, L.stream, b, T, s, ctr));
-        mark_ev(8);
-        mark_ev(9);
-        chk(launch_k(L.pdl, k_bclear, L.num_sms * 8, 256, 0, L.stream, s, ctr));
-        chk(launch_k(L.pdl, k_finish<32>, L.num_sms * 8, 256, 0, L.stream, b, T, s, ctr, L.rule));
-        mark_ev(10);
-        const cudaError_t e = cudaGetLastError();
-        return le != cudaSuccess ? le : e;
-    }
     front_fn f_mark, f_cls;
     pick_front(L.tune, &f_mark, &f_cls);
     // conflict-word width of every kernel of the batch (an unsupported tiling
     // falls back to 256 x 4 with 32-cell words in pick_front)
     const bool wide_words = L.tune.word_bits == 64 && tiling_supported(L.tune.block, L.tune.ipt, 64);
+    cudaError_t le = cudaSuccess;  // the first failed launch
+    auto chk = [&](cudaError_t e) {
+        if (le == cudaSuccess) le = e;
+    };
     chk(f_mark(L, b, T, s, ctr));
     mark_ev(1);
     {

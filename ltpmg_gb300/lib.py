@@ -24,9 +24,6 @@ FLAG_STAGE_TIMING = 1
 MODE_STREAM, MODE_GRAPH, MODE_PERSISTENT = 0, 1, 2
 # per-kernel stage times of a batch (ordered rule; under the priority rule
 # stages 2-4 are the min-writer, abort and execute kernels)
-# the cell-bucket path (TUNE_BUCKET)
-BUCKET_STAGE_NAMES = ["hot_select", "gen", "bucket_sort", "bucket", "hot_dbase", "hot_sort", "unused6", "hot_apply",
-                      "unused8", "finish", "unused10", "total"]
 STAGE_NAMES = ["mark", "ids", "classify", "sort_pass0", "sort_pass1", "sort_pass2", "sort_pass3", "apply",
                "insert", "finish", "unused", "total"]
 
@@ -50,12 +47,11 @@ class Stats(ctypes.Structure):
     _fields_ = [("txns", ctypes.c_uint64), ("ops", ctypes.c_uint64), ("committed", ctypes.c_uint64),
                 ("aborted", ctypes.c_uint64), ("contended_ops", ctypes.c_uint64),
                 ("contended_cells", ctypes.c_uint64), ("touched_words", ctypes.c_uint64),
-                ("bytes_algorithmic", ctypes.c_uint64), ("ms_stage", ctypes.c_float * 12),
-                ("bucket_ops", ctypes.c_uint64), ("path", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("bytes_algorithmic", ctypes.c_uint64), ("ms_stage", ctypes.c_float * 12)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "ms_stage"}
-        d["ms_stage"] = dict(zip(BUCKET_STAGE_NAMES if self.path == 1 else STAGE_NAMES, list(self.ms_stage)))
+        d["ms_stage"] = dict(zip(STAGE_NAMES, list(self.ms_stage)))
         return d
 
 
@@ -100,7 +96,6 @@ class Tuning(ctypes.Structure):
 
 
 TUNE_MARK_PRECHECK = 1
-TUNE_BUCKET = 2
 
 
 _lib = None

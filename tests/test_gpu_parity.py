@@ -26,14 +26,10 @@ def lib_loaded():
     return G.load()
 
 
-def run_and_check(rule, rows, cols, batches, seed=SEED, fixed=0, ctx_kwargs=None, tab0=None, threads=0, tuning=None):
+def run_and_check(rule, rows, cols, batches, seed=SEED, fixed=0, ctx_kwargs=None, tab0=None, threads=0):
     """Executes the batches in order on a fresh context and compares each
-    batch's outputs and the final table with the oracle.  tuning: (block,
-    ipt, word_bits, flags) for every size bucket."""
+    batch's outputs and the final table with the oracle."""
     with G.Context(device=0, rule=rule, **(ctx_kwargs or {})) as ctx:
-        if tuning:
-            for bucket in range(64):
-                ctx.set_tuning(bucket, *tuning)
         t = ctx.create_table(rows, cols)
         if tab0 is None:
             ctx.fill_seeded(t, seed)
