@@ -1056,7 +1056,9 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
     if (block_err(ctr)) return;
     const u64 n = ctr->n_c;
     const u32 tiles = (u32)((n + kApplyTile - 1) / kApplyTile);
-    const u64 *list = s.list[sort_passes_dev(ctr->M) & 1];
+    // a select, not s.list[runtime index]: indexing the parameter's pointer
+    // pair at run time copies the whole Scratch to every thread's stack
+    const u64 *list = (sort_passes_dev(ctr->M) & 1) ? s.list[1] : s.list[0];
     const bool packed = rec_packed(ctr->M, b.n_ops);
     constexpr int NW = BLK / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1534,7 +1536,7 @@ __device__ __forceinline__ void phase_finish(const BatchDev &b, const TablesDev 
     for (u64 j = g0; j < t_apply; j += gsz) s.st_apply[j] = 0;
     const int passes = sort_passes_dev(ctr->M);
     if (passes > 0) {
-        u32 *st = s.st_sort[(passes - 1) & 1];
+        u32 *st = ((passes - 1) & 1) ? s.st_sort[1] : s.st_sort[0];  // select: see phase_apply
         const u64 t_sort = (nc + kSortTile - 1) / kSortTile;
         for (u64 j = g0; j < t_sort * 256; j += gsz) st[j] = 0;
     }
