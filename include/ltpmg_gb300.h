@@ -523,7 +523,7 @@ int ltp_debug_stall_next(ltp_ctx *ctx, uint32_t ms);
  * this entry point on that device again in the same process. */
 #define LTP_NOALLOC_MAX_OPS (1ull << 18)
 #define LTP_NOALLOC_MAX_CELLS (1ull << 23)
-#define LTP_NOALLOC_SCRATCH_BYTES 16076288ull
+#define LTP_NOALLOC_SCRATCH_BYTES 18173696ull
 int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table, uint64_t rows_cap, uint64_t n_rows,
                         uint32_t n_cols, uint64_t n_txns, const uint32_t *txn_first, uint32_t ops_per_txn,
                         uint64_t n_ops, const uint64_t *keys, const uint32_t *opw, int32_t *out, uint8_t *commit,

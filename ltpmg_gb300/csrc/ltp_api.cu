@@ -79,7 +79,9 @@ void free_scratch_ops(Scratch &s) {
 
 void free_scratch_words(Scratch &s) {
     cudaFree(s.words);
+    cudaFree(s.cview);
     s.words = nullptr;
+    s.cview = nullptr;
 }
 
 // Sizes the bitmaps to the cell space and the per-op scratch to n_ops.
@@ -92,6 +94,8 @@ int ensure_scratch(ltp_ctx *ctx, uint64_t n_ops) {
         // one spare entry: the 64-cell layout of the same buffer rounds up
         CK(dalloc(&s.words, words + 1));
         CK(cudaMemset(s.words, 0, (words + 1) * sizeof(WordState)));
+        CK(dalloc(&s.cview, words + 1));  // 8 B per 32 cells; the 64-cell view takes 16 B per word
+        CK(cudaMemset(s.cview, 0, (words + 1) * sizeof(uint2)));
         ctx->alloc_words = words;
     }
     s.n_words = words;

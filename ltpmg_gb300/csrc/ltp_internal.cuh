@@ -98,12 +98,13 @@ struct __align__(16) WordState {
     u32 touch;   // cell touched at least once in the batch
     u32 wbits;   // cell written (RMW) at least once
     u32 multi;   // cell touched at least twice
-    u32 prefix;  // dense id of the word's first contended cell (multi & wbits)
+    u32 pad;     // keeps a word to one 16-byte access (the dense ids live in Scratch::cview)
 };
 
 // Scratch owned by the context, sized by the cell space and the batch capacity.
 struct Scratch {
     WordState *words; // [n_words]
+    uint2 *cview;     // [n_words + 1] per 32 cells {contended mask, first dense id} (16 B per 64-cell word)
     u32 *tw_list;   // [cap_ops] touched words
     u64 *list[2];   // [cap_ops] contended-op records, ping-pong for the sort
     u64 *dcell;     // [cap_ops] cell of each contended-cell id

@@ -204,8 +204,9 @@ __device__ __forceinline__ OpRef decode_op(const TablesDev &T, u64 key, u32 w) {
 // Cell values are handled as 64-bit; int32 cells are sign-extended on load and
 // truncated on store, which is exactly 32-bit two's-complement arithmetic.
 // ---- L2 eviction-priority hints ---------------------------------------------
-// Conflict words are re-read by later kernels of the batch: keep them in L2.
-// Uncontended table cells are touched once: let them leave L2 first.
+// Conflict words (the mark kernel's atomics) and their compact view (read
+// by classify) are touched by every batch: keep them in L2.  Uncontended
+// table cells are touched once: let them leave L2 first.
 __device__ __forceinline__ u64 pol_evict_last() {
     u64 p;
     asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
@@ -231,6 +232,29 @@ __device__ __forceinline__ uint4 ld_word_hint(const void *ptr, u64 pol) {
                  : "l"(ptr), "l"(pol));
     return v;
 }
+// OR into a conflict word with an L2 eviction-priority hint: with the old
+// value (atom) or without (red)
+__device__ __forceinline__ u32 atom_or_hint(u32 *p, u32 v, u64 pol) {
+    u32 old;
+    asm volatile("atom.global.or.L2::cache_hint.b32 %0, [%1], %2, %3;" : "=r"(old) : "l"(p), "r"(v), "l"(pol) : "memory");
+    return old;
+}
+__device__ __forceinline__ u64 atom_or_hint(u64 *p, u64 v, u64 pol) {
+    u64 old;
+    asm volatile("atom.global.or.L2::cache_hint.b64 %0, [%1], %2, %3;" : "=l"(old) : "l"(p), "l"(v), "l"(pol) : "memory");
+    return old;
+}
+__device__ __forceinline__ void red_or_hint(u32 *p, u32 v, u64 pol) {
+    asm volatile("red.global.or.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void red_or_hint(u64 *p, u64 v, u64 pol) {
+    asm volatile("red.global.or.L2::cache_hint.b64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ uint2 ld_view_hint(const void *ptr, u64 pol) {
+    uint2 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;" : "=r"(v.x), "=r"(v.y) : "l"(ptr), "l"(pol));
+    return v;
+}
 // ---- programmatic dependent launch -------------------------------------------
 // The batch kernels are launched with programmatic stream serialization, so a
 // kernel may be launched while its predecessor drains.  Each one first waits
@@ -245,14 +269,22 @@ __device__ __forceinline__ void pdl_begin() {
 
 // ---- conflict words ----------------------------------------------------------
 // A conflict word covers 32 cells (WordState, 16 B: touched, written and
-// touched-twice masks, the word's first contended id) or 64 cells
-// (WordState64, 32 B: written and touched-twice masks in its first 16 bytes,
-// then the touched mask and the first id).  Both take 16 bytes per 32 cells,
+// touched-twice masks and a spare word) or 64 cells (WordState64, 32 B:
+// written and touched-twice masks in its first 16 bytes, then the touched
+// mask and a spare).  Both take 16 bytes per 32 cells,
 // so one scratch buffer serves either width; the width is a tuning knob of
 // the stream and graph launches (the persistent kernel uses 32).
+//
+// The ids kernel also writes a compact view of every word that holds a
+// contended cell: its contended mask (written & touched twice) and its first
+// dense id -- 8 B per 32 cells (uint2), 16 B per 64 (uint4) in the cview
+// buffer.  Words without a contended cell keep the cleared view {0, 0}.  The
+// executing kernels read only the view: half the footprint of the words (42 MB
+// for 2^24 x 10 cells) stays in L2 far better while the table streams past.
+// The finish kernel clears the views through the contended cells' list.
 struct WordState64 {
     u64 wbits, multi, touch;
-    u32 prefix, pad;
+    u64 pad;
 };
 
 template <int WB>
@@ -264,17 +296,9 @@ struct Wd<32> {
     struct V {
         u32 wbits, multi, prefix;
     };
-    static __device__ __forceinline__ V load_hint(const Scratch &s, u64 w, u64 pol) {
-        const uint4 v = ld_word_hint(&s.words[w], pol);
-        return V{v.y, v.z, v.w};
-    }
-    static __device__ __forceinline__ V load_ro(const Scratch &s, u64 w) {
-        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(&s.words[w]));
-        return V{v.y, v.z, v.w};
-    }
-    static __device__ __forceinline__ V load(const Scratch &s, u64 w) {
+    static __device__ __forceinline__ V load(const Scratch &s, u64 w) {  // masks only (prefix 0)
         const uint4 v = *reinterpret_cast<const uint4 *>(&s.words[w]);
-        return V{v.y, v.z, v.w};
+        return V{v.y, v.z, 0u};
     }
     // written and touched-twice masks, as the mark kernel's pre-check reads them
     static __device__ __forceinline__ void load_relaxed(const Scratch &s, u64 w, T *wbits, T *multi) {
@@ -285,10 +309,22 @@ struct Wd<32> {
     static __device__ __forceinline__ T *touch(const Scratch &s, u64 w) { return &s.words[w].touch; }
     static __device__ __forceinline__ T *wbits(const Scratch &s, u64 w) { return &s.words[w].wbits; }
     static __device__ __forceinline__ T *multi(const Scratch &s, u64 w) { return &s.words[w].multi; }
-    static __device__ __forceinline__ u32 *prefix(const Scratch &s, u64 w) { return &s.words[w].prefix; }
     static __device__ __forceinline__ void clear(const Scratch &s, u64 w) {
         *reinterpret_cast<uint4 *>(&s.words[w]) = make_uint4(0u, 0u, 0u, 0u);
     }
+    // the compact view, as V{contended mask, all ones, first id}
+    static __device__ __forceinline__ V load_view(const Scratch &s, u64 w, u64 pol) {
+        const uint2 v = ld_view_hint(&s.cview[w], pol);
+        return V{v.x, ~0u, v.y};
+    }
+    static __device__ __forceinline__ V load_view_ro(const Scratch &s, u64 w) {
+        const uint2 v = __ldg(&s.cview[w]);
+        return V{v.x, ~0u, v.y};
+    }
+    static __device__ __forceinline__ void set_view(const Scratch &s, u64 w, T cw, u32 first) {
+        s.cview[w] = make_uint2(cw, first);
+    }
+    static __device__ __forceinline__ void clear_view(const Scratch &s, u64 w) { s.cview[w] = make_uint2(0u, 0u); }
     static __device__ __forceinline__ u64 n_words(const Scratch &s) { return s.n_words; }
     static __device__ __forceinline__ int popc(T x) { return __popc(x); }
     static __device__ __forceinline__ int ffs(T x) { return __ffs(x); }
@@ -304,19 +340,9 @@ struct Wd<64> {
     static __device__ __forceinline__ WordState64 *at(const Scratch &s, u64 w) {
         return reinterpret_cast<WordState64 *>(s.words) + w;
     }
-    static __device__ __forceinline__ V load_hint(const Scratch &s, u64 w, u64 pol) {
-        const uint4 a = ld_word_hint(at(s, w), pol);
-        const uint4 b = ld_word_hint(reinterpret_cast<const char *>(at(s, w)) + 16, pol);
-        return V{((u64)a.y << 32) | a.x, ((u64)a.w << 32) | a.z, b.z};
-    }
-    static __device__ __forceinline__ V load_ro(const Scratch &s, u64 w) {
-        const uint4 a = __ldg(reinterpret_cast<const uint4 *>(at(s, w)));
-        const u32 pre = __ldg(&at(s, w)->prefix);
-        return V{((u64)a.y << 32) | a.x, ((u64)a.w << 32) | a.z, pre};
-    }
-    static __device__ __forceinline__ V load(const Scratch &s, u64 w) {
+    static __device__ __forceinline__ V load(const Scratch &s, u64 w) {  // masks only (prefix 0)
         const WordState64 *p = at(s, w);
-        return V{p->wbits, p->multi, p->prefix};
+        return V{p->wbits, p->multi, 0u};
     }
     static __device__ __forceinline__ void load_relaxed(const Scratch &s, u64 w, T *wbits, T *multi) {
         const uint4 a = ld_word_relaxed(at(s, w));
@@ -326,12 +352,24 @@ struct Wd<64> {
     static __device__ __forceinline__ T *touch(const Scratch &s, u64 w) { return &at(s, w)->touch; }
     static __device__ __forceinline__ T *wbits(const Scratch &s, u64 w) { return &at(s, w)->wbits; }
     static __device__ __forceinline__ T *multi(const Scratch &s, u64 w) { return &at(s, w)->multi; }
-    static __device__ __forceinline__ u32 *prefix(const Scratch &s, u64 w) { return &at(s, w)->prefix; }
     static __device__ __forceinline__ void clear(const Scratch &s, u64 w) {
         uint4 *p = reinterpret_cast<uint4 *>(at(s, w));
         p[0] = make_uint4(0u, 0u, 0u, 0u);
         p[1] = make_uint4(0u, 0u, 0u, 0u);
     }
+    static __device__ __forceinline__ uint4 *view(const Scratch &s, u64 w) { return reinterpret_cast<uint4 *>(s.cview) + w; }
+    static __device__ __forceinline__ V load_view(const Scratch &s, u64 w, u64 pol) {
+        const uint4 v = ld_word_hint(view(s, w), pol);
+        return V{((u64)v.y << 32) | v.x, ~0ull, v.z};
+    }
+    static __device__ __forceinline__ V load_view_ro(const Scratch &s, u64 w) {
+        const uint4 v = __ldg(view(s, w));
+        return V{((u64)v.y << 32) | v.x, ~0ull, v.z};
+    }
+    static __device__ __forceinline__ void set_view(const Scratch &s, u64 w, T cw, u32 first) {
+        *view(s, w) = make_uint4((u32)cw, (u32)(cw >> 32), first, 0u);
+    }
+    static __device__ __forceinline__ void clear_view(const Scratch &s, u64 w) { *view(s, w) = make_uint4(0u, 0u, 0u, 0u); }
     // 64-cell words over the same buffer: half as many, rounded up
     static __device__ __forceinline__ u64 n_words(const Scratch &s) { return (s.n_words + 1) / 2; }
     static __device__ __forceinline__ int popc(T x) { return __popcll(x); }
@@ -410,7 +448,7 @@ __device__ __forceinline__ bool insert_link_ok(const BatchDev &b, const TableDev
 template <int WB>
 __device__ __forceinline__ bool contended_id(const Scratch &s, u64 cell, u32 *m) {
     typedef typename Wd<WB>::T WT;
-    const typename Wd<WB>::V v = Wd<WB>::load_ro(s, cell >> Wd<WB>::kShift);
+    const typename Wd<WB>::V v = Wd<WB>::load_view_ro(s, cell >> Wd<WB>::kShift);
     const WT cw = v.wbits & v.multi, bit = (WT)1 << (cell & (WB - 1));
     *m = v.prefix + Wd<WB>::popc(cw & (bit - 1));
     return (cw & bit) != 0;
@@ -452,6 +490,9 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
     typedef typename Wd<WB>::T WT;
     if (block_err(ctr)) return;
     const bool precheck = (b.flags & LTP_TUNE_MARK_PRECHECK) != 0u;
+    // the words stay in L2 from batch to batch (hot words are touched by
+    // every batch); the executing kernels read only the compact view
+    const u64 pol_keep = pol_evict_last();
     constexpr u32 TILE = (u32)BLOCK * IPT;
     constexpr u32 H = 2 * TILE;  // at most TILE distinct words: load factor <= 1/2
     u32 *hk = ltp_dyn_smem;  // H keys, then 3 * H masks (dynamic)
@@ -542,7 +583,7 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
             const u32 j = threadIdx.x + q * BLOCK;
             const bool need = fw[q] != kEmptyKey && ((ft[q] & ~cur_m[q]) || (hw[j] & ~cur_w[q])) &&
                               LTP_IN_BOUNDS(ctr, fw[q], Wd<WB>::n_words(s));
-            old[q] = need ? atomicOr(Wd<WB>::touch(s, fw[q]), ft[q]) : 0;
+            old[q] = need ? atom_or_hint(Wd<WB>::touch(s, fw[q]), ft[q], pol_keep) : 0;
             if (need) dmask |= 1u << q;
         }
         u32 fmask = 0, nfirst = 0;
@@ -551,8 +592,8 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
             const u32 j = threadIdx.x + q * BLOCK;
             if (dmask & (1u << q)) {
                 const WT m = (old[q] & ft[q]) | hd[j];
-                if (m & ~cur_m[q]) atomicOr(Wd<WB>::multi(s, fw[q]), m);
-                if (hw[j] & ~cur_w[q]) atomicOr(Wd<WB>::wbits(s, fw[q]), hw[j]);
+                if (m & ~cur_m[q]) red_or_hint(Wd<WB>::multi(s, fw[q]), m, pol_keep);
+                if (hw[j] & ~cur_w[q]) red_or_hint(Wd<WB>::wbits(s, fw[q]), hw[j], pol_keep);
                 if (old[q] == 0) {
                     fmask |= 1u << q;
                     nfirst++;
@@ -690,8 +731,8 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             u64 j = t0 + (u64)k * BLK;
-            if (j < n) {
-                *Wd<WB>::prefix(s, wd[k]) = (u32)pre;
+            if (j < n && cw[k]) {
+                Wd<WB>::set_view(s, wd[k], cw[k], (u32)pre);
                 WT bits = cw[k];
                 while (bits) {  // the cells' values are read by k_dbase, fully parallel
                     const int bpos = Wd<WB>::ffs(bits) - 1;
@@ -771,7 +812,7 @@ __device__ __forceinline__ void phase_classify(const BatchDev &b, const TablesDe
             u64 i = wbase + (u64)k * 32 + lane;
             r[k] = decode_op(T, key[k], w[k]);
             r[k].valid = r[k].valid && i < n;
-            if (r[k].valid) ws[k] = Wd<WB>::load_hint(s, r[k].cell >> Wd<WB>::kShift, pol_keep);
+            if (r[k].valid) ws[k] = Wd<WB>::load_view(s, r[k].cell >> Wd<WB>::kShift, pol_keep);
             else ws[k].wbits = ws[k].multi = 0, ws[k].prefix = 0;
         }
         u64 rec[IPT];
@@ -1531,6 +1572,14 @@ __device__ __forceinline__ void phase_finish(const BatchDev &b, const TablesDev 
         for (u64 j = g0; j < ntw; j += gsz)
             if (LTP_IN_BOUNDS(ctr, s.tw_list[j], nw)) Wd<WB>::clear(s, s.tw_list[j]);
     }
+    // the compact views of the words that held contended cells, found
+    // through the contended cells themselves
+    const u64 M = ctr->M;
+    for (u64 m = g0; m < M; m += gsz) {
+        if (!LTP_IN_BOUNDS(ctr, m, s.cap_ops)) continue;
+        const u64 w = (s.dcell[m] & ~(1ull << 63)) >> Wd<WB>::kShift;
+        if (LTP_IN_BOUNDS(ctr, w, nw)) Wd<WB>::clear_view(s, w);
+    }
     const u64 nc = ctr->n_c;
     const u64 t_apply = (nc + kApplyTile - 1) / kApplyTile;
     for (u64 j = g0; j < t_apply; j += gsz) s.st_apply[j] = 0;
@@ -1944,6 +1993,7 @@ int persistent_grid(int num_sms) {
 
 cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s) {
     cudaMemsetAsync(s.words, 0, (s.n_words + 1) * sizeof(WordState), st);  // + the 64-cell layout's spare entry
+    cudaMemsetAsync(s.cview, 0, (s.n_words + 1) * sizeof(uint2), st);
     cudaMemsetAsync(s.st_sort[0], 0, s.cap_sort_tiles * 256 * 4, st);
     cudaMemsetAsync(s.st_sort[1], 0, s.cap_sort_tiles * 256 * 4, st);
     cudaMemsetAsync(s.st_cls, 0, s.cap_tiles * 8, st);

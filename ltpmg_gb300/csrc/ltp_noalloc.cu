@@ -44,7 +44,8 @@ constexpr u64 align256(u64 x) { return (x + 255) & ~255ull; }
 
 // byte offsets of the scratch regions inside the static array
 constexpr u64 kOffWords = 0;
-constexpr u64 kOffTw = kOffWords + align256(kNaWords * sizeof(WordState));
+constexpr u64 kOffView = kOffWords + align256(kNaWords * sizeof(WordState));
+constexpr u64 kOffTw = kOffView + align256(kNaWords * sizeof(uint2));
 constexpr u64 kOffList0 = kOffTw + align256(kNaMaxOps * 4);
 constexpr u64 kOffList1 = kOffList0 + align256(kNaMaxOps * 8);
 constexpr u64 kOffDcell = kOffList1 + align256(kNaMaxOps * 8);
@@ -120,6 +121,7 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     Scratch s;
     memset(&s, 0, sizeof(s));
     s.words = (WordState *)(base + kOffWords);
+    s.cview = (uint2 *)(base + kOffView);
     s.tw_list = (u32 *)(base + kOffTw);
     s.list[0] = (u64 *)(base + kOffList0);
     s.list[1] = (u64 *)(base + kOffList1);
