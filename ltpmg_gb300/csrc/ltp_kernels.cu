@@ -250,6 +250,11 @@ __device__ __forceinline__ void red_or_hint(u32 *p, u32 v, u64 pol) {
 __device__ __forceinline__ void red_or_hint(u64 *p, u64 v, u64 pol) {
     asm volatile("red.global.or.L2::cache_hint.b64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
 }
+__device__ __forceinline__ void st_word_hint(void *ptr, uint4 v, u64 pol) {
+    asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(ptr), "r"(v.x), "r"(v.y), "r"(v.z),
+                 "r"(v.w), "l"(pol)
+                 : "memory");
+}
 __device__ __forceinline__ uint2 ld_view_hint(const void *ptr, u64 pol) {
     uint2 v;
     asm volatile("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;" : "=r"(v.x), "=r"(v.y) : "l"(ptr), "l"(pol));
@@ -312,6 +317,9 @@ struct Wd<32> {
     static __device__ __forceinline__ void clear(const Scratch &s, u64 w) {
         *reinterpret_cast<uint4 *>(&s.words[w]) = make_uint4(0u, 0u, 0u, 0u);
     }
+    static __device__ __forceinline__ void clear_hint(const Scratch &s, u64 w, u64 pol) {
+        st_word_hint(&s.words[w], make_uint4(0u, 0u, 0u, 0u), pol);
+    }
     // the compact view, as V{contended mask, all ones, first id}
     static __device__ __forceinline__ V load_view(const Scratch &s, u64 w, u64 pol) {
         const uint2 v = ld_view_hint(&s.cview[w], pol);
@@ -356,6 +364,11 @@ struct Wd<64> {
         uint4 *p = reinterpret_cast<uint4 *>(at(s, w));
         p[0] = make_uint4(0u, 0u, 0u, 0u);
         p[1] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    static __device__ __forceinline__ void clear_hint(const Scratch &s, u64 w, u64 pol) {
+        uint4 *p = reinterpret_cast<uint4 *>(at(s, w));
+        st_word_hint(p, make_uint4(0u, 0u, 0u, 0u), pol);
+        st_word_hint(p + 1, make_uint4(0u, 0u, 0u, 0u), pol);
     }
     static __device__ __forceinline__ uint4 *view(const Scratch &s, u64 w) { return reinterpret_cast<uint4 *>(s.cview) + w; }
     static __device__ __forceinline__ V load_view(const Scratch &s, u64 w, u64 pol) {
@@ -485,6 +498,14 @@ __device__ __forceinline__ u32 hash_word(u32 w) { return (w * 0x9E3779B1u) ^ (w 
 template <int BLOCK, int IPT, int WB>
 constexpr size_t mark_smem_bytes() { return 2ull * BLOCK * IPT * (4 + 3 * (WB / 8)); }
 
+// A batch whose keys and opwords take most of the L2 cannot keep them there
+// until classify reads them again: mark streams them (evict-first), so they
+// do not push the conflict words out (Zipf, 2^24 ops with 32-bit keys, 134
+// MB: mark 0.300 -> 0.285 ms).  A smaller batch loads them normally and
+// classify finds them in L2 (order entry, 5.5 M ops with 64-bit keys, 66 MB:
+// streaming them cost 2%).
+constexpr u64 kStreamOpsBytes = 96ull << 20;
+
 template <int BLOCK, int IPT, int WB>
 __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
     typedef typename Wd<WB>::T WT;
@@ -493,6 +514,7 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
     // the words stay in L2 from batch to batch (hot words are touched by
     // every batch); the executing kernels read only the compact view
     const u64 pol_keep = pol_evict_last();
+    const bool stream_ops = b.n_ops * ((b.keys32 ? 4ull : 8ull) + 4ull) > kStreamOpsBytes;
     constexpr u32 TILE = (u32)BLOCK * IPT;
     constexpr u32 H = 2 * TILE;  // at most TILE distinct words: load factor <= 1/2
     u32 *hk = ltp_dyn_smem;  // H keys, then 3 * H masks (dynamic)
@@ -514,8 +536,8 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             u64 i = wbase + (u64)k * 32 + lane;
-            key[k] = i < n ? op_key(b, i) : 0;
-            w[k] = i < n ? b.opw[i] : 0xFFFFFFFFu;
+            key[k] = i < n ? (stream_ops ? op_key_stream(b, i) : op_key(b, i)) : 0;
+            w[k] = i < n ? (stream_ops ? __ldcs(&b.opw[i]) : b.opw[i]) : 0xFFFFFFFFu;
         }
         __syncthreads();
 #pragma unroll
