@@ -152,10 +152,10 @@ def load_peaks():
 # workload (profiles/batch_kernels_zipf.md, profiles/k_mark_insert_tpcc.md);
 # a launch's traffic is this figure times the units it processed
 MEASURED_TRAFFIC = {
-    ("zipf", "classify"): (41.2, "ops"),  # 32-bit keys
-    ("zipf", "mark"): (17.7, "ops"),  # 32-bit keys
-    ("zipf", "apply"): (33.3, "contended_ops"),
-    ("zipf", "ids"): (8.0, "ops"),  # k_ids + k_dbase
+    ("zipf", "classify"): (37.4, "ops"),  # 32-bit keys
+    ("zipf", "mark"): (14.1, "ops"),  # 32-bit keys
+    ("zipf", "apply"): (30.3, "contended_ops"),
+    ("zipf", "ids"): (6.9, "ops"),  # k_ids + k_dbase
     ("tpcc", "insert"): (59.3, "ops"),  # 32-bit keys
     ("tpcc", "mark"): (15.7, "ops"),  # 32-bit keys
 }
@@ -172,15 +172,16 @@ def random_access_roof(G, device, sh, st, avg, config):
     workload's table and conflict-word sizes) give a floor time; frac = floor
     over the measured kernel time."""
     table_b = sh["rows"] * sh["cols"] * 4
-    words_b = max(4096, (sh["rows"] * sh["cols"] + 31) // 32 * 16)
+    words_b = max(4096, (sh["rows"] * sh["cols"] + 31) // 32 * 16)  # conflict words (mark's atomics)
+    view_b = max(4096, (sh["rows"] * sh["cols"] + 31) // 32 * 8)  # their compact view (classify's reads)
     pr = G.lib.probe_random_access
-    c = {"load_table": pr(device, table_b, G.lib.PROBE_LOAD), "load_words": pr(device, words_b, G.lib.PROBE_LOAD),
+    c = {"load_table": pr(device, table_b, G.lib.PROBE_LOAD), "load_views": pr(device, view_b, G.lib.PROBE_LOAD),
          "atomic_words": pr(device, words_b, G.lib.PROBE_ATOMIC),
          "reduce_words": pr(device, words_b, G.lib.PROBE_REDUCE)}
-    out = {"ceilings_per_s": c, "array_bytes": {"table": table_b, "words": words_b}}
+    out = {"ceilings_per_s": c, "array_bytes": {"table": table_b, "words": words_b, "views": view_b}}
     ops, unc = st["ops"], st["ops"] - st["contended_ops"]
-    floor = ops / c["load_words"] + unc / c["load_table"]
-    out["classify"] = {"random_reads": {"words": ops, "cells": unc}, "floor_ms": floor * 1e3,
+    floor = ops / c["load_views"] + unc / c["load_table"]
+    out["classify"] = {"random_reads": {"views": ops, "cells": unc}, "floor_ms": floor * 1e3,
                        "ms": avg["classify"], "frac": floor * 1e3 / avg["classify"]}
     if config in MEASURED_ATOMICS:
         a, r = MEASURED_ATOMICS[config]
