@@ -250,11 +250,6 @@ __device__ __forceinline__ void red_or_hint(u32 *p, u32 v, u64 pol) {
 __device__ __forceinline__ void red_or_hint(u64 *p, u64 v, u64 pol) {
     asm volatile("red.global.or.L2::cache_hint.b64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
 }
-__device__ __forceinline__ void st_word_hint(void *ptr, uint4 v, u64 pol) {
-    asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(ptr), "r"(v.x), "r"(v.y), "r"(v.z),
-                 "r"(v.w), "l"(pol)
-                 : "memory");
-}
 __device__ __forceinline__ uint2 ld_view_hint(const void *ptr, u64 pol) {
     uint2 v;
     asm volatile("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;" : "=r"(v.x), "=r"(v.y) : "l"(ptr), "l"(pol));
@@ -317,9 +312,6 @@ struct Wd<32> {
     static __device__ __forceinline__ void clear(const Scratch &s, u64 w) {
         *reinterpret_cast<uint4 *>(&s.words[w]) = make_uint4(0u, 0u, 0u, 0u);
     }
-    static __device__ __forceinline__ void clear_hint(const Scratch &s, u64 w, u64 pol) {
-        st_word_hint(&s.words[w], make_uint4(0u, 0u, 0u, 0u), pol);
-    }
     // the compact view, as V{contended mask, all ones, first id}
     static __device__ __forceinline__ V load_view(const Scratch &s, u64 w, u64 pol) {
         const uint2 v = ld_view_hint(&s.cview[w], pol);
@@ -364,11 +356,6 @@ struct Wd<64> {
         uint4 *p = reinterpret_cast<uint4 *>(at(s, w));
         p[0] = make_uint4(0u, 0u, 0u, 0u);
         p[1] = make_uint4(0u, 0u, 0u, 0u);
-    }
-    static __device__ __forceinline__ void clear_hint(const Scratch &s, u64 w, u64 pol) {
-        uint4 *p = reinterpret_cast<uint4 *>(at(s, w));
-        st_word_hint(p, make_uint4(0u, 0u, 0u, 0u), pol);
-        st_word_hint(p + 1, make_uint4(0u, 0u, 0u, 0u), pol);
     }
     static __device__ __forceinline__ uint4 *view(const Scratch &s, u64 w) { return reinterpret_cast<uint4 *>(s.cview) + w; }
     static __device__ __forceinline__ V load_view(const Scratch &s, u64 w, u64 pol) {
