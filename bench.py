@@ -719,7 +719,8 @@ def run_payload(args, config):
     n_e2e = max(32, min(64, args.steps))
     execs_all = (6 if args.mode == "auto" else 0) + args.warmup * 2 + args.steps + timing_steps
     per_batch = np.max([h[5] for h in host], axis=0)
-    extra = per_batch * (execs_all * nb + (0 if args.tiles else 40) + (0 if args.no_e2e else n_e2e + 3))
+    # tuning: ~17 executions of the first batch, then 3 candidates x 3 runs of the list
+    extra = per_batch * (execs_all * nb + (0 if args.tiles else 40 + 9 * nb) + (0 if args.no_e2e else n_e2e + 3))
     ctx = G.Context(device=local, stage_timing=True)
     ctx_tables = wl.create_tables(ctx, extra)
     dev = []
@@ -731,6 +732,8 @@ def run_payload(args, config):
     ctx.sync()
     ctx.set_stage_timing(False)  # tune what the timed region runs: no event nodes
     tiles = fixed_tiles(ctx, dev, args.tiles) if args.tiles else AT.tune_buckets(ctx, dev[:1], reps=1)
+    if not args.tiles:  # the single-batch choice, checked on the batch list itself
+        tiles = {k: AT.refine_pipeline(ctx, dev, v) for k, v in tiles.items()}
     if args.mode == "auto":
         mode, mode_ms = AT.tune_mode(ctx, dev)
     else:

@@ -113,6 +113,59 @@ def tune_mode(ctx, batches, reps=2, modes=(L.MODE_GRAPH, L.MODE_PERSISTENT)):
     return min(out, key=out.get), out
 
 
+def parse_choice(name):
+    """(block, ipt, word_bits, flags) of a candidate name such as 512x4,
+    512x2w64 or 512x4+precheck."""
+    base, _, opt = name.partition("+")
+    base, _, wb = base.partition("w")
+    blk, ipt = (int(x) for x in base.split("x"))
+    return blk, ipt, int(wb) if wb else 32, L.TUNE_MARK_PRECHECK if opt == "precheck" else 0
+
+
+def _time_list(ctx, batches, reps, mode=L.MODE_GRAPH):
+    """Best over reps of one multi-batch call over the list (after a warm-up
+    call that captures the graph)."""
+    import torch
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ctx.execute_many(batches, mode=mode)
+    ctx.sync()
+    ms = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.execute_many(batches, mode=mode)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    for b in batches:
+        b.finish()
+    return min(ms)
+
+
+def refine_pipeline(ctx, batches, choice, top=3, reps=2, mode=L.MODE_GRAPH):
+    """Re-times a size bucket's fastest single-batch candidates on the whole
+    list of batches, executed the way the workload runs them (one captured
+    graph by default), and keeps the fastest there.  One batch repeated in
+    isolation misjudges tilings whose L2 footprint differs when different
+    batches follow each other (order entry: 512x2 with 64-cell words looks
+    as fast as 512x4 alone, and is 2% slower over four batches).  Every
+    candidate runs reps + 1 times over the list: a payload workload needs
+    that many executions' worth of insert capacity."""
+    ranked = sorted(choice["candidates"], key=choice["candidates"].get)[:top]
+    timed = {}
+    for name in ranked:
+        blk, ipt, wb, flags = parse_choice(name)
+        ctx.set_tuning(choice["bucket"], blk, ipt, word_bits=wb, flags=flags)
+        timed[name] = _time_list(ctx, batches, reps, mode)
+    best = min(timed, key=timed.get)
+    blk, ipt, wb, flags = parse_choice(best)
+    ctx.set_tuning(choice["bucket"], blk, ipt, word_bits=wb, flags=flags)
+    out = dict(choice)
+    out.update({"block": blk, "ipt": ipt, "word_bits": wb, "flags": flags, "pipeline_ms": timed})
+    return out
+
+
 def tune_buckets(ctx, batches, reps=3, copies=1):
     """One representative batch per size bucket; returns {bucket: choice}."""
     seen = {}

@@ -94,6 +94,35 @@ def test_tune_buckets_uses_the_largest_batch_of_each_bucket(monkeypatch):
     assert sorted(out) == [5, 9, 20]
 
 
+def test_parse_choice_names():
+    assert AT.parse_choice("512x4") == (512, 4, 32, 0)
+    assert AT.parse_choice("512x2w64") == (512, 2, 64, 0)
+    assert AT.parse_choice("256x8w64+precheck") == (256, 8, 64, L.TUNE_MARK_PRECHECK)
+    assert AT.parse_choice("128x1+precheck") == (128, 1, 32, L.TUNE_MARK_PRECHECK)
+
+
+def test_refine_pipeline_keeps_the_fastest_over_the_batch_list(monkeypatch):
+    # single-batch order: 512x2w64+precheck < 512x4 < 256x2 < 128x1; over the
+    # list 512x4 wins, and only the three fastest single-batch candidates run
+    choice = {"bucket": 22, "block": 512, "ipt": 2, "word_bits": 64, "flags": L.TUNE_MARK_PRECHECK, "ms": 0.30,
+              "candidates": {"512x2w64+precheck": 0.30, "512x4": 0.31, "256x2": 0.33, "128x1": 0.50}}
+    list_ms = {(512, 2, 64, L.TUNE_MARK_PRECHECK): 2.89, (512, 4, 32, 0): 2.82, (256, 2, 32, 0): 2.95}
+    seen = []
+
+    def fake_list(ctx, batches, reps, mode=L.MODE_GRAPH):
+        t = ctx.tuning[22]
+        seen.append(t)
+        return list_ms[t]
+
+    monkeypatch.setattr(AT, "_time_list", fake_list)
+    ctx = FakeCtx()
+    out = AT.refine_pipeline(ctx, [FakeBatch(1 << 22)] * 4, choice)
+    assert len(seen) == 3 and (128, 1, 32, 0) not in seen
+    assert (out["block"], out["ipt"], out["word_bits"], out["flags"]) == (512, 4, 32, 0)
+    assert ctx.tuning[22] == (512, 4, 32, 0)
+    assert out["pipeline_ms"]["512x4"] == 2.82
+
+
 def test_save_and_load_round_trip(tmp_path):
     choices = {14: {"block": 128, "ipt": 1, "word_bits": 32, "flags": 0, "ms": 0.02},
                22: {"block": 512, "ipt": 2, "word_bits": 64, "flags": L.TUNE_MARK_PRECHECK, "ms": 0.3}}
