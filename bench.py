@@ -719,8 +719,8 @@ def run_payload(args, config):
     n_e2e = max(32, min(64, args.steps))
     execs_all = (6 if args.mode == "auto" else 0) + args.warmup * 2 + args.steps + timing_steps
     per_batch = np.max([h[5] for h in host], axis=0)
-    # tuning: ~17 executions of the first batch, then 3 candidates x 3 runs of the list
-    extra = per_batch * (execs_all * nb + (0 if args.tiles else 40 + 9 * nb) + (0 if args.no_e2e else n_e2e + 3))
+    # tuning: ~17 executions of the first batch, then 4 candidates x 3 runs of the list
+    extra = per_batch * (execs_all * nb + (0 if args.tiles else 40 + 12 * nb) + (0 if args.no_e2e else n_e2e + 3))
     ctx = G.Context(device=local, stage_timing=True)
     ctx_tables = wl.create_tables(ctx, extra)
     dev = []
@@ -1213,11 +1213,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     ap.add_argument("--loadgen-threads", type=int, default=8, help="serving sweep: load-generator threads")
-    ap.add_argument("--ycsb-loads", default="700,800,850,900",
+    ap.add_argument("--ycsb-loads", default="750,850,875,900",
                     help="request-log serving of the Zipf YCSB transactions alone: offered loads in M txn/s")
     ap.add_argument("--ingest-jit", type=int, default=1,
                     help="serve: request log queues a batch only once the one ahead is past its sort (1) or at once (0)")
-    ap.add_argument("--ingest-loads", default="250,300,350,375",
+    ap.add_argument("--ingest-loads", default="300,350,365,380",
                     help="serving from a device-resident request log: offered loads in M txn/s ('' = skip)")
     ap.add_argument("--serve-point-s", type=float, default=1.0, help="serve: seconds of arrivals per sweep point")
     ap.add_argument("--no-serving", action="store_true", help="default workload: skip the serving section")

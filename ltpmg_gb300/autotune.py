@@ -143,16 +143,24 @@ def _time_list(ctx, batches, reps, mode=L.MODE_GRAPH):
     return min(ms)
 
 
-def refine_pipeline(ctx, batches, choice, top=3, reps=2, mode=L.MODE_GRAPH):
-    """Re-times a size bucket's fastest single-batch candidates on the whole
-    list of batches, executed the way the workload runs them (one captured
-    graph by default), and keeps the fastest there.  One batch repeated in
-    isolation misjudges tilings whose L2 footprint differs when different
-    batches follow each other (order entry: 512x2 with 64-cell words looks
-    as fast as 512x4 alone, and is 2% slower over four batches).  Every
-    candidate runs reps + 1 times over the list: a payload workload needs
-    that many executions' worth of insert capacity."""
-    ranked = sorted(choice["candidates"], key=choice["candidates"].get)[:top]
+def refine_pipeline(ctx, batches, choice, top=2, reps=2, mode=L.MODE_GRAPH):
+    """Re-times a size bucket's `top` fastest single-batch tilings, each with
+    and without the mark pre-check, on the whole list of batches executed the
+    way the workload runs them (one captured graph by default), and keeps the
+    fastest there.  One batch repeated in isolation misjudges tilings whose
+    L2 footprint differs when different batches follow each other (order
+    entry: 512x2 with 64-cell words looks as fast as 512x4 alone, and is 2%
+    slower over four batches).  Every candidate runs reps + 1 times over the
+    list: a payload workload needs 2 * top * (reps + 1) executions' worth of
+    insert capacity."""
+    bases = []
+    for name in sorted(choice["candidates"], key=choice["candidates"].get):
+        base = name.partition("+")[0]
+        if base not in bases:
+            bases.append(base)
+        if len(bases) == top:
+            break
+    ranked = [b + sfx for b in bases for sfx in ("", "+precheck")]
     timed = {}
     for name in ranked:
         blk, ipt, wb, flags = parse_choice(name)
