@@ -950,14 +950,24 @@ def serving_measure(args, local, rank, point_s):
         """Keys as 32-bit keys when they fit: the request log stores them so."""
         return k.astype(np.uint32) if len(k) and int(k.max()) < (1 << 32) else k
 
-    host_loads = [float(x) * 1e6 for x in args.loads.split(",")] if args.loads else []
-    blend_loads = [float(x) * 1e6 for x in args.ingest_loads.split(",")] if args.ingest_loads else []
-    ycsb_loads = [float(x) * 1e6 for x in args.ycsb_loads.split(",")] if args.ycsb_loads else []
+    def loads_of(spec, plain):
+        """Offered loads in txn/s: "a,b,..." in M txn/s, or "xf1,f2,..." as
+        multiples of the plain path's rate on the same tables (the knee of
+        the p99 curve sits at a steady fraction of it)."""
+        if not spec:
+            return []
+        if spec.startswith("x"):
+            return [round(float(f) * plain / 1e6) * 1e6 for f in spec[1:].split(",")]
+        return [float(x) * 1e6 for x in spec.split(",")]
+
+    host_loads = loads_of(args.loads, 0.0)
     t_host = [max(point_s, min(2.0, 20e6 / r)) for r in host_loads]
-    # insert-table room for the most transactions one point can run; the
+    # insert-table room for the most transactions one point can run (a
+    # relative blend grid is bounded with a plain rate of 600 M txn/s); the
     # insert tables are truncated between points
+    blend_bound = loads_of(args.ingest_loads, 600e6)
     per_txn = np.asarray(t_ins, np.float64) / (2 * n_each)
-    most = max([r * t for r, t in zip(host_loads, t_host)] + [r * point_s for r in blend_loads] +
+    most = max([r * t for r, t in zip(host_loads, t_host)] + [r * point_s for r in blend_bound] +
                [13 * n_pool]) * 1.25 + n_pool
     ctx = G.Context(device=local)
     t = ctx.create_table(sh["rows"], sh["cols"])
@@ -1042,10 +1052,11 @@ def serving_measure(args, local, rank, point_s):
            "client_streams": 256}
     t_start = time.perf_counter()
     # 1. Zipf YCSB alone, request log
-    if ycsb_loads:
+    if args.ycsb_loads:
         ny = 1 << 20
         ytf, yk, yw = tf[:ny + 1], keys[:int(tf[ny])], opw[:int(tf[ny])]
         plain_y = plain_rate(ytf, yk, yw)
+        ycsb_loads = loads_of(args.ycsb_loads, plain_y)
         tuning_y = tune_for(ytf, yk, yw, None, None)
         ing = G.Ingest(ctx, ytf, yk, yw, deadline_us=250, depth=2, budget_bytes=4 << 30, max_txns=1 << 20,
                        max_ops=1 << 24, eager=True, jit=bool(args.ingest_jit))
@@ -1055,6 +1066,7 @@ def serving_measure(args, local, rank, point_s):
                                        pool_txns=ny, workload="zipf0.99 YCSB, 16 ops, 80/20")
     # 2. the 50/50 blend, request log
     plain_b = plain_rate(ptf, pk, pw, ppay)
+    blend_loads = [min(r, b) for r, b in zip(loads_of(args.ingest_loads, plain_b), blend_bound)]
     if blend_loads:
         tuning_b = tune_for(ptf, pk, pw, ppf, ppay)
         ing = G.Ingest(ctx, ptf, pk, pw, ppf, ppay, deadline_us=250, depth=2, budget_bytes=4 << 30,
@@ -1213,12 +1225,14 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     ap.add_argument("--loadgen-threads", type=int, default=8, help="serving sweep: load-generator threads")
-    ap.add_argument("--ycsb-loads", default="750,850,875,900",
-                    help="request-log serving of the Zipf YCSB transactions alone: offered loads in M txn/s")
+    ap.add_argument("--ycsb-loads", default="x0.82,0.9,0.94,0.97",
+                    help="request-log serving of the Zipf YCSB transactions alone: offered loads in M txn/s, "
+                         "or x-prefixed multiples of the plain batch path's rate on the same tables")
     ap.add_argument("--ingest-jit", type=int, default=1,
                     help="serve: request log queues a batch only once the one ahead is past its sort (1) or at once (0)")
-    ap.add_argument("--ingest-loads", default="300,350,365,380",
-                    help="serving from a device-resident request log: offered loads in M txn/s ('' = skip)")
+    ap.add_argument("--ingest-loads", default="x0.82,0.88,0.91,0.94",
+                    help="serving the blend from a device-resident request log: offered loads in M txn/s, or "
+                         "x-prefixed multiples of the plain batch path's rate ('' = skip)")
     ap.add_argument("--serve-point-s", type=float, default=1.0, help="serve: seconds of arrivals per sweep point")
     ap.add_argument("--no-serving", action="store_true", help="default workload: skip the serving section")
     ap.add_argument("--serve-mode", default="persistent", choices=["persistent", "stream"],
