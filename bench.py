@@ -156,7 +156,7 @@ MEASURED_TRAFFIC = {
     ("zipf", "mark"): (14.1, "ops"),  # 32-bit keys
     ("zipf", "apply"): (30.3, "contended_ops"),
     ("zipf", "ids"): (6.9, "ops"),  # k_ids + k_dbase
-    ("tpcc", "insert"): (59.3, "ops"),  # 32-bit keys
+    ("tpcc", "insert"): (59.1, "ops"),  # 32-bit keys
     ("tpcc", "mark"): (15.7, "ops"),  # 32-bit keys
 }
 
