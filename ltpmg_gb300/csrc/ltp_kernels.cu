@@ -496,6 +496,15 @@ constexpr u64 kStreamOpsBytes = 96ull << 20;
 template <int BLOCK, int IPT, int WB>
 __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
     typedef typename Wd<WB>::T WT;
+    // A batch with at least twice as many ops as conflict words touches
+    // most of them: ids and finish will visit every word in address order,
+    // so no touched-word list is built, only its length counted, per warp
+    // across its tiles (the list cost a global atomic round trip and two
+    // barriers per tile: Zipf mark 0.278 -> 0.272 ms).  Every block records
+    // the choice before it touches a word, so finish clears every word
+    // whenever any block marked one.
+    const bool no_list = b.n_ops >= 2ull * Wd<WB>::n_words(s);
+    if (no_list && threadIdx.x == 0) ctr->dense = 1u;
     if (block_err(ctr)) return;
     const bool precheck = (b.flags & LTP_TUNE_MARK_PRECHECK) != 0u;
     // the words stay in L2 from batch to batch (hot words are touched by
@@ -509,6 +518,7 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
     __shared__ u32 s_ins[LTP_MAX_TABLES];  // insert ops of the tile per table
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const u64 n = b.n_ops;
+    u64 n_first = 0;  // no_list: first-touched words of this warp's share of the tiles
     for (u64 base = (u64)blockIdx.x * TILE; base < n; base += (u64)gridDim.x * TILE) {
         for (u32 i = threadIdx.x; i < H; i += BLOCK) {
             hk[i] = kEmptyKey;
@@ -609,6 +619,11 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
                 }
             }
         }
+        if (no_list) {  // count the first-touched words only, per warp across its tiles
+            n_first += __reduce_add_sync(FULL_MASK, nfirst);
+            __syncthreads();
+            continue;
+        }
         // first-touched words go to the touched-word list with one global
         // atomic per tile (a per-warp counter on one address serialises)
         u32 incl = nfirst;
@@ -640,6 +655,7 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
             }
         __syncthreads();
     }
+    if (no_list && lane == 0 && n_first) atomicAdd(&ctr->n_tw, n_first);  // one add per warp
 }
 
 template <int BLOCK, int IPT, int WB>
@@ -653,10 +669,12 @@ __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch
 // ============================================================================
 // When a batch touches more than a quarter of the conflict words, the ids
 // scan and the clean-up stream over every word in address order instead of
-// visiting the touched-word list in first-touch (random) order.
+// visiting the touched-word list in first-touch (random) order.  A batch
+// with at least twice as many ops as words is taken as such without
+// counting: mark builds no list for it (see phase_mark).
 template <int WB>
 __device__ __forceinline__ bool ids_dense(const Scratch &s, const Counters *ctr) {
-    return ctr->n_tw * 4 > Wd<WB>::n_words(s);
+    return ctr->dense || ctr->n_tw * 4 > Wd<WB>::n_words(s);
 }
 
 // Per contended cell: its address width (bit 63 of dcell marks an int64
