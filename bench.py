@@ -153,7 +153,7 @@ def load_peaks():
 # a launch's traffic is this figure times the units it processed
 MEASURED_TRAFFIC = {
     ("zipf", "classify"): (37.4, "ops"),  # 32-bit keys
-    ("zipf", "mark"): (14.1, "ops"),  # 32-bit keys
+    ("zipf", "mark"): (13.3, "ops"),  # 32-bit keys
     ("zipf", "apply"): (30.3, "contended_ops"),
     ("zipf", "ids"): (6.9, "ops"),  # k_ids + k_dbase
     ("tpcc", "insert"): (59.1, "ops"),  # 32-bit keys
@@ -1225,12 +1225,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     ap.add_argument("--loadgen-threads", type=int, default=8, help="serving sweep: load-generator threads")
-    ap.add_argument("--ycsb-loads", default="x0.82,0.9,0.94,0.97",
+    ap.add_argument("--ycsb-loads", default="x0.88,0.93,0.95,0.965",
                     help="request-log serving of the Zipf YCSB transactions alone: offered loads in M txn/s, "
                          "or x-prefixed multiples of the plain batch path's rate on the same tables")
     ap.add_argument("--ingest-jit", type=int, default=1,
                     help="serve: request log queues a batch only once the one ahead is past its sort (1) or at once (0)")
-    ap.add_argument("--ingest-loads", default="x0.82,0.88,0.91,0.94",
+    ap.add_argument("--ingest-loads", default="x0.88,0.92,0.95,0.975",
                     help="serving the blend from a device-resident request log: offered loads in M txn/s, or "
                          "x-prefixed multiples of the plain batch path's rate ('' = skip)")
     ap.add_argument("--serve-point-s", type=float, default=1.0, help="serve: seconds of arrivals per sweep point")
