@@ -240,6 +240,48 @@ def test_malformed_op_rejected_and_context_survives(lib_loaded):
         assert vals.tolist() == [int(before[0, 1]) + 1, int(before[0, 1]) + 1]
 
 
+@pytest.mark.parametrize("rule", [0, 1])
+def test_dense_batches_build_no_list_and_recover_from_errors(lib_loaded, rule):
+    """Batches with at least twice as many ops as conflict words take the
+    path on which mark builds no touched-word list (ids and finish visit
+    every word).  A malformed op in such a batch is rejected with the table
+    unchanged, and the sparse and dense batches after it still equal the
+    oracle: every word the failed batch marked was cleared."""
+    rows, cols = 1 << 10, 4  # 4096 cells: 129 conflict words of 32 cells
+    dense = gen(11, rows, cols, 4, 8, 0.6, 0.9, 0, 400)  # ~2400 ops >= 2 x 129
+    sparse = gen(11, rows, cols, 1, 2, 0.6, 0.9, 1, 40)  # ~60 ops: the list path
+    assert len(dense[1]) >= 2 * 129 and len(sparse[1]) < 2 * 129
+    with G.Context(device=0, rule=rule) as ctx:
+        t = ctx.create_table(rows, cols)
+        ctx.fill_seeded(t, 11)
+        ref = O.table_init(11, rows, cols)
+        b = ctx.batch(400, len(dense[1]))
+
+        def run(tf, keys, opw):
+            nonlocal ref
+            b.load(tf, keys, opw)
+            b.execute()
+            commit, vals, st = b.results()
+            ref, rc, ro = O.replay(rule, ref, tf, keys, opw)
+            assert np.array_equal(commit, rc) and np.array_equal(vals, ro)
+            return st
+
+        assert run(*dense).touched_words > 0
+        tf, keys, opw = dense
+        bad = keys.copy()
+        bad[len(bad) // 2] = rows + 3  # a row past the table, mid-batch
+        before = ctx.download(t)
+        b.load(tf, bad, opw)
+        b.execute()
+        with pytest.raises(G.LtpError) as ei:
+            b.results()
+        assert ei.value.status == G.lib.LTP_E_BADARG
+        assert np.array_equal(before, ctx.download(t)), "a rejected batch must not change the table"
+        run(*sparse)
+        run(*dense)
+        assert np.array_equal(ctx.download(t), ref)
+
+
 def test_bad_column_and_table(lib_loaded):
     with G.Context(device=0) as ctx:
         t = ctx.create_table(64, 2)
