@@ -10,6 +10,8 @@
 // operations of new-order and payment (cuda/src/gpuquery.cu:2474-2734).
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <typeinfo>
@@ -37,9 +39,30 @@ struct CompatState {
 
 CompatState g;
 
+// Opt-in summary for integrators: with LTPMG_COMPAT_REPORT set in the
+// environment, one line on stderr at process exit -- batches executed
+// through execute_on_GPU, transactions they committed, and the first failing
+// status with its message (the reference's host program checks none of the
+// entry points' outcomes).
+struct CompatReport {
+    uint64_t batches = 0, committed = 0;
+    int first_status = 0;
+    std::string first_error;
+    ~CompatReport() {
+        if (!std::getenv("LTPMG_COMPAT_REPORT")) return;
+        std::fprintf(stderr, "ltp_compat: batches=%llu committed=%llu status=%d%s%s\n", (unsigned long long)batches,
+                     (unsigned long long)committed, first_status, first_error.empty() ? "" : " ", first_error.c_str());
+    }
+};
+CompatReport g_report;
+
 void set_status(int st, const std::string &msg) {
     g.status = st;
     g.error = msg;
+    if (st != 0 && g_report.first_status == 0) {
+        g_report.first_status = st;
+        g_report.first_error = msg;
+    }
 }
 
 int check(int rc, const char *where) {
@@ -332,6 +355,8 @@ void execute_on_GPU(std::shared_ptr<Param> param) {
     ltp_stats st;
     if (check(ltp_batch_finish(g.ctx, g.batch, &st, nullptr), "ltp_batch_finish")) return;
     const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    g_report.batches++;
+    g_report.committed += st.committed;
     if (param) param->result.cost = s;  // as GPUlauncher sets it (cuda/src/gpulauncher.cu:1071-1077)
 }
 

@@ -8,6 +8,7 @@ GPU: the driver runs the reference's Scheduler::start sequence for YCSB_A..E
 oracle's serial replay of the expanded batch, bit for bit.
 """
 import os
+import re
 import subprocess
 
 import numpy as np
@@ -119,6 +120,32 @@ def test_reference_host_program_links_against_the_library():
         assert sym in und, sym
     deps = subprocess.run(["ldd", REF_HOST], capture_output=True, text=True).stdout
     assert "libltpmg_gb300.so" in deps and "not found" not in deps
+
+
+@pytest.mark.gpu
+def test_reference_host_program_runs_its_epochs_on_the_library():
+    """The reference's whole host program -- its own main, Database::generate,
+    Query::generate_txn and Scheduler::start, compiled from its sources with
+    the flag and log stand-ins -- runs four YCSB_A epochs of 2^14 Zipf 0.99
+    transactions over 10^6 rows against libltpmg_gb300.so: every epoch is
+    executed here and commits its whole batch (the library's exit report),
+    and the reference's own timing lines report each measured epoch."""
+    if not os.path.exists(REF_HOST):
+        pytest.skip("reference host program not built (reference sources absent)")
+    env = dict(os.environ, LTPMG_COMPAT_REPORT="1", LTPMG_SHIM_LOG="1")
+    cwd = os.path.join(os.path.dirname(REF_HOST), "src", "src")  # it reads its schemas from ../data
+    r = subprocess.run([REF_HOST, "--benchmark=YCSB_A", "--table_size=1", "--batch_size=16384", "--epoch_tp=4",
+                        "--deviceIDs=0", "--data_distribution=zipf", "--zipf_config=0.99"],
+                       cwd=cwd, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    rep = [line for line in r.stderr.splitlines() if line.startswith("ltp_compat:")]
+    assert rep, r.stderr[-2000:]
+    m = re.match(r"ltp_compat: batches=(\d+) committed=(\d+) status=(-?\d+)", rep[-1])
+    assert m and m.group(3) == "0", rep[-1]
+    assert int(m.group(1)) == 4 and int(m.group(2)) == 4 * 16384, rep[-1]
+    # Scheduler::start logs the epochs strictly between 10% and 90% of the run
+    times = [float(x) for x in re.findall(r"Execution time: ([0-9.eE+-]+) s\.", r.stderr)]
+    assert len(times) == 3 and all(t > 0 for t in times), times
 
 
 TPCC_INT_COLS = [1, 3, 5, 3, 5, 7, 8, 5, 2]  # int attributes of data/TPCC.json's nine tables
