@@ -194,7 +194,7 @@ __device__ __forceinline__ OpRef decode_op(const TablesDev &T, u64 key, u32 w) {
     u32 tb = opw_table(w), col = opw_col(w), kind = opw_kind(w);
     r.valid = tb < T.n && kind <= 1u;
     const TableDev &t = T.t[r.valid ? tb : 0];
-    r.valid = r.valid && key < __ldg(&T.rows_now[r.valid ? tb : 0]) && col < t.n_cols;
+    r.valid = r.valid && key < T.rows_now[r.valid ? tb : 0] && col < t.n_cols;  // advanced by finish
     r.wide = r.valid && col_wide(t, col);
     r.cell = r.valid ? t.cell_base + key * t.n_cols + col : ~0ull;
     r.ptr = r.valid ? t.data + col_off(t, col) + key * (r.wide ? 8ull : 4ull) : nullptr;
@@ -225,11 +225,16 @@ __device__ __forceinline__ uint4 ld_word_relaxed(const void *ptr) {
                  : "memory");
     return v;
 }
+// Loads of scratch state with an L2 eviction-priority hint.  Coherent (not
+// .nc): the persistent kernel writes this state and reads it again within one
+// launch, where only the grid barrier's acquire orders the two, and the
+// non-coherent path is defined only for data read-only for a whole kernel.
 __device__ __forceinline__ uint4 ld_word_hint(const void *ptr, u64 pol) {
     uint4 v;
-    asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+    asm volatile("ld.global.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
                  : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                 : "l"(ptr), "l"(pol));
+                 : "l"(ptr), "l"(pol)
+                 : "memory");
     return v;
 }
 // OR into a conflict word with an L2 eviction-priority hint: with the old
@@ -257,7 +262,10 @@ __device__ __forceinline__ void st_word_hint(void *ptr, uint4 v, u64 pol) {
 }
 __device__ __forceinline__ uint2 ld_view_hint(const void *ptr, u64 pol) {
     uint2 v;
-    asm volatile("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;" : "=r"(v.x), "=r"(v.y) : "l"(ptr), "l"(pol));
+    asm volatile("ld.global.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+                 : "=r"(v.x), "=r"(v.y)
+                 : "l"(ptr), "l"(pol)
+                 : "memory");
     return v;
 }
 // ---- programmatic dependent launch -------------------------------------------
@@ -326,7 +334,7 @@ struct Wd<32> {
         return V{v.x, ~0u, v.y};
     }
     static __device__ __forceinline__ V load_view_ro(const Scratch &s, u64 w) {
-        const uint2 v = __ldg(&s.cview[w]);
+        const uint2 v = s.cview[w];
         return V{v.x, ~0u, v.y};
     }
     static __device__ __forceinline__ void set_view(const Scratch &s, u64 w, T cw, u32 first) {
@@ -376,7 +384,7 @@ struct Wd<64> {
         return V{((u64)v.y << 32) | v.x, ~0ull, v.z};
     }
     static __device__ __forceinline__ V load_view_ro(const Scratch &s, u64 w) {
-        const uint4 v = __ldg(view(s, w));
+        const uint4 v = *view(s, w);
         return V{((u64)v.y << 32) | v.x, ~0ull, v.z};
     }
     static __device__ __forceinline__ void set_view(const Scratch &s, u64 w, T cw, u32 first) {
@@ -1288,18 +1296,18 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
                 const u32 op = rec_op(e[k], packed);
                 if (!LTP_IN_BOUNDS(ctr, op, b.n_ops) || !LTP_IN_BOUNDS(ctr, m, s.cap_ops)) continue;
                 if (!WIDE) {
-                    const int32_t val = (int32_t)((u32)__ldg(&s.dbase[m]) + (u32)tot);
+                    const int32_t val = (int32_t)((u32)s.dbase[m] + (u32)tot);
                     b.out[op] = val;
                     if (b.out64) b.out64[op] = val;
                     if (tail[k]) {
                         bool wd;
-                        char *p = cell_ptr(T, __ldg(&s.dcell[m]), &wd);
+                        char *p = cell_ptr(T, s.dcell[m], &wd);
                         *reinterpret_cast<int32_t *>(p) = val;
                     }
                 } else {
                     // bit 63 of dcell marks an int64 cell
-                    const u64 dc = __ldg(&s.dcell[m]);
-                    long long val = (long long)((u64)__ldg(&s.dbase[m]) + (u64)tot);
+                    const u64 dc = s.dcell[m];
+                    long long val = (long long)((u64)s.dbase[m] + (u64)tot);
                     if (!(dc >> 63)) val = (int32_t)val;
                     b.out[op] = (int32_t)val;
                     if ((dc >> 63) && b.out64) b.out64[op] = val;  // int32 cells: widened from out on fetch
