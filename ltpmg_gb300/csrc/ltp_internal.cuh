@@ -87,7 +87,9 @@ struct Counters {
     u32 tile_ctr[N_SLOTS];
     u32 hist[kMaxPasses][256];  // radix digit histograms of the contended list
     u32 stall;         // polled by the debug stall kernel; never set
-    u32 dense;         // set by mark when it built no touched-word list: ids and finish visit every word
+    u32 dense;         // set by mark when it built no touched-word list: ids and finish visit every word of the range below
+    u32 wlo_inv;       // ~(lowest conflict word mark touched); 0: none
+    u32 whi1;          // highest conflict word mark touched + 1; 0: none
     u32 ins_total[LTP_MAX_TABLES];      // insert ops per table in the batch
     u32 ins_committed[LTP_MAX_TABLES];  // committed inserts per table
 };

@@ -540,6 +540,12 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const u64 n = b.n_ops;
     u64 n_first = 0;  // no_list: first-touched words of this warp's share of the tiles
+    // range of the words each warp flushed, kept in shared memory across tiles
+    __shared__ u32 s_wlo[BLOCK / 32], s_whi1[BLOCK / 32];
+    if (lane == 0) {
+        s_wlo[warp] = 0xFFFFFFFFu;
+        s_whi1[warp] = 0u;
+    }
     for (u64 base = (u64)blockIdx.x * TILE; base < n; base += (u64)gridDim.x * TILE) {
         for (u32 i = threadIdx.x; i < H; i += BLOCK) {
             hk[i] = kEmptyKey;
@@ -617,6 +623,21 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
             cur_w[q] = cur_m[q] = 0;
             if (hot) Wd<WB>::load_relaxed(s, fw[q], &cur_w[q], &cur_m[q]);
         }
+        {
+            u32 lo = 0xFFFFFFFFu, hi1 = 0u;
+#pragma unroll
+            for (int q = 0; q < SPT; q++)
+                if (fw[q] != kEmptyKey) {
+                    lo = min(lo, fw[q]);
+                    hi1 = max(hi1, fw[q] + 1u);
+                }
+            lo = __reduce_min_sync(FULL_MASK, lo);
+            hi1 = __reduce_max_sync(FULL_MASK, hi1);
+            if (lane == 0) {
+                s_wlo[warp] = min(s_wlo[warp], lo);
+                s_whi1[warp] = max(s_whi1[warp], hi1);
+            }
+        }
         u32 dmask = 0;  // slots that issued their atomics
 #pragma unroll
         for (int q = 0; q < SPT; q++) {
@@ -677,6 +698,22 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
         __syncthreads();
     }
     if (no_list && lane == 0 && n_first) atomicAdd(&ctr->n_tw, n_first);  // one add per warp
+    // the range of touched words, one pair of atomics per block: ids and
+    // finish stream over it in address order when it is densely touched
+    // (a batch on one table of a context with larger ones touches a small
+    // part of the word space)
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        u32 wlo = s_wlo[0], whi1 = s_whi1[0];
+        for (int i = 1; i < BLOCK / 32; i++) {
+            wlo = min(wlo, s_wlo[i]);
+            whi1 = max(whi1, s_whi1[i]);
+        }
+        if (whi1) {
+            atomicMax(&ctr->wlo_inv, ~wlo);
+            atomicMax(&ctr->whi1, whi1);
+        }
+    }
 }
 
 template <int BLOCK, int IPT, int WB>
@@ -688,14 +725,16 @@ __global__ void __launch_bounds__(BLOCK) k_mark(BatchDev b, TablesDev T, Scratch
 // ============================================================================
 // ids: dense ids of contended cells (touched twice and written)
 // ============================================================================
-// When a batch touches more than a quarter of the conflict words, the ids
-// scan and the clean-up stream over every word in address order instead of
-// visiting the touched-word list in first-touch (random) order.  A batch
-// with at least twice as many ops as words is taken as such without
-// counting: mark builds no list for it (see phase_mark).
-template <int WB>
-__device__ __forceinline__ bool ids_dense(const Scratch &s, const Counters *ctr) {
-    return ctr->dense || ctr->n_tw * 4 > Wd<WB>::n_words(s);
+// When a batch touches more than a quarter of the conflict words between
+// the lowest and the highest it touched, the ids scan and the clean-up
+// stream over that range in address order instead of visiting the
+// touched-word list in first-touch (random) order.  A batch with at least
+// twice as many ops as words is taken as such without counting: mark builds
+// no list for it (see phase_mark).
+__device__ __forceinline__ u64 touched_lo(const Counters *ctr) { return ctr->whi1 ? (u64)~ctr->wlo_inv : 0ull; }
+__device__ __forceinline__ u64 touched_hi(const Counters *ctr) { return (u64)ctr->whi1; }
+__device__ __forceinline__ bool ids_dense(const Counters *ctr) {
+    return ctr->dense || ctr->n_tw * 4 > touched_hi(ctr) - touched_lo(ctr);
 }
 
 // Per contended cell: its address width (bit 63 of dcell marks an int64
@@ -724,8 +763,9 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
     typedef typename Wd<WB>::T WT;
     constexpr u32 IPT = kIdsTile / BLK;
     if (block_err(ctr)) return;
-    const bool dense = ids_dense<WB>(s, ctr);
-    const u64 n = dense ? Wd<WB>::n_words(s) : ctr->n_tw;
+    const bool dense = ids_dense(ctr);
+    const u64 wlo = touched_lo(ctr), whi = min(touched_hi(ctr), Wd<WB>::n_words(s));
+    const u64 n = dense ? (whi > wlo ? whi - wlo : 0ull) : ctr->n_tw;
     const u32 tiles = (u32)((n + kIdsTile - 1) / kIdsTile);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ u32 s_warp[BLK / 32];
@@ -744,7 +784,7 @@ __device__ __forceinline__ void phase_ids(const TablesDev &T, const Scratch &s, 
 #pragma unroll
         for (int k = 0; k < IPT; k++) {
             u64 j = t0 + (u64)k * BLK;
-            wd[k] = j < n ? (dense ? (u32)j : s.tw_list[j]) : 0u;
+            wd[k] = j < n ? (dense ? (u32)(wlo + j) : s.tw_list[j]) : 0u;
             if (j < n) {
                 const typename Wd<WB>::V v = Wd<WB>::load(s, wd[k]);
                 cw[k] = v.wbits & v.multi;
@@ -1612,14 +1652,15 @@ __device__ __forceinline__ void phase_finish(const BatchDev &b, const TablesDev 
         for (u64 j = g0; j < t_ins * LTP_MAX_TABLES; j += gsz) s.st_ins[j] = 0;
     }
     const u64 ntw = ctr->n_tw;
-    const bool dense = ids_dense<WB>(s, ctr);
+    const bool dense = ids_dense(ctr);
     const u64 nw = Wd<WB>::n_words(s);
     if (dense) {
-        // every word: the next batch's mark finds the cleared lines in L2,
-        // kept there by the evict-last hint (Zipf mark 0.270 -> 0.263 ms;
-        // evict-first instead: 0.303 ms)
+        // every word of the touched range: the next batch's mark finds the
+        // cleared lines in L2, kept there by the evict-last hint (Zipf mark
+        // 0.270 -> 0.263 ms; evict-first instead: 0.303 ms)
         const u64 pol_keep = pol_evict_last();
-        for (u64 j = g0; j < nw; j += gsz) Wd<WB>::clear_hint(s, j, pol_keep);
+        const u64 whi = min(touched_hi(ctr), nw);
+        for (u64 j = touched_lo(ctr) + g0; j < whi; j += gsz) Wd<WB>::clear_hint(s, j, pol_keep);
     } else {
         for (u64 j = g0; j < ntw; j += gsz)
             if (LTP_IN_BOUNDS(ctr, s.tw_list[j], nw)) Wd<WB>::clear(s, s.tw_list[j]);
