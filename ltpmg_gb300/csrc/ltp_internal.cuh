@@ -90,6 +90,7 @@ struct Counters {
     u32 dense;         // set by mark when it built no touched-word list: ids and finish visit every word of the range below
     u32 wlo_inv;       // ~(lowest conflict word mark touched); 0: none
     u32 whi1;          // highest conflict word mark touched + 1; 0: none
+    u32 wide_ops;      // set by mark when some valid op is on an int64 cell
     u32 ins_total[LTP_MAX_TABLES];      // insert ops per table in the batch
     u32 ins_committed[LTP_MAX_TABLES];  // committed inserts per table
 };

@@ -542,10 +542,12 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
     u64 n_first = 0;  // no_list: first-touched words of this warp's share of the tiles
     // range of the words each warp flushed, kept in shared memory across tiles
     __shared__ u32 s_wlo[BLOCK / 32], s_whi1[BLOCK / 32];
+    __shared__ u32 s_wide;  // some op of the block is on an int64 cell
     if (lane == 0) {
         s_wlo[warp] = 0xFFFFFFFFu;
         s_whi1[warp] = 0u;
     }
+    if (threadIdx.x == 0) s_wide = 0u;
     for (u64 base = (u64)blockIdx.x * TILE; base < n; base += (u64)gridDim.x * TILE) {
         for (u32 i = threadIdx.x; i < H; i += BLOCK) {
             hk[i] = kEmptyKey;
@@ -584,6 +586,7 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
                 set_err(ctr, LTP_E_BADARG);
                 continue;
             }
+            if (r.wide) s_wide = 1u;
             const u32 word = (u32)(r.cell >> Wd<WB>::kShift);
             const WT bit = (WT)1 << (r.cell & (WB - 1));
             u32 slot = hash_word(word) & (H - 1);
@@ -713,6 +716,7 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
             atomicMax(&ctr->wlo_inv, ~wlo);
             atomicMax(&ctr->whi1, whi1);
         }
+        if (s_wide) atomicOr(&ctr->wide_ops, 1u);
     }
 }
 
@@ -1335,10 +1339,9 @@ __device__ __forceinline__ void phase_apply(const BatchDev &b, const TablesDev &
                 const S tot = sf[k] ? sv[k] : sv[k] + carry;
                 const u32 op = rec_op(e[k], packed);
                 if (!LTP_IN_BOUNDS(ctr, op, b.n_ops) || !LTP_IN_BOUNDS(ctr, m, s.cap_ops)) continue;
-                if (!WIDE) {
+                if (!WIDE) {  // every cell is int32: out64 (if any) is widened from out on fetch
                     const int32_t val = (int32_t)((u32)s.dbase[m] + (u32)tot);
                     b.out[op] = val;
-                    if (b.out64) b.out64[op] = val;
                     if (tail[k]) {
                         bool wd;
                         char *p = cell_ptr(T, s.dcell[m], &wd);
@@ -1367,6 +1370,15 @@ template <typename S>
 __global__ void __launch_bounds__(kApplyBlock, 4) k_apply(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
     pdl_begin();
     phase_apply<kApplyBlock, S>(b, T, s, ctr);
+}
+
+// In a context with int64 columns the scan is 64-bit only for a batch that
+// has an op on an int64 cell (mark records it); a batch on int32 tables
+// alone scans in 32 bits, as in a context without int64 columns.
+__global__ void __launch_bounds__(kApplyBlock, 4) k_apply_auto(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    pdl_begin();
+    if (*(volatile u32 *)&ctr->wide_ops) phase_apply<kApplyBlock, u64>(b, T, s, ctr);
+    else phase_apply<kApplyBlock, u32>(b, T, s, ctr);
 }
 
 // ============================================================================
@@ -1900,7 +1912,7 @@ cudaError_t launch_execute(const Launch &L_in, const BatchDev &b_in, const Table
         static int gs = 0, ga = 0, sms = 0;
         if (sms != L.num_sms) {
             gs = occ_grid(k_sort_pass<0>, kSortBlock, L.num_sms);
-            ga = occ_grid(k_apply<u64>, kApplyBlock, L.num_sms);
+            ga = occ_grid(k_apply_auto, kApplyBlock, L.num_sms);
             sms = L.num_sms;
         }
         const int gsort = capped(gs, (b.n_ops + kSortTile - 1) / kSortTile);
@@ -1916,7 +1928,7 @@ cudaError_t launch_execute(const Launch &L_in, const BatchDev &b_in, const Table
         if (max_passes > 3) chk(launch_k(L.pdl, k_sort_pass<3>, gsort, kSortBlock, 0, L.stream, s, ctr, b.n_ops));
         mark_ev(7);
         const int gapp = capped(ga, (b.n_ops + kApplyTile - 1) / kApplyTile);
-        chk(launch_k(L.pdl, T.any_wide ? k_apply<u64> : k_apply<u32>, gapp, kApplyBlock, 0, L.stream, b, T, s, ctr));
+        chk(launch_k(L.pdl, T.any_wide ? k_apply_auto : k_apply<u32>, gapp, kApplyBlock, 0, L.stream, b, T, s, ctr));
         mark_ev(8);
     } else {
         chk(launch_k(L.pdl, wide_words ? k_r1_minw<64> : k_r1_minw<32>, gstream, 256, 0, L.stream, b, T, s, ctr));
@@ -2025,7 +2037,7 @@ __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
                 phase_sort_pass<kPBlock>(P, a.s, a.ctr, b.n_ops);
                 grid_sync(a.bar, nb, a.ctr);
             }
-            if (a.T.any_wide) phase_apply<kPBlock, u64>(b, a.T, a.s, a.ctr);
+            if (a.T.any_wide && *(volatile u32 *)&a.ctr->wide_ops) phase_apply<kPBlock, u64>(b, a.T, a.s, a.ctr);
             else phase_apply<kPBlock, u32>(b, a.T, a.s, a.ctr);
         } else {
             phase_r1_minw<32>(b, a.T, a.s, a.ctr);
