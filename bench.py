@@ -65,11 +65,12 @@ KERNEL_BYTES = {  # st["key_bytes"]: 8, or 4 for batches loaded with 32-bit keys
 def kernels_per_batch(n_ops, has_payload):
     """Kernels one batch launches under the ordered rule: mark, ids, dbase,
     classify, one radix pass per 8 bits of the largest possible contended id
-    (n_ops - 1), apply, insert (only with a payload), finish."""
+    (n_ops - 1), apply, the insert prefix and insert (only with a payload),
+    finish."""
     passes = 1
     while passes < 4 and ((max(n_ops, 1) - 1) >> (8 * passes)) != 0:
         passes += 1
-    return 4 + passes + 1 + (1 if has_payload else 0) + 1
+    return 4 + passes + 1 + (2 if has_payload else 0) + 1
 
 
 def dist_env():

@@ -66,7 +66,9 @@ void free_scratch_ops(Scratch &s) {
     cudaFree(s.st_cls);
     cudaFree(s.st_apply);
     cudaFree(s.st_ins);
+    cudaFree(s.ins_pre);
     s.st_ins = nullptr;
+    s.ins_pre = nullptr;
     s.tw_list = nullptr;
     s.list[0] = s.list[1] = nullptr;
     s.dcell = nullptr;
@@ -117,6 +119,7 @@ int ensure_scratch(ltp_ctx *ctx, uint64_t n_ops) {
         CK(dalloc(&s.st_cls, tiles));
         CK(dalloc(&s.st_apply, tiles));
         CK(dalloc(&s.st_ins, tiles * LTP_MAX_TABLES));
+        CK(dalloc(&s.ins_pre, tiles * LTP_MAX_TABLES));
         s.cap_ops = cap;
         s.cap_tiles = tiles;
         s.cap_sort_tiles = stiles;

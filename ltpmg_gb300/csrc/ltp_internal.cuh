@@ -117,6 +117,7 @@ struct Scratch {
     u64 *st_cls;    // [tiles] classify look-back status (dense record offsets)
     u64 *st_apply;  // [tiles] segmented-apply look-back status
     u32 *st_ins;    // [tiles * LTP_MAX_TABLES] insert-slot look-back status
+    u32 *ins_pre;   // [tiles * LTP_MAX_TABLES] per insert tile and table: insert ops (mark), then their exclusive prefix
     u64 n_words;
     u64 cap_ops;
     u64 cap_tiles;  // tiles of the smallest look-back tile size at cap_ops

@@ -533,6 +533,7 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
     const u64 pol_keep = pol_evict_last();
     const bool stream_ops = b.n_ops * ((b.keys32 ? 4ull : 8ull) + 4ull) > kStreamOpsBytes;
     constexpr u32 TILE = (u32)BLOCK * IPT;
+    static_assert(kInsTile % TILE == 0, "a mark tile lies inside one insert tile");
     constexpr u32 H = 2 * TILE;  // at most TILE distinct words: load factor <= 1/2
     u32 *hk = ltp_dyn_smem;  // H keys, then 3 * H masks (dynamic)
     WT *ht = reinterpret_cast<WT *>(hk + H), *hd = ht + H, *hw = hd + H;
@@ -600,7 +601,12 @@ __device__ __forceinline__ void phase_mark(const BatchDev &b, const TablesDev &T
             if (opw_kind(w[k]) != LTP_OP_READ) atomicOr(&hw[slot], bit);
         }
         __syncthreads();
-        if (threadIdx.x < LTP_MAX_TABLES && s_ins[threadIdx.x]) atomicAdd(&ctr->ins_total[threadIdx.x], s_ins[threadIdx.x]);
+        if (threadIdx.x < LTP_MAX_TABLES && s_ins[threadIdx.x]) {
+            // per table: the batch's inserts, and those of this tile's insert tile
+            atomicAdd(&ctr->ins_total[threadIdx.x], s_ins[threadIdx.x]);
+            const u64 slot = (base / kInsTile) * LTP_MAX_TABLES + threadIdx.x;
+            if (LTP_IN_BOUNDS(ctr, slot, s.cap_tiles * LTP_MAX_TABLES)) atomicAdd(&s.ins_pre[slot], s_ins[threadIdx.x]);
+        }
         // flush: every thread issues the touch atomics of all its slots before
         // consuming any result, so the returning atomics overlap
         constexpr int SPT = H / BLOCK;
@@ -1496,7 +1502,8 @@ __global__ void __launch_bounds__(256) k_r1_exec(BatchDev b, TablesDev T, Scratc
 // look-back) -- then the payload row is copied into its slot
 // ============================================================================
 template <int BLK>
-__device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr) {
+__device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr,
+                                             bool prefixed) {
     constexpr u32 IIPT = kInsTile / BLK;
     if (block_err(ctr)) return;
     u32 any = 0;
@@ -1510,6 +1517,14 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
     __shared__ u64 s_base[LTP_MAX_TABLES];
     __shared__ u32 s_tcnt[LTP_MAX_TABLES], s_toff[LTP_MAX_TABLES];
     __shared__ u32 s_item0[LTP_MAX_TABLES + 1];  // first (table, column, row) item of each table
+    __shared__ u32 s_pair0[LTP_MAX_TABLES + 1];  // first (table, column) pair of each table
+    // per (table, column) pair of the tile's new rows: its first item, the
+    // address of its first new row, and slot | column << 8 | wide << 14 |
+    // table << 16 -- so that a cell's copy needs no division and no lookup
+    // of the table's descriptor
+    __shared__ u32 s_pitem[LTP_MAX_TABLES * LTP_MAX_COLS + 1];
+    __shared__ char *s_pdst[LTP_MAX_TABLES * LTP_MAX_COLS];
+    __shared__ u32 s_pmeta[LTP_MAX_TABLES * LTP_MAX_COLS];
     // staging of the tile's inserts in the dynamic shared memory (kInsSmem bytes)
     u32 *s_off = ltp_dyn_smem;                                                  // [kInsTile] payload offsets
     long long *s_lv = reinterpret_cast<long long *>(ltp_dyn_smem + kInsTile);  // [kInsTile] link values
@@ -1530,7 +1545,7 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
                 const u32 w = b.opw[i];
                 if (opw_kind(w) == LTP_OP_INSERT) {
                     t = opw_table(w);
-                    ins = b.commit[op_tid(b, i)] != 0;
+                    ins = prefixed || b.commit[op_tid(b, i)] != 0;  // prefixed: every transaction commits
                     if (!ins) store_out(b, i, 0);
                 }
             }
@@ -1554,7 +1569,11 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
             u32 *st = s.st_ins;
             u32 excl = 0;
             u32 *slot = &st[(u64)tile * LTP_MAX_TABLES + t];
-            if (tile == 0) {
+            if (prefixed) {
+                // every transaction commits (ordered rule): the tile's offset
+                // is the prefix of the insert counts mark took, no look-back
+                excl = s.ins_pre[(u64)tile * LTP_MAX_TABLES + t];
+            } else if (tile == 0) {
                 st_status32(slot, (2u << 30) | run);
             } else {
                 st_status32(slot, (1u << 30) | run);
@@ -1582,15 +1601,33 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
         }
         __syncthreads();
         if (threadIdx.x == 0) {  // the tile's inserts, grouped by table, in rank order
-            u32 run = 0, items = 0;
+            u32 run = 0, items = 0, pairs = 0;
             for (int t = 0; t < LTP_MAX_TABLES; t++) {
                 s_toff[t] = run;
                 run += s_tcnt[t];
                 s_item0[t] = items;
-                items += (u32)t < T.n ? s_tcnt[t] * T.t[t].n_cols : 0u;
+                s_pair0[t] = pairs;
+                if ((u32)t < T.n && s_tcnt[t]) {
+                    items += s_tcnt[t] * T.t[t].n_cols;
+                    pairs += T.t[t].n_cols;
+                }
             }
             s_item0[LTP_MAX_TABLES] = items;
+            s_pair0[LTP_MAX_TABLES] = pairs;
         }
+        __syncthreads();
+        for (u32 q = threadIdx.x; q < s_pair0[LTP_MAX_TABLES]; q += BLK) {  // thread q describes pair q
+            u32 t = 0;
+            while (s_pair0[t + 1] <= q) t++;
+            const TableDev &tab = T.t[t];
+            const u32 c = q - s_pair0[t];
+            const bool wc = col_wide(tab, c);
+            const u32 slot = c + (u32)__popcll(c ? (tab.wide & ((1ull << c) - 1ull)) : 0ull);  // payload slot of column c
+            s_pitem[q] = s_item0[t] + c * s_tcnt[t];
+            s_pdst[q] = tab.data + col_off(tab, c) + s_base[t] * (wc ? 8ull : 4ull);
+            s_pmeta[q] = slot | (c << 8) | ((wc ? 1u : 0u) << 14) | (t << 16);
+        }
+        if (threadIdx.x == 0) s_pitem[s_pair0[LTP_MAX_TABLES]] = s_item0[LTP_MAX_TABLES];
         __syncthreads();
         // every insert notes its payload row and link; its output is its row id
 #pragma unroll
@@ -1613,7 +1650,7 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
         // rows of a column, and a thread's items issue their loads together
         const u32 n_items = s_item0[LTP_MAX_TABLES];
         constexpr int U = 4;  // items per thread in flight: their loads issue before their stores
-        u32 t = 0;            // items of a thread only move forward through the tables
+        u32 pr = 0;           // items of a thread only move forward through the pairs
         for (u32 it0 = threadIdx.x; it0 < n_items; it0 += U * BLK) {
             long long v[U];
             char *dst[U];
@@ -1623,18 +1660,15 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
                 const u32 it = it0 + q * BLK;
                 dst[q] = nullptr;
                 if (it >= n_items) continue;
-                while (s_item0[t + 1] <= it) t++;
-                const TableDev &tab = T.t[t];
-                const u32 cnt = s_tcnt[t], rem = it - s_item0[t];
-                const u32 c = rem / cnt, j = rem - c * cnt;
-                wc[q] = col_wide(tab, c);
-                const u32 slot = c + (u32)__popcll(c ? (tab.wide & ((1ull << c) - 1ull)) : 0ull);  // payload slot of column c
+                while (s_pitem[pr + 1] <= it) pr++;
+                const u32 meta = s_pmeta[pr], j = it - s_pitem[pr];
+                const u32 t = meta >> 16, c = (meta >> 8) & 63u, slot = meta & 255u;
+                wc[q] = (meta >> 14) & 1u;
                 const u32 e = s_toff[t] + j;
                 const int32_t *src = b.payload + s_off[e] + slot;
                 v[q] = wc[q] ? (long long)(((u64)(u32)src[1] << 32) | (u64)(u32)src[0]) : (long long)src[0];
                 if (s_lc[e] == c) v[q] = s_lv[e];
-                if (LTP_IN_BOUNDS(ctr, s_base[t] + j, tab.rows_cap))
-                    dst[q] = tab.data + col_off(tab, c) + (s_base[t] + j) * (wc[q] ? 8ull : 4ull);
+                if (LTP_IN_BOUNDS(ctr, s_base[t] + j, T.t[t].rows_cap)) dst[q] = s_pdst[pr] + (u64)j * (wc[q] ? 8ull : 4ull);
             }
 #pragma unroll
             for (int q = 0; q < U; q++)
@@ -1644,9 +1678,46 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
     }
 }
 
-__global__ void __launch_bounds__(kInsBlock) k_insert(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+__global__ void __launch_bounds__(kInsBlock) k_insert(BatchDev b, TablesDev T, Scratch s, Counters *ctr, int prefixed) {
     pdl_begin();
-    phase_insert<kInsBlock>(b, T, s, ctr);
+    phase_insert<kInsBlock>(b, T, s, ctr, prefixed != 0);
+}
+
+// Ordered rule: every insert commits, so the rank of an insert among its
+// table's inserts is known once mark has counted them per insert tile.  One
+// block turns the counts into exclusive prefixes in place, table by table
+// (thread j scans a run of consecutive tiles), so the insert kernel needs no
+// look-back across tiles.
+constexpr u32 kInsPrefixBlock = 1024;
+__global__ void __launch_bounds__(kInsPrefixBlock) k_ins_prefix(BatchDev b, TablesDev T, Scratch s, Counters *ctr) {
+    pdl_begin();
+    if (block_err(ctr)) return;
+    const u64 tiles = (b.n_ops + kInsTile - 1) / kInsTile;
+    const u64 per = (tiles + kInsPrefixBlock - 1) / kInsPrefixBlock;
+    const u64 t0 = (u64)threadIdx.x * per, t1 = min(t0 + per, tiles);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ u32 s_wsum[kInsPrefixBlock / 32];
+    for (u32 tb = 0; tb < T.n; tb++) {
+        if (!ctr->ins_total[tb]) continue;  // the same for every thread
+        u32 sum = 0;
+        for (u64 t = t0; t < t1; t++) sum += s.ins_pre[t * LTP_MAX_TABLES + tb];
+        u32 incl = sum;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const u32 v = __shfl_up_sync(FULL_MASK, incl, d);
+            if (lane >= d) incl += v;
+        }
+        if (lane == 31) s_wsum[warp] = incl;
+        __syncthreads();
+        u32 pre = incl - sum;
+        for (int i = 0; i < warp; i++) pre += s_wsum[i];
+        for (u64 t = t0; t < t1; t++) {
+            const u32 c = s.ins_pre[t * LTP_MAX_TABLES + tb];
+            s.ins_pre[t * LTP_MAX_TABLES + tb] = pre;
+            pre += c;
+        }
+        __syncthreads();  // s_wsum is reused by the next table
+    }
 }
 
 // ============================================================================
@@ -1661,7 +1732,10 @@ __device__ __forceinline__ void phase_finish(const BatchDev &b, const TablesDev 
     if (blockIdx.x == 0 && threadIdx.x < T.n && !ctr->err) T.rows_now[threadIdx.x] += ctr->ins_committed[threadIdx.x];
     if (any_ins) {
         const u64 t_ins = (b.n_ops + kInsTile - 1) / kInsTile;
-        for (u64 j = g0; j < t_ins * LTP_MAX_TABLES; j += gsz) s.st_ins[j] = 0;
+        for (u64 j = g0; j < t_ins * LTP_MAX_TABLES; j += gsz) {
+            s.st_ins[j] = 0;
+            s.ins_pre[j] = 0;
+        }
     }
     const u64 ntw = ctr->n_tw;
     const bool dense = ids_dense(ctr);
@@ -1945,9 +2019,12 @@ cudaError_t launch_execute(const Launch &L_in, const BatchDev &b_in, const Table
             gins = occ_grid(k_insert, kInsBlock, L.num_sms, kInsSmem);
             sms = L.num_sms;
         }
-        if (b.payload_len)  // a batch without payload has no valid insert
+        if (b.payload_len) {  // a batch without payload has no valid insert
+            const int prefixed = L.rule != LTP_RULE_PRIORITY;
+            if (prefixed) chk(launch_k(L.pdl, k_ins_prefix, 1, kInsPrefixBlock, 0, L.stream, b, T, s, ctr));
             chk(launch_k(L.pdl, k_insert, capped(gins, (b.n_ops + kInsTile - 1) / kInsTile), kInsBlock, kInsSmem, L.stream, b,
-                         T, s, ctr));
+                         T, s, ctr, prefixed));
+        }
     }
     mark_ev(9);
     chk(launch_k(L.pdl, wide_words ? k_finish<64> : k_finish<32>, gstream, 256, 0, L.stream, b, T, s, ctr, L.rule));
@@ -2048,7 +2125,7 @@ __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
         }
         grid_sync(a.bar, nb, a.ctr);
         if (b.payload_len) {  // a batch without payload has no valid insert
-            phase_insert<kPBlock>(b, a.T, a.s, a.ctr);
+            phase_insert<kPBlock>(b, a.T, a.s, a.ctr, false);
             grid_sync(a.bar, nb, a.ctr);
         }
         phase_finish<32>(b, a.T, a.s, a.ctr, a.rule);
@@ -2104,6 +2181,7 @@ cudaError_t launch_reset_scratch(cudaStream_t st, const Scratch &s) {
     cudaMemsetAsync(s.st_cls, 0, s.cap_tiles * 8, st);
     cudaMemsetAsync(s.st_apply, 0, s.cap_tiles * 8, st);
     cudaMemsetAsync(s.st_ins, 0, s.cap_tiles * LTP_MAX_TABLES * 4, st);
+    if (s.ins_pre != s.st_ins) cudaMemsetAsync(s.ins_pre, 0, s.cap_tiles * LTP_MAX_TABLES * 4, st);
     return cudaGetLastError();
 }
 

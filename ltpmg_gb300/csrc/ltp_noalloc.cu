@@ -133,6 +133,9 @@ extern "C" int ltp_execute_noalloc(int32_t device, int32_t rule, int32_t *table,
     s.st_cls = (u64 *)(base + kOffCls);
     s.st_apply = (u64 *)(base + kOffApply);
     s.st_ins = (u32 *)(base + kOffIns);
+    // these batches carry no insert payload, so mark counts no insert and
+    // neither array is used: the prefix array shares the status region
+    s.ins_pre = s.st_ins;
     s.n_words = (n_rows * n_cols + 31) / 32 + 1;
     s.cap_ops = kNaMaxOps;
     s.cap_tiles = kNaTiles;
