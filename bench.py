@@ -1231,7 +1231,7 @@ def main():
                          "or x-prefixed multiples of the plain batch path's rate on the same tables")
     ap.add_argument("--ingest-jit", type=int, default=1,
                     help="serve: request log queues a batch only once the one ahead is past its sort (1) or at once (0)")
-    ap.add_argument("--ingest-loads", default="x0.88,0.92,0.95,0.975",
+    ap.add_argument("--ingest-loads", default="x0.9,0.92,0.935,0.95,0.965",
                     help="serving the blend from a device-resident request log: offered loads in M txn/s, or "
                          "x-prefixed multiples of the plain batch path's rate ('' = skip)")
     ap.add_argument("--serve-point-s", type=float, default=1.0, help="serve: seconds of arrivals per sweep point")
