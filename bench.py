@@ -149,15 +149,16 @@ def load_peaks():
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit of work,
-# from one ncu --set full capture of each kernel on one batch of the same
-# workload (profiles/batch_kernels_zipf.md, profiles/k_mark_insert_tpcc.md);
+# from one ncu capture of each kernel on one batch of the same workload
+# (profiles/batch_kernels_zipf.md, profiles/k_mark_insert_tpcc.md,
+# profiles/k_insert_tpcc.md);
 # a launch's traffic is this figure times the units it processed
 MEASURED_TRAFFIC = {
     ("zipf", "classify"): (37.4, "ops"),  # 32-bit keys
     ("zipf", "mark"): (13.3, "ops"),  # 32-bit keys
     ("zipf", "apply"): (30.3, "contended_ops"),
     ("zipf", "ids"): (6.9, "ops"),  # k_ids + k_dbase
-    ("tpcc", "insert"): (59.1, "ops"),  # 32-bit keys
+    ("tpcc", "insert"): (55.5, "ops"),  # 32-bit keys
     ("tpcc", "mark"): (15.7, "ops"),  # 32-bit keys
 }
 
