@@ -1501,7 +1501,16 @@ __global__ void __launch_bounds__(256) k_r1_exec(BatchDev b, TablesDev T, Scratc
 // 16-way ordered prefix sum (warp match_any ranks, per-table decoupled
 // look-back) -- then the payload row is copied into its slot
 // ============================================================================
-template <int BLK>
+// The separate insert kernel copies rows through per-(table, column)
+// descriptors kept in its dynamic shared memory after the staging arrays;
+// the persistent kernel, whose shared memory every phase shares, keeps the
+// flattened per-cell loop (16 KB more there would leave two blocks per SM
+// almost no L1).
+constexpr u32 kInsPairs = LTP_MAX_TABLES * LTP_MAX_COLS;
+constexpr u32 kInsSmemDesc = kInsSmem + kInsPairs * 8 + (kInsPairs + 1) * 4 + kInsPairs * 4;
+static_assert(kInsSmem % 8 == 0, "the descriptors' addresses start 8-byte aligned");
+
+template <int BLK, bool DESC>
 __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev &T, const Scratch &s, Counters *ctr,
                                              bool prefixed) {
     constexpr u32 IIPT = kInsTile / BLK;
@@ -1518,17 +1527,17 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
     __shared__ u32 s_tcnt[LTP_MAX_TABLES], s_toff[LTP_MAX_TABLES];
     __shared__ u32 s_item0[LTP_MAX_TABLES + 1];  // first (table, column, row) item of each table
     __shared__ u32 s_pair0[LTP_MAX_TABLES + 1];  // first (table, column) pair of each table
-    // per (table, column) pair of the tile's new rows: its first item, the
-    // address of its first new row, and slot | column << 8 | wide << 14 |
-    // table << 16 -- so that a cell's copy needs no division and no lookup
-    // of the table's descriptor
-    __shared__ u32 s_pitem[LTP_MAX_TABLES * LTP_MAX_COLS + 1];
-    __shared__ char *s_pdst[LTP_MAX_TABLES * LTP_MAX_COLS];
-    __shared__ u32 s_pmeta[LTP_MAX_TABLES * LTP_MAX_COLS];
     // staging of the tile's inserts in the dynamic shared memory (kInsSmem bytes)
     u32 *s_off = ltp_dyn_smem;                                                  // [kInsTile] payload offsets
     long long *s_lv = reinterpret_cast<long long *>(ltp_dyn_smem + kInsTile);  // [kInsTile] link values
     unsigned char *s_lc = reinterpret_cast<unsigned char *>(s_lv + kInsTile);  // [kInsTile] link columns
+    // DESC: per (table, column) pair of the tile's new rows, its first item,
+    // the address of its first new row, and slot | column << 8 | wide << 14
+    // | table << 16 -- so that a cell's copy needs no division and no lookup
+    // of the table's descriptor (dynamic, after the staging arrays)
+    char **s_pdst = reinterpret_cast<char **>(reinterpret_cast<unsigned char *>(ltp_dyn_smem) + kInsSmem);  // [kInsPairs]
+    u32 *s_pitem = reinterpret_cast<u32 *>(s_pdst + kInsPairs);  // [kInsPairs + 1]
+    u32 *s_pmeta = s_pitem + kInsPairs + 1;                       // [kInsPairs]
     for (;;) {
         const u32 tile = claim_tile(ctr, SLOT_INSERT);
         if (tile >= tiles) break;
@@ -1616,19 +1625,21 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
             s_pair0[LTP_MAX_TABLES] = pairs;
         }
         __syncthreads();
-        for (u32 q = threadIdx.x; q < s_pair0[LTP_MAX_TABLES]; q += BLK) {  // thread q describes pair q
-            u32 t = 0;
-            while (s_pair0[t + 1] <= q) t++;
-            const TableDev &tab = T.t[t];
-            const u32 c = q - s_pair0[t];
-            const bool wc = col_wide(tab, c);
-            const u32 slot = c + (u32)__popcll(c ? (tab.wide & ((1ull << c) - 1ull)) : 0ull);  // payload slot of column c
-            s_pitem[q] = s_item0[t] + c * s_tcnt[t];
-            s_pdst[q] = tab.data + col_off(tab, c) + s_base[t] * (wc ? 8ull : 4ull);
-            s_pmeta[q] = slot | (c << 8) | ((wc ? 1u : 0u) << 14) | (t << 16);
+        if constexpr (DESC) {
+            for (u32 q = threadIdx.x; q < s_pair0[LTP_MAX_TABLES]; q += BLK) {  // thread q describes pair q
+                u32 t = 0;
+                while (s_pair0[t + 1] <= q) t++;
+                const TableDev &tab = T.t[t];
+                const u32 c = q - s_pair0[t];
+                const bool wc = col_wide(tab, c);
+                const u32 slot = c + (u32)__popcll(c ? (tab.wide & ((1ull << c) - 1ull)) : 0ull);  // payload slot of column c
+                s_pitem[q] = s_item0[t] + c * s_tcnt[t];
+                s_pdst[q] = tab.data + col_off(tab, c) + s_base[t] * (wc ? 8ull : 4ull);
+                s_pmeta[q] = slot | (c << 8) | ((wc ? 1u : 0u) << 14) | (t << 16);
+            }
+            if (threadIdx.x == 0) s_pitem[s_pair0[LTP_MAX_TABLES]] = s_item0[LTP_MAX_TABLES];
+            __syncthreads();
         }
-        if (threadIdx.x == 0) s_pitem[s_pair0[LTP_MAX_TABLES]] = s_item0[LTP_MAX_TABLES];
-        __syncthreads();
         // every insert notes its payload row and link; its output is its row id
 #pragma unroll
         for (int k = 0; k < IIPT; k++) {
@@ -1650,7 +1661,7 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
         // rows of a column, and a thread's items issue their loads together
         const u32 n_items = s_item0[LTP_MAX_TABLES];
         constexpr int U = 4;  // items per thread in flight: their loads issue before their stores
-        u32 pr = 0;           // items of a thread only move forward through the pairs
+        u32 pr = 0;           // items of a thread only move forward through the pairs (tables)
         for (u32 it0 = threadIdx.x; it0 < n_items; it0 += U * BLK) {
             long long v[U];
             char *dst[U];
@@ -1660,15 +1671,33 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
                 const u32 it = it0 + q * BLK;
                 dst[q] = nullptr;
                 if (it >= n_items) continue;
-                while (s_pitem[pr + 1] <= it) pr++;
-                const u32 meta = s_pmeta[pr], j = it - s_pitem[pr];
-                const u32 t = meta >> 16, c = (meta >> 8) & 63u, slot = meta & 255u;
-                wc[q] = (meta >> 14) & 1u;
+                u32 t, c, j, slot;
+                if constexpr (DESC) {
+                    while (s_pitem[pr + 1] <= it) pr++;
+                    const u32 meta = s_pmeta[pr];
+                    j = it - s_pitem[pr];
+                    t = meta >> 16;
+                    c = (meta >> 8) & 63u;
+                    slot = meta & 255u;
+                    wc[q] = (meta >> 14) & 1u;
+                } else {
+                    while (s_item0[pr + 1] <= it) pr++;
+                    t = pr;
+                    const TableDev &tab = T.t[t];
+                    const u32 cnt = s_tcnt[t], rem = it - s_item0[t];
+                    c = rem / cnt;
+                    j = rem - c * cnt;
+                    wc[q] = col_wide(tab, c);
+                    slot = c + (u32)__popcll(c ? (tab.wide & ((1ull << c) - 1ull)) : 0ull);  // payload slot of column c
+                }
                 const u32 e = s_toff[t] + j;
                 const int32_t *src = b.payload + s_off[e] + slot;
                 v[q] = wc[q] ? (long long)(((u64)(u32)src[1] << 32) | (u64)(u32)src[0]) : (long long)src[0];
                 if (s_lc[e] == c) v[q] = s_lv[e];
-                if (LTP_IN_BOUNDS(ctr, s_base[t] + j, T.t[t].rows_cap)) dst[q] = s_pdst[pr] + (u64)j * (wc[q] ? 8ull : 4ull);
+                if (LTP_IN_BOUNDS(ctr, s_base[t] + j, T.t[t].rows_cap)) {
+                    if constexpr (DESC) dst[q] = s_pdst[pr] + (u64)j * (wc[q] ? 8ull : 4ull);
+                    else dst[q] = T.t[t].data + col_off(T.t[t], c) + (s_base[t] + j) * (wc[q] ? 8ull : 4ull);
+                }
             }
 #pragma unroll
             for (int q = 0; q < U; q++)
@@ -1680,7 +1709,7 @@ __device__ __forceinline__ void phase_insert(const BatchDev &b, const TablesDev 
 
 __global__ void __launch_bounds__(kInsBlock) k_insert(BatchDev b, TablesDev T, Scratch s, Counters *ctr, int prefixed) {
     pdl_begin();
-    phase_insert<kInsBlock>(b, T, s, ctr, prefixed != 0);
+    phase_insert<kInsBlock, true>(b, T, s, ctr, prefixed != 0);
 }
 
 // Ordered rule: every insert commits, so the rank of an insert among its
@@ -2015,15 +2044,15 @@ cudaError_t launch_execute(const Launch &L_in, const BatchDev &b_in, const Table
     {
         static int gins = 0, sms = 0;
         if (sms != L.num_sms) {
-            chk(cudaFuncSetAttribute(k_insert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInsSmem));
-            gins = occ_grid(k_insert, kInsBlock, L.num_sms, kInsSmem);
+            chk(cudaFuncSetAttribute(k_insert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInsSmemDesc));
+            gins = occ_grid(k_insert, kInsBlock, L.num_sms, kInsSmemDesc);
             sms = L.num_sms;
         }
         if (b.payload_len) {  // a batch without payload has no valid insert
             const int prefixed = L.rule != LTP_RULE_PRIORITY;
             if (prefixed) chk(launch_k(L.pdl, k_ins_prefix, 1, kInsPrefixBlock, 0, L.stream, b, T, s, ctr));
-            chk(launch_k(L.pdl, k_insert, capped(gins, (b.n_ops + kInsTile - 1) / kInsTile), kInsBlock, kInsSmem, L.stream, b,
-                         T, s, ctr, prefixed));
+            chk(launch_k(L.pdl, k_insert, capped(gins, (b.n_ops + kInsTile - 1) / kInsTile), kInsBlock, kInsSmemDesc,
+                         L.stream, b, T, s, ctr, prefixed));
         }
     }
     mark_ev(9);
@@ -2125,7 +2154,7 @@ __global__ void __launch_bounds__(kPBlock, 2) k_persist(PersistArgs a) {
         }
         grid_sync(a.bar, nb, a.ctr);
         if (b.payload_len) {  // a batch without payload has no valid insert
-            phase_insert<kPBlock>(b, a.T, a.s, a.ctr, false);
+            phase_insert<kPBlock, false>(b, a.T, a.s, a.ctr, false);
             grid_sync(a.bar, nb, a.ctr);
         }
         phase_finish<32>(b, a.T, a.s, a.ctr, a.rule);
