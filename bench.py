@@ -1227,12 +1227,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pipeline pass")
     ap.add_argument("--loads", default="1,2,5,10,20,50", help="serving sweep: offered loads in M txn/s")
     ap.add_argument("--loadgen-threads", type=int, default=8, help="serving sweep: load-generator threads")
-    ap.add_argument("--ycsb-loads", default="x0.94,0.955,0.97,0.98,0.99",
+    ap.add_argument("--ycsb-loads", default="x0.94,0.955,0.97,0.975,0.98,0.99",
                     help="request-log serving of the Zipf YCSB transactions alone: offered loads in M txn/s, "
                          "or x-prefixed multiples of the plain batch path's rate on the same tables")
     ap.add_argument("--ingest-jit", type=int, default=1,
                     help="serve: request log queues a batch only once the one ahead is past its sort (1) or at once (0)")
-    ap.add_argument("--ingest-loads", default="x0.9,0.92,0.935,0.95,0.965",
+    ap.add_argument("--ingest-loads", default="x0.92,0.935,0.943,0.95,0.957,0.965",
                     help="serving the blend from a device-resident request log: offered loads in M txn/s, or "
                          "x-prefixed multiples of the plain batch path's rate ('' = skip)")
     ap.add_argument("--serve-point-s", type=float, default=1.0, help="serve: seconds of arrivals per sweep point")
